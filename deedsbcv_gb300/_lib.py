@@ -1,0 +1,103 @@
+"""ctypes binding of libdeeds_gpu.so (the C ABI declared in include/deeds_gpu.h).
+
+There is no fallback: if the library is missing or cannot be loaded the import
+of the functions that need it raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libdeeds_gpu.so")
+MAX_LEVELS = 10
+
+DEEDS_OK = 0
+ERR_NAMES = {1: "DEEDS_ERR_INVALID", 2: "DEEDS_ERR_CUDA", 3: "DEEDS_ERR_NOMEM", 4: "DEEDS_ERR_TIMEOUT",
+             5: "DEEDS_ERR_INTERNAL"}
+
+# every symbol include/deeds_gpu.h declares
+EXPORTS = [
+    "deeds_default_params", "deeds_create", "deeds_destroy", "deeds_last_error", "deeds_version",
+    "deeds_register", "deeds_register_dev", "deeds_warp_segmentation", "deeds_apply_flow",
+    "deeds_mind_ssc_dev", "deeds_data_cost_dev", "deeds_mst_edges_dev", "deeds_image_stats",
+    "deeds_prims_from_sad", "deeds_tree_bp_dev", "deeds_upsample_dev", "deeds_warp_affine_dev",
+    "deeds_warp_image_dev", "deeds_warp_seg_dev", "deeds_consistent_dev", "deeds_jacobian_dev",
+    "deeds_set_profiling", "deeds_stage_times", "deeds_reset_stage_times", "deeds_kernel_launches",
+    "deeds_measure_popc_rate",
+]
+STAGES = ["mind", "datacost", "mst_edges", "bp_up", "bp_down", "transform", "consistent", "tree_wait"]
+
+
+class DeedsParams(C.Structure):
+    _fields_ = [
+        ("levels", C.c_int),
+        ("grid", C.c_int * MAX_LEVELS),
+        ("radius", C.c_int * MAX_LEVELS),
+        ("quant", C.c_int * MAX_LEVELS),
+        ("alpha", C.c_float),
+        ("intensity_shift", C.c_float),
+        ("verbose", C.c_int),
+    ]
+
+
+class DeedsError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"{ERR_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+_lib = None
+
+
+def load():
+    """Load the library (build it first with deedsbcv_gb300.build.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"libdeeds_gpu.so not built ({LIB_PATH}); run python -m deedsbcv_gb300.build")
+    L = C.CDLL(LIB_PATH)
+    P, I, F, S = C.c_void_p, C.c_int, C.c_float, C.c_size_t
+    L.deeds_default_params.argtypes = [C.POINTER(DeedsParams)]
+    L.deeds_default_params.restype = None
+    L.deeds_create.argtypes = [C.POINTER(P), I]
+    L.deeds_destroy.argtypes = [P]
+    L.deeds_destroy.restype = None
+    L.deeds_last_error.argtypes = [P]
+    L.deeds_last_error.restype = C.c_char_p
+    L.deeds_version.restype = C.c_char_p
+    L.deeds_register.argtypes = [P, P, P, I, I, I, P, C.POINTER(DeedsParams), P, P]
+    L.deeds_register_dev.argtypes = [P, P, P, I, I, I, P, C.POINTER(DeedsParams), P, P, P]
+    L.deeds_warp_segmentation.argtypes = [P, P, P]
+    L.deeds_apply_flow.argtypes = [P, P, S, I, P, P, I, I, I, I, P]
+    L.deeds_mind_ssc_dev.argtypes = [P, P, I, I, I, I, P, P]
+    L.deeds_data_cost_dev.argtypes = [P, P, P, I, I, I, I, I, I, F, P, P]
+    L.deeds_mst_edges_dev.argtypes = [P, P, I, I, I, I, P, P]
+    L.deeds_image_stats.argtypes = [P, S, P, P]
+    L.deeds_prims_from_sad.argtypes = [P, F, I, I, I, I, P, P, P]
+    L.deeds_tree_bp_dev.argtypes = [P, P, P, P, P, I, I, I, I, I, P, P, P, P, P, P, P, P]
+    L.deeds_upsample_dev.argtypes = [P, P, P, I, I, I, P, P, P, I, I, I, P]
+    L.deeds_warp_affine_dev.argtypes = [P, P, P, P, P, I, I, I, P, P]
+    L.deeds_warp_image_dev.argtypes = [P, P, P, P, I, I, I, P, P]
+    L.deeds_warp_seg_dev.argtypes = [P, P, P, P, P, I, I, I, P, P]
+    L.deeds_consistent_dev.argtypes = [P, P, P, P, P, P, P, I, I, I, I, P]
+    L.deeds_jacobian_dev.argtypes = [P, P, P, P, I, I, I, I, P, P, P]
+    L.deeds_set_profiling.argtypes = [P, I]
+    L.deeds_stage_times.argtypes = [P, P, P]
+    L.deeds_reset_stage_times.argtypes = [P]
+    L.deeds_kernel_launches.argtypes = []
+    L.deeds_measure_popc_rate.argtypes = [P, P]
+    for name in EXPORTS:
+        fn = getattr(L, name)
+        if name not in ("deeds_default_params", "deeds_destroy", "deeds_last_error", "deeds_version"):
+            fn.restype = I
+    L.deeds_kernel_launches.restype = C.c_longlong
+    _lib = L
+    return L
+
+
+def check(status, ctx=None):
+    if status != DEEDS_OK:
+        msg = load().deeds_last_error(ctx)
+        raise DeedsError(status, msg.decode() if msg else "")

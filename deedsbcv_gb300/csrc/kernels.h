@@ -1,0 +1,67 @@
+// Kernel launchers of libdeeds_gpu (host-callable, C++ linkage, internal).
+#pragma once
+#include <atomic>
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace deeds {
+
+// Process-wide count of kernels launched by this library (for accounting).
+extern std::atomic<long long> g_kernel_launches;
+inline void count_launches(int n) { g_kernel_launches.fetch_add(n, std::memory_order_relaxed); }
+
+// Device-side description of one MST for the belief-propagation kernels.
+struct BpTree {
+    int len;                 // 2*hw+1
+    float q;                 // label quantisation
+    int n_up;                // number of upward work items (nodes with children)
+    const int* up_nodes;     // [n_up] parent node of each item, deepest first
+    const int* child_ptr;    // [n_up+1] CSR into children
+    const int* children;     // children of each item, in MST ordering order
+    const int* wait_idx;     // [sz1] item index of a node if it has children, else -1
+    const float* edgemst;    // [sz1] weight of the edge to the parent
+    const float* u0;         // [sz1] current displacement (label offsets are relative)
+    const float* v0;
+    const float* w0;
+    int n_levels;            // breadth levels
+    const int* level_start;  // [n_levels+1] ranges into ordered
+    const int* ordered;      // [sz1] breadth-level order
+    const int* parents;      // [sz1]
+};
+
+// A displacement field given at full resolution (mode 1), on a control grid
+// to be upsampled on the fly (mode 2), or zero (mode 0).
+struct FieldRef {
+    int mode;
+    const float* u;
+    const float* v;
+    const float* w;
+    int m1, n1, o1;
+};
+
+cudaError_t launch_mind_ssc(const float* d_im, int m, int n, int o, int qs, const float thr[5], float* d_scratch,
+                            uint64_t* d_codes, cudaStream_t s);
+cudaError_t launch_data_cost(const uint64_t* d_F, const uint64_t* d_M, int m, int n, int o, int g, int hw, int q,
+                             int sy, int sx, int sz, float alpha1, float* d_cost, cudaStream_t s);
+cudaError_t launch_edge_sad(const float* d_im, int m, int n, int o, int g, float* d_sad, cudaStream_t s);
+size_t bp_up_smem_bytes(int len);
+cudaError_t launch_bp_up(const BpTree& t, float* d_cost, short* d_allinds, int* d_work, int* d_flags, int epoch,
+                         int* d_err, int max_ctas, cudaStream_t s);
+cudaError_t launch_bp_down(const BpTree& t, const float* d_cost, short* d_allinds, int* d_sel, float* d_u1,
+                           float* d_v1, float* d_w1, int* d_err, cudaStream_t s);
+cudaError_t launch_shift(const float* d_in, float* d_out, int64_t n, float shift, cudaStream_t s);
+cudaError_t launch_upsample(const float* u0, const float* v0, const float* w0, int m2, int n2, int o2, float* u,
+                            float* v, float* w, int m, int n, int o, cudaStream_t s);
+cudaError_t launch_warp_affine(const float* d_in, const float* X, const FieldRef& f, int m, int n, int o, float* d_out,
+                               float* keep_u, float* keep_v, float* keep_w, cudaStream_t s);
+cudaError_t launch_warp_image(const float* d_in, const FieldRef& f, int m, int n, int o, float* d_out, cudaStream_t s);
+cudaError_t launch_warp_seg(const short* d_in, const float* X, const FieldRef& f, int m, int n, int o, short* d_out,
+                            cudaStream_t s);
+cudaError_t launch_consistent(float* u, float* v, float* w, float* u2, float* v2, float* w2, int m, int n, int o, int g,
+                              float* scratch, cudaStream_t s);
+cudaError_t launch_popc_probe(int blocks, int threads, int iters, unsigned long long* d_sink, cudaStream_t s);
+cudaError_t launch_jacobian(const float* u, const float* v, const float* w, int m, int n, int o, int g, double* d_acc,
+                            cudaStream_t s);
+
+}  // namespace deeds

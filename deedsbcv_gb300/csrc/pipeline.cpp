@@ -1,0 +1,871 @@
+// libdeeds_gpu host side: the C ABI of include/deeds_gpu.h, the context (device
+// scratch, streams, pinned staging) and the per-pair level loop that replaces
+// main() of src/deedsBCV0.cpp:183-356.
+//
+// Per pair, on the caller's stream:
+//   shift (+1024) -> affine warp of the moving image (warped0)
+//   side stream: block SADs of fixed and warped0 for every level's grid ->
+//   host: image statistics, Prim and the BP schedules for all 2*levels trees,
+//         on worker threads, overlapped with the GPU level loop;
+//   per level, forward then backward: grid upsample -> fused full-res
+//   upsample + warp -> MIND-SSC -> Hamming cost volume -> (wait for that tree)
+//   upload schedule -> upward BP -> downward BP; then inverse consistency.
+// Compiled with -ffp-contract=off (host float arithmetic follows the reference).
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <future>
+#include <map>
+#include <memory>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/deeds_gpu.h"
+#include "kernels.h"
+#include "tree_host.h"
+
+using namespace deeds;
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+};
+struct HostBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+};
+
+struct deeds_ctx {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;  // used by the host-pointer entry points
+    cudaStream_t side = nullptr;    // MST edge costs and their copies
+    cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+    std::string err;
+    std::map<std::string, DevBuf> dev;
+    std::map<std::string, HostBuf> host;
+    int epoch = 0;
+    // per-stage tracing (deeds_set_profiling)
+    bool prof = false;
+    std::vector<cudaEvent_t> ev_pool;
+    size_t ev_used = 0;
+    struct Mark { int stage; cudaEvent_t a, b; };
+    std::vector<Mark> marks;
+    double stage_ms[DEEDS_NUM_STAGES] = {0};
+    long long stage_launches[DEEDS_NUM_STAGES] = {0};
+    // the last registration's full-resolution field (for deeds_warp_segmentation)
+    bool have_field = false;
+    int fm = 0, fn = 0, fo = 0;
+    float fX[16];
+};
+
+namespace deeds {
+std::atomic<long long> g_kernel_launches{0};
+}
+
+namespace {
+
+thread_local std::string g_create_err;
+
+cudaEvent_t pool_event(deeds_ctx* c) {
+    if (c->ev_used == c->ev_pool.size()) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        c->ev_pool.push_back(e);
+    }
+    return c->ev_pool[c->ev_used++];
+}
+
+// Brackets one stage of the pipeline with CUDA events on `s` (and counts its
+// kernel launches) when profiling is on; a no-op otherwise.
+struct StageScope {
+    deeds_ctx* c;
+    int stage;
+    cudaStream_t s;
+    cudaEvent_t a = nullptr;
+    long long launches0;
+    StageScope(deeds_ctx* c_, int stage_, cudaStream_t s_) : c(c_), stage(stage_), s(s_) {
+        launches0 = deeds::g_kernel_launches.load();
+        if (c->prof && (a = pool_event(c))) cudaEventRecord(a, s);
+    }
+    ~StageScope() {
+        if (!c->prof) return;
+        c->stage_launches[stage] += deeds::g_kernel_launches.load() - launches0;
+        cudaEvent_t b = a ? pool_event(c) : nullptr;
+        if (b) {
+            cudaEventRecord(b, s);
+            c->marks.push_back({stage, a, b});
+        }
+    }
+};
+
+void collect_marks(deeds_ctx* c) {
+    for (auto& mk : c->marks) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, mk.a, mk.b) == cudaSuccess) c->stage_ms[mk.stage] += ms;
+    }
+    c->marks.clear();
+    c->ev_used = 0;
+    cudaGetLastError();
+}
+
+deeds_status fail(deeds_ctx* c, deeds_status st, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    else g_create_err = buf;
+    return st;
+}
+
+#define CK(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) return fail(ctx, DEEDS_ERR_CUDA, "%s: %s (%s:%d)", #call,           \
+                                           cudaGetErrorString(e_), __FILE__, __LINE__);           \
+    } while (0)
+
+template <class T>
+T* dbuf(deeds_ctx* ctx, const std::string& name, size_t count, deeds_status* st, bool zero = false) {
+    DevBuf& b = ctx->dev[name];
+    const size_t bytes = std::max<size_t>(count * sizeof(T), 16);
+    if (b.cap < bytes) {
+        if (b.p) cudaFree(b.p);
+        b.p = nullptr;
+        b.cap = 0;
+        if (cudaMalloc(&b.p, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            *st = fail(ctx, DEEDS_ERR_NOMEM, "cudaMalloc of %zu bytes for %s failed", bytes, name.c_str());
+            return nullptr;
+        }
+        b.cap = bytes;
+        if (zero && cudaMemset(b.p, 0, bytes) != cudaSuccess) {
+            *st = fail(ctx, DEEDS_ERR_CUDA, "cudaMemset %s failed", name.c_str());
+            return nullptr;
+        }
+    }
+    return static_cast<T*>(b.p);
+}
+
+template <class T>
+T* hbuf(deeds_ctx* ctx, const std::string& name, size_t count, deeds_status* st) {
+    HostBuf& b = ctx->host[name];
+    const size_t bytes = std::max<size_t>(count * sizeof(T), 16);
+    if (b.cap < bytes) {
+        if (b.p) cudaFreeHost(b.p);
+        b.p = nullptr;
+        b.cap = 0;
+        if (cudaHostAlloc(&b.p, bytes, cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            *st = fail(ctx, DEEDS_ERR_NOMEM, "cudaHostAlloc of %zu bytes for %s failed", bytes, name.c_str());
+            return nullptr;
+        }
+        b.cap = bytes;
+    }
+    return static_cast<T*>(b.p);
+}
+
+void mind_thresholds(float thr[5]) {
+    for (int c = 0; c < 5; c++) thr[c] = -std::log(((float)c + 1.5f) / 6);  // logf, src/MINDSSCbox.h:177-180
+}
+
+int mind_step(int q) { return (int)std::floor(0.5f * (float)q + 1.0f); }  // src/deedsBCV0.cpp:183-186
+
+// alpha1 = float(0.5*(g/(alpha*q))/maxsamp), sampling strides for RAND_SAMPLES=1
+// (src/dataCostD.h:141-163).
+void data_cost_params(int g, int q, float alpha, int* sy, int* sx, int* sz, float* alpha1) {
+    *sy = 1; *sx = 1; *sz = 1;
+    if (g > 4) { *sx = 2; *sz = 2; }
+    const float maxsamp = std::ceil((float)g / (float)*sx) * std::ceil((float)g / (float)*sz) *
+                          std::ceil((float)g / (float)*sy);
+    const float alphai = (float)g / (alpha * (float)q);
+    *alpha1 = (float)(0.5 * alphai / (float)maxsamp);
+}
+
+deeds_status check_params(deeds_ctx* ctx, const deeds_params* p, int m, int n, int o) {
+    if (!p) return fail(ctx, DEEDS_ERR_INVALID, "params is NULL");
+    if (p->levels < 1 || p->levels > DEEDS_MAX_LEVELS)
+        return fail(ctx, DEEDS_ERR_INVALID, "levels=%d outside 1..%d", p->levels, DEEDS_MAX_LEVELS);
+    if (m < 1 || n < 1 || o < 1) return fail(ctx, DEEDS_ERR_INVALID, "bad dims %dx%dx%d", m, n, o);
+    for (int l = 0; l < p->levels; l++) {
+        const int g = p->grid[l], hw = p->radius[l], q = p->quant[l];
+        if (g < 1 || hw < 0 || q < 1)
+            return fail(ctx, DEEDS_ERR_INVALID, "level %d: grid=%d radius=%d quant=%d", l, g, hw, q);
+        if (hw > 10) return fail(ctx, DEEDS_ERR_INVALID, "level %d: search radius %d > 10 unsupported", l, hw);
+        if (m / g < 1 || n / g < 1 || o / g < 1)
+            return fail(ctx, DEEDS_ERR_INVALID, "level %d: grid %d larger than the volume", l, g);
+        const int qs = mind_step(q);
+        if (qs > 7) return fail(ctx, DEEDS_ERR_INVALID, "level %d: MIND radius %d > 7 unsupported", l, qs);
+        if (m < 2 * qs + 1 || n < 2 * qs + 1 || o < 2 * qs + 1)
+            return fail(ctx, DEEDS_ERR_INVALID, "volume %dx%dx%d too small for MIND radius %d", m, n, o, qs);
+    }
+    return DEEDS_OK;
+}
+
+// One tree's host arrays packed for a single H2D copy.
+struct PackedTree {
+    int sz = 0, n_up = 0, n_levels = 0;
+    size_t o_ordered, o_parents, o_wait, o_children, o_up, o_cptr, o_lstart, o_edgemst, total;  // in 4-byte words
+};
+
+PackedTree pack_layout(int sz) {
+    PackedTree t;
+    t.sz = sz;
+    size_t o = 0;
+    t.o_ordered = o; o += sz;
+    t.o_parents = o; o += sz;
+    t.o_wait = o; o += sz;
+    t.o_children = o; o += sz;
+    t.o_up = o; o += sz;
+    t.o_cptr = o; o += sz + 1;
+    t.o_lstart = o; o += sz + 1;
+    t.o_edgemst = o; o += sz;
+    t.total = o;
+    return t;
+}
+
+// Build one tree on the host into the packed pinned block `blk`.
+void build_tree(const float* sad, float stddev, int m1, int n1, int o1, int g, uint32_t* blk, PackedTree& t) {
+    const int sz = m1 * n1 * o1;
+    int* ordered = reinterpret_cast<int*>(blk + t.o_ordered);
+    int* parents = reinterpret_cast<int*>(blk + t.o_parents);
+    float* edgemst = reinterpret_cast<float*>(blk + t.o_edgemst);
+    prims_from_sad(sad, stddev, m1, n1, o1, g, ordered, parents, edgemst);
+    TreeSchedule s;
+    build_schedule(ordered, parents, sz, s);
+    t.n_up = (int)s.up_nodes.size();
+    t.n_levels = s.n_levels;
+    std::memcpy(blk + t.o_wait, s.wait_idx.data(), sizeof(int) * sz);
+    std::memcpy(blk + t.o_children, s.children.data(), sizeof(int) * s.children.size());
+    std::memcpy(blk + t.o_up, s.up_nodes.data(), sizeof(int) * s.up_nodes.size());
+    std::memcpy(blk + t.o_cptr, s.child_ptr.data(), sizeof(int) * s.child_ptr.size());
+    std::memcpy(blk + t.o_lstart, s.level_start.data(), sizeof(int) * s.level_start.size());
+}
+
+BpTree device_tree(const PackedTree& t, const uint32_t* dblk, int len, float q, const float* u0, const float* v0,
+                   const float* w0) {
+    BpTree b;
+    b.len = len;
+    b.q = q;
+    b.n_up = t.n_up;
+    b.up_nodes = reinterpret_cast<const int*>(dblk + t.o_up);
+    b.child_ptr = reinterpret_cast<const int*>(dblk + t.o_cptr);
+    b.children = reinterpret_cast<const int*>(dblk + t.o_children);
+    b.wait_idx = reinterpret_cast<const int*>(dblk + t.o_wait);
+    b.edgemst = reinterpret_cast<const float*>(dblk + t.o_edgemst);
+    b.u0 = u0; b.v0 = v0; b.w0 = w0;
+    b.n_levels = t.n_levels;
+    b.level_start = reinterpret_cast<const int*>(dblk + t.o_lstart);
+    b.ordered = reinterpret_cast<const int*>(dblk + t.o_ordered);
+    b.parents = reinterpret_cast<const int*>(dblk + t.o_parents);
+    return b;
+}
+
+int bp_max_ctas(deeds_ctx* ctx, int len) {
+    // persistent grid: as many CTAs as can be resident (shared memory limited)
+    const size_t smem = bp_up_smem_bytes(len);
+    int per_sm = (int)(200 * 1024 / (smem + 1024));
+    if (per_sm < 1) per_sm = 1;
+    if (per_sm > 8) per_sm = 8;
+    return per_sm * ctx->sm_count;
+}
+
+// Run BP on one tree: upload its schedule, upward pass, downward pass.
+deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTree& pt, const uint32_t* h_blk,
+                         float* d_cost, short* d_allinds, int len, int q, const float* u0, const float* v0,
+                         const float* w0, float* u1, float* v1, float* w1, int* d_err, cudaStream_t s) {
+    deeds_status st = DEEDS_OK;
+    uint32_t* d_blk = dbuf<uint32_t>(ctx, "tree_" + tag, pt.total, &st);
+    int* d_flags = dbuf<int>(ctx, "flags_" + tag, (size_t)pt.sz + 1, &st, true);
+    int* d_work = dbuf<int>(ctx, "work_" + tag, 1, &st);
+    int* d_sel = dbuf<int>(ctx, "sel_" + tag, pt.sz, &st);
+    if (st) return st;
+    CK(cudaMemcpyAsync(d_blk, h_blk, pt.total * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    const BpTree bt = device_tree(pt, d_blk, len, (float)q, u0, v0, w0);
+    const int epoch = ++ctx->epoch;
+    {
+        StageScope sc(ctx, DEEDS_STAGE_BP_UP, s);
+        CK(launch_bp_up(bt, d_cost, d_allinds, d_work, d_flags, epoch, d_err, bp_max_ctas(ctx, len), s));
+    }
+    {
+        StageScope sc(ctx, DEEDS_STAGE_BP_DOWN, s);
+        CK(launch_bp_down(bt, d_cost, d_allinds, d_sel, u1, v1, w1, d_err, s));
+    }
+    return DEEDS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* deeds_version(void) { return "deeds-gb300 0.1 (sm_103a)"; }
+
+void deeds_default_params(deeds_params* p) {
+    std::memset(p, 0, sizeof(*p));
+    p->levels = 5;
+    const int G[5] = {8, 7, 6, 5, 4}, L[5] = {8, 7, 6, 5, 4}, Q[5] = {5, 4, 3, 2, 1};
+    for (int i = 0; i < 5; i++) { p->grid[i] = G[i]; p->radius[i] = L[i]; p->quant[i] = Q[i]; }
+    p->alpha = 1.6f;
+    p->intensity_shift = 1024.0f;
+    p->verbose = 0;
+}
+
+deeds_status deeds_create(deeds_ctx** out, int device) {
+    if (!out) return fail(nullptr, DEEDS_ERR_INVALID, "ctx pointer is NULL");
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return fail(nullptr, DEEDS_ERR_CUDA, "no CUDA device available (%s)", cudaGetErrorString(e));
+    if (device < 0 || device >= ndev) return fail(nullptr, DEEDS_ERR_INVALID, "device %d of %d", device, ndev);
+    std::unique_ptr<deeds_ctx> c(new deeds_ctx());
+    c->device = device;
+    deeds_ctx* ctx = c.get();
+    CK(cudaSetDevice(device));
+    CK(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device));
+    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&c->ev_a, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->ev_b, cudaEventDisableTiming));
+    *out = c.release();
+    return DEEDS_OK;
+}
+
+void deeds_destroy(deeds_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->side) cudaStreamSynchronize(ctx->side);
+    for (auto& kv : ctx->dev) if (kv.second.p) cudaFree(kv.second.p);
+    for (auto& kv : ctx->host) if (kv.second.p) cudaFreeHost(kv.second.p);
+    for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
+    if (ctx->ev_a) cudaEventDestroy(ctx->ev_a);
+    if (ctx->ev_b) cudaEventDestroy(ctx->ev_b);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
+    delete ctx;
+}
+
+const char* deeds_last_error(const deeds_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_err.c_str(); }
+
+deeds_status deeds_image_stats(const float* im, size_t count, float* mean, float* stddev) {
+    if (!im || !mean || !stddev || count == 0) return fail(nullptr, DEEDS_ERR_INVALID, "deeds_image_stats: bad args");
+    image_stats(im, count, mean, stddev);
+    return DEEDS_OK;
+}
+
+deeds_status deeds_prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int g, int* ordered,
+                                  int* parents, float* edgemst) {
+    if (!sad || !ordered || !parents || !edgemst || m1 < 1 || n1 < 1 || o1 < 1 || g < 1)
+        return fail(nullptr, DEEDS_ERR_INVALID, "deeds_prims_from_sad: bad args");
+    prims_from_sad(sad, stddev, m1, n1, o1, g, ordered, parents, edgemst);
+    return DEEDS_OK;
+}
+
+deeds_status deeds_mind_ssc_dev(deeds_ctx* ctx, const float* d_im, int m, int n, int o, int qs, uint64_t* d_codes,
+                                void* stream) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!d_im || !d_codes) return fail(ctx, DEEDS_ERR_INVALID, "null pointer");
+    if (qs < 1 || qs > 7) return fail(ctx, DEEDS_ERR_INVALID, "MIND radius %d outside 1..7", qs);
+    if (m < 2 * qs + 1 || n < 2 * qs + 1 || o < 2 * qs + 1)
+        return fail(ctx, DEEDS_ERR_INVALID, "volume %dx%dx%d too small for radius %d", m, n, o, qs);
+    CK(cudaSetDevice(ctx->device));
+    deeds_status st = DEEDS_OK;
+    float* scratch = dbuf<float>(ctx, "mind", (size_t)6 * m * n * o, &st);
+    if (st) return st;
+    float thr[5];
+    mind_thresholds(thr);
+    CK(launch_mind_ssc(d_im, m, n, o, qs, thr, scratch, d_codes, (cudaStream_t)stream));
+    return DEEDS_OK;
+}
+
+deeds_status deeds_data_cost_dev(deeds_ctx* ctx, const uint64_t* d_F, const uint64_t* d_M, int m, int n, int o, int g,
+                                 int hw, int q, float alpha, float* d_cost, void* stream) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!d_F || !d_M || !d_cost) return fail(ctx, DEEDS_ERR_INVALID, "null pointer");
+    if (g < 1 || hw < 0 || q < 1 || m / g < 1 || n / g < 1 || o / g < 1)
+        return fail(ctx, DEEDS_ERR_INVALID, "bad grid %d / radius %d / quant %d", g, hw, q);
+    CK(cudaSetDevice(ctx->device));
+    int sy, sx, sz;
+    float alpha1;
+    data_cost_params(g, q, alpha, &sy, &sx, &sz, &alpha1);
+    CK(launch_data_cost(d_F, d_M, m, n, o, g, hw, q, sy, sx, sz, alpha1, d_cost, (cudaStream_t)stream));
+    return DEEDS_OK;
+}
+
+deeds_status deeds_mst_edges_dev(deeds_ctx* ctx, const float* d_im, int m, int n, int o, int g, float* d_sad,
+                                 void* stream) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!d_im || !d_sad || g < 1 || m / g < 1 || n / g < 1 || o / g < 1)
+        return fail(ctx, DEEDS_ERR_INVALID, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    CK(launch_edge_sad(d_im, m, n, o, g, d_sad, (cudaStream_t)stream));
+    return DEEDS_OK;
+}
+
+deeds_status deeds_tree_bp_dev(deeds_ctx* ctx, float* d_cost, const float* d_u0, const float* d_v0, const float* d_w0,
+                               int m1, int n1, int o1, int hw, int q, const int* ordered, const int* parents,
+                               const float* edgemst, float* d_u1, float* d_v1, float* d_w1, int16_t* d_allinds,
+                               void* stream) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!d_cost || !d_u0 || !d_v0 || !d_w0 || !ordered || !parents || !edgemst || !d_u1 || !d_v1 || !d_w1)
+        return fail(ctx, DEEDS_ERR_INVALID, "null pointer");
+    if (hw < 0 || hw > 10 || q < 1) return fail(ctx, DEEDS_ERR_INVALID, "radius %d / quant %d", hw, q);
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = (cudaStream_t)stream;
+    const int sz = m1 * n1 * o1;
+    const int len = 2 * hw + 1;
+    const size_t len3 = (size_t)len * len * len;
+    deeds_status st = DEEDS_OK;
+    PackedTree pt = pack_layout(sz);
+    uint32_t* h = hbuf<uint32_t>(ctx, "tree_stage", pt.total, &st);
+    short* allinds = d_allinds ? reinterpret_cast<short*>(d_allinds) : dbuf<short>(ctx, "allinds_stage", sz * len3, &st);
+    int* d_err = dbuf<int>(ctx, "err_stage", 1, &st);
+    if (st) return st;
+    CK(cudaStreamSynchronize(s));  // the pinned staging block is reused across calls
+    std::memcpy(h + pt.o_ordered, ordered, sizeof(int) * sz);
+    std::memcpy(h + pt.o_parents, parents, sizeof(int) * sz);
+    std::memcpy(h + pt.o_edgemst, edgemst, sizeof(float) * sz);
+    TreeSchedule sch;
+    build_schedule(ordered, parents, sz, sch);
+    pt.n_up = (int)sch.up_nodes.size();
+    pt.n_levels = sch.n_levels;
+    std::memcpy(h + pt.o_wait, sch.wait_idx.data(), sizeof(int) * sz);
+    std::memcpy(h + pt.o_children, sch.children.data(), sizeof(int) * sch.children.size());
+    std::memcpy(h + pt.o_up, sch.up_nodes.data(), sizeof(int) * sch.up_nodes.size());
+    std::memcpy(h + pt.o_cptr, sch.child_ptr.data(), sizeof(int) * sch.child_ptr.size());
+    std::memcpy(h + pt.o_lstart, sch.level_start.data(), sizeof(int) * sch.level_start.size());
+    CK(cudaMemsetAsync(d_err, 0, sizeof(int), s));
+    st = run_tree_bp(ctx, "stage", pt, h, d_cost, allinds, len, q, d_u0, d_v0, d_w0, d_u1, d_v1, d_w1, d_err, s);
+    if (st) return st;
+    int herr = 0;
+    CK(cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (herr) return fail(ctx, DEEDS_ERR_TIMEOUT, "belief propagation: a bounded wait expired");
+    return DEEDS_OK;
+}
+
+deeds_status deeds_upsample_dev(const float* d_u0, const float* d_v0, const float* d_w0, int m2, int n2, int o2,
+                                float* d_u, float* d_v, float* d_w, int m, int n, int o, void* stream) {
+    deeds_ctx* ctx = nullptr;
+    if (!d_u0 || !d_v0 || !d_w0 || !d_u || !d_v || !d_w || m2 < 1 || n2 < 1 || o2 < 1 || m < 1 || n < 1 || o < 1)
+        return fail(nullptr, DEEDS_ERR_INVALID, "deeds_upsample_dev: bad arguments");
+    CK(launch_upsample(d_u0, d_v0, d_w0, m2, n2, o2, d_u, d_v, d_w, m, n, o, (cudaStream_t)stream));
+    return DEEDS_OK;
+}
+
+deeds_status deeds_warp_affine_dev(const float* d_in, const float X[16], const float* d_u, const float* d_v,
+                                   const float* d_w, int m, int n, int o, float* d_out, void* stream) {
+    deeds_ctx* ctx = nullptr;
+    if (!d_in || !X || !d_out || m < 1 || n < 1 || o < 1)
+        return fail(nullptr, DEEDS_ERR_INVALID, "deeds_warp_affine_dev: bad arguments");
+    FieldRef f{(d_u && d_v && d_w) ? 1 : 0, d_u, d_v, d_w, 0, 0, 0};
+    CK(launch_warp_affine(d_in, X, f, m, n, o, d_out, nullptr, nullptr, nullptr, (cudaStream_t)stream));
+    return DEEDS_OK;
+}
+
+deeds_status deeds_warp_image_dev(const float* d_in, const float* d_u, const float* d_v, const float* d_w, int m, int n,
+                                  int o, float* d_out, void* stream) {
+    deeds_ctx* ctx = nullptr;
+    if (!d_in || !d_u || !d_v || !d_w || !d_out || m < 1 || n < 1 || o < 1)
+        return fail(nullptr, DEEDS_ERR_INVALID, "deeds_warp_image_dev: bad arguments");
+    FieldRef f{1, d_u, d_v, d_w, 0, 0, 0};
+    CK(launch_warp_image(d_in, f, m, n, o, d_out, (cudaStream_t)stream));
+    return DEEDS_OK;
+}
+
+deeds_status deeds_warp_seg_dev(const int16_t* d_in, const float X[16], const float* d_u, const float* d_v,
+                                const float* d_w, int m, int n, int o, int16_t* d_out, void* stream) {
+    deeds_ctx* ctx = nullptr;
+    if (!d_in || !X || !d_out || m < 1 || n < 1 || o < 1)
+        return fail(nullptr, DEEDS_ERR_INVALID, "deeds_warp_seg_dev: bad arguments");
+    FieldRef f{(d_u && d_v && d_w) ? 1 : 0, d_u, d_v, d_w, 0, 0, 0};
+    CK(launch_warp_seg(reinterpret_cast<const short*>(d_in), X, f, m, n, o, reinterpret_cast<short*>(d_out),
+                       (cudaStream_t)stream));
+    return DEEDS_OK;
+}
+
+deeds_status deeds_consistent_dev(deeds_ctx* ctx, float* d_u, float* d_v, float* d_w, float* d_u2, float* d_v2,
+                                  float* d_w2, int m, int n, int o, int g, void* stream) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!d_u || !d_v || !d_w || !d_u2 || !d_v2 || !d_w2 || m < 1 || n < 1 || o < 1 || g < 1)
+        return fail(ctx, DEEDS_ERR_INVALID, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    deeds_status st = DEEDS_OK;
+    float* scratch = dbuf<float>(ctx, "consistent", (size_t)12 * m * n * o, &st);
+    if (st) return st;
+    CK(launch_consistent(d_u, d_v, d_w, d_u2, d_v2, d_w2, m, n, o, g, scratch, (cudaStream_t)stream));
+    return DEEDS_OK;
+}
+
+deeds_status deeds_jacobian_dev(deeds_ctx* ctx, const float* d_u, const float* d_v, const float* d_w, int m, int n,
+                                int o, int g, float* jstd, float* neg_frac, void* stream) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!d_u || !d_v || !d_w || m < 1 || n < 1 || o < 1 || g < 1) return fail(ctx, DEEDS_ERR_INVALID, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    deeds_status st = DEEDS_OK;
+    double* acc = dbuf<double>(ctx, "jac", 3, &st);
+    if (st) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    CK(launch_jacobian(d_u, d_v, d_w, m, n, o, g, acc, s));
+    double h[3];
+    CK(cudaMemcpyAsync(h, acc, sizeof(h), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const double cnt = (double)m * n * o;
+    const double mean = h[0] / cnt;
+    const double var = cnt > 1 ? (h[1] - cnt * mean * mean) / (cnt - 1) : 0.0;
+    if (jstd) *jstd = (float)std::sqrt(var > 0 ? var : 0.0);
+    if (neg_frac) *neg_frac = (float)(h[2] / cnt);
+    return DEEDS_OK;
+}
+
+deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, int m, int n, int o,
+                                const float X[16], const deeds_params* P, float* d_flow_out, float* d_warped_out,
+                                void* stream) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!d_fixed || !d_moving || !X || !d_flow_out) return fail(ctx, DEEDS_ERR_INVALID, "null pointer");
+    deeds_status st = check_params(ctx, P, m, n, o);
+    if (st) return st;
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = (cudaStream_t)stream;
+    const int L = P->levels;
+    const size_t sz = (size_t)m * n * o;
+    float thr[5];
+    mind_thresholds(thr);
+
+    // ---- buffers
+    float* fix = dbuf<float>(ctx, "fix", sz, &st);
+    float* mov = dbuf<float>(ctx, "mov", sz, &st);
+    float* warp0 = dbuf<float>(ctx, "warp0", sz, &st);
+    float* warped = dbuf<float>(ctx, "warped", sz, &st);
+    uint64_t* c_fix = dbuf<uint64_t>(ctx, "c_fix", sz, &st);
+    uint64_t* c_mov = dbuf<uint64_t>(ctx, "c_mov", sz, &st);
+    uint64_t* c_warp = dbuf<uint64_t>(ctx, "c_warp", sz, &st);
+    float* mind_scr = dbuf<float>(ctx, "mind", 6 * sz, &st);
+    int* d_err = dbuf<int>(ctx, "err", 2, &st);
+    size_t max_cost = 0, max_sz1 = 0;
+    std::vector<int> m1s(L), n1s(L), o1s(L);
+    for (int l = 0; l < L; l++) {
+        const int g = P->grid[l], len = 2 * P->radius[l] + 1;
+        m1s[l] = m / g; n1s[l] = n / g; o1s[l] = o / g;
+        const size_t sz1 = (size_t)m1s[l] * n1s[l] * o1s[l];
+        max_sz1 = std::max(max_sz1, sz1);
+        max_cost = std::max(max_cost, sz1 * len * len * len);
+    }
+    {
+        const size_t s0 = (size_t)(m / P->grid[0]) * (n / P->grid[0]) * (o / P->grid[0]);
+        max_sz1 = std::max(max_sz1, s0);
+    }
+    // per-direction BP buffers at the largest level's size, so nothing is
+    // reallocated (cudaFree) while kernels of this pair are in flight
+    for (const char* tag : {"f", "b"}) {
+        dbuf<uint32_t>(ctx, std::string("tree_") + tag, pack_layout((int)max_sz1).total, &st);
+        dbuf<int>(ctx, std::string("flags_") + tag, max_sz1 + 1, &st, true);
+        dbuf<int>(ctx, std::string("work_") + tag, 1, &st);
+        dbuf<int>(ctx, std::string("sel_") + tag, max_sz1, &st);
+    }
+    float* cost = dbuf<float>(ctx, "cost", max_cost, &st);
+    short* allinds = dbuf<short>(ctx, "allinds", max_cost, &st);
+    float* grid = dbuf<float>(ctx, "grid", 21 * max_sz1, &st);  // fields on the control grids
+    float* ku = dbuf<float>(ctx, "keep_u", sz, &st);
+    float* kv = dbuf<float>(ctx, "keep_v", sz, &st);
+    float* kw = dbuf<float>(ctx, "keep_w", sz, &st);
+    float* cons_scr = dbuf<float>(ctx, "consistent", 12 * max_sz1, &st);
+    if (st) return st;
+    float* prev[6];   // u1 v1 w1 u1i v1i w1i on the previous grid
+    float* cur0[3];   // u0 v0 w0 on the current grid
+    float* nxt[6];    // new fields on the current grid
+    for (int i = 0; i < 6; i++) prev[i] = grid + i * max_sz1;
+    for (int i = 0; i < 3; i++) cur0[i] = grid + (6 + i) * max_sz1;
+    for (int i = 0; i < 6; i++) nxt[i] = grid + (9 + i) * max_sz1;
+    float* keep = grid + 15 * max_sz1;  // unused slack
+    (void)keep;
+
+    // ---- inputs, affine-only warp of the moving image
+    CK(cudaMemsetAsync(d_err, 0, 2 * sizeof(int), s));
+    CK(launch_shift(d_fixed, fix, (int64_t)sz, P->intensity_shift, s));
+    CK(launch_shift(d_moving, mov, (int64_t)sz, P->intensity_shift, s));
+    FieldRef zero{0, nullptr, nullptr, nullptr, 0, 0, 0};
+    CK(launch_warp_affine(mov, X, zero, m, n, o, warp0, nullptr, nullptr, nullptr, s));
+
+    // ---- MST inputs on the side stream, then host trees on worker threads
+    CK(cudaEventRecord(ctx->ev_a, s));
+    CK(cudaStreamWaitEvent(ctx->side, ctx->ev_a, 0));
+    float* h_fix = hbuf<float>(ctx, "h_fix", sz, &st);
+    float* h_w0 = hbuf<float>(ctx, "h_w0", sz, &st);
+    std::vector<float*> h_sad(2 * L);
+    std::vector<PackedTree> pts(2 * L);
+    std::vector<uint32_t*> h_tree(2 * L);
+    for (int l = 0; l < L; l++) {
+        const size_t sz1 = (size_t)m1s[l] * n1s[l] * o1s[l];
+        for (int d = 0; d < 2; d++) {
+            const int t = 2 * l + d;
+            h_sad[t] = hbuf<float>(ctx, "h_sad" + std::to_string(t), 6 * sz1, &st);
+            pts[t] = pack_layout((int)sz1);
+            h_tree[t] = hbuf<uint32_t>(ctx, "h_tree" + std::to_string(t), pts[t].total, &st);
+            float* d_sad = dbuf<float>(ctx, "sad" + std::to_string(t), 6 * sz1, &st);
+            if (st) return st;
+            {
+                StageScope sc(ctx, DEEDS_STAGE_MST, ctx->side);
+                CK(launch_edge_sad(d == 0 ? fix : warp0, m, n, o, P->grid[l], d_sad, ctx->side));
+            }
+            CK(cudaMemcpyAsync(h_sad[t], d_sad, 6 * sz1 * sizeof(float), cudaMemcpyDeviceToHost, ctx->side));
+        }
+    }
+    if (st) return st;
+    CK(cudaMemcpyAsync(h_fix, fix, sz * sizeof(float), cudaMemcpyDeviceToHost, ctx->side));
+    CK(cudaMemcpyAsync(h_w0, warp0, sz * sizeof(float), cudaMemcpyDeviceToHost, ctx->side));
+    CK(cudaEventRecord(ctx->ev_b, ctx->side));
+    std::vector<std::promise<void>> ready(2 * L);
+    std::vector<std::shared_future<void>> ready_f(2 * L);
+    for (int t = 0; t < 2 * L; t++) ready_f[t] = ready[t].get_future().share();
+    cudaEvent_t ev_inputs = ctx->ev_b;
+    const int dev = ctx->device;
+    std::thread builder([&, ev_inputs, dev]() {
+        cudaSetDevice(dev);
+        cudaEventSynchronize(ev_inputs);
+        float mean_f, sd_f, mean_w, sd_w;
+        std::thread tw([&]() { image_stats(h_w0, sz, &mean_w, &sd_w); });
+        image_stats(h_fix, sz, &mean_f, &sd_f);
+        tw.join();
+        // finest trees are the slowest: start the workers in reverse level order
+        std::vector<std::thread> workers;
+        for (int t = 2 * L - 1; t >= 0; t--) {
+            workers.emplace_back([&, t]() {
+                const int l = t / 2, d = t % 2;
+                try {
+                    build_tree(h_sad[t], d == 0 ? sd_f : sd_w, m1s[l], n1s[l], o1s[l], P->grid[l], h_tree[t], pts[t]);
+                    ready[t].set_value();
+                } catch (...) {
+                    ready[t].set_exception(std::current_exception());
+                }
+            });
+        }
+        for (auto& w : workers) w.join();
+    });
+    struct Joiner {
+        std::thread& t;
+        ~Joiner() { if (t.joinable()) t.join(); }
+    } joiner{builder};
+
+    // ---- level loop (src/deedsBCV0.cpp:222-330)
+    int m2 = m1s[0], n2 = n1s[0], o2 = o1s[0];
+    CK(cudaMemsetAsync(grid, 0, 6 * max_sz1 * sizeof(float), s));
+    int prev_step = -1;
+    for (int l = 0; l < L; l++) {
+        const int g = P->grid[l], hw = P->radius[l], q = P->quant[l];
+        const int qs = mind_step(q);
+        const int m1 = m1s[l], n1 = n1s[l], o1 = o1s[l];
+        const int len = 2 * hw + 1;
+        if (P->verbose)
+            printf("Level %d grid=%d with sizes: %dx%dx%d hw=%d quant=%d\n", l, g, m1, n1, o1, hw, q);
+        if (l == 0 || qs != prev_step) {
+            StageScope sc(ctx, DEEDS_STAGE_MIND, s);
+            CK(launch_mind_ssc(warp0, m, n, o, qs, thr, mind_scr, c_mov, s));
+            CK(launch_mind_ssc(fix, m, n, o, qs, thr, mind_scr, c_fix, s));
+        }
+        prev_step = qs;
+        int sy, sx, szs;
+        float alpha1;
+        data_cost_params(g, q, P->alpha, &sy, &sx, &szs, &alpha1);
+        for (int d = 0; d < 2; d++) {
+            float** pv = prev + 3 * d;
+            {
+                StageScope sc(ctx, DEEDS_STAGE_TRANSFORM, s);
+                CK(launch_upsample(pv[0], pv[1], pv[2], m2, n2, o2, cur0[0], cur0[1], cur0[2], m1, n1, o1, s));
+                FieldRef f{2, cur0[0], cur0[1], cur0[2], m1, n1, o1};
+                if (d == 0) CK(launch_warp_affine(mov, X, f, m, n, o, warped, nullptr, nullptr, nullptr, s));
+                else CK(launch_warp_image(fix, f, m, n, o, warped, s));
+            }
+            {
+                StageScope sc(ctx, DEEDS_STAGE_MIND, s);
+                CK(launch_mind_ssc(warped, m, n, o, qs, thr, mind_scr, c_warp, s));
+            }
+            {
+                StageScope sc(ctx, DEEDS_STAGE_DATACOST, s);
+                CK(launch_data_cost(d == 0 ? c_fix : c_mov, c_warp, m, n, o, g, hw, q, sy, sx, szs, alpha1, cost, s));
+            }
+            const int t = 2 * l + d;
+            {
+                const auto w0 = std::chrono::steady_clock::now();
+                try {
+                    ready_f[t].get();
+                } catch (const std::exception& ex) {
+                    return fail(ctx, DEEDS_ERR_INTERNAL, "MST construction failed: %s", ex.what());
+                }
+                if (ctx->prof)
+                    ctx->stage_ms[DEEDS_STAGE_TREE_WAIT] +=
+                        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
+            }
+            st = run_tree_bp(ctx, d == 0 ? "f" : "b", pts[t], h_tree[t], cost, allinds, len, q, cur0[0], cur0[1],
+                             cur0[2], nxt[3 * d], nxt[3 * d + 1], nxt[3 * d + 2], d_err + d, s);
+            if (st) return st;
+        }
+        {
+            StageScope sc(ctx, DEEDS_STAGE_CONSISTENT, s);
+            CK(launch_consistent(nxt[0], nxt[1], nxt[2], nxt[3], nxt[4], nxt[5], m1, n1, o1, g, cons_scr, s));
+        }
+        if (P->verbose) {
+            float js = 0, neg = 0;
+            deeds_status js_st = deeds_jacobian_dev(ctx, nxt[0], nxt[1], nxt[2], m1, n1, o1, g, &js, &neg, s);
+            if (js_st == DEEDS_OK) printf("std(J)=%.2f (J<0)=%.2fe-7\n", std::round(js * 100) / 100.0, std::round(neg * 1e7) / 100.0);
+        }
+        for (int i = 0; i < 6; i++) std::swap(prev[i], nxt[i]);
+        m2 = m1; n2 = n1; o2 = o1;
+    }
+
+    // ---- outputs (src/deedsBCV0.cpp:339-356)
+    const size_t sz1 = (size_t)m2 * n2 * o2;
+    for (int c = 0; c < 3; c++)
+        CK(cudaMemcpyAsync(d_flow_out + c * sz1, prev[c], sz1 * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    FieldRef f{2, prev[0], prev[1], prev[2], m2, n2, o2};
+    CK(launch_warp_affine(mov, X, f, m, n, o, warped, ku, kv, kw, s));
+    if (d_warped_out) CK(launch_shift(warped, d_warped_out, (int64_t)sz, -P->intensity_shift, s));
+    int herr[2] = {0, 0};
+    CK(cudaMemcpyAsync(herr, d_err, sizeof(herr), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (builder.joinable()) builder.join();
+    if (ctx->prof) collect_marks(ctx);
+    if (herr[0] || herr[1]) return fail(ctx, DEEDS_ERR_TIMEOUT, "belief propagation: a bounded wait expired");
+    ctx->have_field = true;
+    ctx->fm = m; ctx->fn = n; ctx->fo = o;
+    std::memcpy(ctx->fX, X, sizeof(ctx->fX));
+    return DEEDS_OK;
+}
+
+deeds_status deeds_register(deeds_ctx* ctx, const float* fixed, const float* moving, int m, int n, int o,
+                            const float X[16], const deeds_params* params, float* flow_out, float* warped_out) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!fixed || !moving || !X || !flow_out) return fail(ctx, DEEDS_ERR_INVALID, "null pointer");
+    deeds_status st = check_params(ctx, params, m, n, o);
+    if (st) return st;
+    CK(cudaSetDevice(ctx->device));
+    const size_t sz = (size_t)m * n * o;
+    const int gl = params->grid[params->levels - 1];
+    const size_t sz1 = (size_t)(m / gl) * (n / gl) * (o / gl);
+    float* d_f = dbuf<float>(ctx, "in_fixed", sz, &st);
+    float* d_m = dbuf<float>(ctx, "in_moving", sz, &st);
+    float* d_flow = dbuf<float>(ctx, "out_flow", 3 * sz1, &st);
+    float* d_w = warped_out ? dbuf<float>(ctx, "out_warped", sz, &st) : nullptr;
+    if (st) return st;
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(d_f, fixed, sz * sizeof(float), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_m, moving, sz * sizeof(float), cudaMemcpyHostToDevice, s));
+    st = deeds_register_dev(ctx, d_f, d_m, m, n, o, X, params, d_flow, d_w, s);
+    if (st) return st;
+    CK(cudaMemcpyAsync(flow_out, d_flow, 3 * sz1 * sizeof(float), cudaMemcpyDeviceToHost, s));
+    if (warped_out) CK(cudaMemcpyAsync(warped_out, d_w, sz * sizeof(float), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return DEEDS_OK;
+}
+
+deeds_status deeds_warp_segmentation(deeds_ctx* ctx, const int16_t* seg, int16_t* seg_out) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!seg || !seg_out) return fail(ctx, DEEDS_ERR_INVALID, "null pointer");
+    if (!ctx->have_field) return fail(ctx, DEEDS_ERR_INVALID, "no registration has been run on this context");
+    CK(cudaSetDevice(ctx->device));
+    const size_t sz = (size_t)ctx->fm * ctx->fn * ctx->fo;
+    deeds_status st = DEEDS_OK;
+    short* d_in = dbuf<short>(ctx, "seg_in", sz, &st);
+    short* d_out = dbuf<short>(ctx, "seg_out", sz, &st);
+    if (st) return st;
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(d_in, seg, sz * sizeof(short), cudaMemcpyHostToDevice, s));
+    FieldRef f{1, static_cast<float*>(ctx->dev["keep_u"].p), static_cast<float*>(ctx->dev["keep_v"].p),
+               static_cast<float*>(ctx->dev["keep_w"].p), 0, 0, 0};
+    CK(launch_warp_seg(d_in, ctx->fX, f, ctx->fm, ctx->fn, ctx->fo, d_out, s));
+    CK(cudaMemcpyAsync(seg_out, d_out, sz * sizeof(short), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return DEEDS_OK;
+}
+
+deeds_status deeds_apply_flow(deeds_ctx* ctx, const float* flow, size_t flow_len, int g, const float X[16],
+                              const void* in, int dtype, int m, int n, int o, void* out) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!flow || !X || !in || !out || m < 1 || n < 1 || o < 1 || (dtype != 0 && dtype != 1))
+        return fail(ctx, DEEDS_ERR_INVALID, "bad arguments");
+    if (flow_len < 3 || flow_len % 3) return fail(ctx, DEEDS_ERR_INVALID, "flow length %zu is not 3*sz1", flow_len);
+    const size_t sz = (size_t)m * n * o;
+    const size_t sz3 = flow_len / 3;
+    if (g <= 0) {  // grid step from the file size (src/applyBCV.cpp:163-164)
+        const float ratio = (float)sz / (float)sz3;
+        g = (int)std::round(std::pow((double)ratio, 0.3333333));
+    }
+    if (g < 1) return fail(ctx, DEEDS_ERR_INVALID, "inferred grid step %d", g);
+    const int m1 = m / g, n1 = n / g, o1 = o / g;
+    if ((size_t)m1 * n1 * o1 != sz3 || m1 < 1 || n1 < 1 || o1 < 1)
+        return fail(ctx, DEEDS_ERR_INVALID, "flow of %zu nodes does not match grid step %d on %dx%dx%d", sz3, g, m, n, o);
+    CK(cudaSetDevice(ctx->device));
+    deeds_status st = DEEDS_OK;
+    float* d_flow = dbuf<float>(ctx, "apply_flow", flow_len, &st);
+    const size_t esz = dtype == 0 ? sizeof(short) : sizeof(float);
+    void* d_in = dbuf<char>(ctx, "apply_in", sz * esz, &st);
+    void* d_out = dbuf<char>(ctx, "apply_out", sz * esz, &st);
+    if (st) return st;
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(d_flow, flow, flow_len * sizeof(float), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_in, in, sz * esz, cudaMemcpyHostToDevice, s));
+    FieldRef f{2, d_flow, d_flow + sz3, d_flow + 2 * sz3, m1, n1, o1};
+    if (dtype == 0)
+        CK(launch_warp_seg(static_cast<short*>(d_in), X, f, m, n, o, static_cast<short*>(d_out), s));
+    else
+        CK(launch_warp_affine(static_cast<float*>(d_in), X, f, m, n, o, static_cast<float*>(d_out), nullptr, nullptr,
+                              nullptr, s));
+    CK(cudaMemcpyAsync(out, d_out, sz * esz, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return DEEDS_OK;
+}
+
+deeds_status deeds_set_profiling(deeds_ctx* ctx, int on) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    ctx->prof = on != 0;
+    return DEEDS_OK;
+}
+
+deeds_status deeds_stage_times(deeds_ctx* ctx, float* ms, long long* launches) {
+    if (!ctx || !ms) return fail(ctx, DEEDS_ERR_INVALID, "bad arguments");
+    for (int i = 0; i < DEEDS_NUM_STAGES; i++) {
+        ms[i] = (float)ctx->stage_ms[i];
+        if (launches) launches[i] = ctx->stage_launches[i];
+    }
+    return DEEDS_OK;
+}
+
+deeds_status deeds_reset_stage_times(deeds_ctx* ctx) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    for (int i = 0; i < DEEDS_NUM_STAGES; i++) { ctx->stage_ms[i] = 0; ctx->stage_launches[i] = 0; }
+    return DEEDS_OK;
+}
+
+long long deeds_kernel_launches(void) { return deeds::g_kernel_launches.load(); }
+
+deeds_status deeds_measure_popc_rate(deeds_ctx* ctx, double* rate) {
+    if (!ctx || !rate) return fail(ctx, DEEDS_ERR_INVALID, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    deeds_status st = DEEDS_OK;
+    unsigned long long* sink = dbuf<unsigned long long>(ctx, "popc_sink", 1, &st);
+    if (st) return st;
+    const int threads = 256, blocks = ctx->sm_count * 8, iters = 1 << 14;
+    cudaStream_t s = ctx->stream;
+    CK(launch_popc_probe(blocks, threads, 256, sink, s));  // warm-up
+    cudaEvent_t a = pool_event(ctx), b = pool_event(ctx);
+    CK(cudaEventRecord(a, s));
+    CK(launch_popc_probe(blocks, threads, iters, sink, s));
+    CK(cudaEventRecord(b, s));
+    CK(cudaEventSynchronize(b));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, a, b));
+    ctx->ev_used = 0;
+    *rate = (double)blocks * threads * iters * 8.0 / (ms * 1e-3);
+    return DEEDS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,203 @@
+/*
+ * deeds_gpu.h — C ABI of the GB300 (sm_103a) implementation of the deeds dense
+ * discrete registration hot path (libdeeds_gpu.so).
+ *
+ * The reference (mattiaspaul/deedsBCV) has no library API: its stages are
+ * header-inlined functions that take raw pointers and read process globals
+ * (image_m/n/o, RAND_SAMPLES, SSD0/1; src/deedsBCV0.cpp:24-28).  Each entry point
+ * below replaces one of those functions (cited per declaration) with explicit
+ * dimensions, no globals, caller-owned buffers and an int status.
+ *
+ * Conventions
+ *  - Volumes are m x n x o with i (size m, "y") fastest: index i + j*m + k*m*n
+ *    (src/MINDSSCbox.h:84).  Displacements: u = x (dim 2), v = y (dim 1),
+ *    w = z (dim 3), in voxels (src/deedsBCV0.cpp:193-194).
+ *  - A control grid of spacing g has m1 = m/g, n1 = n/g, o1 = o/g nodes.
+ *  - The affine matrix X is 16 floats, rows y, x, z at X[0..3], X[4..7],
+ *    X[8..11] (src/dataCostD.h:281-283), as read from a linearBCV matrix file
+ *    (src/deedsBCV0.cpp:159-165).
+ *  - Functions named *_dev take device pointers and run on `stream` (a
+ *    cudaStream_t passed as void*; NULL = the legacy default stream).  They are
+ *    asynchronous unless stated otherwise.  All other pointers are host memory.
+ *  - Every function returns DEEDS_OK (0) or an error code; deeds_last_error()
+ *    gives the message.  No function calls exit().
+ *  - A context holds the device scratch memory and is not thread-safe: use one
+ *    context per host thread.
+ */
+#ifndef DEEDS_GPU_H
+#define DEEDS_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int deeds_status;
+#define DEEDS_OK 0
+#define DEEDS_ERR_INVALID 1   /* bad argument (dims, level parameters, null pointer) */
+#define DEEDS_ERR_CUDA 2      /* a CUDA runtime call failed */
+#define DEEDS_ERR_NOMEM 3     /* device or host allocation failed */
+#define DEEDS_ERR_TIMEOUT 4   /* a bounded device-side wait gave up (kernel returned early) */
+#define DEEDS_ERR_INTERNAL 5
+
+#define DEEDS_MAX_LEVELS 10
+
+typedef struct deeds_ctx deeds_ctx;
+
+/* Registration parameters: the -a/-l/-G/-L/-Q flags of deedsBCV
+ * (src/parseArguments.h:12-174, defaults src/deedsBCV0.cpp:76-79). */
+typedef struct deeds_params {
+    int levels;                      /* number of levels (<= DEEDS_MAX_LEVELS) */
+    int grid[DEEDS_MAX_LEVELS];      /* -G grid spacing per level */
+    int radius[DEEDS_MAX_LEVELS];    /* -L search radius (label half-width) per level */
+    int quant[DEEDS_MAX_LEVELS];     /* -Q label quantisation per level */
+    float alpha;                     /* -a regularisation weight (default 1.6) */
+    float intensity_shift;           /* added to both images before registering (1024 for CT, src/deedsBCV0.cpp:139-144) */
+    int verbose;                     /* print per-level progress like the reference */
+} deeds_params;
+
+/* Fill the reference defaults: 5 levels, G 8x7x6x5x4, L 8x7x6x5x4, Q 5x4x3x2x1, alpha 1.6, shift 1024. */
+void deeds_default_params(deeds_params* p);
+
+/* Create / destroy a context on CUDA device `device`. */
+deeds_status deeds_create(deeds_ctx** ctx, int device);
+void deeds_destroy(deeds_ctx* ctx);
+/* Message of the last error on this context (or of the last failed deeds_create when ctx is NULL). */
+const char* deeds_last_error(const deeds_ctx* ctx);
+/* Library version string. */
+const char* deeds_version(void);
+
+/* ---------------------------------------------------------------------------
+ * Whole registration (replaces main()'s level loop and output stage,
+ * src/deedsBCV0.cpp:183-356).
+ *
+ * fixed, moving: host float volumes (m*n*o) as read from file (HU for CT);
+ * params->intensity_shift is added to both.  flow_out: host, 3*sz1 floats
+ * [u|v|w] on the last level's grid, exactly the *_displacements.dat payload
+ * (src/deedsBCV0.cpp:341-349).  warped_out (nullable): the moving image warped by
+ * the final field, with the shift removed again (src/deedsBCV0.cpp:350-356).
+ * Synchronous.  The full-resolution field of the last call stays on the device
+ * for deeds_warp_segmentation().
+ */
+deeds_status deeds_register(deeds_ctx* ctx, const float* fixed, const float* moving, int m, int n, int o,
+                            const float X[16], const deeds_params* params, float* flow_out, float* warped_out);
+
+/* Same with device-resident inputs/outputs; d_fixed/d_moving are not modified.
+ * Host-side work (Prim's MST, schedules) still runs inside the call; returns
+ * after the result is on the device. */
+deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, int m, int n, int o,
+                                const float X[16], const deeds_params* params, float* d_flow_out,
+                                float* d_warped_out, void* stream);
+
+/* Warp a label volume with the last deeds_register() result: nearest-neighbour,
+ * clamp-to-edge (the -S output, src/deedsBCV0.cpp:361-379 via warpAffineS,
+ * src/dataCostD.h:241-266).  Host buffers; synchronous. */
+deeds_status deeds_warp_segmentation(deeds_ctx* ctx, const int16_t* seg, int16_t* seg_out);
+
+/* applyBCV / applyBCVfloat: upsample a grid flow (3*sz1, grid step g inferred from
+ * its length as src/applyBCV.cpp:161-164 does, or given if g > 0) to full
+ * resolution and warp `in`.  dtype 0: int16 labels, nearest (src/applyBCV.cpp:186-198);
+ * dtype 1: float image, trilinear (src/applyBCVfloat.cpp:190-198).  Host buffers. */
+deeds_status deeds_apply_flow(deeds_ctx* ctx, const float* flow, size_t flow_len, int g, const float X[16],
+                              const void* in, int dtype, int m, int n, int o, void* out);
+
+/* ---------------------------------------------------------------------------
+ * Stage entry points (device pointers, asynchronous on `stream`).
+ */
+
+/* descriptor(): MIND-SSC with patch radius qs, quantised to one 64-bit code per
+ * voxel (src/MINDSSCbox.h:127-232).  Bit-exact with the reference. */
+deeds_status deeds_mind_ssc_dev(deeds_ctx* ctx, const float* d_im, int m, int n, int o, int qs,
+                                uint64_t* d_codes, void* stream);
+
+/* dataCostCL(): Hamming cost volume cost[node*len3 + label], len3=(2hw+1)^3,
+ * label = ly + lx*len + lz*len^2 (src/dataCostD.h:108-210).  Bit-exact. */
+deeds_status deeds_data_cost_dev(deeds_ctx* ctx, const uint64_t* d_fixed_codes, const uint64_t* d_moving_codes,
+                                 int m, int n, int o, int g, int hw, int q, float alpha, float* d_cost,
+                                 void* stream);
+
+/* The edge-cost half of primsGraph(): per-node block SADs to the 6 neighbours,
+ * d_sad[nb*sz1 + node], nb order -x,+x,-y,+y,-z,+z (src/primsMST.h:75-100). */
+deeds_status deeds_mst_edges_dev(deeds_ctx* ctx, const float* d_im, int m, int n, int o, int g, float* d_sad,
+                                 void* stream);
+
+/* The tree half of primsGraph() (host): image statistics (src/primsMST.h:101-110)
+ * and Prim's algorithm over the SAD edge weights, giving the breadth-level
+ * ordering, parents and per-child edge weights (src/primsMST.h:112-211). */
+deeds_status deeds_image_stats(const float* im, size_t count, float* mean, float* stddev);
+deeds_status deeds_prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int g, int* ordered,
+                                  int* parents, float* edgemst);
+
+/* regularisationCL(): exact min-sum belief propagation on the MST with 3-D
+ * quadratic distance-transform messages (src/regularisation.h:6-303).
+ * d_cost (sz1*len3) is overwritten with the upward-pass state (each non-root
+ * row = that node's message, root row = its total), as the reference leaves it.
+ * ordered/parents/edgemst are host arrays (from deeds_prims_from_sad).
+ * d_allinds (nullable, sz1*len3 int16) receives the argmin tables. Synchronous. */
+deeds_status deeds_tree_bp_dev(deeds_ctx* ctx, float* d_cost, const float* d_u0, const float* d_v0,
+                               const float* d_w0, int m1, int n1, int o1, int hw, int q, const int* ordered,
+                               const int* parents, const float* edgemst, float* d_u1, float* d_v1, float* d_w1,
+                               int16_t* d_allinds, void* stream);
+
+/* upsampleDeformationsCL(): trilinear resample of a (m2,n2,o2) field to (m,n,o)
+ * (src/transformations.h:245-279). */
+deeds_status deeds_upsample_dev(const float* d_u0, const float* d_v0, const float* d_w0, int m2, int n2, int o2,
+                                float* d_u, float* d_v, float* d_w, int m, int n, int o, void* stream);
+
+/* warpAffine(): affine + dense field, trilinear, clamp-to-edge
+ * (src/dataCostD.h:267-298). d_u/d_v/d_w may be NULL for a zero field. */
+deeds_status deeds_warp_affine_dev(const float* d_in, const float X[16], const float* d_u, const float* d_v,
+                                   const float* d_w, int m, int n, int o, float* d_out, void* stream);
+
+/* warpImageCL(): warp by a field relative to the voxel position (src/dataCostD.h:213-239). */
+deeds_status deeds_warp_image_dev(const float* d_in, const float* d_u, const float* d_v, const float* d_w, int m,
+                                  int n, int o, float* d_out, void* stream);
+
+/* warpAffineS(): nearest-neighbour label warp (src/dataCostD.h:241-266). */
+deeds_status deeds_warp_seg_dev(const int16_t* d_in, const float X[16], const float* d_u, const float* d_v,
+                                const float* d_w, int m, int n, int o, int16_t* d_out, void* stream);
+
+/* consistentMappingCL(): 10 inverse-consistency iterations on both grid fields,
+ * in place (src/transformations.h:189-242). */
+deeds_status deeds_consistent_dev(deeds_ctx* ctx, float* d_u, float* d_v, float* d_w, float* d_u2, float* d_v2,
+                                  float* d_w2, int m, int n, int o, int g, void* stream);
+
+/* jacobian(): std of the Jacobian determinant and fraction of J<0 of a grid
+ * field (src/transformations.h:84-185; a diagnostic, parallel reduction, not
+ * bit-exact).  Synchronous. */
+deeds_status deeds_jacobian_dev(deeds_ctx* ctx, const float* d_u, const float* d_v, const float* d_w, int m, int n,
+                                int o, int g, float* jstd, float* neg_frac, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Tracing and accounting (the reference times each stage with gettimeofday and
+ * prints per-level seconds, src/deedsBCV0.cpp:228-308; here CUDA events).
+ */
+#define DEEDS_STAGE_MIND 0       /* MIND-SSC descriptors */
+#define DEEDS_STAGE_DATACOST 1   /* Hamming cost volumes */
+#define DEEDS_STAGE_MST 2        /* MST edge SADs (GPU side of primsGraph) */
+#define DEEDS_STAGE_BP_UP 3      /* upward belief propagation */
+#define DEEDS_STAGE_BP_DOWN 4    /* root argmin + downward pass */
+#define DEEDS_STAGE_TRANSFORM 5  /* upsampling and warps */
+#define DEEDS_STAGE_CONSISTENT 6 /* inverse-consistent mapping */
+#define DEEDS_STAGE_TREE_WAIT 7  /* host time spent waiting for Prim trees */
+#define DEEDS_NUM_STAGES 8
+
+/* Enable/disable per-stage CUDA-event timing in deeds_register*(). */
+deeds_status deeds_set_profiling(deeds_ctx* ctx, int on);
+/* Milliseconds per stage accumulated since the last reset (DEEDS_NUM_STAGES
+ * floats); `launches` (nullable) receives per-stage kernel launch counts. */
+deeds_status deeds_stage_times(deeds_ctx* ctx, float* ms, long long* launches);
+deeds_status deeds_reset_stage_times(deeds_ctx* ctx);
+/* Number of kernels this library has launched in the process so far. */
+long long deeds_kernel_launches(void);
+/* Measure this GPU's 64-bit population-count throughput (XOR + 2 POPC + add per
+ * element, the cost-volume inner loop) with a register-only probe kernel;
+ * returns popc64 operations per second. Synchronous, ~0.2 s. */
+deeds_status deeds_measure_popc_rate(deeds_ctx* ctx, double* popc64_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DEEDS_GPU_H */

@@ -1,0 +1,143 @@
+"""CPU-side checks of the product: the C ABI library loads and exports every
+declared symbol, its host-side MST code matches the reference, and the
+command-line / file-format boundary behaves like the reference's."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import pyoracle as orc
+from deedsbcv_gb300 import _lib, nifti, phantom
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+BUILD = os.path.join(ROOT, "deedsbcv_gb300", "_build")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(_lib.LIB_PATH):
+        from deedsbcv_gb300 import build
+        build.build()
+    return _lib.load()
+
+
+def header_symbols():
+    text = open(os.path.join(ROOT, "include", "deeds_gpu.h")).read()
+    return sorted(set(re.findall(r"\b(deeds_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    declared = header_symbols()
+    assert len(declared) >= 20
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert set(declared) == set(_lib.EXPORTS)
+
+
+def test_create_without_gpu_reports_error(lib):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = C.c_void_p()
+    st = lib.deeds_create(C.byref(h), 0)
+    assert st == 2  # DEEDS_ERR_CUDA, no crash, no exit()
+    assert lib.deeds_last_error(None)
+    assert lib.deeds_version().startswith(b"deeds")
+
+
+@pytest.mark.parametrize("gs", [4, 5, 6, 8])
+def test_host_prims_matches_reference(lib, golden, gs):
+    p = golden("prims")
+    m, n, o = (int(x) for x in p["dims"])
+    sad = orc.edge_sad(p["image"], m, n, o, gs)
+    mean = np.zeros(1, np.float32)
+    sd = np.zeros(1, np.float32)
+    im = np.ascontiguousarray(p["image"], np.float32)
+    ptr = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    assert lib.deeds_image_stats(ptr(im), im.size, ptr(mean), ptr(sd)) == 0
+    assert (float(mean[0]), float(sd[0])) == orc.image_stats(im)
+    m1, n1, o1 = m // gs, n // gs, o // gs
+    ordered = np.zeros(m1 * n1 * o1, np.int32)
+    parents = np.zeros_like(ordered)
+    edgemst = np.zeros(m1 * n1 * o1, np.float32)
+    assert lib.deeds_prims_from_sad(ptr(sad), C.c_float(sd[0]), m1, n1, o1, gs, ptr(ordered), ptr(parents),
+                                    ptr(edgemst)) == 0
+    assert np.array_equal(ordered, p[f"ordered_{gs}"])
+    assert np.array_equal(parents, p[f"parents_{gs}"])
+    assert edgemst.tobytes() == p[f"edgemst_{gs}"].tobytes()
+
+
+def test_nifti_roundtrip(tmp_path):
+    vol = np.asfortranarray(np.random.default_rng(0).normal(size=(7, 5, 6)).astype(np.float32))
+    for name in ("a.nii.gz", "a.nii"):
+        nifti.write(tmp_path / name, vol)
+        back, hdr = nifti.read(tmp_path / name)
+        assert back.shape == vol.shape and np.array_equal(back, vol)
+        assert len(hdr) == 352
+    seg = np.asfortranarray(np.arange(7 * 5 * 6, dtype=np.int16).reshape(7, 5, 6, order="F"))
+    nifti.write(tmp_path / "s.nii.gz", seg)
+    back, _ = nifti.read(tmp_path / "s.nii.gz")
+    assert back.dtype == np.int16 and np.array_equal(back, seg)
+
+
+def test_truncated_nifti_raises(tmp_path):
+    p = tmp_path / "t.nii.gz"
+    nifti.write(p, np.zeros((4, 4, 4), np.float32))
+    import gzip
+    raw = gzip.open(p).read()[:400]
+    with gzip.open(p, "wb") as f:
+        f.write(raw)
+    with pytest.raises(ValueError):
+        nifti.read(p)
+
+
+@pytest.mark.parametrize("g", [4, 5, 6, 8])
+def test_grid_step_inferred_from_dat_size(g):
+    m, n, o = 192, 160, 256
+    sz1 = (m // g) * (n // g) * (o // g)
+    assert nifti.grid_step_from_dat(3 * sz1, m, n, o) == g
+
+
+def _cli(*args):
+    exe = os.path.join(BUILD, "deedsBCV")
+    if not os.path.exists(exe):
+        pytest.skip("CLI not built")
+    return subprocess.run([exe, *args], capture_output=True, text=True, timeout=60)
+
+
+@pytest.fixture()
+def pair_files(tmp_path):
+    pair = phantom.make_pair((24, 20, 28), seed=1, n_organs=4, max_disp=2.0)
+    f, m = tmp_path / "f.nii.gz", tmp_path / "m.nii.gz"
+    nifti.write(f, pair["fixed"])
+    nifti.write(m, pair["moving"])
+    return str(f), str(m), str(tmp_path / "out")
+
+
+@pytest.mark.parametrize("flags,expect", [
+    ([], "levels=5 G=8x7x6x5x4 L=8x7x6x5x4 Q=5x4x3x2x1 alpha=1.6"),
+    (["-G", "6x5x4", "-L", "5x4x3", "-Q", "3x2x1", "-a", "2"], "levels=3 G=6x5x4 L=5x4x3 Q=3x2x1 alpha=2"),
+    # -l is overridden once any of -G/-L/-Q is given (src/parseArguments.h:122-124)
+    (["-l", "3", "-L", "6x5"], "levels=5 G=8x7x6x5x4 L=6x5x6x5x4 Q=5x4x3x2x1"),
+    # levels beyond 5 take the built-in defaults (src/parseArguments.h:42-44)
+    (["-l", "6"], "levels=6 G=8x7x6x5x4x3 L=8x7x6x5x4x3 Q=5x4x3x2x1x1"),
+])
+def test_cli_parses_like_reference(pair_files, flags, expect):
+    f, m, out = pair_files
+    r = _cli("-F", f, "-M", m, "-O", out, *flags)
+    assert expect in r.stdout, r.stdout + r.stderr
+
+
+def test_cli_rejects_non_gz(tmp_path, pair_files):
+    f, m, out = pair_files
+    r = _cli("-F", f.replace(".nii.gz", ".nii"), "-M", m, "-O", out)
+    assert "images must have nii.gz format" in r.stdout
+
+
+def test_cli_mismatch_warning(pair_files):
+    f, m, out = pair_files
+    r = _cli("-F", f, "-M", m, "-O", out, "-G", "6x5x4", "-L", "5x4")
+    assert "#grid=3, #search=2" in r.stdout
