@@ -2,26 +2,35 @@
 // src/regularisation.h:6-303).
 //
 // Upward sweep (leaves to root).  The reference walks breadth levels from the
-// deepest up; per level it scales each child's row by its edge weight, runs the
-// separable quadratic min-convolution (messageDT) and then, serially in MST
-// ordering order, adds (message - min(message)) into the parent's row
-// (:190-238).  Here one work item is one PARENT: a persistent grid claims items
-// in deepest-first order with an atomic counter; an item first waits (bounded
-// spin) until every child that is itself a parent has been finished, then
-// processes its children in ordering order entirely in shared memory — scale,
-// y/x/z min-convolution passes with the reference's strict '<' (first minimiser
-// wins), block min, and the in-order accumulation into the parent's row — and
-// finally publishes its own row.  Because a parent only waits on items claimed
-// before it by CTAs that are already running, the schedule cannot deadlock at
-// any grid size.  Children's rows are left holding their messages, as the
-// reference leaves costall.
+// deepest up: per level it scales each node's row by its edge weight, runs the
+// separable quadratic min-convolution (messageDT, :6-113) and then, serially in
+// MST ordering order, adds (message - min(message)) into the parent's row
+// (:190-238).  The same arithmetic is scheduled here as a wait-free bottom-up
+// reduction: a persistent grid claims leaves (deepest first) from an atomic
+// counter; a CTA computes its node's message entirely in shared memory, stores
+// it with its minimum, and increments the parent's arrival counter.  The CTA
+// that completes a parent's set of children — the last arriver — builds the
+// parent's row from its data cost plus every child's (message - min) in MST
+// ordering order (the reference's rounding sequence) and continues upward with
+// the parent's own message.  No CTA ever waits for another, so there is no
+// spin loop and no deadlock at any grid size; the critical path is one
+// message per tree level.  Children's rows are left holding their messages and
+// the root row its total, as the reference leaves costall.
 //
-// Downward pass (root to leaves, :258-293): one CTA per tree picks the root's
-// first minimum and then resolves one breadth level per step from the argmin
-// tables (allinds).
+// The distance transform of a len^3 block is three axis passes; one thread owns
+// one line of len values, holds them and the 2*len parabola values in
+// registers and produces all len outputs of its line (len^2 candidates, fully
+// unrolled for the compile-time label width), keeping the reference's strict
+// '<' so the first minimiser wins.
 //
-// Roofline: dependency/latency bound; algorithmic traffic is one read and one
-// write of the cost volume plus the int16 argmin tables.
+// Downward pass (root to leaves, :258-293): one CTA per tree takes the root's
+// first minimum, then resolves one breadth level per step from the argmin
+// tables, keeping the previous level's labels in shared memory and prefetching
+// the argmin rows of the next levels into L2.
+//
+// Roofline: dependency bound (tree depth 265-987 per tree at 192x160x256).
+// Algorithmic traffic: one read + one write of the cost volume and one write of
+// the int16 argmin tables per tree.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -29,38 +38,41 @@ namespace deeds {
 
 namespace {
 
-constexpr int kBpThreads = 256;
-constexpr long long kSpinLimit = 1LL << 22;  // x ~256 ns sleep ~= 1 s before giving up
-
 __device__ __forceinline__ float ld_cg(const float* p) { return __ldcg(p); }
 
-// One axis pass of the min-convolution over a len^3 block held in shared memory.
-// For every output position, the minimum over source positions s along the axis
-// of in[base + s*stride] + zt[pos - s + len], first minimiser kept.
-// `idx_in` maps a source position to the label chain so far (nullptr for the
-// first pass, whose chain is the position itself).
-__device__ __forceinline__ void dt_pass(const float* in, float* out, const short* idx_in, short* idx_out,
-                                        const float* zt, int len, int axis) {
-    const int len2 = len * len, len3 = len2 * len;
-    const int stride = axis == 0 ? 1 : (axis == 1 ? len : len2);
-    for (int l = threadIdx.x; l < len3; l += blockDim.x) {
-        const int pos = axis == 0 ? l % len : (axis == 1 ? (l / len) % len : l / len2);
-        const int base = l - pos * stride;
-        float best = in[base] + zt[pos + len];
-        int bs = 0;
-        for (int s = 0; s < len; s++) {
-            const float c = in[base + s * stride] + zt[pos - s + len];
-            if (c < best) { best = c; bs = s; }
-        }
-        out[l] = best;
-        idx_out[l] = idx_in ? idx_in[base + bs * stride] : (short)(base + bs * stride);
-    }
+constexpr int bp_threads(int len) {
+    return ((len * len + 31) / 32) * 32 < 64 ? 64 : ((len * len + 31) / 32) * 32;
 }
 
-__device__ __forceinline__ void fill_parabola(float* zt, int len, float off) {
-    for (int t = threadIdx.x; t < 2 * len; t += blockDim.x) {
-        const float d = (float)(t - len) + off;
-        zt[t] = d * d;
+// One axis pass of the min-convolution: out[line, i] = min_s in[line, s] + (i - s + off)^2.
+template <int LEN, int AXIS>
+__device__ __forceinline__ void dt_lines(const float* in, float* out, const short* idx_in, short* idx_out,
+                                         float off) {
+    constexpr int LEN2 = LEN * LEN;
+    constexpr int STRIDE = AXIS == 0 ? 1 : (AXIS == 1 ? LEN : LEN2);
+    const int t = threadIdx.x;
+    if (t >= LEN2) return;
+    const int base = AXIS == 0 ? t * LEN : (AXIS == 1 ? (t % LEN) + (t / LEN) * LEN2 : t);
+    float v[LEN];
+#pragma unroll
+    for (int s = 0; s < LEN; s++) v[s] = in[base + s * STRIDE];
+    float z[2 * LEN];
+#pragma unroll
+    for (int u = 0; u < 2 * LEN; u++) {
+        const float d = (float)(u - LEN) + off;
+        z[u] = d * d;
+    }
+#pragma unroll
+    for (int i = 0; i < LEN; i++) {
+        float best = v[0] + z[i + LEN];
+        int bs = 0;
+#pragma unroll
+        for (int s = 1; s < LEN; s++) {
+            const float c = v[s] + z[i - s + LEN];
+            if (c < best) { best = c; bs = s; }
+        }
+        out[base + i * STRIDE] = best;
+        idx_out[base + i * STRIDE] = idx_in ? idx_in[base + bs * STRIDE] : (short)(base + bs * STRIDE);
     }
 }
 
@@ -76,101 +88,119 @@ __device__ float block_min(float v, float* red) {
         if (lane == 0) red[0] = v;
     }
     __syncthreads();
-    const float r = red[0];
-    return r;
+    return red[0];
 }
 
-__global__ void __launch_bounds__(kBpThreads) k_bp_up(BpTree t, float* __restrict__ cost, short* __restrict__ allinds,
-                                                      int* __restrict__ work, int* __restrict__ flags, int epoch,
-                                                      int* __restrict__ err) {
+template <int LEN>
+__global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __restrict__ cost,
+                                                           short* __restrict__ allinds, float* __restrict__ mins,
+                                                           int* __restrict__ arrived, int* __restrict__ work) {
+    constexpr int LEN3 = LEN * LEN * LEN;
+    constexpr int T = bp_threads(LEN);
+    constexpr int NL = (LEN3 + T - 1) / T;
     extern __shared__ float smem[];
-    const int len = t.len, len2 = len * len, len3 = len2 * len;
-    float* prow = smem;
-    float* A = prow + len3;
-    float* B = A + len3;
-    float* zt = B + len3;            // 2*len
-    float* red = zt + 2 * len + 2;   // 32
-    short* ia = reinterpret_cast<short*>(red + 32);
-    short* ib = ia + len3;
-    __shared__ int s_item;
-    __shared__ int s_abort;
+    float* A = smem;
+    float* B = A + LEN3;
+    short* ia = reinterpret_cast<short*>(B + LEN3);
+    short* ib = ia + LEN3;
+    __shared__ float red[32];
+    __shared__ int s_node, s_last;
+    const int tid = threadIdx.x;
     for (;;) {
-        if (threadIdx.x == 0) {
-            s_item = atomicAdd(work, 1);
-            s_abort = *(volatile int*)err != 0;
+        __syncthreads();  // previous chain finished with s_node / smem
+        if (tid == 0) {
+            const int it = atomicAdd(work, 1);
+            s_node = it < t.n_leaves ? t.leaves[it] : -1;
         }
         __syncthreads();
-        const int it = s_item;
-        if (it >= t.n_up || s_abort) return;
-        const int p = t.up_nodes[it];
-        const float up0 = t.u0[p], vp0 = t.v0[p], wp0 = t.w0[p];
-        for (int l = threadIdx.x; l < len3; l += blockDim.x) prow[l] = ld_cg(cost + (int64_t)p * len3 + l);
-        for (int ci = t.child_ptr[it]; ci < t.child_ptr[it + 1]; ci++) {
-            const int c = t.children[ci];
-            const int wi = t.wait_idx[c];
-            if (threadIdx.x == 0 && wi >= 0) {
-                long long spins = 0;
-                while (*(volatile int*)(flags + wi) != epoch) {
-                    if (++spins > kSpinLimit || *(volatile int*)err != 0) {
-                        atomicCAS(err, 0, 1);
-                        s_abort = 1;
-                        break;
-                    }
-                    __nanosleep(256);
-                }
+        int node = s_node;
+        if (node < 0) return;
+        {
+            const float e = t.edgemst[node];
+            const float* row = cost + (int64_t)node * LEN3;
+            for (int l = tid; l < LEN3; l += T) A[l] = __fmul_rn(ld_cg(row + l), e);
+        }
+        for (;;) {
+            const int p = t.parents[node];
+            const float ox = __fdiv_rn(t.u0[p] - t.u0[node], t.q);
+            const float oy = __fdiv_rn(t.v0[p] - t.v0[node], t.q);
+            const float oz = __fdiv_rn(t.w0[p] - t.w0[node], t.q);
+            __syncthreads();
+            dt_lines<LEN, 0>(A, B, nullptr, ia, oy);
+            __syncthreads();
+            dt_lines<LEN, 1>(B, A, ia, ib, ox);
+            __syncthreads();
+            dt_lines<LEN, 2>(A, B, ib, ia, oz);  // message in B, argmin chain in ia
+            __syncthreads();
+            float mn = INFINITY;
+            float* crow = cost + (int64_t)node * LEN3;
+            short* arow = allinds + (int64_t)node * LEN3;
+            for (int l = tid; l < LEN3; l += T) {
+                const float v = B[l];
+                mn = fminf(mn, v);
+                crow[l] = v;
+                arow[l] = ia[l];
+            }
+            mn = block_min(mn, red);  // ends with a barrier: all stores of this CTA precede
+            if (tid == 0) {
+                mins[node] = mn;
+                __threadfence();
+                const int nch = t.child_ptr[p + 1] - t.child_ptr[p];
+                s_last = atomicAdd(arrived + p, 1) == nch - 1;
                 __threadfence();
             }
             __syncthreads();
-            if (s_abort) return;
-            const float e = t.edgemst[c];
-            const float* crow = cost + (int64_t)c * len3;
-            for (int l = threadIdx.x; l < len3; l += blockDim.x) A[l] = __fmul_rn(ld_cg(crow + l), e);
-            const float ox = __fdiv_rn(up0 - t.u0[c], t.q);
-            const float oy = __fdiv_rn(vp0 - t.v0[c], t.q);
-            const float oz = __fdiv_rn(wp0 - t.w0[c], t.q);
-            fill_parabola(zt, len, oy);
-            __syncthreads();
-            dt_pass(A, B, nullptr, ia, zt, len, 0);
-            __syncthreads();
-            fill_parabola(zt, len, ox);
-            __syncthreads();
-            dt_pass(B, A, ia, ib, zt, len, 1);
-            __syncthreads();
-            fill_parabola(zt, len, oz);
-            __syncthreads();
-            dt_pass(A, B, ib, ia, zt, len, 2);  // message in B, argmin chain in ia
-            __syncthreads();
-            float mn = INFINITY;
-            for (int l = threadIdx.x; l < len3; l += blockDim.x) {
-                const float v = B[l];
-                mn = fminf(mn, v);
-                cost[(int64_t)c * len3 + l] = v;
-                allinds[(int64_t)c * len3 + l] = ia[l];
+            if (!s_last) break;
+            // last arriver: the parent's row = data cost + sum over children in
+            // MST ordering order of (message - min), then the parent continues
+            const int c0 = t.child_ptr[p], c1 = t.child_ptr[p + 1];
+            float acc[NL];
+            const float* prow = cost + (int64_t)p * LEN3;
+#pragma unroll
+            for (int k = 0; k < NL; k++) {
+                const int l = tid + k * T;
+                acc[k] = l < LEN3 ? ld_cg(prow + l) : 0.0f;
             }
-            mn = block_min(mn, red);
-            for (int l = threadIdx.x; l < len3; l += blockDim.x) prow[l] = prow[l] + (B[l] - mn);
-            // the next child's passes overwrite A/B/ia/zt only after this barrier
-            __syncthreads();
-        }
-        for (int l = threadIdx.x; l < len3; l += blockDim.x) cost[(int64_t)p * len3 + l] = prow[l];
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            __threadfence();
-            atomicExch(flags + it, epoch);
+            for (int ci = c0; ci < c1; ci++) {
+                const int ch = t.children[ci];
+                const float mch = ld_cg(mins + ch);
+                const float* chrow = cost + (int64_t)ch * LEN3;
+#pragma unroll
+                for (int k = 0; k < NL; k++) {
+                    const int l = tid + k * T;
+                    if (l < LEN3) acc[k] = acc[k] + (ld_cg(chrow + l) - mch);
+                }
+            }
+            if (p == t.root) {
+                float* rrow = cost + (int64_t)p * LEN3;
+#pragma unroll
+                for (int k = 0; k < NL; k++) {
+                    const int l = tid + k * T;
+                    if (l < LEN3) rrow[l] = acc[k];
+                }
+                break;
+            }
+            const float e = t.edgemst[p];
+#pragma unroll
+            for (int k = 0; k < NL; k++) {
+                const int l = tid + k * T;
+                if (l < LEN3) A[l] = __fmul_rn(acc[k], e);
+            }
+            node = p;
         }
     }
 }
 
-// Root argmin (first minimum) and breadth-level backtrack for one tree per CTA.
+// Root argmin (first minimum) and breadth-level backtrack for one tree.
 __global__ void __launch_bounds__(1024) k_bp_down(BpTree t, const float* __restrict__ cost,
-                                                 short* __restrict__ allinds, int* __restrict__ sel,
-                                                 float* __restrict__ u1, float* __restrict__ v1,
-                                                 float* __restrict__ w1, int* __restrict__ err) {
+                                                 short* __restrict__ allinds, float* __restrict__ u1,
+                                                 float* __restrict__ v1, float* __restrict__ w1,
+                                                 int* __restrict__ err) {
+    extern __shared__ int s_sel[];  // two buffers of max_width labels
     __shared__ float s_val[32];
     __shared__ int s_idx[32];
-    // the argmin tables are only valid if the upward pass completed
-    if (*(volatile int*)err != 0) return;
     const int len = t.len, len3 = len * len * len, hw = (len - 1) / 2;
+    const int W = t.max_width;
     const int root = t.ordered[0];
     const float* rr = cost + (int64_t)root * len3;
     float bv = INFINITY;
@@ -197,7 +227,7 @@ __global__ void __launch_bounds__(1024) k_bp_down(BpTree t, const float* __restr
             if (ov < bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
         }
         if (lane == 0) {
-            sel[root] = bi;
+            s_sel[0] = bi;
             const int i = bi % len, j = (bi / len) % len, k = bi / (len * len);
             u1[root] = (float)(j - hw) * t.q + t.u0[root];
             v1[root] = (float)(i - hw) * t.q + t.v0[root];
@@ -205,17 +235,29 @@ __global__ void __launch_bounds__(1024) k_bp_down(BpTree t, const float* __restr
         }
     }
     __syncthreads();
+    const int row_lines = (len3 * 2 + 127) / 128;
     for (int lev = 1; lev < t.n_levels; lev++) {
-        const int b = t.level_start[lev], e = t.level_start[lev + 1];
+        const int b = t.level_start[lev], e = t.level_start[lev + 1], pb = t.level_start[lev - 1];
+        const int* prev = s_sel + ((lev - 1) & 1) * W;
+        int* cur = s_sel + (lev & 1) * W;
+        // warm L2 with the argmin rows two levels ahead
+        if (lev + 2 < t.n_levels) {
+            const int b2 = t.level_start[lev + 2], e2 = t.level_start[lev + 3];
+            for (int q = threadIdx.x; q < (e2 - b2) * row_lines; q += blockDim.x) {
+                const int c = t.ordered[b2 + q / row_lines];
+                const char* a = reinterpret_cast<const char*>(allinds + (int64_t)c * len3) + (q % row_lines) * 128;
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+            }
+        }
         for (int ti = b + threadIdx.x; ti < e; ti += blockDim.x) {
             const int c = t.ordered[ti];
-            const int p = t.parents[c];
-            int l = allinds[(int64_t)c * len3 + sel[p]];
+            const int sp = prev[t.parent_pos[ti] - pb];
+            int l = allinds[(int64_t)c * len3 + sp];
             if (l < 0 || l >= len3) {  // never for a completed upward pass; keeps reads in bounds
                 atomicCAS(err, 0, 2);
                 l = 0;
             }
-            sel[c] = l;
+            cur[ti - b] = l;
             const int i = l % len, j = (l / len) % len, k = l / (len * len);
             u1[c] = (float)(j - hw) * t.q + t.u0[c];
             v1[c] = (float)(i - hw) * t.q + t.v0[c];
@@ -225,30 +267,60 @@ __global__ void __launch_bounds__(1024) k_bp_down(BpTree t, const float* __restr
     }
 }
 
-}  // namespace
-
-size_t bp_up_smem_bytes(int len) {
-    const size_t len3 = (size_t)len * len * len;
-    return (3 * len3 + 2 * len + 2 + 32) * sizeof(float) + 2 * len3 * sizeof(short);
-}
-
-cudaError_t launch_bp_up(const BpTree& t, float* d_cost, short* d_allinds, int* d_work, int* d_flags, int epoch,
-                         int* d_err, int max_ctas, cudaStream_t s) {
-    if (t.n_up <= 0) return cudaSuccess;
-    const size_t smem = bp_up_smem_bytes(t.len);
-    cudaError_t e = cudaFuncSetAttribute(k_bp_up, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+template <int LEN>
+cudaError_t launch_up(const BpTree& t, float* cost, short* allinds, float* mins, int* arrived, int* work,
+                      int sm_count, cudaStream_t s) {
+    constexpr int LEN3 = LEN * LEN * LEN;
+    constexpr int T = bp_threads(LEN);
+    const size_t smem = (size_t)LEN3 * (2 * sizeof(float) + 2 * sizeof(short));
+    cudaError_t e = cudaFuncSetAttribute(k_bp_up<LEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(d_work, 0, sizeof(int), s);
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bp_up<LEN>, T, smem);
     if (e != cudaSuccess) return e;
-    const int ctas = t.n_up < max_ctas ? t.n_up : max_ctas;
-    k_bp_up<<<ctas, kBpThreads, smem, s>>>(t, d_cost, d_allinds, d_work, d_flags, epoch, d_err);
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    int ctas = per_sm * sm_count;
+    if (ctas > t.n_leaves) ctas = t.n_leaves;
+    k_bp_up<LEN><<<ctas, T, smem, s>>>(t, cost, allinds, mins, arrived, work);
     count_launches(1);
     return cudaGetLastError();
 }
 
-cudaError_t launch_bp_down(const BpTree& t, const float* d_cost, short* d_allinds, int* d_sel, float* d_u1,
-                           float* d_v1, float* d_w1, int* d_err, cudaStream_t s) {
-    k_bp_down<<<1, 1024, 0, s>>>(t, d_cost, d_allinds, d_sel, d_u1, d_v1, d_w1, d_err);
+}  // namespace
+
+cudaError_t launch_bp_up(const BpTree& t, float* d_cost, short* d_allinds, float* d_mins, int* d_arrived, int* d_work,
+                         int sm_count, cudaStream_t s) {
+    if (t.n_leaves <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(d_arrived, 0, sizeof(int) * (size_t)t.sz, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_work, 0, sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    switch (t.len) {
+        case 1: return launch_up<1>(t, d_cost, d_allinds, d_mins, d_arrived, d_work, sm_count, s);
+        case 3: return launch_up<3>(t, d_cost, d_allinds, d_mins, d_arrived, d_work, sm_count, s);
+        case 5: return launch_up<5>(t, d_cost, d_allinds, d_mins, d_arrived, d_work, sm_count, s);
+        case 7: return launch_up<7>(t, d_cost, d_allinds, d_mins, d_arrived, d_work, sm_count, s);
+        case 9: return launch_up<9>(t, d_cost, d_allinds, d_mins, d_arrived, d_work, sm_count, s);
+        case 11: return launch_up<11>(t, d_cost, d_allinds, d_mins, d_arrived, d_work, sm_count, s);
+        case 13: return launch_up<13>(t, d_cost, d_allinds, d_mins, d_arrived, d_work, sm_count, s);
+        case 15: return launch_up<15>(t, d_cost, d_allinds, d_mins, d_arrived, d_work, sm_count, s);
+        case 17: return launch_up<17>(t, d_cost, d_allinds, d_mins, d_arrived, d_work, sm_count, s);
+        case 19: return launch_up<19>(t, d_cost, d_allinds, d_mins, d_arrived, d_work, sm_count, s);
+        case 21: return launch_up<21>(t, d_cost, d_allinds, d_mins, d_arrived, d_work, sm_count, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+size_t bp_down_smem_bytes(int max_width) { return (size_t)2 * max_width * sizeof(int); }
+
+cudaError_t launch_bp_down(const BpTree& t, const float* d_cost, short* d_allinds, float* d_u1, float* d_v1,
+                           float* d_w1, int* d_err, cudaStream_t s) {
+    const size_t smem = bp_down_smem_bytes(t.max_width);
+    if (smem > 200 * 1024) return cudaErrorInvalidValue;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_bp_down, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    k_bp_down<<<1, 1024, smem, s>>>(t, d_cost, d_allinds, d_u1, d_v1, d_w1, d_err);
     count_launches(1);
     return cudaGetLastError();
 }

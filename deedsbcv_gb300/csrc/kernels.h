@@ -15,19 +15,22 @@ inline void count_launches(int n) { g_kernel_launches.fetch_add(n, std::memory_o
 struct BpTree {
     int len;                 // 2*hw+1
     float q;                 // label quantisation
-    int n_up;                // number of upward work items (nodes with children)
-    const int* up_nodes;     // [n_up] parent node of each item, deepest first
-    const int* child_ptr;    // [n_up+1] CSR into children
-    const int* children;     // children of each item, in MST ordering order
-    const int* wait_idx;     // [sz1] item index of a node if it has children, else -1
-    const float* edgemst;    // [sz1] weight of the edge to the parent
-    const float* u0;         // [sz1] current displacement (label offsets are relative)
+    int sz;                  // nodes
+    int root;                // ordered[0]
+    int n_leaves;            // nodes without children (root excluded)
+    const int* leaves;       // [n_leaves] deepest first
+    const int* child_ptr;    // [sz+1] CSR of children per node
+    const int* children;     // children of each node, in MST ordering order
+    const int* parents;      // [sz]
+    const float* edgemst;    // [sz] weight of the edge to the parent
+    const float* u0;         // [sz] current displacement (label offsets are relative)
     const float* v0;
     const float* w0;
     int n_levels;            // breadth levels
+    int max_width;           // widest breadth level
     const int* level_start;  // [n_levels+1] ranges into ordered
-    const int* ordered;      // [sz1] breadth-level order
-    const int* parents;      // [sz1]
+    const int* ordered;      // [sz] breadth-level order
+    const int* parent_pos;   // [sz] position in `ordered` of the parent of ordered[t]
 };
 
 // A displacement field given at full resolution (mode 1), on a control grid
@@ -45,11 +48,11 @@ cudaError_t launch_mind_ssc(const float* d_im, int m, int n, int o, int qs, cons
 cudaError_t launch_data_cost(const uint64_t* d_F, const uint64_t* d_M, int m, int n, int o, int g, int hw, int q,
                              int sy, int sx, int sz, float alpha1, float* d_cost, cudaStream_t s);
 cudaError_t launch_edge_sad(const float* d_im, int m, int n, int o, int g, float* d_sad, cudaStream_t s);
-size_t bp_up_smem_bytes(int len);
-cudaError_t launch_bp_up(const BpTree& t, float* d_cost, short* d_allinds, int* d_work, int* d_flags, int epoch,
-                         int* d_err, int max_ctas, cudaStream_t s);
-cudaError_t launch_bp_down(const BpTree& t, const float* d_cost, short* d_allinds, int* d_sel, float* d_u1,
-                           float* d_v1, float* d_w1, int* d_err, cudaStream_t s);
+cudaError_t launch_bp_up(const BpTree& t, float* d_cost, short* d_allinds, float* d_mins, int* d_arrived, int* d_work,
+                         int sm_count, cudaStream_t s);
+size_t bp_down_smem_bytes(int max_width);
+cudaError_t launch_bp_down(const BpTree& t, const float* d_cost, short* d_allinds, float* d_u1, float* d_v1,
+                           float* d_w1, int* d_err, cudaStream_t s);
 cudaError_t launch_shift(const float* d_in, float* d_out, int64_t n, float shift, cudaStream_t s);
 cudaError_t launch_upsample(const float* u0, const float* v0, const float* w0, int m2, int n2, int o2, float* u,
                             float* v, float* w, int m, int n, int o, cudaStream_t s);

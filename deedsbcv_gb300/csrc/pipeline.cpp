@@ -46,7 +46,8 @@ struct deeds_ctx {
     int sm_count = 0;
     cudaStream_t stream = nullptr;  // used by the host-pointer entry points
     cudaStream_t side = nullptr;    // MST edge costs and their copies
-    cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+    cudaStream_t stream_b = nullptr;  // backward-direction chain of deeds_register*
+    cudaEvent_t ev_a = nullptr, ev_b = nullptr, ev_c = nullptr, ev_d = nullptr;
     std::string err;
     std::map<std::string, DevBuf> dev;
     std::map<std::string, HostBuf> host;
@@ -210,10 +211,10 @@ deeds_status check_params(deeds_ctx* ctx, const deeds_params* p, int m, int n, i
     return DEEDS_OK;
 }
 
-// One tree's host arrays packed for a single H2D copy.
+// One tree's host arrays packed for a single H2D copy (4-byte words).
 struct PackedTree {
-    int sz = 0, n_up = 0, n_levels = 0;
-    size_t o_ordered, o_parents, o_wait, o_children, o_up, o_cptr, o_lstart, o_edgemst, total;  // in 4-byte words
+    int sz = 0, n_leaves = 0, n_levels = 0, max_width = 0;
+    size_t o_ordered, o_parents, o_edgemst, o_cptr, o_children, o_leaves, o_lstart, o_ppos, total;
 };
 
 PackedTree pack_layout(int sz) {
@@ -222,14 +223,25 @@ PackedTree pack_layout(int sz) {
     size_t o = 0;
     t.o_ordered = o; o += sz;
     t.o_parents = o; o += sz;
-    t.o_wait = o; o += sz;
-    t.o_children = o; o += sz;
-    t.o_up = o; o += sz;
-    t.o_cptr = o; o += sz + 1;
-    t.o_lstart = o; o += sz + 1;
     t.o_edgemst = o; o += sz;
+    t.o_cptr = o; o += sz + 1;
+    t.o_children = o; o += sz;
+    t.o_leaves = o; o += sz;
+    t.o_lstart = o; o += sz + 1;
+    t.o_ppos = o; o += sz;
     t.total = o;
     return t;
+}
+
+void pack_schedule(const TreeSchedule& s, uint32_t* blk, PackedTree& t) {
+    t.n_leaves = (int)s.leaves.size();
+    t.n_levels = s.n_levels;
+    t.max_width = s.max_width;
+    std::memcpy(blk + t.o_cptr, s.child_ptr.data(), sizeof(int) * s.child_ptr.size());
+    std::memcpy(blk + t.o_children, s.children.data(), sizeof(int) * s.children.size());
+    std::memcpy(blk + t.o_leaves, s.leaves.data(), sizeof(int) * s.leaves.size());
+    std::memcpy(blk + t.o_lstart, s.level_start.data(), sizeof(int) * s.level_start.size());
+    std::memcpy(blk + t.o_ppos, s.parent_pos.data(), sizeof(int) * s.parent_pos.size());
 }
 
 // Build one tree on the host into the packed pinned block `blk`.
@@ -241,41 +253,29 @@ void build_tree(const float* sad, float stddev, int m1, int n1, int o1, int g, u
     prims_from_sad(sad, stddev, m1, n1, o1, g, ordered, parents, edgemst);
     TreeSchedule s;
     build_schedule(ordered, parents, sz, s);
-    t.n_up = (int)s.up_nodes.size();
-    t.n_levels = s.n_levels;
-    std::memcpy(blk + t.o_wait, s.wait_idx.data(), sizeof(int) * sz);
-    std::memcpy(blk + t.o_children, s.children.data(), sizeof(int) * s.children.size());
-    std::memcpy(blk + t.o_up, s.up_nodes.data(), sizeof(int) * s.up_nodes.size());
-    std::memcpy(blk + t.o_cptr, s.child_ptr.data(), sizeof(int) * s.child_ptr.size());
-    std::memcpy(blk + t.o_lstart, s.level_start.data(), sizeof(int) * s.level_start.size());
+    pack_schedule(s, blk, t);
 }
 
-BpTree device_tree(const PackedTree& t, const uint32_t* dblk, int len, float q, const float* u0, const float* v0,
-                   const float* w0) {
+BpTree device_tree(const PackedTree& t, const uint32_t* dblk, const uint32_t* hblk, int len, float q, const float* u0,
+                   const float* v0, const float* w0) {
     BpTree b;
     b.len = len;
     b.q = q;
-    b.n_up = t.n_up;
-    b.up_nodes = reinterpret_cast<const int*>(dblk + t.o_up);
+    b.sz = t.sz;
+    b.root = reinterpret_cast<const int*>(hblk + t.o_ordered)[0];
+    b.n_leaves = t.n_leaves;
+    b.leaves = reinterpret_cast<const int*>(dblk + t.o_leaves);
     b.child_ptr = reinterpret_cast<const int*>(dblk + t.o_cptr);
     b.children = reinterpret_cast<const int*>(dblk + t.o_children);
-    b.wait_idx = reinterpret_cast<const int*>(dblk + t.o_wait);
+    b.parents = reinterpret_cast<const int*>(dblk + t.o_parents);
     b.edgemst = reinterpret_cast<const float*>(dblk + t.o_edgemst);
     b.u0 = u0; b.v0 = v0; b.w0 = w0;
     b.n_levels = t.n_levels;
+    b.max_width = t.max_width;
     b.level_start = reinterpret_cast<const int*>(dblk + t.o_lstart);
     b.ordered = reinterpret_cast<const int*>(dblk + t.o_ordered);
-    b.parents = reinterpret_cast<const int*>(dblk + t.o_parents);
+    b.parent_pos = reinterpret_cast<const int*>(dblk + t.o_ppos);
     return b;
-}
-
-int bp_max_ctas(deeds_ctx* ctx, int len) {
-    // persistent grid: as many CTAs as can be resident (shared memory limited)
-    const size_t smem = bp_up_smem_bytes(len);
-    int per_sm = (int)(200 * 1024 / (smem + 1024));
-    if (per_sm < 1) per_sm = 1;
-    if (per_sm > 8) per_sm = 8;
-    return per_sm * ctx->sm_count;
 }
 
 // Run BP on one tree: upload its schedule, upward pass, downward pass.
@@ -284,20 +284,21 @@ deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTre
                          const float* w0, float* u1, float* v1, float* w1, int* d_err, cudaStream_t s) {
     deeds_status st = DEEDS_OK;
     uint32_t* d_blk = dbuf<uint32_t>(ctx, "tree_" + tag, pt.total, &st);
-    int* d_flags = dbuf<int>(ctx, "flags_" + tag, (size_t)pt.sz + 1, &st, true);
+    float* d_mins = dbuf<float>(ctx, "mins_" + tag, pt.sz, &st);
+    int* d_arrived = dbuf<int>(ctx, "arrived_" + tag, pt.sz, &st);
     int* d_work = dbuf<int>(ctx, "work_" + tag, 1, &st);
-    int* d_sel = dbuf<int>(ctx, "sel_" + tag, pt.sz, &st);
     if (st) return st;
+    if (bp_down_smem_bytes(pt.max_width) > 200 * 1024)
+        return fail(ctx, DEEDS_ERR_INVALID, "MST breadth level of %d nodes is too wide", pt.max_width);
     CK(cudaMemcpyAsync(d_blk, h_blk, pt.total * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
-    const BpTree bt = device_tree(pt, d_blk, len, (float)q, u0, v0, w0);
-    const int epoch = ++ctx->epoch;
+    const BpTree bt = device_tree(pt, d_blk, h_blk, len, (float)q, u0, v0, w0);
     {
         StageScope sc(ctx, DEEDS_STAGE_BP_UP, s);
-        CK(launch_bp_up(bt, d_cost, d_allinds, d_work, d_flags, epoch, d_err, bp_max_ctas(ctx, len), s));
+        CK(launch_bp_up(bt, d_cost, d_allinds, d_mins, d_arrived, d_work, ctx->sm_count, s));
     }
     {
         StageScope sc(ctx, DEEDS_STAGE_BP_DOWN, s);
-        CK(launch_bp_down(bt, d_cost, d_allinds, d_sel, u1, v1, w1, d_err, s));
+        CK(launch_bp_down(bt, d_cost, d_allinds, u1, v1, w1, d_err, s));
     }
     return DEEDS_OK;
 }
@@ -335,6 +336,9 @@ deeds_status deeds_create(deeds_ctx** out, int device) {
     CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&c->ev_a, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c->ev_b, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->ev_c, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->ev_d, cudaEventDisableTiming));
+    CK(cudaStreamCreateWithFlags(&c->stream_b, cudaStreamNonBlocking));
     *out = c.release();
     return DEEDS_OK;
 }
@@ -342,15 +346,15 @@ deeds_status deeds_create(deeds_ctx** out, int device) {
 void deeds_destroy(deeds_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
-    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    if (ctx->side) cudaStreamSynchronize(ctx->side);
+    for (cudaStream_t st : {ctx->stream, ctx->stream_b, ctx->side})
+        if (st) cudaStreamSynchronize(st);
     for (auto& kv : ctx->dev) if (kv.second.p) cudaFree(kv.second.p);
     for (auto& kv : ctx->host) if (kv.second.p) cudaFreeHost(kv.second.p);
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
-    if (ctx->ev_a) cudaEventDestroy(ctx->ev_a);
-    if (ctx->ev_b) cudaEventDestroy(ctx->ev_b);
-    if (ctx->stream) cudaStreamDestroy(ctx->stream);
-    if (ctx->side) cudaStreamDestroy(ctx->side);
+    for (cudaEvent_t e : {ctx->ev_a, ctx->ev_b, ctx->ev_c, ctx->ev_d})
+        if (e) cudaEventDestroy(e);
+    for (cudaStream_t st : {ctx->stream, ctx->stream_b, ctx->side})
+        if (st) cudaStreamDestroy(st);
     delete ctx;
 }
 
@@ -436,20 +440,14 @@ deeds_status deeds_tree_bp_dev(deeds_ctx* ctx, float* d_cost, const float* d_u0,
     std::memcpy(h + pt.o_edgemst, edgemst, sizeof(float) * sz);
     TreeSchedule sch;
     build_schedule(ordered, parents, sz, sch);
-    pt.n_up = (int)sch.up_nodes.size();
-    pt.n_levels = sch.n_levels;
-    std::memcpy(h + pt.o_wait, sch.wait_idx.data(), sizeof(int) * sz);
-    std::memcpy(h + pt.o_children, sch.children.data(), sizeof(int) * sch.children.size());
-    std::memcpy(h + pt.o_up, sch.up_nodes.data(), sizeof(int) * sch.up_nodes.size());
-    std::memcpy(h + pt.o_cptr, sch.child_ptr.data(), sizeof(int) * sch.child_ptr.size());
-    std::memcpy(h + pt.o_lstart, sch.level_start.data(), sizeof(int) * sch.level_start.size());
+    pack_schedule(sch, h, pt);
     CK(cudaMemsetAsync(d_err, 0, sizeof(int), s));
     st = run_tree_bp(ctx, "stage", pt, h, d_cost, allinds, len, q, d_u0, d_v0, d_w0, d_u1, d_v1, d_w1, d_err, s);
     if (st) return st;
     int herr = 0;
     CK(cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    if (herr) return fail(ctx, DEEDS_ERR_TIMEOUT, "belief propagation: a bounded wait expired");
+    if (herr) return fail(ctx, DEEDS_ERR_INTERNAL, "belief propagation produced an out-of-range argmin index");
     return DEEDS_OK;
 }
 
@@ -535,22 +533,15 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
     deeds_status st = check_params(ctx, P, m, n, o);
     if (st) return st;
     CK(cudaSetDevice(ctx->device));
+    // forward chain on the caller's stream, backward chain on the context's second stream
     cudaStream_t s = (cudaStream_t)stream;
+    cudaStream_t sd[2] = {s, ctx->stream_b};
     const int L = P->levels;
     const size_t sz = (size_t)m * n * o;
     float thr[5];
     mind_thresholds(thr);
 
-    // ---- buffers
-    float* fix = dbuf<float>(ctx, "fix", sz, &st);
-    float* mov = dbuf<float>(ctx, "mov", sz, &st);
-    float* warp0 = dbuf<float>(ctx, "warp0", sz, &st);
-    float* warped = dbuf<float>(ctx, "warped", sz, &st);
-    uint64_t* c_fix = dbuf<uint64_t>(ctx, "c_fix", sz, &st);
-    uint64_t* c_mov = dbuf<uint64_t>(ctx, "c_mov", sz, &st);
-    uint64_t* c_warp = dbuf<uint64_t>(ctx, "c_warp", sz, &st);
-    float* mind_scr = dbuf<float>(ctx, "mind", 6 * sz, &st);
-    int* d_err = dbuf<int>(ctx, "err", 2, &st);
+    // ---- sizes
     size_t max_cost = 0, max_sz1 = 0;
     std::vector<int> m1s(L), n1s(L), o1s(L);
     for (int l = 0; l < L; l++) {
@@ -560,48 +551,40 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
         max_sz1 = std::max(max_sz1, sz1);
         max_cost = std::max(max_cost, sz1 * len * len * len);
     }
-    {
-        const size_t s0 = (size_t)(m / P->grid[0]) * (n / P->grid[0]) * (o / P->grid[0]);
-        max_sz1 = std::max(max_sz1, s0);
+    // ---- buffers: everything is sized up front, so nothing is reallocated
+    // (cudaFree) while kernels of this pair are in flight
+    float* fix = dbuf<float>(ctx, "fix", sz, &st);
+    float* mov = dbuf<float>(ctx, "mov", sz, &st);
+    float* warp0 = dbuf<float>(ctx, "warp0", sz, &st);
+    uint64_t* c_fix = dbuf<uint64_t>(ctx, "c_fix", sz, &st);
+    uint64_t* c_mov = dbuf<uint64_t>(ctx, "c_mov", sz, &st);
+    int* d_err = dbuf<int>(ctx, "err", 2, &st);
+    float* warped[2];
+    uint64_t* c_warp[2];
+    float* mind_scr[2];
+    float* cost[2];
+    short* allinds[2];
+    const char* tags[2] = {"f", "b"};
+    for (int d = 0; d < 2; d++) {
+        const std::string tg = tags[d];
+        warped[d] = dbuf<float>(ctx, "warped_" + tg, sz, &st);
+        c_warp[d] = dbuf<uint64_t>(ctx, "c_warp_" + tg, sz, &st);
+        mind_scr[d] = dbuf<float>(ctx, "mind_" + tg, 6 * sz, &st);
+        cost[d] = dbuf<float>(ctx, "cost_" + tg, max_cost, &st);
+        allinds[d] = dbuf<short>(ctx, "allinds_" + tg, max_cost, &st);
+        dbuf<uint32_t>(ctx, "tree_" + tg, pack_layout((int)max_sz1).total, &st);
+        dbuf<float>(ctx, "mins_" + tg, max_sz1, &st);
+        dbuf<int>(ctx, "arrived_" + tg, max_sz1, &st);
+        dbuf<int>(ctx, "work_" + tg, 1, &st);
     }
-    // per-direction BP buffers at the largest level's size, so nothing is
-    // reallocated (cudaFree) while kernels of this pair are in flight
-    for (const char* tag : {"f", "b"}) {
-        dbuf<uint32_t>(ctx, std::string("tree_") + tag, pack_layout((int)max_sz1).total, &st);
-        dbuf<int>(ctx, std::string("flags_") + tag, max_sz1 + 1, &st, true);
-        dbuf<int>(ctx, std::string("work_") + tag, 1, &st);
-        dbuf<int>(ctx, std::string("sel_") + tag, max_sz1, &st);
-    }
-    float* cost = dbuf<float>(ctx, "cost", max_cost, &st);
-    short* allinds = dbuf<short>(ctx, "allinds", max_cost, &st);
-    float* grid = dbuf<float>(ctx, "grid", 21 * max_sz1, &st);  // fields on the control grids
+    float* grid = dbuf<float>(ctx, "grid", 18 * max_sz1, &st);  // fields on the control grids
     float* ku = dbuf<float>(ctx, "keep_u", sz, &st);
     float* kv = dbuf<float>(ctx, "keep_v", sz, &st);
     float* kw = dbuf<float>(ctx, "keep_w", sz, &st);
     float* cons_scr = dbuf<float>(ctx, "consistent", 12 * max_sz1, &st);
-    if (st) return st;
-    float* prev[6];   // u1 v1 w1 u1i v1i w1i on the previous grid
-    float* cur0[3];   // u0 v0 w0 on the current grid
-    float* nxt[6];    // new fields on the current grid
-    for (int i = 0; i < 6; i++) prev[i] = grid + i * max_sz1;
-    for (int i = 0; i < 3; i++) cur0[i] = grid + (6 + i) * max_sz1;
-    for (int i = 0; i < 6; i++) nxt[i] = grid + (9 + i) * max_sz1;
-    float* keep = grid + 15 * max_sz1;  // unused slack
-    (void)keep;
-
-    // ---- inputs, affine-only warp of the moving image
-    CK(cudaMemsetAsync(d_err, 0, 2 * sizeof(int), s));
-    CK(launch_shift(d_fixed, fix, (int64_t)sz, P->intensity_shift, s));
-    CK(launch_shift(d_moving, mov, (int64_t)sz, P->intensity_shift, s));
-    FieldRef zero{0, nullptr, nullptr, nullptr, 0, 0, 0};
-    CK(launch_warp_affine(mov, X, zero, m, n, o, warp0, nullptr, nullptr, nullptr, s));
-
-    // ---- MST inputs on the side stream, then host trees on worker threads
-    CK(cudaEventRecord(ctx->ev_a, s));
-    CK(cudaStreamWaitEvent(ctx->side, ctx->ev_a, 0));
     float* h_fix = hbuf<float>(ctx, "h_fix", sz, &st);
     float* h_w0 = hbuf<float>(ctx, "h_w0", sz, &st);
-    std::vector<float*> h_sad(2 * L);
+    std::vector<float*> h_sad(2 * L), d_sad(2 * L);
     std::vector<PackedTree> pts(2 * L);
     std::vector<uint32_t*> h_tree(2 * L);
     for (int l = 0; l < L; l++) {
@@ -611,31 +594,61 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
             h_sad[t] = hbuf<float>(ctx, "h_sad" + std::to_string(t), 6 * sz1, &st);
             pts[t] = pack_layout((int)sz1);
             h_tree[t] = hbuf<uint32_t>(ctx, "h_tree" + std::to_string(t), pts[t].total, &st);
-            float* d_sad = dbuf<float>(ctx, "sad" + std::to_string(t), 6 * sz1, &st);
-            if (st) return st;
-            {
-                StageScope sc(ctx, DEEDS_STAGE_MST, ctx->side);
-                CK(launch_edge_sad(d == 0 ? fix : warp0, m, n, o, P->grid[l], d_sad, ctx->side));
-            }
-            CK(cudaMemcpyAsync(h_sad[t], d_sad, 6 * sz1 * sizeof(float), cudaMemcpyDeviceToHost, ctx->side));
+            d_sad[t] = dbuf<float>(ctx, "sad" + std::to_string(t), 6 * sz1, &st);
         }
     }
     if (st) return st;
+    float* prev[6];  // u1 v1 w1 u1i v1i w1i on the previous grid
+    float* cur0[6];  // u0 v0 w0 on the current grid, per direction
+    float* nxt[6];   // new fields on the current grid
+    for (int i = 0; i < 6; i++) {
+        prev[i] = grid + i * max_sz1;
+        cur0[i] = grid + (6 + i) * max_sz1;
+        nxt[i] = grid + (12 + i) * max_sz1;
+    }
+
+    // ---- inputs, affine-only warp of the moving image
+    CK(cudaMemsetAsync(d_err, 0, 2 * sizeof(int), s));
+    CK(launch_shift(d_fixed, fix, (int64_t)sz, P->intensity_shift, s));
+    CK(launch_shift(d_moving, mov, (int64_t)sz, P->intensity_shift, s));
+    {
+        StageScope sc(ctx, DEEDS_STAGE_TRANSFORM, s);
+        FieldRef zero{0, nullptr, nullptr, nullptr, 0, 0, 0};
+        CK(launch_warp_affine(mov, X, zero, m, n, o, warp0, nullptr, nullptr, nullptr, s));
+    }
+
+    // ---- MST inputs on the side stream: both images to the host first (for the
+    // statistics), then every level's block SADs; host trees on worker threads
+    CK(cudaEventRecord(ctx->ev_a, s));
+    CK(cudaStreamWaitEvent(ctx->side, ctx->ev_a, 0));
     CK(cudaMemcpyAsync(h_fix, fix, sz * sizeof(float), cudaMemcpyDeviceToHost, ctx->side));
     CK(cudaMemcpyAsync(h_w0, warp0, sz * sizeof(float), cudaMemcpyDeviceToHost, ctx->side));
     CK(cudaEventRecord(ctx->ev_b, ctx->side));
+    for (int l = L - 1; l >= 0; l--) {  // finest first: those trees take longest on the host
+        const size_t sz1 = (size_t)m1s[l] * n1s[l] * o1s[l];
+        for (int d = 0; d < 2; d++) {
+            const int t = 2 * l + d;
+            {
+                StageScope sc(ctx, DEEDS_STAGE_MST, ctx->side);
+                CK(launch_edge_sad(d == 0 ? fix : warp0, m, n, o, P->grid[l], d_sad[t], ctx->side));
+            }
+            CK(cudaMemcpyAsync(h_sad[t], d_sad[t], 6 * sz1 * sizeof(float), cudaMemcpyDeviceToHost, ctx->side));
+        }
+    }
+    CK(cudaEventRecord(ctx->ev_c, ctx->side));
     std::vector<std::promise<void>> ready(2 * L);
     std::vector<std::shared_future<void>> ready_f(2 * L);
     for (int t = 0; t < 2 * L; t++) ready_f[t] = ready[t].get_future().share();
-    cudaEvent_t ev_inputs = ctx->ev_b;
+    cudaEvent_t ev_images = ctx->ev_b, ev_sads = ctx->ev_c;
     const int dev = ctx->device;
-    std::thread builder([&, ev_inputs, dev]() {
+    std::thread builder([&, ev_images, ev_sads, dev]() {
         cudaSetDevice(dev);
-        cudaEventSynchronize(ev_inputs);
+        cudaEventSynchronize(ev_images);
         float mean_f, sd_f, mean_w, sd_w;
         std::thread tw([&]() { image_stats(h_w0, sz, &mean_w, &sd_w); });
         image_stats(h_fix, sz, &mean_f, &sd_f);
         tw.join();
+        cudaEventSynchronize(ev_sads);
         // finest trees are the slowest: start the workers in reverse level order
         std::vector<std::thread> workers;
         for (int t = 2 * L - 1; t >= 0; t--) {
@@ -669,30 +682,38 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
             printf("Level %d grid=%d with sizes: %dx%dx%d hw=%d quant=%d\n", l, g, m1, n1, o1, hw, q);
         if (l == 0 || qs != prev_step) {
             StageScope sc(ctx, DEEDS_STAGE_MIND, s);
-            CK(launch_mind_ssc(warp0, m, n, o, qs, thr, mind_scr, c_mov, s));
-            CK(launch_mind_ssc(fix, m, n, o, qs, thr, mind_scr, c_fix, s));
+            CK(launch_mind_ssc(warp0, m, n, o, qs, thr, mind_scr[0], c_mov, s));
+            CK(launch_mind_ssc(fix, m, n, o, qs, thr, mind_scr[0], c_fix, s));
         }
         prev_step = qs;
         int sy, sx, szs;
         float alpha1;
         data_cost_params(g, q, P->alpha, &sy, &sx, &szs, &alpha1);
+        // the backward chain starts once the level's shared inputs are ready
+        CK(cudaEventRecord(ctx->ev_d, s));
+        CK(cudaStreamWaitEvent(sd[1], ctx->ev_d, 0));
         for (int d = 0; d < 2; d++) {
+            cudaStream_t sdd = sd[d];
             float** pv = prev + 3 * d;
+            float** c0 = cur0 + 3 * d;
             {
-                StageScope sc(ctx, DEEDS_STAGE_TRANSFORM, s);
-                CK(launch_upsample(pv[0], pv[1], pv[2], m2, n2, o2, cur0[0], cur0[1], cur0[2], m1, n1, o1, s));
-                FieldRef f{2, cur0[0], cur0[1], cur0[2], m1, n1, o1};
-                if (d == 0) CK(launch_warp_affine(mov, X, f, m, n, o, warped, nullptr, nullptr, nullptr, s));
-                else CK(launch_warp_image(fix, f, m, n, o, warped, s));
+                StageScope sc(ctx, DEEDS_STAGE_TRANSFORM, sdd);
+                CK(launch_upsample(pv[0], pv[1], pv[2], m2, n2, o2, c0[0], c0[1], c0[2], m1, n1, o1, sdd));
+                FieldRef f{2, c0[0], c0[1], c0[2], m1, n1, o1};
+                if (d == 0) CK(launch_warp_affine(mov, X, f, m, n, o, warped[d], nullptr, nullptr, nullptr, sdd));
+                else CK(launch_warp_image(fix, f, m, n, o, warped[d], sdd));
             }
             {
-                StageScope sc(ctx, DEEDS_STAGE_MIND, s);
-                CK(launch_mind_ssc(warped, m, n, o, qs, thr, mind_scr, c_warp, s));
+                StageScope sc(ctx, DEEDS_STAGE_MIND, sdd);
+                CK(launch_mind_ssc(warped[d], m, n, o, qs, thr, mind_scr[d], c_warp[d], sdd));
             }
             {
-                StageScope sc(ctx, DEEDS_STAGE_DATACOST, s);
-                CK(launch_data_cost(d == 0 ? c_fix : c_mov, c_warp, m, n, o, g, hw, q, sy, sx, szs, alpha1, cost, s));
+                StageScope sc(ctx, DEEDS_STAGE_DATACOST, sdd);
+                CK(launch_data_cost(d == 0 ? c_fix : c_mov, c_warp[d], m, n, o, g, hw, q, sy, sx, szs, alpha1,
+                                    cost[d], sdd));
             }
+        }
+        for (int d = 0; d < 2; d++) {
             const int t = 2 * l + d;
             {
                 const auto w0 = std::chrono::steady_clock::now();
@@ -705,10 +726,13 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
                     ctx->stage_ms[DEEDS_STAGE_TREE_WAIT] +=
                         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
             }
-            st = run_tree_bp(ctx, d == 0 ? "f" : "b", pts[t], h_tree[t], cost, allinds, len, q, cur0[0], cur0[1],
-                             cur0[2], nxt[3 * d], nxt[3 * d + 1], nxt[3 * d + 2], d_err + d, s);
+            st = run_tree_bp(ctx, tags[d], pts[t], h_tree[t], cost[d], allinds[d], len, q, cur0[3 * d],
+                             cur0[3 * d + 1], cur0[3 * d + 2], nxt[3 * d], nxt[3 * d + 1], nxt[3 * d + 2], d_err + d,
+                             sd[d]);
             if (st) return st;
         }
+        CK(cudaEventRecord(ctx->ev_d, sd[1]));
+        CK(cudaStreamWaitEvent(s, ctx->ev_d, 0));
         {
             StageScope sc(ctx, DEEDS_STAGE_CONSISTENT, s);
             CK(launch_consistent(nxt[0], nxt[1], nxt[2], nxt[3], nxt[4], nxt[5], m1, n1, o1, g, cons_scr, s));
@@ -716,7 +740,8 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
         if (P->verbose) {
             float js = 0, neg = 0;
             deeds_status js_st = deeds_jacobian_dev(ctx, nxt[0], nxt[1], nxt[2], m1, n1, o1, g, &js, &neg, s);
-            if (js_st == DEEDS_OK) printf("std(J)=%.2f (J<0)=%.2fe-7\n", std::round(js * 100) / 100.0, std::round(neg * 1e7) / 100.0);
+            if (js_st == DEEDS_OK)
+                printf("std(J)=%.2f (J<0)=%.2fe-7\n", std::round(js * 100) / 100.0, std::round(neg * 1e7) / 100.0);
         }
         for (int i = 0; i < 6; i++) std::swap(prev[i], nxt[i]);
         m2 = m1; n2 = n1; o2 = o1;
@@ -726,15 +751,19 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
     const size_t sz1 = (size_t)m2 * n2 * o2;
     for (int c = 0; c < 3; c++)
         CK(cudaMemcpyAsync(d_flow_out + c * sz1, prev[c], sz1 * sizeof(float), cudaMemcpyDeviceToDevice, s));
-    FieldRef f{2, prev[0], prev[1], prev[2], m2, n2, o2};
-    CK(launch_warp_affine(mov, X, f, m, n, o, warped, ku, kv, kw, s));
-    if (d_warped_out) CK(launch_shift(warped, d_warped_out, (int64_t)sz, -P->intensity_shift, s));
+    {
+        StageScope sc(ctx, DEEDS_STAGE_TRANSFORM, s);
+        FieldRef f{2, prev[0], prev[1], prev[2], m2, n2, o2};
+        CK(launch_warp_affine(mov, X, f, m, n, o, warped[0], ku, kv, kw, s));
+        if (d_warped_out) CK(launch_shift(warped[0], d_warped_out, (int64_t)sz, -P->intensity_shift, s));
+    }
     int herr[2] = {0, 0};
     CK(cudaMemcpyAsync(herr, d_err, sizeof(herr), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     if (builder.joinable()) builder.join();
     if (ctx->prof) collect_marks(ctx);
-    if (herr[0] || herr[1]) return fail(ctx, DEEDS_ERR_TIMEOUT, "belief propagation: a bounded wait expired");
+    if (herr[0] || herr[1])
+        return fail(ctx, DEEDS_ERR_INTERNAL, "belief propagation produced an out-of-range argmin index");
     ctx->have_field = true;
     ctx->fm = m; ctx->fn = n; ctx->fo = o;
     std::memcpy(ctx->fX, X, sizeof(ctx->fX));

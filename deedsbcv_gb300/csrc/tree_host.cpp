@@ -33,9 +33,13 @@ void image_stats(const float* im, size_t sz, float* mean_out, float* std_out) {
 }
 
 namespace {
+// A candidate edge: weight and (from vertex, direction).  The reference stores
+// the weight as double; comparing the float is the same order, and the heap
+// algorithm only sees comparison results, so the pop order (ties included) is
+// unchanged while the element shrinks to 8 bytes.
 struct QueuedEdge {
-    double weight;
-    int from, to;
+    float weight;
+    uint32_t from_dir;  // from * 8 + nb
     // std heaps are max-heaps: inverting '<' pops the lightest edge first
     bool operator<(const QueuedEdge& b) const { return weight > b.weight; }
 };
@@ -74,7 +78,7 @@ void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int 
         for (int nb = 0; nb < 6; nb++) {
             const int v = nbr(last, nb);
             if (v >= 0) {
-                heap.push_back(QueuedEdge{(double)w[(size_t)nb * sz + last], last, v});
+                heap.push_back(QueuedEdge{w[(size_t)nb * sz + last], (uint32_t)last * 8u + (uint32_t)nb});
                 std::push_heap(heap.begin(), heap.end());
             }
         }
@@ -83,8 +87,9 @@ void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int 
             const QueuedEdge e = heap.front();
             std::pop_heap(heap.begin(), heap.end());
             heap.pop_back();
-            const bool a = in_tree[e.from], b = in_tree[e.to];
-            if (a != b) { from = a ? e.from : e.to; to = a ? e.to : e.from; }
+            const int ef = (int)(e.from_dir >> 3), et = nbr(ef, (int)(e.from_dir & 7u));
+            const bool a = in_tree[ef], b = in_tree[et];
+            if (a != b) { from = a ? ef : et; to = a ? et : ef; }
         }
         in_tree[to] = 1;
         depth[to] = depth[from] + 1;
@@ -108,48 +113,37 @@ void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int 
 }
 
 void build_schedule(const int* ordered, const int* parents, int sz, TreeSchedule& s) {
-    s.depth.assign(sz, 0);
-    for (int t = 1; t < sz; t++) s.depth[ordered[t]] = s.depth[parents[ordered[t]]] + 1;
+    // breadth levels from the ordering (src/regularisation.h:145-169)
+    std::vector<int> depth(sz, 0), pos(sz, 0);
+    for (int t = 0; t < sz; t++) pos[ordered[t]] = t;
+    for (int t = 1; t < sz; t++) depth[ordered[t]] = depth[parents[ordered[t]]] + 1;
     int maxd = 0;
-    for (int v = 0; v < sz; v++) maxd = std::max(maxd, s.depth[v]);
+    for (int v = 0; v < sz; v++) maxd = std::max(maxd, depth[v]);
     s.n_levels = maxd + 1;
     s.level_start.assign(s.n_levels + 1, 0);
-    for (int v = 0; v < sz; v++) s.level_start[s.depth[v] + 1]++;
+    for (int v = 0; v < sz; v++) s.level_start[depth[v] + 1]++;
     for (int l = 1; l <= s.n_levels; l++) s.level_start[l] += s.level_start[l - 1];
-    // upward items: for each breadth level from the deepest, the distinct parents
-    // of that level's nodes in order of first appearance; children in ordering order
-    s.wait_idx.assign(sz, -1);
-    s.up_nodes.clear();
-    s.child_ptr.clear();
-    s.children.clear();
-    std::vector<int> count;
-    for (int lev = s.n_levels - 1; lev >= 1; lev--) {
-        const int b = s.level_start[lev], e = s.level_start[lev + 1];
-        const int first_item = (int)s.up_nodes.size();
-        for (int t = b; t < e; t++) {
-            const int p = parents[ordered[t]];
-            if (s.wait_idx[p] < 0) {
-                s.wait_idx[p] = (int)s.up_nodes.size();
-                s.up_nodes.push_back(p);
-                count.push_back(0);
-            }
-            count[s.wait_idx[p]]++;
-        }
-        const int n_items = (int)s.up_nodes.size();
-        // CSR offsets for this level's items, then fill in ordering order
-        std::vector<int> fill(n_items - first_item, 0);
-        const int base = (int)s.children.size();
-        std::vector<int> off(n_items - first_item + 1, 0);
-        for (int it = first_item; it < n_items; it++) off[it - first_item + 1] = off[it - first_item] + count[it];
-        s.children.resize(base + off.back());
-        for (int t = b; t < e; t++) {
-            const int c = ordered[t];
-            const int it = s.wait_idx[parents[c]] - first_item;
-            s.children[base + off[it] + fill[it]++] = c;
-        }
-        for (int it = first_item; it < n_items; it++) s.child_ptr.push_back(base + off[it - first_item]);
+    s.max_width = 0;
+    for (int l = 0; l < s.n_levels; l++) s.max_width = std::max(s.max_width, s.level_start[l + 1] - s.level_start[l]);
+    // children per node in ordering order (ordering is breadth-level, so a
+    // parent's children appear in the order the reference adds them)
+    s.child_ptr.assign(sz + 1, 0);
+    for (int t = 1; t < sz; t++) s.child_ptr[parents[ordered[t]] + 1]++;
+    for (int v = 0; v < sz; v++) s.child_ptr[v + 1] += s.child_ptr[v];
+    s.children.assign(sz > 0 ? sz - 1 : 0, 0);
+    std::vector<int> fill(s.child_ptr.begin(), s.child_ptr.end() - 1);
+    for (int t = 1; t < sz; t++) {
+        const int c = ordered[t];
+        s.children[fill[parents[c]]++] = c;
     }
-    s.child_ptr.push_back((int)s.children.size());
+    // leaves, deepest first (long chains start early)
+    s.leaves.clear();
+    for (int t = sz - 1; t >= 1; t--) {
+        const int v = ordered[t];
+        if (s.child_ptr[v + 1] == s.child_ptr[v]) s.leaves.push_back(v);
+    }
+    s.parent_pos.assign(sz, 0);
+    for (int t = 1; t < sz; t++) s.parent_pos[t] = pos[parents[ordered[t]]];
 }
 
 }  // namespace deeds

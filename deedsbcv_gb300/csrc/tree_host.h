@@ -7,12 +7,12 @@ namespace deeds {
 
 struct TreeSchedule {
     int n_levels = 0;
-    std::vector<int> depth;        // per node
+    int max_width = 0;
     std::vector<int> level_start;  // [n_levels+1] ranges into ordered
-    std::vector<int> up_nodes;     // upward work items (parents), deepest first
-    std::vector<int> child_ptr;    // [n_up+1]
-    std::vector<int> children;     // per item, in ordering order
-    std::vector<int> wait_idx;     // per node: its item index or -1
+    std::vector<int> child_ptr;    // [sz+1] CSR of children per node
+    std::vector<int> children;     // in MST ordering order
+    std::vector<int> leaves;       // nodes without children (root excluded), deepest first
+    std::vector<int> parent_pos;   // [sz] position in ordered of the parent of ordered[t]
 };
 
 void image_stats(const float* im, size_t sz, float* mean_out, float* std_out);

@@ -39,7 +39,7 @@ typedef int deeds_status;
 #define DEEDS_ERR_INVALID 1   /* bad argument (dims, level parameters, null pointer) */
 #define DEEDS_ERR_CUDA 2      /* a CUDA runtime call failed */
 #define DEEDS_ERR_NOMEM 3     /* device or host allocation failed */
-#define DEEDS_ERR_TIMEOUT 4   /* a bounded device-side wait gave up (kernel returned early) */
+#define DEEDS_ERR_TIMEOUT 4   /* reserved: a bounded device-side wait gave up */
 #define DEEDS_ERR_INTERNAL 5
 
 #define DEEDS_MAX_LEVELS 10

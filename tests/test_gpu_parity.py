@@ -266,7 +266,10 @@ def test_register_full_size_properties(api):
 def test_invalid_arguments_raise(api):
     from deedsbcv_gb300._lib import DeedsError
     params = api.default_params()
+    with pytest.raises(DeedsError):  # grid spacing 8 does not fit a 4^3 volume
+        api.register(np.zeros((4, 4, 4), np.float32), np.zeros((4, 4, 4), np.float32), params=params)
+    bad = api.default_params(grid=[4], radius=[11], quant=[1])  # label radius above the supported 10
     with pytest.raises(DeedsError):
-        api.register(np.zeros((8, 8, 8), np.float32), np.zeros((8, 8, 8), np.float32), params=params)
+        api.register(np.zeros((16, 16, 16), np.float32), np.zeros((16, 16, 16), np.float32), params=bad)
     with pytest.raises(DeedsError):
         api.apply_flow(np.zeros(7, np.float32), np.zeros((8, 8, 8), np.int16))
