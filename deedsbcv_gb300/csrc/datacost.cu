@@ -2,16 +2,27 @@
 //
 // cost[node][label] = alpha1 * sum over the node's sampled g^3 block of
 //   popcount(F[p] ^ M[clamp(p + d(label))]),
-// d(label) = (ly, lx, lz) * q - q*hw, label = ly + lx*len + lz*len^2.  The
-// reference materialises a clamp-to-edge padded copy of M (:124-138); here the
-// clamp is folded into the address computation, which reads the same values.
+// d(label) = (ly, lx, lz) * q - q*hw, label = ly + lx*len + lz*len^2.
 //
-// Work decomposition: one CTA per control node; its sampled fixed codes are
-// staged in shared memory (broadcast reads), each thread owns labels and keeps
-// an exact int32 Hamming sum.  The moving codes (8 B/voxel) stay L2-resident
-// (63 MB at 192x160x256, L2 = 129 MB); consecutive lanes own consecutive ly,
-// i.e. addresses q*8 B apart along the fastest axis.
-// Roofline: integer-pipe bound, two POPC per 64-bit sample (16 POPC/clk/SM).
+// Main path (grid spacing 2..8): the moving codes are first copied into a
+// clamp-to-edge padded volume (the reference's data2p, :124-138), with an even
+// row pitch so that every row is 16-byte aligned for TMA.  One CTA owns a tile
+// of NY consecutive control nodes along y (same x, z) and one z label offset lz;
+// it walks the len x-offsets lx.  For each (lx, lz) the halo it needs is one 3-D
+// box of the padded volume — all y rows of the tile plus the label reach, the
+// sampled x columns and z slices — which a single cp.async.bulk.tensor.3d
+// copies into shared memory (element strides 2 in x and z skip the unsampled
+// columns, as the reference's skipx/skipz do).  Two boxes are in flight
+// (double buffering on two mbarriers).  Threads own one (node, ly) label each
+// and reduce the node's samples with fully unrolled loops: per sample one
+// 64-bit shared load of the moving code, one broadcast load of the fixed code,
+// XOR, two POPC and an add.  The fixed codes of the tile are staged once.
+// NY is chosen per level by the autotuner in pipeline.cpp.
+//
+// Roofline: integer-pipe bound (two 32-bit POPC per 64-bit sample; GB300 issues
+// 16 POPC/clk/SM).  Work per launch = sz1 * len^3 * samples popc64.
+#include <cuda.h>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -19,6 +30,148 @@ namespace deeds {
 
 namespace {
 
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, int count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];"
+        ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2)
+        : "memory");
+}
+
+constexpr long long kWaitLimit = 1LL << 20;  // try_wait rounds (each suspends up to a hardware time slice)
+
+// Bounded wait of one thread on an mbarrier phase; false if the limit expired.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+    for (long long i = 0; i < kWaitLimit; i++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// clamp-to-edge padded copy of the moving codes, row pitch mpp (even)
+__global__ void k_pad_codes(const uint64_t* __restrict__ M, uint64_t* __restrict__ Mp, int m, int n, int o, int pad,
+                            int mpp, int np, int op) {
+    const int y = blockIdx.x * blockDim.x + threadIdx.x;
+    const int x = blockIdx.y, z = blockIdx.z;
+    if (y >= mpp) return;
+    const int64_t src = clampi(y - pad, 0, m - 1) + (int64_t)clampi(x - pad, 0, n - 1) * m +
+                        (int64_t)clampi(z - pad, 0, o - 1) * m * n;
+    Mp[y + (int64_t)x * mpp + (int64_t)z * mpp * np] = __ldg(M + src);
+}
+
+template <int G>
+__global__ void __launch_bounds__(256) k_data_cost_tma(const __grid_constant__ CUtensorMap map,
+                                                       const uint64_t* __restrict__ F, float* __restrict__ cost,
+                                                       int m, int n, int o, int len, int q, int ny_tile, int yb,
+                                                       float alpha1, int* __restrict__ err) {
+    constexpr int S = G > 4 ? 2 : 1;  // x and z sampling stride (RAND_SAMPLES=1, src/dataCostD.h:141-155)
+    constexpr int NX = (G + S - 1) / S, NZ = (G + S - 1) / S;
+    constexpr int NS = NX * NZ * G;
+    extern __shared__ __align__(128) uint64_t smem_raw[];
+    // TMA destinations must start on 128-byte boundaries: align explicitly
+    uint64_t* smem = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
+    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ int s_ok;
+    const int box = NZ * NX * yb;
+    const int bstride = (box + 15) & ~15;  // each TMA destination starts on a 128-byte boundary
+    uint64_t* buf0 = smem;
+    uint64_t* buf1 = smem + bstride;
+    uint64_t* Fs = smem + 2 * bstride;
+    const int m1 = m / G, n1 = n / G;
+    const int tiles_y = (m1 + ny_tile - 1) / ny_tile;
+    int b = blockIdx.x;
+    const int ty = b % tiles_y;
+    b /= tiles_y;
+    const int nxn = b % n1, nzn = b / n1;
+    const int lz = blockIdx.y;
+    const int y_first = ty * ny_tile;
+    const int ny_here = min(ny_tile, m1 - y_first);
+    const int y0 = y_first * G;  // padded y of the tile's first sampled voxel shifted by -pad
+    const int y_al = y0 & ~1;    // TMA: the innermost coordinate must be 16-byte aligned
+    const int yoff = y0 - y_al;
+    const int tid = threadIdx.x;
+    const int len2 = len * len, len3 = len2 * len;
+    const int64_t mn = (int64_t)m * n;
+    const uint32_t box_bytes = (uint32_t)box * 8u;
+    if (tid == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_ok = 1;
+    }
+    __syncthreads();
+    const int xbase = nxn * G, zbase = nzn * G + lz * q;
+    if (tid == 0) {
+        mbar_expect_tx(&bars[0], box_bytes);
+        tma_load_3d(buf0, &map, &bars[0], y_al, xbase, zbase);
+        if (len > 1) {
+            mbar_expect_tx(&bars[1], box_bytes);
+            tma_load_3d(buf1, &map, &bars[1], y_al, xbase + q, zbase);
+        }
+    }
+    // the tile's sampled fixed codes, node-major, (k, j, i) within a node
+    for (int e = tid; e < ny_here * NS; e += blockDim.x) {
+        const int nn = e / NS, s = e % NS;
+        const int i = s % G, j = (s / G) % NX, k = s / (G * NX);
+        Fs[e] = F[(y0 + nn * G + i) + (int64_t)(xbase + j * S) * m + (int64_t)(nzn * G + k * S) * mn];
+    }
+    const int work = ny_here * len;
+    const int nn = tid / len, ly = tid - (tid / len) * len;
+    for (int lx = 0; lx < len; lx++) {
+        const int slot = lx & 1;
+        uint64_t* sb = slot ? buf1 : buf0;
+        if (tid == 0) {
+            if (!mbar_wait_bounded(&bars[slot], (uint32_t)((lx >> 1) & 1))) s_ok = 0;
+        }
+        __syncthreads();
+        if (!s_ok) break;
+        if (tid < work) {
+            const uint64_t* srow = sb + yoff + nn * G + ly * q;
+            const uint64_t* frow = Fs + nn * NS;
+            int acc = 0;
+#pragma unroll
+            for (int k = 0; k < NZ; k++)
+#pragma unroll
+                for (int j = 0; j < NX; j++) {
+                    const uint64_t* sr = srow + (k * NX + j) * yb;
+#pragma unroll
+                    for (int i = 0; i < G; i++) acc += __popcll(frow[(k * NX + j) * G + i] ^ sr[i]);
+                }
+            const int node = (y_first + nn) + nxn * m1 + nzn * m1 * n1;
+            cost[(int64_t)node * len3 + ly + lx * len + lz * len2] = __fmul_rn((float)acc, alpha1);
+        }
+        __syncthreads();  // every thread is done with this buffer
+        if (tid == 0 && lx + 2 < len) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_expect_tx(&bars[slot], box_bytes);
+            tma_load_3d(sb, &map, &bars[slot], y_al, xbase + (lx + 2) * q, zbase);
+        }
+    }
+    if (!s_ok && tid == 0) {
+        atomicCAS(err, 0, 3);
+        // wait (bounded) for the copies this CTA may still have in flight
+        for (int sl = 0; sl < 2; sl++)
+            for (int ph = 0; ph < 2; ph++) mbar_wait_bounded(&bars[sl], (uint32_t)ph);
+    }
+}
+
+// Generic path (any grid spacing): one CTA per node, clamped global reads.
 __global__ void __launch_bounds__(256) k_data_cost(const uint64_t* __restrict__ F, const uint64_t* __restrict__ M,
                                                    float* __restrict__ cost, int m, int n, int o, int g, int hw,
                                                    int q, int sy, int sx, int sz, float alpha1) {
@@ -32,7 +185,6 @@ __global__ void __launch_bounds__(256) k_data_cost(const uint64_t* __restrict__ 
     const int ny = (g + sy - 1) / sy, nx = (g + sx - 1) / sx, nz = (g + sz - 1) / sz;
     const int ns = ny * nx * nz;
     const int y1 = y * g, x1 = x * g, z1 = z * g;
-    // stage the sampled fixed codes in (k, j, i) order
     for (int s = threadIdx.x; s < ns; s += blockDim.x) {
         const int si = s % ny, sj = (s / ny) % nx, sk = s / (ny * nx);
         s_f[s] = F[(y1 + si * sy) + (int64_t)(x1 + sj * sx) * m + (int64_t)(z1 + sk * sz) * mn];
@@ -43,29 +195,107 @@ __global__ void __launch_bounds__(256) k_data_cost(const uint64_t* __restrict__ 
         const int yb = y1 + ly * q - pad, xb = x1 + lx * q - pad, zb = z1 + lz * q - pad;
         int acc = 0;
         int s = 0;
-        if (yb >= 0 && yb + g - 1 < m) {
-            for (int k = 0; k < nz; k++) {
-                const int64_t zo = (int64_t)clampi(zb + k * sz, 0, o - 1) * mn;
-                for (int jj = 0; jj < nx; jj++) {
-                    const uint64_t* row = M + zo + (int64_t)clampi(xb + jj * sx, 0, n - 1) * m + yb;
-                    for (int i = 0; i < ny; i++, s++) acc += __popcll(s_f[s] ^ __ldg(row + i * sy));
-                }
-            }
-        } else {
-            for (int k = 0; k < nz; k++) {
-                const int64_t zo = (int64_t)clampi(zb + k * sz, 0, o - 1) * mn;
-                for (int jj = 0; jj < nx; jj++) {
-                    const uint64_t* row = M + zo + (int64_t)clampi(xb + jj * sx, 0, n - 1) * m;
-                    for (int i = 0; i < ny; i++, s++)
-                        acc += __popcll(s_f[s] ^ __ldg(row + clampi(yb + i * sy, 0, m - 1)));
-                }
+        for (int k = 0; k < nz; k++) {
+            const int64_t zo = (int64_t)clampi(zb + k * sz, 0, o - 1) * mn;
+            for (int jj = 0; jj < nx; jj++) {
+                const uint64_t* row = M + zo + (int64_t)clampi(xb + jj * sx, 0, n - 1) * m;
+                for (int i = 0; i < ny; i++, s++) acc += __popcll(s_f[s] ^ __ldg(row + clampi(yb + i * sy, 0, m - 1)));
             }
         }
         cost[(int64_t)node * len3 + l] = __fmul_rn((float)acc, alpha1);
     }
 }
 
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+        cudaGetLastError();
+    }
+    return fn;
+}
+
+template <int G>
+cudaError_t launch_tma(const uint64_t* d_F, const uint64_t* d_Mp, int mpp, int np, int op, int m, int n, int o,
+                       int hw, int q, int ny_tile, float alpha1, float* d_cost, int* d_err, cudaStream_t s) {
+    constexpr int S = G > 4 ? 2 : 1;
+    constexpr int NX = (G + S - 1) / S, NZ = (G + S - 1) / S;
+    constexpr int NS = NX * NZ * G;
+    const int len = 2 * hw + 1;
+    const int yb = ((ny_tile * G + (len - 1) * q + 1) + 1) & ~1;  // +1 for the alignment shift, rounded to even
+    CUtensorMap map;
+    const cuuint64_t dims[3] = {(cuuint64_t)mpp, (cuuint64_t)np, (cuuint64_t)op};
+    const cuuint64_t strides[2] = {(cuuint64_t)mpp * 8, (cuuint64_t)mpp * np * 8};
+    const cuuint32_t boxd[3] = {(cuuint32_t)yb, (cuuint32_t)(NX * S), (cuuint32_t)(NZ * S)};
+    const cuuint32_t estr[3] = {1, (cuuint32_t)S, (cuuint32_t)S};
+    EncodeTiledFn enc = encode_fn();
+    if (!enc) return cudaErrorNotSupported;
+    if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<uint64_t*>(d_Mp), dims, strides, boxd, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    const size_t smem = (size_t)(2 * ((NZ * NX * yb + 15) & ~15) + ny_tile * NS) * sizeof(uint64_t) + 128;
+    cudaError_t e = cudaFuncSetAttribute(k_data_cost_tma<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int m1 = m / G, n1 = n / G, o1 = o / G;
+    const int tiles_y = (m1 + ny_tile - 1) / ny_tile;
+    const int threads = ((ny_tile * len + 31) / 32) * 32;
+    dim3 grid((unsigned)(tiles_y * n1 * o1), (unsigned)len);
+    k_data_cost_tma<G><<<grid, threads, smem, s>>>(map, d_F, d_cost, m, n, o, len, q, ny_tile, yb, alpha1, d_err);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
 }  // namespace
+
+bool data_cost_tma_supported(int g, int hw, int q, int ny_tile) {
+    if (g < 2 || g > 8 || ny_tile < 1) return false;
+    const int len = 2 * hw + 1;
+    if (ny_tile * len > 256) return false;
+    const int yb = ((ny_tile * g + (len - 1) * q + 1) + 1) & ~1;
+    if (yb > 256) return false;
+    const int S = g > 4 ? 2 : 1, NX = (g + S - 1) / S;
+    const size_t smem = (size_t)(2 * ((NX * NX * yb + 15) & ~15) + ny_tile * NX * NX * g) * 8 + 128;
+    return smem <= 200 * 1024 && encode_fn() != nullptr;
+}
+
+size_t padded_codes_count(int m, int n, int o, int pad) {
+    const size_t mpp = (size_t)((m + 2 * pad + 1) & ~1);
+    return mpp * (size_t)(n + 2 * pad) * (size_t)(o + 2 * pad);
+}
+
+cudaError_t launch_data_cost_tma(const uint64_t* d_F, const uint64_t* d_M, uint64_t* d_Mpad, int m, int n, int o,
+                                 int g, int hw, int q, int ny_tile, float alpha1, float* d_cost, int* d_err,
+                                 cudaStream_t s) {
+    const int pad = q * hw;
+    const int mpp = (m + 2 * pad + 1) & ~1, np = n + 2 * pad, op = o + 2 * pad;
+    {
+        dim3 blk(128), grd((mpp + 127) / 128, np, op);
+        k_pad_codes<<<grd, blk, 0, s>>>(d_M, d_Mpad, m, n, o, pad, mpp, np, op);
+        count_launches(1);
+    }
+    switch (g) {
+        case 2: return launch_tma<2>(d_F, d_Mpad, mpp, np, op, m, n, o, hw, q, ny_tile, alpha1, d_cost, d_err, s);
+        case 3: return launch_tma<3>(d_F, d_Mpad, mpp, np, op, m, n, o, hw, q, ny_tile, alpha1, d_cost, d_err, s);
+        case 4: return launch_tma<4>(d_F, d_Mpad, mpp, np, op, m, n, o, hw, q, ny_tile, alpha1, d_cost, d_err, s);
+        case 5: return launch_tma<5>(d_F, d_Mpad, mpp, np, op, m, n, o, hw, q, ny_tile, alpha1, d_cost, d_err, s);
+        case 6: return launch_tma<6>(d_F, d_Mpad, mpp, np, op, m, n, o, hw, q, ny_tile, alpha1, d_cost, d_err, s);
+        case 7: return launch_tma<7>(d_F, d_Mpad, mpp, np, op, m, n, o, hw, q, ny_tile, alpha1, d_cost, d_err, s);
+        case 8: return launch_tma<8>(d_F, d_Mpad, mpp, np, op, m, n, o, hw, q, ny_tile, alpha1, d_cost, d_err, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
 
 cudaError_t launch_data_cost(const uint64_t* d_F, const uint64_t* d_M, int m, int n, int o, int g, int hw, int q,
                              int sy, int sx, int sz, float alpha1, float* d_cost, cudaStream_t s) {

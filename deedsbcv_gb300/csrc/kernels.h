@@ -47,6 +47,11 @@ cudaError_t launch_mind_ssc(const float* d_im, int m, int n, int o, int qs, cons
                             uint64_t* d_codes, cudaStream_t s);
 cudaError_t launch_data_cost(const uint64_t* d_F, const uint64_t* d_M, int m, int n, int o, int g, int hw, int q,
                              int sy, int sx, int sz, float alpha1, float* d_cost, cudaStream_t s);
+bool data_cost_tma_supported(int g, int hw, int q, int ny_tile);
+size_t padded_codes_count(int m, int n, int o, int pad);
+cudaError_t launch_data_cost_tma(const uint64_t* d_F, const uint64_t* d_M, uint64_t* d_Mpad, int m, int n, int o,
+                                 int g, int hw, int q, int ny_tile, float alpha1, float* d_cost, int* d_err,
+                                 cudaStream_t s);
 cudaError_t launch_edge_sad(const float* d_im, int m, int n, int o, int g, float* d_sad, cudaStream_t s);
 cudaError_t launch_bp_up(const BpTree& t, float* d_cost, short* d_allinds, float* d_mins, int* d_arrived, int* d_work,
                          int sm_count, cudaStream_t s);

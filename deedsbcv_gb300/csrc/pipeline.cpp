@@ -60,6 +60,8 @@ struct deeds_ctx {
     std::vector<Mark> marks;
     double stage_ms[DEEDS_NUM_STAGES] = {0};
     long long stage_launches[DEEDS_NUM_STAGES] = {0};
+    // cost-volume tile sizes chosen by the autotuner, per (m,n,o,g,hw,q)
+    std::map<std::vector<int>, int> dc_tile;
     // the last registration's full-resolution field (for deeds_warp_segmentation)
     bool have_field = false;
     int fm = 0, fn = 0, fo = 0;
@@ -189,6 +191,46 @@ void data_cost_params(int g, int q, float alpha, int* sy, int* sx, int* sz, floa
                           std::ceil((float)g / (float)*sy);
     const float alphai = (float)g / (alpha * (float)q);
     *alpha1 = (float)(0.5 * alphai / (float)maxsamp);
+}
+
+// Cost volume through the TMA-staged kernel when the shape allows it, with the
+// node-tile height chosen once per shape by timing the candidates (tiles only
+// change the schedule; every candidate writes the same bits).  Other shapes use
+// the generic kernel.
+cudaError_t data_cost_auto(deeds_ctx* ctx, const uint64_t* F, const uint64_t* M, uint64_t* Mpad, int m, int n, int o,
+                           int g, int hw, int q, float alpha, float* cost, int* d_err, cudaStream_t s) {
+    int sy, sx, sz;
+    float alpha1;
+    data_cost_params(g, q, alpha, &sy, &sx, &sz, &alpha1);
+    const std::vector<int> key{m, n, o, g, hw, q};
+    auto it = ctx->dc_tile.find(key);
+    int tile;
+    if (it != ctx->dc_tile.end()) {
+        tile = it->second;
+    } else {
+        static const int cands[] = {2, 4, 6, 8, 12, 16, 24};
+        tile = 0;
+        float best = 1e30f;
+        cudaEvent_t a, b;
+        if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) return cudaErrorUnknown;
+        for (int c : cands) {
+            if (!data_cost_tma_supported(g, hw, q, c) || c > m / g) continue;
+            cudaError_t e = launch_data_cost_tma(F, M, Mpad, m, n, o, g, hw, q, c, alpha1, cost, d_err, s);
+            if (e != cudaSuccess) { cudaGetLastError(); continue; }
+            cudaEventRecord(a, s);
+            for (int r = 0; r < 2; r++) launch_data_cost_tma(F, M, Mpad, m, n, o, g, hw, q, c, alpha1, cost, d_err, s);
+            cudaEventRecord(b, s);
+            if (cudaEventSynchronize(b) != cudaSuccess) { cudaGetLastError(); continue; }
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, a, b);
+            if (ms < best) { best = ms; tile = c; }
+        }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        ctx->dc_tile[key] = tile;
+    }
+    if (tile > 0) return launch_data_cost_tma(F, M, Mpad, m, n, o, g, hw, q, tile, alpha1, cost, d_err, s);
+    return launch_data_cost(F, M, m, n, o, g, hw, q, sy, sx, sz, alpha1, cost, s);
 }
 
 deeds_status check_params(deeds_ctx* ctx, const deeds_params* p, int m, int n, int o) {
@@ -398,10 +440,17 @@ deeds_status deeds_data_cost_dev(deeds_ctx* ctx, const uint64_t* d_F, const uint
     if (g < 1 || hw < 0 || q < 1 || m / g < 1 || n / g < 1 || o / g < 1)
         return fail(ctx, DEEDS_ERR_INVALID, "bad grid %d / radius %d / quant %d", g, hw, q);
     CK(cudaSetDevice(ctx->device));
-    int sy, sx, sz;
-    float alpha1;
-    data_cost_params(g, q, alpha, &sy, &sx, &sz, &alpha1);
-    CK(launch_data_cost(d_F, d_M, m, n, o, g, hw, q, sy, sx, sz, alpha1, d_cost, (cudaStream_t)stream));
+    deeds_status st = DEEDS_OK;
+    uint64_t* mpad = dbuf<uint64_t>(ctx, "mpad_stage", padded_codes_count(m, n, o, q * hw), &st);
+    int* d_err = dbuf<int>(ctx, "err_dc_stage", 1, &st);
+    if (st) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    CK(cudaMemsetAsync(d_err, 0, sizeof(int), s));
+    CK(data_cost_auto(ctx, d_F, d_M, mpad, m, n, o, g, hw, q, alpha, d_cost, d_err, s));
+    int herr = 0;
+    CK(cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (herr) return fail(ctx, DEEDS_ERR_TIMEOUT, "cost volume: a bounded wait for a TMA copy expired");
     return DEEDS_OK;
 }
 
@@ -564,6 +613,9 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
     float* mind_scr[2];
     float* cost[2];
     short* allinds[2];
+    uint64_t* mpad[2];
+    size_t max_pad = 0;
+    for (int l = 0; l < L; l++) max_pad = std::max(max_pad, padded_codes_count(m, n, o, P->quant[l] * P->radius[l]));
     const char* tags[2] = {"f", "b"};
     for (int d = 0; d < 2; d++) {
         const std::string tg = tags[d];
@@ -572,6 +624,7 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
         mind_scr[d] = dbuf<float>(ctx, "mind_" + tg, 6 * sz, &st);
         cost[d] = dbuf<float>(ctx, "cost_" + tg, max_cost, &st);
         allinds[d] = dbuf<short>(ctx, "allinds_" + tg, max_cost, &st);
+        mpad[d] = dbuf<uint64_t>(ctx, "mpad_" + tg, max_pad, &st);
         dbuf<uint32_t>(ctx, "tree_" + tg, pack_layout((int)max_sz1).total, &st);
         dbuf<float>(ctx, "mins_" + tg, max_sz1, &st);
         dbuf<int>(ctx, "arrived_" + tg, max_sz1, &st);
@@ -709,8 +762,8 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
             }
             {
                 StageScope sc(ctx, DEEDS_STAGE_DATACOST, sdd);
-                CK(launch_data_cost(d == 0 ? c_fix : c_mov, c_warp[d], m, n, o, g, hw, q, sy, sx, szs, alpha1,
-                                    cost[d], sdd));
+                CK(data_cost_auto(ctx, d == 0 ? c_fix : c_mov, c_warp[d], mpad[d], m, n, o, g, hw, q, P->alpha,
+                                  cost[d], d_err + d, sdd));
             }
         }
         for (int d = 0; d < 2; d++) {
@@ -762,6 +815,7 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
     CK(cudaStreamSynchronize(s));
     if (builder.joinable()) builder.join();
     if (ctx->prof) collect_marks(ctx);
+    if (herr[0] == 3 || herr[1] == 3) return fail(ctx, DEEDS_ERR_TIMEOUT, "cost volume: a bounded wait for a TMA copy expired");
     if (herr[0] || herr[1])
         return fail(ctx, DEEDS_ERR_INTERNAL, "belief propagation produced an out-of-range argmin index");
     ctx->have_field = true;

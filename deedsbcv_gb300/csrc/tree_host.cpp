@@ -5,8 +5,8 @@
 // whenever two candidate edges have bit-equal weights, which is common on CT
 // backgrounds (weights are exp() of block SADs quantised to float).  To give
 // the reference's tree node for node, it runs on the host with the same binary
-// heap discipline (std::push_heap / std::pop_heap over the same edge sequence and
-// comparator).  The edge SADs come from the GPU (deeds_mst_edges_dev); the
+// heap algorithm as the reference's std::push_heap / std::pop_heap, over the same
+// edge sequence and comparison.  The edge SADs come from the GPU (deeds_mst_edges_dev); the
 // statistics are sequential float sums as in the reference.  Compiled with
 // -ffp-contract=off.
 #include <algorithm>
@@ -35,13 +35,73 @@ void image_stats(const float* im, size_t sz, float* mean_out, float* std_out) {
 namespace {
 // A candidate edge: weight and (from vertex, direction).  The reference stores
 // the weight as double; comparing the float is the same order, and the heap
-// algorithm only sees comparison results, so the pop order (ties included) is
-// unchanged while the element shrinks to 8 bytes.
+// only sees comparison results, so the pop order (ties included) is unchanged
+// while the element shrinks to 8 bytes.
 struct QueuedEdge {
     float weight;
     uint32_t from_dir;  // from * 8 + nb
-    // std heaps are max-heaps: inverting '<' pops the lightest edge first
-    bool operator<(const QueuedEdge& b) const { return weight > b.weight; }
+};
+
+// The reference's priority queue is a binary max-heap under an inverted
+// comparison (src/primsMST.h:24-26) driven by std::push_heap / std::pop_heap.
+// Which of several equal-weight edges pops first depends on the exact sequence
+// of element moves, so this heap performs the same algorithm step for step:
+//   push: append, then move the new element up while its parent compares
+//         "less" (parent weight > new weight);
+//   pop:  take the root; move a hole from the root down to a leaf, always into
+//         the child that compares greater (the lighter edge; the left child
+//         when the right one is not strictly lighter), including the
+//         single-child case at the end of an even-length heap; then place the
+//         former last element at the hole and move it up as in push.
+// It differs only in being branch-free in the descent and prefetching the
+// grandchildren, which changes timing, not order.
+class EdgeHeap {
+  public:
+    explicit EdgeHeap(size_t reserve) { a_.reserve(reserve); }
+    bool empty() const { return a_.empty(); }
+    void push(QueuedEdge e) {
+        a_.push_back(e);
+        sift_up(a_.size() - 1, 0, e);
+    }
+    QueuedEdge pop() {
+        const QueuedEdge top = a_[0];
+        const QueuedEdge last = a_.back();
+        a_.pop_back();
+        const size_t len = a_.size();
+        if (len == 0) return top;
+        QueuedEdge* d = a_.data();
+        size_t hole = 0, child = 0;
+        while (child < (len - 1) / 2) {
+            child = 2 * (child + 1);  // right child
+            const size_t gc = 2 * child + 1;
+            if (gc < len) __builtin_prefetch(d + gc);
+            if (gc - 2 < len) __builtin_prefetch(d + gc - 2);
+            // the left child wins unless the right one is strictly lighter
+            child -= (size_t)(d[child].weight > d[child - 1].weight);
+            d[hole] = d[child];
+            hole = child;
+        }
+        if ((len & 1) == 0 && child == (len - 2) / 2) {
+            child = 2 * (child + 1);
+            d[hole] = d[child - 1];
+            hole = child - 1;
+        }
+        sift_up(hole, 0, last);
+        return top;
+    }
+
+  private:
+    void sift_up(size_t hole, size_t top, QueuedEdge v) {
+        QueuedEdge* d = a_.data();
+        size_t parent = (hole - 1) / 2;
+        while (hole > top && d[parent].weight > v.weight) {
+            d[hole] = d[parent];
+            hole = parent;
+            parent = (hole - 1) / 2;
+        }
+        d[hole] = v;
+    }
+    std::vector<QueuedEdge> a_;
 };
 }  // namespace
 
@@ -53,21 +113,10 @@ void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int 
     const float g3 = (float)std::pow((double)g, 3.0);
     const float twostd = 2.0f * stddev;
     for (size_t e = 0; e < (size_t)sz * 6; e++) w[e] = -std::exp(-(sad[e] / g3) / twostd);
-    const int stride_n = m1, stride_o = m1 * n1;
-    // neighbour of v in direction nb (-x,+x,-y,+y,-z,+z) or -1
-    auto nbr = [&](int v, int nb) -> int {
-        const int k = v / stride_o, j = (v / m1) % n1, i = v % m1;
-        switch (nb) {
-            case 0: return j > 0 ? v - stride_n : -1;
-            case 1: return j + 1 < n1 ? v + stride_n : -1;
-            case 2: return i > 0 ? v - 1 : -1;
-            case 3: return i + 1 < m1 ? v + 1 : -1;
-            case 4: return k > 0 ? v - stride_o : -1;
-            default: return k + 1 < o1 ? v + stride_o : -1;
-        }
-    };
-    std::vector<QueuedEdge> heap;
-    heap.reserve((size_t)sz * 3);
+    const int mn1 = m1 * n1;
+    // neighbour offsets in the reference's direction order -x,+x,-y,+y,-z,+z (src/primsMST.h:70-72)
+    const int off[6] = {-m1, m1, -1, 1, -mn1, mn1};
+    EdgeHeap heap((size_t)sz * 3);
     std::vector<uint8_t> in_tree(sz, 0);
     std::vector<int> depth(sz, 0);
     for (int v = 0; v < sz; v++) parents[v] = -1;
@@ -75,19 +124,15 @@ void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int 
     in_tree[root] = 1;
     int last = root;
     for (int added = 1; added < sz; added++) {
-        for (int nb = 0; nb < 6; nb++) {
-            const int v = nbr(last, nb);
-            if (v >= 0) {
-                heap.push_back(QueuedEdge{w[(size_t)nb * sz + last], (uint32_t)last * 8u + (uint32_t)nb});
-                std::push_heap(heap.begin(), heap.end());
-            }
-        }
+        // push the new vertex's edges to its in-grid neighbours, in direction order
+        const int k = last / mn1, rem = last - k * mn1, j = rem / m1, i = rem - j * m1;
+        const bool ok[6] = {j > 0, j + 1 < n1, i > 0, i + 1 < m1, k > 0, k + 1 < o1};
+        for (int nb = 0; nb < 6; nb++)
+            if (ok[nb]) heap.push(QueuedEdge{w[(size_t)nb * sz + last], (uint32_t)last * 8u + (uint32_t)nb});
         int from = -1, to = -1;
         while (to < 0) {
-            const QueuedEdge e = heap.front();
-            std::pop_heap(heap.begin(), heap.end());
-            heap.pop_back();
-            const int ef = (int)(e.from_dir >> 3), et = nbr(ef, (int)(e.from_dir & 7u));
+            const QueuedEdge e = heap.pop();
+            const int ef = (int)(e.from_dir >> 3), et = ef + off[e.from_dir & 7u];
             const bool a = in_tree[ef], b = in_tree[et];
             if (a != b) { from = a ? ef : et; to = a ? et : ef; }
         }
@@ -104,11 +149,16 @@ void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int 
     for (int l = 1; l <= maxd + 1; l++) start[l] += start[l - 1];
     for (int v = 0; v < sz; v++) ordered[start[depth[v]]++] = v;
     // weight of each child's edge to its parent (src/primsMST.h:198-211)
+    // The reference forms the neighbour index without a bounds check here, so on
+    // grids with a dimension of 1 an out-of-grid direction can alias the parent;
+    // the same unchecked index (last match wins) is used.
     for (int v = 0; v < sz; v++) edgemst[v] = 0.0f;
     for (int t = 1; t < sz; t++) {
         const int c = ordered[t], p = parents[c];
+        const int k = c / mn1, rem = c - k * mn1, j = rem / m1, i = rem - j * m1;
+        const int dxs[6] = {-1, 1, 0, 0, 0, 0}, dys[6] = {0, 0, -1, 1, 0, 0}, dzs[6] = {0, 0, 0, 0, -1, 1};
         for (int nb = 0; nb < 6; nb++)
-            if (nbr(c, nb) == p) edgemst[c] = -w[(size_t)nb * sz + c];
+            if (i + dys[nb] + (j + dxs[nb]) * m1 + (k + dzs[nb]) * mn1 == p) edgemst[c] = -w[(size_t)nb * sz + c];
     }
 }
 

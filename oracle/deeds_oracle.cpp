@@ -342,11 +342,16 @@ void orc_prims_from_sad(const float* sad, float stdim, int m1, int n1, int o1, i
     for (int l = 1; l <= maxlev + 1; l++) start[l] += start[l - 1];
     for (int v = 0; v < sz; v++) ordered[start[level[v]]++] = v;
     // weight of the edge to the parent, exp(-c) in (0,1] (src/primsMST.h:198-211)
+    // the neighbour index is formed without a bounds check, as the reference does
+    // (last match wins; matters only on grids with a dimension of 1)
     for (int v = 0; v < sz; v++) edgemst[v] = 0.0f;
     for (int t = 1; t < sz; t++) {
         const int c = ordered[t], p = parents[c];
-        for (int nb = 0; nb < 6; nb++)
-            if (nbr(c, nb) == p) edgemst[c] = -w[(size_t)nb * sz + c];
+        const int k = c / (m1 * n1), j = (c - k * m1 * n1) / m1, i = c - k * m1 * n1 - j * m1;
+        for (int nb = 0; nb < 6; nb++) {
+            const int idx = i + ddy[nb] + (j + ddx[nb]) * m1 + (k + ddz[nb]) * m1 * n1;
+            if (idx == p) edgemst[c] = -w[(size_t)nb * sz + c];
+        }
     }
 }
 
