@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="96x80x128 workload (profiling runs)")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 16-pair batched measurement")
+    ap.add_argument("--lanes", type=int, default=3, help="pairs in flight for the batched form")
     return ap.parse_args()
 
 
@@ -131,6 +133,41 @@ class ClockSampler:
 def make_workload(shape):
     from deedsbcv_gb300 import phantom
     return phantom.make_pair(shape, seed=SEED, n_organs=13, max_disp=10.0)
+
+
+def batched_pairs(n=16, seed=100):
+    """16 pairs with dims drawn uniformly from 128x112x144 .. 224x192x288 (max
+    10-voxel deformation), the uneven-size batch workload."""
+    from deedsbcv_gb300 import phantom
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        shape = (int(rng.integers(128, 225)), int(rng.integers(112, 193)), int(rng.integers(144, 289)))
+        p = phantom.make_pair(shape, seed=seed + 1 + i, max_disp=10.0)
+        out.append((p["fixed"], p["moving"]))
+    return out
+
+
+def measure_batched(api, ctx, lanes):
+    """Plain (one pair per call) vs batched (deeds_register_batch) on the same
+    16 uneven pairs; both after one untimed pass that sizes buffers and tiles."""
+    pairs = batched_pairs()
+    params = api.default_params()
+    api.register_batch(pairs, params=params, lanes=lanes, ctx=ctx)  # warm: buffers, tiles, lanes
+    for f, mv in pairs[:2]:
+        api.register(f, mv, params=params, want_warped=False, ctx=ctx)
+    t0 = time.perf_counter()
+    plain = [api.register(f, mv, params=params, want_warped=False, ctx=ctx)[0] for f, mv in pairs]
+    t_plain = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    batched = api.register_batch(pairs, params=params, lanes=lanes, ctx=ctx)
+    t_batch = time.perf_counter() - t0
+    same = all(np.array_equal(a, b[0]) for a, b in zip(plain, batched))
+    voxels = sum(int(np.prod(f.shape)) for f, _ in pairs)
+    return {"pairs": len(pairs), "lanes": lanes, "mean_voxels": voxels // len(pairs),
+            "plain_pairs_per_s": len(pairs) / t_plain, "batched_pairs_per_s": len(pairs) / t_batch,
+            "speedup": t_plain / t_batch, "flows_identical": bool(same),
+            "workload": "16 pairs, dims uniform in 128x112x144..224x192x288, host buffers end to end"}
 
 
 def cpu_reference_pair(pair, shape):
@@ -299,6 +336,11 @@ def main():
                      "frac": (mind_bytes / (mind_ms / 1000.0) / 1e9 / hbm_peak) if mind_ms else None},
     }
 
+    # ---- batched form on 16 uneven pairs (rank 0)
+    batched = None
+    if rank == 0 and not args.no_batched and not args.small:
+        batched = measure_batched(api, ctx, args.lanes)
+
     # ---- CPU baseline and full-size parity (rank 0, N=1)
     cpu = None
     parity = None
@@ -336,6 +378,7 @@ def main():
             "stage_launches_per_pair": {k: v[1] // max(args.steps, 1) for k, v in stages.items()},
             "cpu_baseline": cpu,
             "parity": parity,
+            "batched": batched,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:

@@ -24,7 +24,7 @@ EXPORTS = [
     "deeds_prims_from_sad", "deeds_tree_bp_dev", "deeds_upsample_dev", "deeds_warp_affine_dev",
     "deeds_warp_image_dev", "deeds_warp_seg_dev", "deeds_consistent_dev", "deeds_jacobian_dev",
     "deeds_set_profiling", "deeds_stage_times", "deeds_reset_stage_times", "deeds_kernel_launches",
-    "deeds_measure_popc_rate",
+    "deeds_measure_popc_rate", "deeds_register_batch",
 ]
 STAGES = ["mind", "datacost", "mst_edges", "bp_up", "bp_down", "transform", "consistent", "tree_wait"]
 
@@ -38,6 +38,19 @@ class DeedsParams(C.Structure):
         ("alpha", C.c_float),
         ("intensity_shift", C.c_float),
         ("verbose", C.c_int),
+    ]
+
+
+class DeedsPair(C.Structure):
+    _fields_ = [
+        ("fixed", C.c_void_p),
+        ("moving", C.c_void_p),
+        ("m", C.c_int),
+        ("n", C.c_int),
+        ("o", C.c_int),
+        ("X", C.c_void_p),
+        ("flow_out", C.c_void_p),
+        ("warped_out", C.c_void_p),
     ]
 
 
@@ -88,6 +101,7 @@ def load():
     L.deeds_reset_stage_times.argtypes = [P]
     L.deeds_kernel_launches.argtypes = []
     L.deeds_measure_popc_rate.argtypes = [P, P]
+    L.deeds_register_batch.argtypes = [P, P, I, C.POINTER(DeedsParams), I]
     for name in EXPORTS:
         fn = getattr(L, name)
         if name not in ("deeds_default_params", "deeds_destroy", "deeds_last_error", "deeds_version"):

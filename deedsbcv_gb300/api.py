@@ -303,6 +303,34 @@ def register(fixed, moving, dims=None, X=None, params=None, want_warped=True, ct
     return flow, warped
 
 
+def register_batch(pairs, params=None, lanes=0, want_warped=False, ctx=None):
+    """Register a list of (fixed, moving[, X]) host volume pairs, possibly of
+    different sizes, with several pairs in flight (deeds_register_batch).
+    Returns a list of (flow, warped-or-None)."""
+    ctx = ctx or context(0)
+    params = params or default_params()
+    n = len(pairs)
+    arr = (_lib.DeedsPair * max(n, 1))()
+    keep = []
+    outs = []
+    g = params.grid[params.levels - 1]
+    for i, pr in enumerate(pairs):
+        fixed, moving = pr[0], pr[1]
+        X = pr[2] if len(pr) > 2 else None
+        m, nn, o = (int(d) for d in np.asarray(fixed).shape)
+        f = _host(fixed, np.float32, "fixed")
+        mv = _host(moving, np.float32, "moving")
+        Xa = _affine(X)
+        flow = np.zeros(3 * (m // g) * (nn // g) * (o // g), np.float32)
+        warped = np.zeros(m * nn * o, np.float32) if want_warped else None
+        keep += [f, mv, Xa]
+        outs.append((flow, warped))
+        p = lambda a: a.ctypes.data_as(C.c_void_p).value if a is not None else None  # noqa: E731
+        arr[i] = _lib.DeedsPair(p(f), p(mv), m, nn, o, p(Xa), p(flow), p(warped))
+    ctx.check(ctx._L.deeds_register_batch(ctx.handle, arr, n, C.byref(params), int(lanes)))
+    return outs
+
+
 def register_device(fixed, moving, m, n, o, X=None, params=None, flow_out=None, warped_out=None, ctx=None):
     """Full registration of device-resident volumes (float32 CUDA tensors)."""
     ctx = ctx or context(fixed.device.index or 0)

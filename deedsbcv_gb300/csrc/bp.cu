@@ -191,16 +191,21 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
     }
 }
 
-// Root argmin (first minimum) and breadth-level backtrack for one tree.
+// Root argmin (first minimum) and breadth-level backtrack for one tree.  Per
+// level the only dependent access is the argmin-table gather; the next level's
+// node ids, parent positions and current displacements are loaded before it.
 __global__ void __launch_bounds__(1024) k_bp_down(BpTree t, const float* __restrict__ cost,
                                                  short* __restrict__ allinds, float* __restrict__ u1,
                                                  float* __restrict__ v1, float* __restrict__ w1,
                                                  int* __restrict__ err) {
-    extern __shared__ int s_sel[];  // two buffers of max_width labels
+    extern __shared__ int sm_down[];  // two buffers of max_width labels, then the level ranges
     __shared__ float s_val[32];
     __shared__ int s_idx[32];
     const int len = t.len, len3 = len * len * len, hw = (len - 1) / 2;
     const int W = t.max_width;
+    int* s_sel = sm_down;
+    int* s_ls = sm_down + 2 * W;
+    for (int i = threadIdx.x; i <= t.n_levels; i += blockDim.x) s_ls[i] = t.level_start[i];
     const int root = t.ordered[0];
     const float* rr = cost + (int64_t)root * len3;
     float bv = INFINITY;
@@ -236,32 +241,56 @@ __global__ void __launch_bounds__(1024) k_bp_down(BpTree t, const float* __restr
     }
     __syncthreads();
     const int row_lines = (len3 * 2 + 127) / 128;
+    // first node of the next level owned by this thread, loaded one level ahead
+    int nc = -1, npp = 0;
+    float nu = 0.0f, nv = 0.0f, nw = 0.0f;
+    auto preload = [&](int lev) {
+        nc = -1;
+        if (lev < t.n_levels) {
+            const int ti = s_ls[lev] + (int)threadIdx.x;
+            if (ti < s_ls[lev + 1]) {
+                nc = t.ordered[ti];
+                npp = t.parent_pos[ti];
+                nu = t.u0[nc]; nv = t.v0[nc]; nw = t.w0[nc];
+            }
+        }
+    };
+    preload(1);
     for (int lev = 1; lev < t.n_levels; lev++) {
-        const int b = t.level_start[lev], e = t.level_start[lev + 1], pb = t.level_start[lev - 1];
+        const int b = s_ls[lev], e = s_ls[lev + 1], pb = s_ls[lev - 1];
         const int* prev = s_sel + ((lev - 1) & 1) * W;
         int* cur = s_sel + (lev & 1) * W;
+        const int c = nc, pp = npp;
+        const float cu = nu, cv = nv, cw = nw;
+        preload(lev + 1);
         // warm L2 with the argmin rows two levels ahead
         if (lev + 2 < t.n_levels) {
-            const int b2 = t.level_start[lev + 2], e2 = t.level_start[lev + 3];
-            for (int q = threadIdx.x; q < (e2 - b2) * row_lines; q += blockDim.x) {
-                const int c = t.ordered[b2 + q / row_lines];
-                const char* a = reinterpret_cast<const char*>(allinds + (int64_t)c * len3) + (q % row_lines) * 128;
+            const int b2 = s_ls[lev + 2], e2 = s_ls[lev + 3];
+            for (int qq = threadIdx.x; qq < (e2 - b2) * row_lines; qq += blockDim.x) {
+                const int cc = t.ordered[b2 + qq / row_lines];
+                const char* a = reinterpret_cast<const char*>(allinds + (int64_t)cc * len3) + (qq % row_lines) * 128;
                 asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
             }
         }
         for (int ti = b + threadIdx.x; ti < e; ti += blockDim.x) {
-            const int c = t.ordered[ti];
-            const int sp = prev[t.parent_pos[ti] - pb];
-            int l = allinds[(int64_t)c * len3 + sp];
+            int cc, ppos;
+            float a0, a1, a2;
+            if (ti == b + (int)threadIdx.x) { cc = c; ppos = pp; a0 = cu; a1 = cv; a2 = cw; }
+            else {
+                cc = t.ordered[ti]; ppos = t.parent_pos[ti];
+                a0 = t.u0[cc]; a1 = t.v0[cc]; a2 = t.w0[cc];
+            }
+            const int sp = prev[ppos - pb];
+            int l = allinds[(int64_t)cc * len3 + sp];
             if (l < 0 || l >= len3) {  // never for a completed upward pass; keeps reads in bounds
                 atomicCAS(err, 0, 2);
                 l = 0;
             }
             cur[ti - b] = l;
             const int i = l % len, j = (l / len) % len, k = l / (len * len);
-            u1[c] = (float)(j - hw) * t.q + t.u0[c];
-            v1[c] = (float)(i - hw) * t.q + t.v0[c];
-            w1[c] = (float)(k - hw) * t.q + t.w0[c];
+            u1[cc] = (float)(j - hw) * t.q + a0;
+            v1[cc] = (float)(i - hw) * t.q + a1;
+            w1[cc] = (float)(k - hw) * t.q + a2;
         }
         __syncthreads();
     }
@@ -310,11 +339,13 @@ cudaError_t launch_bp_up(const BpTree& t, float* d_cost, short* d_allinds, float
     }
 }
 
-size_t bp_down_smem_bytes(int max_width) { return (size_t)2 * max_width * sizeof(int); }
+size_t bp_down_smem_bytes(int max_width, int n_levels) {
+    return (size_t)(2 * max_width + n_levels + 1) * sizeof(int);
+}
 
 cudaError_t launch_bp_down(const BpTree& t, const float* d_cost, short* d_allinds, float* d_u1, float* d_v1,
                            float* d_w1, int* d_err, cudaStream_t s) {
-    const size_t smem = bp_down_smem_bytes(t.max_width);
+    const size_t smem = bp_down_smem_bytes(t.max_width, t.n_levels);
     if (smem > 200 * 1024) return cudaErrorInvalidValue;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k_bp_down, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

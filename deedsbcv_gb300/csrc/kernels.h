@@ -55,7 +55,7 @@ cudaError_t launch_data_cost_tma(const uint64_t* d_F, const uint64_t* d_M, uint6
 cudaError_t launch_edge_sad(const float* d_im, int m, int n, int o, int g, float* d_sad, cudaStream_t s);
 cudaError_t launch_bp_up(const BpTree& t, float* d_cost, short* d_allinds, float* d_mins, int* d_arrived, int* d_work,
                          int sm_count, cudaStream_t s);
-size_t bp_down_smem_bytes(int max_width);
+size_t bp_down_smem_bytes(int max_width, int n_levels);
 cudaError_t launch_bp_down(const BpTree& t, const float* d_cost, short* d_allinds, float* d_u1, float* d_v1,
                            float* d_w1, int* d_err, cudaStream_t s);
 cudaError_t launch_shift(const float* d_in, float* d_out, int64_t n, float shift, cudaStream_t s);

@@ -2,17 +2,18 @@
 //
 // Layout in HBM: six distance channels D[l][p] (6 x m*n*o float32, context
 // scratch) and the output codes C[p] (uint64).  Four launches:
-//   1. pass_i: per (j,k,l) line, the shifted squared difference (imshift +
-//      distances, src/MINDSSCbox.h:79-124) streamed into the i-axis box sum;
-//   2. pass_j / 3. pass_k: the j- and k-axis box sums, in place;
-//   4. quantise: the 12 SSC pairs -> min/mean normalisation -> 5 thresholds ->
-//      thermometer code (src/MINDSSCbox.h:175-224).
+//   1. k_pass_i: per (j,k) line and channel, the shifted squared difference
+//      (imshift + distances, src/MINDSSCbox.h:79-124) streamed into the i-axis
+//      box sum, through shared-memory tiles so loads and stores are coalesced;
+//   2. k_pass_jk (j) / 3. k_pass_jk (k): the j- and k-axis box sums, in place;
+//   4. k_quantise: the 12 SSC pairs -> min/mean normalisation -> 5 thresholds
+//      -> thermometer code (src/MINDSSCbox.h:175-224).
 // Box sums keep the reference's sequential float prefix sum along each line and
-// its edge rules (src/MINDSSCbox.h:9-73): one thread owns one line and streams
-// it with a lag of r, keeping the last 2r+2 prefix values in a ring.  Lines of
-// the j and k passes map consecutive i to consecutive lanes (coalesced).
-// Roofline: HBM-bound; per call ~ 4 B read + 6x(4 B write) (pass_i),
-// 2 x 6 x 8 B (pass_j, pass_k), 6 x 4 B read + 8 B write (quantise) per voxel.
+// its edge rules (src/MINDSSCbox.h:9-73): one thread owns one line and streams it
+// with a lag of r, keeping the last 2r+2 prefix values in a ring; a parallel
+// scan would change the rounding and with it codes near thresholds.
+// Roofline: HBM-bound; per call ~ 4 B read + 24 B write (pass i), 2 x 48 B
+// (passes j, k), 24 B read + 8 B write (quantise) per voxel = 152 B/voxel.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -21,30 +22,6 @@ namespace deeds {
 namespace {
 
 constexpr int kRing = 16;  // supports box radius r <= 7 (2r+2 <= 16)
-
-// Streaming box filter of one line.  get(t) yields the t-th input sample,
-// put(t, v) stores the t-th output.  Inputs are consumed strictly before the
-// output at the same position is stored (lag r), so in-place use is safe.
-template <class Get, class Put>
-__device__ __forceinline__ void box_line(int L, int r, Get get, Put put) {
-    float ring[kRing];
-    float P = 0.0f;
-    for (int t = 0; t < L; t++) {
-        const float x = get(t);
-        P = (t == 0) ? x : P + x;
-        ring[t & (kRing - 1)] = P;
-        const int i = t - r;
-        if (i >= 0) {
-            if (i <= r) put(i, P);                                            // i < r+1: P[i+r]
-            else put(i, P - ring[(t - 2 * r - 1) & (kRing - 1)]);           // P[i+r] - P[i-r-1]
-        }
-    }
-    const float last = P;
-    for (int i = (L - r > 0 ? L - r : 0); i < L; i++) {
-        // i >= L-r: P[L-1] - P[i-r-1]  (i-r-1 >= 0 since L >= 2r+1)
-        put(i, last - ring[(i - r - 1) & (kRing - 1)]);
-    }
-}
 
 // Shift vectors of the six distance channels (src/MINDSSCbox.h:132-134).
 __constant__ int c_dx[6] = {1, 1, -1, 0, 1, 0};
@@ -55,30 +32,77 @@ __constant__ int c_sx[12] = {-1, 0, -1, 0, 0, 1, 0, 0, 0, -1, 0, 0};
 __constant__ int c_sy[12] = {0, -1, 0, 1, 0, 0, 0, 1, 0, 0, 0, -1};
 __constant__ int c_sz[12] = {0, 0, 0, 0, -1, 0, -1, 0, -1, 0, -1, 0};
 
-__global__ void k_pass_i(const float* __restrict__ im, float* __restrict__ D, int m, int n, int o, int qs) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const int k = blockIdx.y;
-    const int l = blockIdx.z;
-    if (j >= n) return;
+// i-axis pass: CTA = one k slice x TJ consecutive j lines x all 6 channels.
+// The image neighbourhood of an i-chunk (rows j-q..j+TJ+q at k and k+q, i-q..i+CH+q)
+// is staged in shared memory with coalesced loads; each thread streams one
+// (channel, line) through the sequential box sum; outputs go through a shared
+// tile so that the six channel planes are written with coalesced stores.
+constexpr int TJ = 32;  // lines per CTA
+constexpr int CH = 32;  // i samples per chunk
+
+__global__ void __launch_bounds__(6 * TJ) k_pass_i(const float* __restrict__ im, float* __restrict__ D, int m, int n,
+                                                   int o, int qs) {
+    extern __shared__ float sm[];
+    const int W = CH + 2 * qs + 1;         // padded row length of the image tile
+    const int R = TJ + 2 * qs;             // image rows per k slice
+    float* T = sm;                         // [2][R][W]
+    float* O = sm + 2 * R * W;             // [6][TJ][CH+1]
+    const int k = blockIdx.y, j0 = blockIdx.x * TJ;
+    const int l = threadIdx.x / TJ, jj = threadIdx.x % TJ, j = j0 + jj;
     const int64_t mn = (int64_t)m * n, sz = mn * o;
     const int dx = c_dx[l] * qs, dy = c_dy[l] * qs, dz = c_dz[l] * qs;
-    const int jj = j + dx, kk = k + dz;
-    const bool line_ok = jj >= 0 && jj < n && kk >= 0 && kk < o;
-    const float* self = im + (int64_t)j * m + k * mn;
-    const float* other = im + (int64_t)jj * m + (int64_t)kk * mn;
-    float* out = D + l * sz + (int64_t)j * m + k * mn;
-    box_line(m, qs,
-             [&](int i) {
-                 const float s = self[i];
-                 const int ii = i + dy;
-                 const float v = (line_ok && ii >= 0 && ii < m) ? other[ii] : s;
-                 const float d = v - s;
-                 return d * d;
-             },
-             [&](int i, float v) { out[i] = v; });
+    const bool line_ok = j < n;
+    const bool other_ok = j + dx >= 0 && j + dx < n && k + dz < o;
+    const int kk = dz ? 1 : 0;
+    float ring[kRing];
+    float P = 0.0f;
+    for (int i0 = 0; i0 < m; i0 += CH) {
+        __syncthreads();  // previous chunk's tiles are consumed
+        for (int e = threadIdx.x; e < 2 * R * (CH + 2 * qs); e += blockDim.x) {
+            const int ip = e % (CH + 2 * qs), r = (e / (CH + 2 * qs)) % R, z = e / ((CH + 2 * qs) * R);
+            const int ii = i0 - qs + ip, jr = j0 - qs + r, kz = k + z * qs;
+            float v = 0.0f;
+            if (ii >= 0 && ii < m && jr >= 0 && jr < n && kz < o) v = im[ii + (int64_t)jr * m + (int64_t)kz * mn];
+            T[(z * R + r) * W + ip] = v;
+        }
+        __syncthreads();
+        const int cend = min(CH, m - i0);
+        if (line_ok) {
+            const float* self = T + (jj + qs) * W + qs;
+            const float* oth = T + (kk * R + jj + qs + dx) * W + qs + dy;
+            float* out = O + (l * TJ + jj) * (CH + 1);
+            for (int u = 0; u < cend; u++) {
+                const int t = i0 + u;
+                const float s = self[u];
+                const float v = (other_ok && t + dy >= 0 && t + dy < m) ? oth[u] : s;
+                const float d = v - s;
+                const float x = d * d;
+                P = (t == 0) ? x : P + x;
+                ring[t & (kRing - 1)] = P;
+                const int i = t - qs;  // output position (lag r = qs)
+                if (i >= 0) out[u] = (i <= qs) ? P : P - ring[(t - 2 * qs - 1) & (kRing - 1)];
+            }
+        }
+        __syncthreads();
+        // coalesced store of outputs i0-qs .. i0+cend-1-qs
+        for (int e = threadIdx.x; e < 6 * TJ * cend; e += blockDim.x) {
+            const int u = e % cend, line = e / cend;
+            const int ll = line / TJ, jl = line % TJ, jg = j0 + jl;
+            const int i = i0 + u - qs;
+            if (i >= 0 && jg < n) D[ll * sz + i + (int64_t)jg * m + (int64_t)k * mn] = O[(ll * TJ + jl) * (CH + 1) + u];
+        }
+    }
+    // tail: i in [m-qs, m): P[m-1] - P[i-qs-1]
+    if (line_ok) {
+        float* out = D + l * sz + (int64_t)j * m + (int64_t)k * mn;
+        for (int i = (m - qs > 0 ? m - qs : 0); i < m; i++) out[i] = P - ring[(i - qs - 1) & (kRing - 1)];
+    }
 }
 
 // In-place box pass along j (axis=1) or k (axis=2); threads over consecutive i.
+// Samples are loaded CHUNK at a time before any of the chunk's outputs (which
+// lag by r) are stored, so the loads of a chunk are independent.
+template <int CHUNK>
 __global__ void k_pass_jk(float* __restrict__ D, int m, int n, int o, int qs, int axis) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int b = blockIdx.y;  // the other coordinate: k for axis 1, j for axis 2
@@ -90,7 +114,24 @@ __global__ void k_pass_jk(float* __restrict__ D, int m, int n, int o, int qs, in
     int L;
     if (axis == 1) { base = D + l * sz + i + b * mn; stride = m; L = n; }
     else { base = D + l * sz + i + (int64_t)b * m; stride = mn; L = o; }
-    box_line(L, qs, [&](int t) { return base[t * stride]; }, [&](int t, float v) { base[t * stride] = v; });
+    float ring[kRing];
+    float P = 0.0f;
+    for (int c0 = 0; c0 < L; c0 += CHUNK) {
+        float x[CHUNK];
+#pragma unroll
+        for (int u = 0; u < CHUNK; u++) x[u] = (c0 + u < L) ? base[(c0 + u) * stride] : 0.0f;
+#pragma unroll
+        for (int u = 0; u < CHUNK; u++) {
+            const int t = c0 + u;
+            if (t < L) {
+                P = (t == 0) ? x[u] : P + x[u];
+                ring[t & (kRing - 1)] = P;
+                const int io = t - qs;
+                if (io >= 0) base[io * stride] = (io <= qs) ? P : P - ring[(t - 2 * qs - 1) & (kRing - 1)];
+            }
+        }
+    }
+    for (int io = (L - qs > 0 ? L - qs : 0); io < L; io++) base[io * stride] = P - ring[(io - qs - 1) & (kRing - 1)];
 }
 
 __global__ void k_quantise(const float* __restrict__ D, uint64_t* __restrict__ codes, int m, int n, int o, int qs,
@@ -131,16 +172,21 @@ __global__ void k_quantise(const float* __restrict__ D, uint64_t* __restrict__ c
 cudaError_t launch_mind_ssc(const float* d_im, int m, int n, int o, int qs, const float thr[5], float* d_scratch,
                             uint64_t* d_codes, cudaStream_t s) {
     {
-        dim3 blk(128), grd((n + 127) / 128, o, 6);
-        k_pass_i<<<grd, blk, 0, s>>>(d_im, d_scratch, m, n, o, qs);
+        const size_t smem = (size_t)(2 * (TJ + 2 * qs) * (CH + 2 * qs + 1) + 6 * TJ * (CH + 1)) * sizeof(float);
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(k_pass_i, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+        }
+        dim3 grd((n + TJ - 1) / TJ, o);
+        k_pass_i<<<grd, 6 * TJ, smem, s>>>(d_im, d_scratch, m, n, o, qs);
     }
     {
         dim3 blk(128), grd((m + 127) / 128, o, 6);
-        k_pass_jk<<<grd, blk, 0, s>>>(d_scratch, m, n, o, qs, 1);
+        k_pass_jk<8><<<grd, blk, 0, s>>>(d_scratch, m, n, o, qs, 1);
     }
     {
         dim3 blk(128), grd((m + 127) / 128, n, 6);
-        k_pass_jk<<<grd, blk, 0, s>>>(d_scratch, m, n, o, qs, 2);
+        k_pass_jk<8><<<grd, blk, 0, s>>>(d_scratch, m, n, o, qs, 2);
     }
     {
         dim3 blk(128), grd((m + 127) / 128, n, o);

@@ -62,6 +62,8 @@ struct deeds_ctx {
     long long stage_launches[DEEDS_NUM_STAGES] = {0};
     // cost-volume tile sizes chosen by the autotuner, per (m,n,o,g,hw,q)
     std::map<std::vector<int>, int> dc_tile;
+    // lanes of deeds_register_batch (child contexts on the same device)
+    std::vector<deeds_ctx*> lanes;
     // the last registration's full-resolution field (for deeds_warp_segmentation)
     bool have_field = false;
     int fm = 0, fn = 0, fo = 0;
@@ -330,7 +332,7 @@ deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTre
     int* d_arrived = dbuf<int>(ctx, "arrived_" + tag, pt.sz, &st);
     int* d_work = dbuf<int>(ctx, "work_" + tag, 1, &st);
     if (st) return st;
-    if (bp_down_smem_bytes(pt.max_width) > 200 * 1024)
+    if (bp_down_smem_bytes(pt.max_width, pt.n_levels) > 200 * 1024)
         return fail(ctx, DEEDS_ERR_INVALID, "MST breadth level of %d nodes is too wide", pt.max_width);
     CK(cudaMemcpyAsync(d_blk, h_blk, pt.total * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
     const BpTree bt = device_tree(pt, d_blk, h_blk, len, (float)q, u0, v0, w0);
@@ -387,6 +389,8 @@ deeds_status deeds_create(deeds_ctx** out, int device) {
 
 void deeds_destroy(deeds_ctx* ctx) {
     if (!ctx) return;
+    for (deeds_ctx* lane : ctx->lanes) deeds_destroy(lane);
+    ctx->lanes.clear();
     cudaSetDevice(ctx->device);
     for (cudaStream_t st : {ctx->stream, ctx->stream_b, ctx->side})
         if (st) cudaStreamSynchronize(st);
@@ -847,6 +851,63 @@ deeds_status deeds_register(deeds_ctx* ctx, const float* fixed, const float* mov
     CK(cudaMemcpyAsync(flow_out, d_flow, 3 * sz1 * sizeof(float), cudaMemcpyDeviceToHost, s));
     if (warped_out) CK(cudaMemcpyAsync(warped_out, d_w, sz * sizeof(float), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    return DEEDS_OK;
+}
+
+deeds_status deeds_register_batch(deeds_ctx* ctx, const deeds_pair* pairs, int n_pairs, const deeds_params* params,
+                                  int lanes) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (n_pairs < 0 || (n_pairs > 0 && !pairs)) return fail(ctx, DEEDS_ERR_INVALID, "bad pair list");
+    if (n_pairs == 0) return DEEDS_OK;
+    for (int i = 0; i < n_pairs; i++) {
+        const deeds_pair& p = pairs[i];
+        if (!p.fixed || !p.moving || !p.flow_out) return fail(ctx, DEEDS_ERR_INVALID, "pair %d: null pointer", i);
+        deeds_status st = check_params(ctx, params, p.m, p.n, p.o);
+        if (st) return fail(ctx, st, "pair %d: %s", i, ctx->err.c_str());
+    }
+    if (lanes <= 0) lanes = 3;
+    if (lanes > n_pairs) lanes = n_pairs;
+    while ((int)ctx->lanes.size() < lanes) {
+        deeds_ctx* lane = nullptr;
+        deeds_status st = deeds_create(&lane, ctx->device);
+        if (st) return fail(ctx, st, "batch lane: %s", deeds_last_error(nullptr));
+        lane->dc_tile = ctx->dc_tile;
+        ctx->lanes.push_back(lane);
+    }
+    std::atomic<int> next{0};
+    std::atomic<int> failed{-1};
+    std::vector<deeds_status> lane_st(lanes, DEEDS_OK);
+    std::vector<std::string> lane_err(lanes);
+    std::vector<std::thread> threads;
+    for (int li = 0; li < lanes; li++) {
+        threads.emplace_back([&, li]() {
+            deeds_ctx* lane = ctx->lanes[li];
+            float ident[16];
+            for (int i = 0; i < 16; i++) ident[i] = (i % 5 == 0) ? 1.0f : 0.0f;
+            for (;;) {
+                if (failed.load() >= 0) return;
+                const int i = next.fetch_add(1);
+                if (i >= n_pairs) return;
+                const deeds_pair& p = pairs[i];
+                const deeds_status st = deeds_register(lane, p.fixed, p.moving, p.m, p.n, p.o, p.X ? p.X : ident,
+                                                       params, p.flow_out, p.warped_out);
+                if (st) {
+                    lane_st[li] = st;
+                    lane_err[li] = "pair " + std::to_string(i) + ": " + lane->err;
+                    int expect = -1;
+                    failed.compare_exchange_strong(expect, li);
+                    return;
+                }
+            }
+        });
+    }
+    for (auto& t : threads) t.join();
+    for (deeds_ctx* lane : ctx->lanes)
+        for (auto& kv : lane->dc_tile) ctx->dc_tile.insert(kv);
+    if (failed.load() >= 0) {
+        const int li = failed.load();
+        return fail(ctx, lane_st[li], "%s", lane_err[li].c_str());
+    }
     return DEEDS_OK;
 }
 

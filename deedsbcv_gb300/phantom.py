@@ -22,17 +22,31 @@ import numpy as np
 from scipy import ndimage
 
 
+def _bspline_basis(size, spacing, n_ctrl):
+    """(size, n_ctrl) uniform cubic B-spline weights: voxel v sits at control
+    coordinate v/spacing + 1 (one control point of margin on each side)."""
+    t = np.arange(size, dtype=np.float64) / spacing + 1.0
+    f = np.floor(t).astype(int)
+    u = t - f
+    w = np.stack([(1 - u) ** 3, 3 * u ** 3 - 6 * u ** 2 + 4, -3 * u ** 3 + 3 * u ** 2 + 3 * u + 1, u ** 3], 1) / 6.0
+    B = np.zeros((size, n_ctrl))
+    for r in range(4):
+        B[np.arange(size), np.clip(f - 1 + r, 0, n_ctrl - 1)] += w[:, r]
+    return B
+
+
 def _bspline_field(shape, spacing, max_disp, rng):
-    """Smooth displacement field (3, m, n, o) from random control-point offsets."""
+    """Smooth displacement field (3, m, n, o) from random control-point offsets
+    on a grid of the given spacing, interpolated with cubic B-splines."""
     ctrl = tuple(int(np.ceil(s / spacing)) + 3 for s in shape)
     coarse = rng.uniform(-1.0, 1.0, size=(3,) + ctrl)
+    B = [_bspline_basis(shape[a], spacing, ctrl[a]) for a in range(3)]
     out = np.empty((3,) + tuple(shape), dtype=np.float32)
-    # control point c sits at voxel (c - 1) * spacing; cubic B-spline evaluation
-    coords = [np.arange(s, dtype=np.float64) / spacing + 1.0 for s in shape]
-    grid = np.meshgrid(*coords, indexing="ij")
     for d in range(3):
-        coef = ndimage.spline_filter(coarse[d], order=3, mode="nearest")
-        out[d] = ndimage.map_coordinates(coef, grid, order=3, mode="nearest", prefilter=False)
+        t = np.tensordot(B[0], coarse[d], axes=(1, 0))             # (m, c1, c2)
+        t = np.tensordot(t, B[1], axes=(1, 1))                     # (m, c2, n)
+        t = np.tensordot(t, B[2], axes=(1, 1))                     # (m, n, o)
+        out[d] = t
     peak = float(np.abs(out).max())
     if peak > 0:
         out *= np.float32(max_disp / peak)
@@ -41,23 +55,33 @@ def _bspline_field(shape, spacing, max_disp, rng):
 
 def _organ_labels(shape, n_organs, rng):
     m, n, o = shape
-    yy, xx, zz = np.meshgrid(np.arange(m, dtype=np.float32), np.arange(n, dtype=np.float32),
-                             np.arange(o, dtype=np.float32), indexing="ij")
-    c = np.array([m, n, o], dtype=np.float32) / 2
-    body_r = np.array([m, n, o], dtype=np.float32) * 0.45
-    body = ((yy - c[0]) / body_r[0]) ** 2 + ((xx - c[1]) / body_r[1]) ** 2 + ((zz - c[2]) / body_r[2]) ** 2 <= 1.0
+    dims = np.array([m, n, o], dtype=np.float32)
+    c = dims / 2
+    body_r = dims * 0.45
+    ax = [np.arange(s, dtype=np.float32) for s in shape]
+    body = (((ax[0] - c[0]) / body_r[0]) ** 2)[:, None, None] + (((ax[1] - c[1]) / body_r[1]) ** 2)[None, :, None] \
+        + (((ax[2] - c[2]) / body_r[2]) ** 2)[None, None, :] <= 1.0
     labels = np.zeros(shape, dtype=np.uint8)
     for lab in range(1, n_organs + 1):
         centre = c + rng.uniform(-0.45, 0.45, 3).astype(np.float32) * body_r
-        radii = rng.uniform(0.08, 0.22, 3).astype(np.float32) * np.array([m, n, o], dtype=np.float32)
+        radii = rng.uniform(0.08, 0.22, 3).astype(np.float32) * dims
         q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
         q = q.astype(np.float32)
-        dy, dx, dz = yy - centre[0], xx - centre[1], zz - centre[2]
-        r2 = np.zeros(shape, dtype=np.float32)
+        # the rotated ellipsoid lies inside the sphere of its largest radius
+        rmax = float(radii.max())
+        lo = [max(int(np.floor(centre[a] - rmax)), 0) for a in range(3)]
+        hi = [min(int(np.ceil(centre[a] + rmax)) + 1, shape[a]) for a in range(3)]
+        if any(h <= l for l, h in zip(lo, hi)):
+            continue
+        dy = (ax[0][lo[0]:hi[0]] - centre[0])[:, None, None]
+        dx = (ax[1][lo[1]:hi[1]] - centre[1])[None, :, None]
+        dz = (ax[2][lo[2]:hi[2]] - centre[2])[None, None, :]
+        r2 = np.zeros((hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]), dtype=np.float32)
         for a in range(3):
             proj = q[0, a] * dy + q[1, a] * dx + q[2, a] * dz
             r2 += (proj / radii[a]) ** 2
-        labels[(r2 <= 1.0) & body] = lab
+        sub = labels[lo[0]:hi[0], lo[1]:hi[1], lo[2]:hi[2]]
+        sub[(r2 <= 1.0) & body[lo[0]:hi[0], lo[1]:hi[1], lo[2]:hi[2]]] = lab
     return body, labels
 
 

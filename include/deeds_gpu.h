@@ -91,6 +91,26 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
                                 const float X[16], const deeds_params* params, float* d_flow_out,
                                 float* d_warped_out, void* stream);
 
+/* One pair of a batch: host buffers, any size (pairs of one batch may differ). */
+typedef struct deeds_pair {
+    const float* fixed;   /* m*n*o, raw intensities (params->intensity_shift is added) */
+    const float* moving;  /* m*n*o */
+    int m, n, o;
+    const float* X;       /* 16-float affine matrix, or NULL for identity */
+    float* flow_out;      /* 3*sz1 of the last level, as deeds_register */
+    float* warped_out;    /* m*n*o or NULL */
+} deeds_pair;
+
+/* Batched registration (no counterpart in the reference, which registers one
+ * pair per process): registers n_pairs independent pairs with `lanes` pairs in
+ * flight at a time.  Each lane is an internal context with its own streams and
+ * scratch; while one lane's pair waits for its host-built MSTs, the others keep
+ * the GPU busy.  Results are identical to calling deeds_register per pair.
+ * lanes <= 0 picks a default (3).  Synchronous; returns the first failing
+ * pair's status (its index in the message) after all lanes have stopped. */
+deeds_status deeds_register_batch(deeds_ctx* ctx, const deeds_pair* pairs, int n_pairs, const deeds_params* params,
+                                  int lanes);
+
 /* Warp a label volume with the last deeds_register() result: nearest-neighbour,
  * clamp-to-edge (the -S output, src/deedsBCV0.cpp:361-379 via warpAffineS,
  * src/dataCostD.h:241-266).  Host buffers; synchronous. */

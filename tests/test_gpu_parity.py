@@ -273,3 +273,27 @@ def test_invalid_arguments_raise(api):
         api.register(np.zeros((16, 16, 16), np.float32), np.zeros((16, 16, 16), np.float32), params=bad)
     with pytest.raises(DeedsError):
         api.apply_flow(np.zeros(7, np.float32), np.zeros((8, 8, 8), np.int16))
+
+
+def test_register_batch_matches_single_calls(api):
+    """Uneven pair sizes through deeds_register_batch give the per-pair results."""
+    from deedsbcv_gb300 import phantom
+    shapes = [(48, 40, 56), (56, 48, 40), (40, 56, 48), (64, 40, 48), (48, 48, 48)]
+    pairs = []
+    for i, sh in enumerate(shapes):
+        p = phantom.make_pair(sh, seed=50 + i, n_organs=5, max_disp=4.0)
+        pairs.append((p["fixed"], p["moving"]))
+    params = api.default_params(grid=[6, 5, 4], radius=[5, 4, 3], quant=[3, 2, 1])
+    single = [api.register(f, m, params=params, want_warped=False)[0] for f, m in pairs]
+    for lanes in (1, 3):
+        batched = api.register_batch(pairs, params=params, lanes=lanes)
+        for a, (b, _) in zip(single, batched):
+            assert same_bits(a, b)
+
+
+def test_register_batch_reports_bad_pair(api):
+    from deedsbcv_gb300._lib import DeedsError
+    ok = np.zeros((32, 32, 32), np.float32)
+    tiny = np.zeros((4, 4, 4), np.float32)
+    with pytest.raises(DeedsError, match="pair 1"):
+        api.register_batch([(ok, ok), (tiny, tiny)], params=api.default_params(grid=[4], radius=[2], quant=[1]))
