@@ -122,6 +122,16 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
         }
         for (;;) {
             const int p = t.parents[node];
+            const int c0 = t.child_ptr[p], c1 = t.child_ptr[p + 1];
+            // the parent's row still holds its data cost (it is only written after its
+            // own message): load it now, its latency hides behind the transform
+            float acc[NL];
+            const float* prow = cost + (int64_t)p * LEN3;
+#pragma unroll
+            for (int k = 0; k < NL; k++) {
+                const int l = tid + k * T;
+                acc[k] = l < LEN3 ? ld_cg(prow + l) : 0.0f;
+            }
             const float ox = __fdiv_rn(t.u0[p] - t.u0[node], t.q);
             const float oy = __fdiv_rn(t.v0[p] - t.v0[node], t.q);
             const float oz = __fdiv_rn(t.w0[p] - t.w0[node], t.q);
@@ -142,33 +152,38 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
                 arow[l] = ia[l];
             }
             mn = block_min(mn, red);  // ends with a barrier: all stores of this CTA precede
-            if (tid == 0) {
-                mins[node] = mn;
-                __threadfence();
-                const int nch = t.child_ptr[p + 1] - t.child_ptr[p];
-                s_last = atomicAdd(arrived + p, 1) == nch - 1;
-                __threadfence();
+            // *std::min_element (src/regularisation.h:222) starts from element 0 and only
+            // replaces it on '<': a NaN first element is the result, later NaNs are skipped
+            if (isnan(B[0])) mn = B[0];
+            if (c1 - c0 > 1) {
+                // siblings exist: the last of them to arrive continues with the parent
+                if (tid == 0) {
+                    mins[node] = mn;
+                    __threadfence();
+                    s_last = atomicAdd(arrived + p, 1) == c1 - c0 - 1;
+                    __threadfence();
+                }
+                __syncthreads();
+                if (!s_last) break;
             }
-            __syncthreads();
-            if (!s_last) break;
-            // last arriver: the parent's row = data cost + sum over children in
-            // MST ordering order of (message - min), then the parent continues
-            const int c0 = t.child_ptr[p], c1 = t.child_ptr[p + 1];
-            float acc[NL];
-            const float* prow = cost + (int64_t)p * LEN3;
-#pragma unroll
-            for (int k = 0; k < NL; k++) {
-                const int l = tid + k * T;
-                acc[k] = l < LEN3 ? ld_cg(prow + l) : 0.0f;
-            }
+            // the parent's row = data cost + sum over children in MST ordering
+            // order of (message - min); this CTA's own message is still in B
             for (int ci = c0; ci < c1; ci++) {
                 const int ch = t.children[ci];
-                const float mch = ld_cg(mins + ch);
-                const float* chrow = cost + (int64_t)ch * LEN3;
+                if (ch == node) {
 #pragma unroll
-                for (int k = 0; k < NL; k++) {
-                    const int l = tid + k * T;
-                    if (l < LEN3) acc[k] = acc[k] + (ld_cg(chrow + l) - mch);
+                    for (int k = 0; k < NL; k++) {
+                        const int l = tid + k * T;
+                        if (l < LEN3) acc[k] = acc[k] + (B[l] - mn);
+                    }
+                } else {
+                    const float mch = ld_cg(mins + ch);
+                    const float* chrow = cost + (int64_t)ch * LEN3;
+#pragma unroll
+                    for (int k = 0; k < NL; k++) {
+                        const int l = tid + k * T;
+                        if (l < LEN3) acc[k] = acc[k] + (ld_cg(chrow + l) - mch);
+                    }
                 }
             }
             if (p == t.root) {
@@ -181,6 +196,7 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
                 break;
             }
             const float e = t.edgemst[p];
+            __syncthreads();  // B (this message) has been consumed by every thread
 #pragma unroll
             for (int k = 0; k < NL; k++) {
                 const int l = tid + k * T;
@@ -232,6 +248,9 @@ __global__ void __launch_bounds__(1024) k_bp_down(BpTree t, const float* __restr
             if (ov < bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
         }
         if (lane == 0) {
+            // the reference scans with value=cost[0], index=0 and '<' (src/regularisation.h:258-279):
+            // a NaN at 0 keeps index 0, NaNs elsewhere never win
+            if (isnan(__ldcg(rr)) || bi < 0 || bi >= len3) bi = 0;
             s_sel[0] = bi;
             const int i = bi % len, j = (bi / len) % len, k = bi / (len * len);
             u1[root] = (float)(j - hw) * t.q + t.u0[root];
@@ -280,7 +299,11 @@ __global__ void __launch_bounds__(1024) k_bp_down(BpTree t, const float* __restr
                 cc = t.ordered[ti]; ppos = t.parent_pos[ti];
                 a0 = t.u0[cc]; a1 = t.v0[cc]; a2 = t.w0[cc];
             }
-            const int sp = prev[ppos - pb];
+            int sp = prev[ppos - pb];
+            if (sp < 0 || sp >= len3) {  // never for a completed upward pass; keeps reads in bounds
+                atomicCAS(err, 0, 2);
+                sp = 0;
+            }
             int l = allinds[(int64_t)cc * len3 + sp];
             if (l < 0 || l >= len3) {  // never for a completed upward pass; keeps reads in bounds
                 atomicCAS(err, 0, 2);

@@ -82,17 +82,19 @@ __global__ void __launch_bounds__(256) k_data_cost_tma(const __grid_constant__ C
                                                        float alpha1, int* __restrict__ err) {
     constexpr int S = G > 4 ? 2 : 1;  // x and z sampling stride (RAND_SAMPLES=1, src/dataCostD.h:141-155)
     constexpr int NX = (G + S - 1) / S, NZ = (G + S - 1) / S;
-    constexpr int NS = NX * NZ * G;
+    constexpr int NC = NX * NZ;       // sampled (x, z) columns per node
+    constexpr int WN = 32 / G;        // nodes per warp: lane = node * G + i
+    constexpr int CHUNK = 8;          // labels accumulated per pass over the columns
     extern __shared__ __align__(128) uint64_t smem_raw[];
     // TMA destinations must start on 128-byte boundaries: align explicitly
     uint64_t* smem = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
     __shared__ __align__(8) uint64_t bars[2];
     __shared__ int s_ok;
-    const int box = NZ * NX * yb;
-    const int bstride = (box + 15) & ~15;  // each TMA destination starts on a 128-byte boundary
+    const int box = NC * yb;
+    const int bstride = (box + 15) & ~15;
     uint64_t* buf0 = smem;
     uint64_t* buf1 = smem + bstride;
-    uint64_t* Fs = smem + 2 * bstride;
+    int* red = reinterpret_cast<int*>(smem + 2 * bstride);  // [warps][len][32] partial sums
     const int m1 = m / G, n1 = n / G;
     const int tiles_y = (m1 + ny_tile - 1) / ny_tile;
     int b = blockIdx.x;
@@ -102,13 +104,14 @@ __global__ void __launch_bounds__(256) k_data_cost_tma(const __grid_constant__ C
     const int lz = blockIdx.y;
     const int y_first = ty * ny_tile;
     const int ny_here = min(ny_tile, m1 - y_first);
-    const int y0 = y_first * G;  // padded y of the tile's first sampled voxel shifted by -pad
+    const int y0 = y_first * G;  // padded y of the tile's first row (the pad offset cancels)
     const int y_al = y0 & ~1;    // TMA: the innermost coordinate must be 16-byte aligned
     const int yoff = y0 - y_al;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int len2 = len * len, len3 = len2 * len;
     const int64_t mn = (int64_t)m * n;
     const uint32_t box_bytes = (uint32_t)box * 8u;
+    const int xbase = nxn * G, zbase = nzn * G + lz * q;
     if (tid == 0) {
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
@@ -116,7 +119,6 @@ __global__ void __launch_bounds__(256) k_data_cost_tma(const __grid_constant__ C
         s_ok = 1;
     }
     __syncthreads();
-    const int xbase = nxn * G, zbase = nzn * G + lz * q;
     if (tid == 0) {
         mbar_expect_tx(&bars[0], box_bytes);
         tma_load_3d(buf0, &map, &bars[0], y_al, xbase, zbase);
@@ -125,42 +127,62 @@ __global__ void __launch_bounds__(256) k_data_cost_tma(const __grid_constant__ C
             tma_load_3d(buf1, &map, &bars[1], y_al, xbase + q, zbase);
         }
     }
-    // the tile's sampled fixed codes, node-major, (k, j, i) within a node
-    for (int e = tid; e < ny_here * NS; e += blockDim.x) {
-        const int nn = e / NS, s = e % NS;
-        const int i = s % G, j = (s / G) % NX, k = s / (G * NX);
-        Fs[e] = F[(y0 + nn * G + i) + (int64_t)(xbase + j * S) * m + (int64_t)(nzn * G + k * S) * mn];
+    // this lane's node (within the tile) and sample row i; its fixed codes stay in registers
+    const int wn = lane / G, i = lane - (lane / G) * G;
+    const int tn = warp * WN + wn;  // node index within the tile
+    const bool active = lane < WN * G && tn < ny_here;
+    uint64_t fr[NC];
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+        const int j = c % NX, k = c / NX;
+        fr[c] = active ? F[(y0 + tn * G + i) + (int64_t)(xbase + j * S) * m + (int64_t)(nzn * G + k * S) * mn] : 0ull;
     }
-    const int work = ny_here * len;
-    const int nn = tid / len, ly = tid - (tid / len) * len;
+    int* wred = red + warp * len * 32;
+    const int pos = yoff + tn * G + i;  // this lane's row in the box (for label ly add ly*q)
     for (int lx = 0; lx < len; lx++) {
         const int slot = lx & 1;
-        uint64_t* sb = slot ? buf1 : buf0;
+        const uint64_t* sb = slot ? buf1 : buf0;
         if (tid == 0) {
             if (!mbar_wait_bounded(&bars[slot], (uint32_t)((lx >> 1) & 1))) s_ok = 0;
         }
         __syncthreads();
         if (!s_ok) break;
-        if (tid < work) {
-            const uint64_t* srow = sb + yoff + nn * G + ly * q;
-            const uint64_t* frow = Fs + nn * NS;
-            int acc = 0;
+        if (active) {
+            for (int ly0 = 0; ly0 < len; ly0 += CHUNK) {
+                int acc[CHUNK];
 #pragma unroll
-            for (int k = 0; k < NZ; k++)
+                for (int u = 0; u < CHUNK; u++) acc[u] = 0;
 #pragma unroll
-                for (int j = 0; j < NX; j++) {
-                    const uint64_t* sr = srow + (k * NX + j) * yb;
+                for (int c = 0; c < NC; c++) {
+                    const uint64_t* col = sb + c * yb + pos + ly0 * q;
 #pragma unroll
-                    for (int i = 0; i < G; i++) acc += __popcll(frow[(k * NX + j) * G + i] ^ sr[i]);
+                    for (int u = 0; u < CHUNK; u++)
+                        if (ly0 + u < len) acc[u] += __popcll(fr[c] ^ col[u * q]);
                 }
-            const int node = (y_first + nn) + nxn * m1 + nzn * m1 * n1;
-            cost[(int64_t)node * len3 + ly + lx * len + lz * len2] = __fmul_rn((float)acc, alpha1);
+#pragma unroll
+                for (int u = 0; u < CHUNK; u++)
+                    if (ly0 + u < len) wred[(ly0 + u) * 32 + lane] = acc[u];
+            }
         }
-        __syncthreads();  // every thread is done with this buffer
+        __syncwarp();
+        // sum the G sample rows of each (node, ly) of this warp
+        for (int e = lane; e < WN * len; e += 32) {
+            const int en = e / len, ly = e - (e / len) * len;
+            const int node_t = warp * WN + en;
+            if (node_t < ny_here) {
+                const int* r = wred + ly * 32 + en * G;
+                int sum = 0;
+#pragma unroll
+                for (int ii = 0; ii < G; ii++) sum += r[ii];
+                const int node = (y_first + node_t) + nxn * m1 + nzn * m1 * n1;
+                cost[(int64_t)node * len3 + ly + lx * len + lz * len2] = __fmul_rn((float)sum, alpha1);
+            }
+        }
+        __syncthreads();  // every thread is done with this buffer and with wred
         if (tid == 0 && lx + 2 < len) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_expect_tx(&bars[slot], box_bytes);
-            tma_load_3d(sb, &map, &bars[slot], y_al, xbase + (lx + 2) * q, zbase);
+            tma_load_3d(const_cast<uint64_t*>(sb), &map, &bars[slot], y_al, xbase + (lx + 2) * q, zbase);
         }
     }
     if (!s_ok && tid == 0) {
@@ -226,12 +248,20 @@ EncodeTiledFn encode_fn() {
     return fn;
 }
 
+size_t data_cost_tma_smem(int g, int hw, int q, int ny_tile) {
+    const int S = g > 4 ? 2 : 1, NX = (g + S - 1) / S;
+    const int len = 2 * hw + 1;
+    const int yb = ((ny_tile * g + (len - 1) * q + 1) + 1) & ~1;
+    const int warps = (ny_tile + (32 / g) - 1) / (32 / g);
+    return (size_t)2 * ((NX * NX * yb + 15) & ~15) * 8 + (size_t)warps * len * 32 * 4 + 128;
+}
+
 template <int G>
 cudaError_t launch_tma(const uint64_t* d_F, const uint64_t* d_Mp, int mpp, int np, int op, int m, int n, int o,
                        int hw, int q, int ny_tile, float alpha1, float* d_cost, int* d_err, cudaStream_t s) {
     constexpr int S = G > 4 ? 2 : 1;
     constexpr int NX = (G + S - 1) / S, NZ = (G + S - 1) / S;
-    constexpr int NS = NX * NZ * G;
+    constexpr int WN = 32 / G;
     const int len = 2 * hw + 1;
     const int yb = ((ny_tile * G + (len - 1) * q + 1) + 1) & ~1;  // +1 for the alignment shift, rounded to even
     CUtensorMap map;
@@ -245,14 +275,14 @@ cudaError_t launch_tma(const uint64_t* d_F, const uint64_t* d_Mp, int mpp, int n
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return cudaErrorInvalidValue;
-    const size_t smem = (size_t)(2 * ((NZ * NX * yb + 15) & ~15) + ny_tile * NS) * sizeof(uint64_t) + 128;
+    const int warps = (ny_tile + WN - 1) / WN;
+    const size_t smem = data_cost_tma_smem(G, hw, q, ny_tile);
     cudaError_t e = cudaFuncSetAttribute(k_data_cost_tma<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const int m1 = m / G, n1 = n / G, o1 = o / G;
     const int tiles_y = (m1 + ny_tile - 1) / ny_tile;
-    const int threads = ((ny_tile * len + 31) / 32) * 32;
     dim3 grid((unsigned)(tiles_y * n1 * o1), (unsigned)len);
-    k_data_cost_tma<G><<<grid, threads, smem, s>>>(map, d_F, d_cost, m, n, o, len, q, ny_tile, yb, alpha1, d_err);
+    k_data_cost_tma<G><<<grid, warps * 32, smem, s>>>(map, d_F, d_cost, m, n, o, len, q, ny_tile, yb, alpha1, d_err);
     count_launches(1);
     return cudaGetLastError();
 }
@@ -262,12 +292,11 @@ cudaError_t launch_tma(const uint64_t* d_F, const uint64_t* d_Mp, int mpp, int n
 bool data_cost_tma_supported(int g, int hw, int q, int ny_tile) {
     if (g < 2 || g > 8 || ny_tile < 1) return false;
     const int len = 2 * hw + 1;
-    if (ny_tile * len > 256) return false;
+    const int warps = (ny_tile + (32 / g) - 1) / (32 / g);
+    if (warps * 32 > 256) return false;
     const int yb = ((ny_tile * g + (len - 1) * q + 1) + 1) & ~1;
     if (yb > 256) return false;
-    const int S = g > 4 ? 2 : 1, NX = (g + S - 1) / S;
-    const size_t smem = (size_t)(2 * ((NX * NX * yb + 15) & ~15) + ny_tile * NX * NX * g) * 8 + 128;
-    return smem <= 200 * 1024 && encode_fn() != nullptr;
+    return data_cost_tma_smem(g, hw, q, ny_tile) <= 200 * 1024 && encode_fn() != nullptr;
 }
 
 size_t padded_codes_count(int m, int n, int o, int pad) {

@@ -210,7 +210,8 @@ cudaError_t data_cost_auto(deeds_ctx* ctx, const uint64_t* F, const uint64_t* M,
     if (it != ctx->dc_tile.end()) {
         tile = it->second;
     } else {
-        static const int cands[] = {2, 4, 6, 8, 12, 16, 24};
+        const int wn = 32 / g;  // nodes per warp of the TMA kernel
+        const int cands[] = {wn, 2 * wn, 3 * wn, 4 * wn, 6 * wn, 8 * wn};
         tile = 0;
         float best = 1e30f;
         cudaEvent_t a, b;

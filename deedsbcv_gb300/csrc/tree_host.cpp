@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <stdexcept>
 #include <vector>
 
 #include "tree_host.h"
@@ -131,6 +132,7 @@ void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int 
             if (ok[nb]) heap.push(QueuedEdge{w[(size_t)nb * sz + last], (uint32_t)last * 8u + (uint32_t)nb});
         int from = -1, to = -1;
         while (to < 0) {
+            if (heap.empty()) throw std::runtime_error("Prim: candidate heap exhausted (disconnected grid)");
             const QueuedEdge e = heap.pop();
             const int ef = (int)(e.from_dir >> 3), et = ef + off[e.from_dir & 7u];
             const bool a = in_tree[ef], b = in_tree[et];

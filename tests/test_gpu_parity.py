@@ -293,7 +293,21 @@ def test_register_batch_matches_single_calls(api):
 
 def test_register_batch_reports_bad_pair(api):
     from deedsbcv_gb300._lib import DeedsError
-    ok = np.zeros((32, 32, 32), np.float32)
-    tiny = np.zeros((4, 4, 4), np.float32)
+    rng = np.random.default_rng(3)
+    ok = rng.normal(0, 100, (32, 32, 32)).astype(np.float32)
+    tiny = rng.normal(0, 100, (2, 2, 2)).astype(np.float32)  # too small for a MIND radius of 1
     with pytest.raises(DeedsError, match="pair 1"):
-        api.register_batch([(ok, ok), (tiny, tiny)], params=api.default_params(grid=[4], radius=[2], quant=[1]))
+        api.register_batch([(ok, ok), (tiny, tiny)], params=api.default_params(grid=[2], radius=[2], quant=[1]))
+
+
+def test_constant_images_follow_reference_nan_semantics(api):
+    """A constant image has zero intensity spread, so the MST edge weights are
+    -exp(-0/0) = NaN in the reference as well; the registration must still run
+    and pick the same labels as the oracle (index 0 where every cost is NaN)."""
+    shape = (32, 24, 40)
+    flat = np.zeros(shape, np.float32)
+    params = api.default_params(grid=[6, 4], radius=[3, 2], quant=[2, 1])
+    flow, _ = api.register(flat, flat, params=params, want_warped=False)
+    f = flat.ravel(order="F") + np.float32(1024)
+    ref = orc.register(f, f, *shape, G=(6, 4), L=(3, 2), Q=(2, 1))
+    assert same_bits(flow, ref)
