@@ -22,6 +22,7 @@
 #include <future>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -60,8 +61,12 @@ struct deeds_ctx {
     std::vector<Mark> marks;
     double stage_ms[DEEDS_NUM_STAGES] = {0};
     long long stage_launches[DEEDS_NUM_STAGES] = {0};
-    // cost-volume tile sizes chosen by the autotuner, per (m,n,o,g,hw,q)
-    std::map<std::vector<int>, int> dc_tile;
+    // cost-volume tile sizes chosen by the autotuner, per (g, hw, q); shared with batch lanes
+    struct TuneTable {
+        std::mutex mu;
+        std::map<std::vector<int>, int> tile;
+    };
+    std::shared_ptr<TuneTable> tune = std::make_shared<TuneTable>();
     // lanes of deeds_register_batch (child contexts on the same device)
     std::vector<deeds_ctx*> lanes;
     // the last registration's full-resolution field (for deeds_warp_segmentation)
@@ -204,10 +209,12 @@ cudaError_t data_cost_auto(deeds_ctx* ctx, const uint64_t* F, const uint64_t* M,
     int sy, sx, sz;
     float alpha1;
     data_cost_params(g, q, alpha, &sy, &sx, &sz, &alpha1);
-    const std::vector<int> key{m, n, o, g, hw, q};
-    auto it = ctx->dc_tile.find(key);
+    // the best tile depends on the level parameters, not on the volume size
+    const std::vector<int> key{g, hw, q};
+    std::lock_guard<std::mutex> lock(ctx->tune->mu);
+    auto it = ctx->tune->tile.find(key);
     int tile;
-    if (it != ctx->dc_tile.end()) {
+    if (it != ctx->tune->tile.end()) {
         tile = it->second;
     } else {
         const int wn = 32 / g;  // nodes per warp of the TMA kernel
@@ -230,8 +237,9 @@ cudaError_t data_cost_auto(deeds_ctx* ctx, const uint64_t* F, const uint64_t* M,
         }
         cudaEventDestroy(a);
         cudaEventDestroy(b);
-        ctx->dc_tile[key] = tile;
+        ctx->tune->tile[key] = tile;
     }
+    if (tile > m / g) tile = 0;  // tuned on a larger volume: this one has fewer grid rows
     if (tile > 0) return launch_data_cost_tma(F, M, Mpad, m, n, o, g, hw, q, tile, alpha1, cost, d_err, s);
     return launch_data_cost(F, M, m, n, o, g, hw, q, sy, sx, sz, alpha1, cost, s);
 }
@@ -346,6 +354,96 @@ deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTre
         CK(launch_bp_down(bt, d_cost, d_allinds, u1, v1, w1, d_err, s));
     }
     return DEEDS_OK;
+}
+
+// Every buffer one registration of an m x n x o pair needs, sized up front so
+// that nothing is reallocated (cudaFree) while kernels of the pair are in flight.
+struct PairBuffers {
+    size_t max_sz1 = 0, max_cost = 0, max_pad = 0;
+    std::vector<int> m1s, n1s, o1s;
+    float *fix, *mov, *warp0;
+    uint64_t *c_fix, *c_mov;
+    int* d_err;
+    float* warped[2];
+    uint64_t* c_warp[2];
+    float* mind_scr[2];
+    float* cost[2];
+    short* allinds[2];
+    uint64_t* mpad[2];
+    float *grid, *ku, *kv, *kw, *cons_scr, *h_fix, *h_w0;
+    std::vector<float*> h_sad, d_sad;
+    std::vector<PackedTree> pts;
+    std::vector<uint32_t*> h_tree;
+};
+
+deeds_status acquire_buffers(deeds_ctx* ctx, int m, int n, int o, const deeds_params* P, PairBuffers& B) {
+    deeds_status st = DEEDS_OK;
+    const int L = P->levels;
+    const size_t sz = (size_t)m * n * o;
+    B.m1s.assign(L, 0); B.n1s.assign(L, 0); B.o1s.assign(L, 0);
+    for (int l = 0; l < L; l++) {
+        const int g = P->grid[l], len = 2 * P->radius[l] + 1;
+        B.m1s[l] = m / g; B.n1s[l] = n / g; B.o1s[l] = o / g;
+        const size_t sz1 = (size_t)B.m1s[l] * B.n1s[l] * B.o1s[l];
+        B.max_sz1 = std::max(B.max_sz1, sz1);
+        B.max_cost = std::max(B.max_cost, sz1 * len * len * len);
+        B.max_pad = std::max(B.max_pad, padded_codes_count(m, n, o, P->quant[l] * P->radius[l]));
+    }
+    B.fix = dbuf<float>(ctx, "fix", sz, &st);
+    B.mov = dbuf<float>(ctx, "mov", sz, &st);
+    B.warp0 = dbuf<float>(ctx, "warp0", sz, &st);
+    B.c_fix = dbuf<uint64_t>(ctx, "c_fix", sz, &st);
+    B.c_mov = dbuf<uint64_t>(ctx, "c_mov", sz, &st);
+    B.d_err = dbuf<int>(ctx, "err", 2, &st);
+    const char* tags[2] = {"f", "b"};
+    for (int d = 0; d < 2; d++) {
+        const std::string tg = tags[d];
+        B.warped[d] = dbuf<float>(ctx, "warped_" + tg, sz, &st);
+        B.c_warp[d] = dbuf<uint64_t>(ctx, "c_warp_" + tg, sz, &st);
+        B.mind_scr[d] = dbuf<float>(ctx, "mind_" + tg, 6 * sz, &st);
+        B.cost[d] = dbuf<float>(ctx, "cost_" + tg, B.max_cost, &st);
+        B.allinds[d] = dbuf<short>(ctx, "allinds_" + tg, B.max_cost, &st);
+        B.mpad[d] = dbuf<uint64_t>(ctx, "mpad_" + tg, B.max_pad, &st);
+        dbuf<uint32_t>(ctx, "tree_" + tg, pack_layout((int)B.max_sz1).total, &st);
+        dbuf<float>(ctx, "mins_" + tg, B.max_sz1, &st);
+        dbuf<int>(ctx, "arrived_" + tg, B.max_sz1, &st);
+        dbuf<int>(ctx, "work_" + tg, 1, &st);
+    }
+    B.grid = dbuf<float>(ctx, "grid", 18 * B.max_sz1, &st);
+    B.ku = dbuf<float>(ctx, "keep_u", sz, &st);
+    B.kv = dbuf<float>(ctx, "keep_v", sz, &st);
+    B.kw = dbuf<float>(ctx, "keep_w", sz, &st);
+    B.cons_scr = dbuf<float>(ctx, "consistent", 12 * B.max_sz1, &st);
+    B.h_fix = hbuf<float>(ctx, "h_fix", sz, &st);
+    B.h_w0 = hbuf<float>(ctx, "h_w0", sz, &st);
+    B.h_sad.assign(2 * L, nullptr); B.d_sad.assign(2 * L, nullptr);
+    B.pts.assign(2 * L, PackedTree()); B.h_tree.assign(2 * L, nullptr);
+    for (int l = 0; l < L; l++) {
+        const size_t sz1 = (size_t)B.m1s[l] * B.n1s[l] * B.o1s[l];
+        for (int d = 0; d < 2; d++) {
+            const int t = 2 * l + d;
+            B.h_sad[t] = hbuf<float>(ctx, "h_sad" + std::to_string(t), 6 * sz1, &st);
+            B.pts[t] = pack_layout((int)sz1);
+            B.h_tree[t] = hbuf<uint32_t>(ctx, "h_tree" + std::to_string(t), B.pts[t].total, &st);
+            B.d_sad[t] = dbuf<float>(ctx, "sad" + std::to_string(t), 6 * sz1, &st);
+        }
+    }
+    return st;
+}
+
+// The buffers of deeds_register (host inputs/outputs included) for one pair size.
+deeds_status reserve_buffers(deeds_ctx* ctx, int m, int n, int o, const deeds_params* P, bool warped) {
+    PairBuffers B;
+    deeds_status st = acquire_buffers(ctx, m, n, o, P, B);
+    if (st) return st;
+    const size_t sz = (size_t)m * n * o;
+    const int gl = P->grid[P->levels - 1];
+    const size_t sz1 = (size_t)(m / gl) * (n / gl) * (o / gl);
+    dbuf<float>(ctx, "in_fixed", sz, &st);
+    dbuf<float>(ctx, "in_moving", sz, &st);
+    dbuf<float>(ctx, "out_flow", 3 * sz1, &st);
+    if (warped) dbuf<float>(ctx, "out_warped", sz, &st);
+    return st;
 }
 
 }  // namespace
@@ -595,67 +693,37 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
     float thr[5];
     mind_thresholds(thr);
 
-    // ---- sizes
-    size_t max_cost = 0, max_sz1 = 0;
-    std::vector<int> m1s(L), n1s(L), o1s(L);
-    for (int l = 0; l < L; l++) {
-        const int g = P->grid[l], len = 2 * P->radius[l] + 1;
-        m1s[l] = m / g; n1s[l] = n / g; o1s[l] = o / g;
-        const size_t sz1 = (size_t)m1s[l] * n1s[l] * o1s[l];
-        max_sz1 = std::max(max_sz1, sz1);
-        max_cost = std::max(max_cost, sz1 * len * len * len);
-    }
-    // ---- buffers: everything is sized up front, so nothing is reallocated
-    // (cudaFree) while kernels of this pair are in flight
-    float* fix = dbuf<float>(ctx, "fix", sz, &st);
-    float* mov = dbuf<float>(ctx, "mov", sz, &st);
-    float* warp0 = dbuf<float>(ctx, "warp0", sz, &st);
-    uint64_t* c_fix = dbuf<uint64_t>(ctx, "c_fix", sz, &st);
-    uint64_t* c_mov = dbuf<uint64_t>(ctx, "c_mov", sz, &st);
-    int* d_err = dbuf<int>(ctx, "err", 2, &st);
-    float* warped[2];
-    uint64_t* c_warp[2];
-    float* mind_scr[2];
-    float* cost[2];
-    short* allinds[2];
-    uint64_t* mpad[2];
-    size_t max_pad = 0;
-    for (int l = 0; l < L; l++) max_pad = std::max(max_pad, padded_codes_count(m, n, o, P->quant[l] * P->radius[l]));
-    const char* tags[2] = {"f", "b"};
-    for (int d = 0; d < 2; d++) {
-        const std::string tg = tags[d];
-        warped[d] = dbuf<float>(ctx, "warped_" + tg, sz, &st);
-        c_warp[d] = dbuf<uint64_t>(ctx, "c_warp_" + tg, sz, &st);
-        mind_scr[d] = dbuf<float>(ctx, "mind_" + tg, 6 * sz, &st);
-        cost[d] = dbuf<float>(ctx, "cost_" + tg, max_cost, &st);
-        allinds[d] = dbuf<short>(ctx, "allinds_" + tg, max_cost, &st);
-        mpad[d] = dbuf<uint64_t>(ctx, "mpad_" + tg, max_pad, &st);
-        dbuf<uint32_t>(ctx, "tree_" + tg, pack_layout((int)max_sz1).total, &st);
-        dbuf<float>(ctx, "mins_" + tg, max_sz1, &st);
-        dbuf<int>(ctx, "arrived_" + tg, max_sz1, &st);
-        dbuf<int>(ctx, "work_" + tg, 1, &st);
-    }
-    float* grid = dbuf<float>(ctx, "grid", 18 * max_sz1, &st);  // fields on the control grids
-    float* ku = dbuf<float>(ctx, "keep_u", sz, &st);
-    float* kv = dbuf<float>(ctx, "keep_v", sz, &st);
-    float* kw = dbuf<float>(ctx, "keep_w", sz, &st);
-    float* cons_scr = dbuf<float>(ctx, "consistent", 12 * max_sz1, &st);
-    float* h_fix = hbuf<float>(ctx, "h_fix", sz, &st);
-    float* h_w0 = hbuf<float>(ctx, "h_w0", sz, &st);
-    std::vector<float*> h_sad(2 * L), d_sad(2 * L);
-    std::vector<PackedTree> pts(2 * L);
-    std::vector<uint32_t*> h_tree(2 * L);
-    for (int l = 0; l < L; l++) {
-        const size_t sz1 = (size_t)m1s[l] * n1s[l] * o1s[l];
-        for (int d = 0; d < 2; d++) {
-            const int t = 2 * l + d;
-            h_sad[t] = hbuf<float>(ctx, "h_sad" + std::to_string(t), 6 * sz1, &st);
-            pts[t] = pack_layout((int)sz1);
-            h_tree[t] = hbuf<uint32_t>(ctx, "h_tree" + std::to_string(t), pts[t].total, &st);
-            d_sad[t] = dbuf<float>(ctx, "sad" + std::to_string(t), 6 * sz1, &st);
-        }
-    }
+    PairBuffers B;
+    st = acquire_buffers(ctx, m, n, o, P, B);
     if (st) return st;
+    const size_t max_sz1 = B.max_sz1;
+    const std::vector<int>& m1s = B.m1s;
+    const std::vector<int>& n1s = B.n1s;
+    const std::vector<int>& o1s = B.o1s;
+    float* fix = B.fix;
+    float* mov = B.mov;
+    float* warp0 = B.warp0;
+    uint64_t* c_fix = B.c_fix;
+    uint64_t* c_mov = B.c_mov;
+    int* d_err = B.d_err;
+    float** warped = B.warped;
+    uint64_t** c_warp = B.c_warp;
+    float** mind_scr = B.mind_scr;
+    float** cost = B.cost;
+    short** allinds = B.allinds;
+    uint64_t** mpad = B.mpad;
+    const char* tags[2] = {"f", "b"};
+    float* grid = B.grid;
+    float* ku = B.ku;
+    float* kv = B.kv;
+    float* kw = B.kw;
+    float* cons_scr = B.cons_scr;
+    float* h_fix = B.h_fix;
+    float* h_w0 = B.h_w0;
+    std::vector<float*>& h_sad = B.h_sad;
+    std::vector<float*>& d_sad = B.d_sad;
+    std::vector<PackedTree>& pts = B.pts;
+    std::vector<uint32_t*>& h_tree = B.h_tree;
     float* prev[6];  // u1 v1 w1 u1i v1i w1i on the previous grid
     float* cur0[6];  // u0 v0 w0 on the current grid, per direction
     float* nxt[6];   // new fields on the current grid
@@ -872,8 +940,16 @@ deeds_status deeds_register_batch(deeds_ctx* ctx, const deeds_pair* pairs, int n
         deeds_ctx* lane = nullptr;
         deeds_status st = deeds_create(&lane, ctx->device);
         if (st) return fail(ctx, st, "batch lane: %s", deeds_last_error(nullptr));
-        lane->dc_tile = ctx->dc_tile;
+        lane->tune = ctx->tune;
         ctx->lanes.push_back(lane);
+    }
+    // size every lane's buffers for the largest pair up front: growing a buffer
+    // mid-batch would cudaFree, which synchronises the whole device
+    for (deeds_ctx* lane : ctx->lanes) {
+        for (int i = 0; i < n_pairs; i++) {
+            deeds_status st = reserve_buffers(lane, pairs[i].m, pairs[i].n, pairs[i].o, params, pairs[i].warped_out != nullptr);
+            if (st) return fail(ctx, st, "batch lane: %s", lane->err.c_str());
+        }
     }
     std::atomic<int> next{0};
     std::atomic<int> failed{-1};
@@ -903,8 +979,6 @@ deeds_status deeds_register_batch(deeds_ctx* ctx, const deeds_pair* pairs, int n
         });
     }
     for (auto& t : threads) t.join();
-    for (deeds_ctx* lane : ctx->lanes)
-        for (auto& kv : lane->dc_tile) ctx->dc_tile.insert(kv);
     if (failed.load() >= 0) {
         const int li = failed.load();
         return fail(ctx, lane_st[li], "%s", lane_err[li].c_str());
