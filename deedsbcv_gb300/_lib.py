@@ -24,8 +24,9 @@ EXPORTS = [
     "deeds_prims_from_sad", "deeds_tree_bp_dev", "deeds_upsample_dev", "deeds_warp_affine_dev",
     "deeds_warp_image_dev", "deeds_warp_seg_dev", "deeds_consistent_dev", "deeds_jacobian_dev",
     "deeds_set_profiling", "deeds_stage_times", "deeds_reset_stage_times", "deeds_kernel_launches",
-    "deeds_measure_popc_rate", "deeds_register_batch",
+    "deeds_measure_popc_rate", "deeds_register_batch", "deeds_consistent_noalloc_dev",
 ]
+NOALLOC_MAX_NODES = 131072
 STAGES = ["mind", "datacost", "mst_edges", "bp_up", "bp_down", "transform", "consistent", "tree_wait"]
 
 
@@ -102,6 +103,7 @@ def load():
     L.deeds_kernel_launches.argtypes = []
     L.deeds_measure_popc_rate.argtypes = [P, P]
     L.deeds_register_batch.argtypes = [P, P, I, C.POINTER(DeedsParams), I]
+    L.deeds_consistent_noalloc_dev.argtypes = [P, P, P, P, P, P, I, I, I, I, P]
     for name in EXPORTS:
         fn = getattr(L, name)
         if name not in ("deeds_default_params", "deeds_destroy", "deeds_last_error", "deeds_version"):

@@ -30,7 +30,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompil
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread", "-Wall", "-Wno-unused-function",
              f"-I{CUDA_HOME}/include"]
 
-CU_SOURCES = ["mind.cu", "datacost.cu", "mst.cu", "bp.cu", "transform.cu"]
+CU_SOURCES = ["mind.cu", "datacost.cu", "mst.cu", "bp.cu", "transform.cu", "noalloc.cu"]
 CPP_SOURCES = ["pipeline.cpp", "tree_host.cpp"]
 CLI_SOURCES = {"deedsBCV": ["deedsBCV.cpp", "cli_common.cpp"], "applyBCV": ["applyBCV.cpp", "cli_common.cpp"],
                "applyBCVfloat": ["applyBCV.cpp", "cli_common.cpp"]}

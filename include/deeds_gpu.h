@@ -184,6 +184,23 @@ deeds_status deeds_warp_seg_dev(const int16_t* d_in, const float X[16], const fl
 deeds_status deeds_consistent_dev(deeds_ctx* ctx, float* d_u, float* d_v, float* d_w, float* d_u2, float* d_v2,
                                   float* d_w2, int m, int n, int o, int g, void* stream);
 
+/* consistentMappingCL() for callers that cannot allocate device memory while
+ * they run (no counterpart in the reference): host frameworks whose memory pool
+ * owns the device, real-time loops that size everything at start-up, and code
+ * that must not block on the device synchronisation cudaMalloc/cudaFree can
+ * imply.  Same kernels and results as deeds_consistent_dev, but the 12 grid
+ * fields of scratch live in a fixed device array of DEEDS_NOALLOC_MAX_NODES
+ * nodes that every GPU loading the library holds (6 MiB) until exit; no context
+ * is needed and nothing is allocated.  Grids with more than
+ * DEEDS_NOALLOC_MAX_NODES nodes are rejected with DEEDS_ERR_INVALID.  The first
+ * call on a device resolves the array's device address (with that device
+ * current), so make it before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race.  Errors are reported by status only (no
+ * message is recorded, as that would allocate). */
+#define DEEDS_NOALLOC_MAX_NODES 131072
+deeds_status deeds_consistent_noalloc_dev(float* d_u, float* d_v, float* d_w, float* d_u2, float* d_v2, float* d_w2,
+                                          int m, int n, int o, int g, void* stream);
+
 /* jacobian(): std of the Jacobian determinant and fraction of J<0 of a grid
  * field (src/transformations.h:84-185; a diagnostic, parallel reduction, not
  * bit-exact).  Synchronous. */

@@ -1,0 +1,62 @@
+"""The allocation-free inverse-consistency entry point, through the C ABI.
+
+deeds_consistent_noalloc_dev serves callers that cannot allocate device memory
+while they run (a host framework's memory pool owning the device, start-up-sized
+real-time loops, code that must not block on an allocation's device sync).  Its
+scratch is a fixed device array inside the library, so this test checks it
+against the context-based deeds_consistent_dev on the same inputs, twice in a row
+(the array keeps the previous call's contents), and that oversized grids are
+refused.  The file sorts last so that a stop-at-first-failure run has already run
+every other test.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from deedsbcv_gb300 import _lib
+    return _lib.load()
+
+
+def _fields(seed, shape):
+    rng = np.random.default_rng(seed)
+    n = int(np.prod(shape))
+    return [torch.from_numpy(rng.uniform(-6, 6, n).astype(np.float32)).cuda() for _ in range(6)]
+
+
+def _ptrs(ts):
+    return [C.c_void_p(t.data_ptr()) for t in ts]
+
+
+@pytest.mark.parametrize("shape,g", [((48, 40, 64), 4), ((24, 20, 32), 8)])
+def test_noalloc_matches_context_path_twice(lib, shape, g):
+    from deedsbcv_gb300 import api
+    ctx = api.Context(0)
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for call, seed in enumerate((11, 12)):  # two calls in a row, different inputs
+        ref = _fields(seed, shape)
+        got = [t.clone() for t in ref]
+        assert lib.deeds_consistent_dev(ctx.handle, *_ptrs(ref), *shape, g, stream) == 0
+        assert lib.deeds_consistent_noalloc_dev(*_ptrs(got), *shape, g, stream) == 0
+        torch.cuda.synchronize()
+        for a, b in zip(ref, got):
+            # the consistent-mapping contract is bit-exact
+            assert a.cpu().numpy().tobytes() == b.cpu().numpy().tobytes(), call
+    ctx.close()
+
+
+def test_noalloc_rejects_oversized_grid(lib):
+    from deedsbcv_gb300._lib import NOALLOC_MAX_NODES
+    shape = (64, 64, NOALLOC_MAX_NODES // (64 * 64) + 1)
+    t = torch.zeros(1, device="cuda")
+    p = C.c_void_p(t.data_ptr())
+    st = lib.deeds_consistent_noalloc_dev(p, p, p, p, p, p, *shape, 4, C.c_void_p(0))
+    assert st == 1  # DEEDS_ERR_INVALID, nothing launched
