@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--small", action="store_true", help="96x80x128 workload (profiling runs)")
     ap.add_argument("--no-batched", action="store_true", help="skip the 16-pair batched measurement")
     ap.add_argument("--lanes", type=int, default=3, help="pairs in flight for the batched form")
+    ap.add_argument("--no-soft", action="store_true", help="skip the soft-min (differentiable) measurement")
     return ap.parse_args()
 
 
@@ -168,6 +169,75 @@ def measure_batched(api, ctx, lanes):
             "plain_pairs_per_s": len(pairs) / t_plain, "batched_pairs_per_s": len(pairs) / t_batch,
             "speedup": t_plain / t_batch, "flows_identical": bool(same),
             "workload": "16 pairs, dims uniform in 128x112x144..224x192x288, host buffers end to end"}
+
+
+SOFT_SHAPE = (160, 160, 192)
+SOFT_TAUS = (0.1, 0.5, 2.0)
+
+
+def measure_soft(api, ctx, n_pairs=4, grid=4, radius=3, quant=1):
+    """Differentiable soft-min level on 4 pairs at 160x160x192, label set 7^3,
+    tau in {0.1, 0.5, 2.0}: forward (expected displacement) + backward (hand-written
+    adjoint: gradients w.r.t. both images and alpha) of loss = MSE between the
+    expected displacement and the seeded ground-truth field at the control points.
+    Each pair's MST is built once from its fixed image (a constant of the level)
+    before timing; device time with CUDA events over all pairs per tau."""
+    import torch
+    from deedsbcv_gb300 import phantom
+    m, n, o = SOFT_SHAPE
+    g = grid
+    m1, n1, o1 = m // g, n // g, o // g
+    data = []
+    for i in range(n_pairs):
+        pr = phantom.make_pair(SOFT_SHAPE, seed=200 + i, max_disp=10.0)
+        fx = torch.from_numpy(pr["fixed"].ravel(order="F").astype(np.float32)).cuda()
+        mv = torch.from_numpy(pr["moving"].ravel(order="F").astype(np.float32)).cuda()
+        c = g // 2
+        d = pr["disp"][:, c::g, c::g, c::g][:, :m1, :n1, :o1]  # (y, x, z) components at node voxels
+        gt = -np.stack([d[1], d[0], d[2]]).reshape(3, -1, order="F")  # u (x), v (y), w (z), node order y fastest
+        tree = api.soft_tree(fx, m, n, o, g, ctx)
+        data.append((fx, mv, torch.from_numpy(gt.astype(np.float32)).cuda(), tree))
+
+    def step(fx, mv, gt, tree, tau, backward=True):
+        F = fx.detach().requires_grad_(backward)
+        M = mv.detach().requires_grad_(backward)
+        a = torch.tensor(1.6, requires_grad=backward)
+        disp = api.soft_level(F, M, a, SOFT_SHAPE, grid=g, radius=radius, quant=quant, tau=tau, tree=tree, ctx=ctx)
+        loss = ((disp - gt) ** 2).mean()
+        if backward:
+            loss.backward()
+            return loss.detach(), F.grad, M.grad, a.grad
+        return loss.detach(), None, None, None
+
+    out = {}
+    launches0 = api.kernel_launches()
+    for tau in SOFT_TAUS:
+        for fx, mv, gt, tree in data[:1]:
+            step(fx, mv, gt, tree, tau)  # warm-up: buffers
+        res = {}
+        for mode in ("forward", "forward_backward"):
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            losses = []
+            gnorm = 0.0
+            for fx, mv, gt, tree in data:
+                loss, gf, gm, ga = step(fx, mv, gt, tree, tau, backward=(mode == "forward_backward"))
+                losses.append(loss)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            res[mode + "_ms_per_pair"] = ms / len(data)
+            if mode == "forward_backward":
+                res["pairs_per_s"] = 1000.0 * len(data) / ms
+                res["grad_norms_last_pair"] = {"fixed": float(gf.norm()), "moving": float(gm.norm()),
+                                               "alpha": float(ga)}
+            res["mean_loss"] = float(torch.stack(losses).mean())
+        out[str(tau)] = res
+    return {"workload": f"{n_pairs} pairs {m}x{n}x{o} (seeds 200..{199 + n_pairs}), soft level grid {g}, "
+                        f"label set {2 * radius + 1}^3, quant {quant}, alpha 1.6, eps 0.01; loss = MSE(expected "
+                        f"displacement, ground-truth field at control points); MST per pair built before timing",
+            "per_tau": out, "gpu_launches": api.kernel_launches() - launches0}
 
 
 def cpu_reference_pair(pair, shape):
@@ -341,6 +411,11 @@ def main():
     if rank == 0 and not args.no_batched and not args.small:
         batched = measure_batched(api, ctx, args.lanes)
 
+    # ---- differentiable soft-min form (rank 0)
+    soft = None
+    if rank == 0 and not args.no_soft and not args.small:
+        soft = measure_soft(api, ctx)
+
     # ---- CPU baseline and full-size parity (rank 0, N=1)
     cpu = None
     parity = None
@@ -379,6 +454,7 @@ def main():
             "cpu_baseline": cpu,
             "parity": parity,
             "batched": batched,
+            "soft": soft,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:

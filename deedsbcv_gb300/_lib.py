@@ -25,6 +25,8 @@ EXPORTS = [
     "deeds_warp_image_dev", "deeds_warp_seg_dev", "deeds_consistent_dev", "deeds_jacobian_dev",
     "deeds_set_profiling", "deeds_stage_times", "deeds_reset_stage_times", "deeds_kernel_launches",
     "deeds_measure_popc_rate", "deeds_register_batch", "deeds_consistent_noalloc_dev",
+    "deeds_soft_default_params", "deeds_soft_descriptor_dev", "deeds_soft_cost_dev", "deeds_soft_forward_dev",
+    "deeds_soft_backward_dev",
 ]
 NOALLOC_MAX_NODES = 131072
 STAGES = ["mind", "datacost", "mst_edges", "bp_up", "bp_down", "transform", "consistent", "tree_wait"]
@@ -52,6 +54,18 @@ class DeedsPair(C.Structure):
         ("X", C.c_void_p),
         ("flow_out", C.c_void_p),
         ("warped_out", C.c_void_p),
+    ]
+
+
+class DeedsSoftParams(C.Structure):
+    _fields_ = [
+        ("grid", C.c_int),
+        ("radius", C.c_int),
+        ("quant", C.c_int),
+        ("mind_radius", C.c_int),
+        ("alpha", C.c_float),
+        ("tau", C.c_float),
+        ("eps", C.c_float),
     ]
 
 
@@ -104,9 +118,17 @@ def load():
     L.deeds_measure_popc_rate.argtypes = [P, P]
     L.deeds_register_batch.argtypes = [P, P, I, C.POINTER(DeedsParams), I]
     L.deeds_consistent_noalloc_dev.argtypes = [P, P, P, P, P, P, I, I, I, I, P]
+    SP = C.POINTER(DeedsSoftParams)
+    L.deeds_soft_default_params.argtypes = [SP]
+    L.deeds_soft_default_params.restype = None
+    L.deeds_soft_descriptor_dev.argtypes = [P, P, I, I, I, I, P, P]
+    L.deeds_soft_cost_dev.argtypes = [P, P, P, I, I, I, SP, P, P]
+    L.deeds_soft_forward_dev.argtypes = [P, P, P, I, I, I, SP, P, P, P, P, P]
+    L.deeds_soft_backward_dev.argtypes = [P, P, P, I, I, I, SP, P, P, P, P, P, P, P, P]
     for name in EXPORTS:
         fn = getattr(L, name)
-        if name not in ("deeds_default_params", "deeds_destroy", "deeds_last_error", "deeds_version"):
+        if name not in ("deeds_default_params", "deeds_destroy", "deeds_last_error", "deeds_version",
+                        "deeds_soft_default_params"):
             fn.restype = I
     L.deeds_kernel_launches.restype = C.c_longlong
     _lib = L

@@ -21,7 +21,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import DeedsError, DeedsParams  # noqa: F401
+from ._lib import DeedsError, DeedsParams, DeedsSoftParams  # noqa: F401
 
 try:  # torch is plumbing for device memory and streams only
     import torch
@@ -379,3 +379,118 @@ def apply_flow(flow, volume, dims=None, X=None, grid_step=0, ctx=None):
                                        Xa.ctypes.data_as(C.c_void_p), v.ctypes.data_as(C.c_void_p), dtype, m, n, o,
                                        out.ctypes.data_as(C.c_void_p)))
     return out
+
+
+# ---------------------------------------------------------------------------
+# Soft-min form (no counterpart in the reference): one deeds level relaxed so that
+# it is differentiable in both images and alpha.  See include/deeds_gpu.h.
+
+def soft_params(grid=4, radius=3, quant=1, alpha=1.6, tau=0.5, eps=0.01, mind_radius=0):
+    p = DeedsSoftParams()
+    _lib.load().deeds_soft_default_params(C.byref(p))
+    p.grid, p.radius, p.quant, p.mind_radius = int(grid), int(radius), int(quant), int(mind_radius)
+    p.alpha, p.tau, p.eps = float(alpha), float(tau), float(eps)
+    return p
+
+
+def soft_descriptor(im, m, n, o, qs, ctx=None):
+    """Continuous MIND-SSC levels 6*exp(-mind1): float32 CUDA tensor (12, m*n*o)."""
+    ctx = ctx or context(im.device.index or 0)
+    sz = m * n * o
+    out = torch.empty(12 * sz, dtype=torch.float32, device=im.device)
+    ctx.check(ctx._L.deeds_soft_descriptor_dev(ctx.handle, _dev(im, torch.float32, sz, "im"), m, n, o, int(qs),
+                                                C.c_void_p(out.data_ptr()), _stream()))
+    return out.view(12, sz)
+
+
+def soft_cost(sF, sM, m, n, o, params, ctx=None):
+    """Soft cost volume (sz1, len3) of two soft descriptors."""
+    ctx = ctx or context(sF.device.index or 0)
+    sz = m * n * o
+    g, hw = params.grid, params.radius
+    sz1 = (m // g) * (n // g) * (o // g)
+    len3 = (2 * hw + 1) ** 3
+    out = torch.empty(sz1 * len3, dtype=torch.float32, device=sF.device)
+    ctx.check(ctx._L.deeds_soft_cost_dev(ctx.handle, _dev(sF, torch.float32, 12 * sz, "sF"),
+                                          _dev(sM, torch.float32, 12 * sz, "sM"), m, n, o, C.byref(params),
+                                          C.c_void_p(out.data_ptr()), _stream()))
+    return out.view(sz1, len3)
+
+
+def _tree_arrays(tree):
+    ordered, parents, edgemst = tree
+    return (np.ascontiguousarray(ordered, np.int32), np.ascontiguousarray(parents, np.int32),
+            np.ascontiguousarray(edgemst, np.float32))
+
+
+def _soft_call(ctx, fn, fixed, moving, dims, params, tree, *rest):
+    m, n, o = dims
+    sz = m * n * o
+    ordered, parents, edgemst = tree
+    p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    ctx.check(fn(ctx.handle, _dev(fixed, torch.float32, sz, "fixed"), _dev(moving, torch.float32, sz, "moving"),
+                 m, n, o, C.byref(params), p(ordered), p(parents), p(edgemst), *rest, _stream()))
+
+
+class SoftDeedsLevel(torch.autograd.Function if torch is not None else object):
+    """Expected displacement (3, sz1) [u, v, w] of one soft-min deeds level.
+
+    forward(fixed, moving, alpha, dims, params, tree, ctx): fixed/moving are flat
+    float32 CUDA tensors (i fastest), alpha a 0-d tensor (its value replaces
+    params.alpha), tree = (ordered, parents, edgemst) host arrays of the fixed
+    image's MST at params.grid.  Backward runs the library's adjoint kernels,
+    which recompute the forward sweeps instead of keeping message tensors."""
+
+    @staticmethod
+    def forward(fctx, fixed, moving, alpha, dims, params, tree, dctx):
+        params = soft_params(params.grid, params.radius, params.quant, float(alpha.detach()), params.tau, params.eps,
+                             params.mind_radius)
+        tree = _tree_arrays(tree)
+        m, n, o = dims
+        g = params.grid
+        sz1 = (m // g) * (n // g) * (o // g)
+        out = torch.empty(3 * sz1, dtype=torch.float32, device=fixed.device)
+        fixed_c, moving_c = fixed.detach().contiguous(), moving.detach().contiguous()
+        _soft_call(dctx, dctx._L.deeds_soft_forward_dev, fixed_c, moving_c, dims, params, tree,
+                   C.c_void_p(out.data_ptr()))
+        fctx.save_for_backward(fixed_c, moving_c)
+        fctx.soft = (dims, params, tree, dctx)
+        fctx.alpha_like = (alpha.dtype, alpha.device) if isinstance(alpha, torch.Tensor) else (torch.float32, "cpu")
+        return out.view(3, sz1)
+
+    @staticmethod
+    def backward(fctx, gdisp):
+        fixed, moving = fctx.saved_tensors
+        dims, params, tree, dctx = fctx.soft
+        gdisp = gdisp.detach().contiguous().to(torch.float32)
+        need_f, need_m, need_a = fctx.needs_input_grad[:3]
+        gf = torch.empty_like(fixed) if need_f else None
+        gm = torch.empty_like(moving) if need_m else None
+        ga = C.c_float(0.0)
+        _soft_call(dctx, dctx._L.deeds_soft_backward_dev, fixed, moving, dims, params, tree,
+                   C.c_void_p(gdisp.data_ptr()), C.c_void_p(gf.data_ptr()) if gf is not None else None,
+                   C.c_void_p(gm.data_ptr()) if gm is not None else None, C.byref(ga) if need_a else None)
+        adt, adev = fctx.alpha_like
+        galpha = torch.tensor(ga.value, dtype=adt, device=adev) if need_a else None
+        return gf, gm, galpha, None, None, None, None
+
+
+def soft_tree(fixed, m, n, o, g, ctx=None):
+    """The hard path's MST of the fixed image at grid g (constant for the soft level)."""
+    return primsGraph(fixed.detach().contiguous(), m, n, o, g, ctx)
+
+
+def soft_level(fixed, moving, alpha, dims, grid=4, radius=3, quant=1, tau=0.5, eps=0.01, mind_radius=0, tree=None,
+               ctx=None):
+    """Differentiable soft-min deeds level: expected displacement (3, sz1) [u, v, w].
+
+    Gradients flow to ``fixed`` and ``moving`` (through the continuous MIND-SSC
+    descriptor) and to ``alpha`` (a float or 0-d tensor)."""
+    m, n, o = dims
+    ctx = ctx or context(fixed.device.index or 0)
+    if tree is None:
+        tree = soft_tree(fixed, m, n, o, grid, ctx)
+    if not isinstance(alpha, torch.Tensor):
+        alpha = torch.tensor(float(alpha), dtype=torch.float32)
+    params = soft_params(grid, radius, quant, float(alpha.detach()), tau, eps, mind_radius)
+    return SoftDeedsLevel.apply(fixed, moving, alpha, tuple(dims), params, tree, ctx)

@@ -68,6 +68,32 @@ cudaError_t launch_warp_seg(const short* d_in, const float* X, const FieldRef& f
                             cudaStream_t s);
 cudaError_t launch_consistent(float* u, float* v, float* w, float* u2, float* v2, float* w2, int m, int n, int o, int g,
                               float* scratch, cudaStream_t s);
+// Soft-min level (soft.cu).  Tree arrays on the device; `ordered` is breadth-level
+// order and the host keeps the level ranges.
+struct SoftTreeDev {
+    int len, sz, root, q;
+    float tau;
+    const int* ordered;
+    const int* parents;
+    const float* edgemst;
+    const int* child_ptr;
+    const int* children;
+};
+cudaError_t launch_soft_descriptor(const float* d_im, float* w6a, float* w6b, float* s12, int m, int n, int o, int qs,
+                                   cudaStream_t st);
+cudaError_t launch_soft_descriptor_adj(const float* d_im, float* w6a, float* w6b, const float* sbar12, float* dbar6,
+                                       float* imbar, int m, int n, int o, int qs, cudaStream_t st);
+cudaError_t launch_soft_cost(const float* sF, const float* sM, float* cost, int m, int n, int o, int g, int hw, int q,
+                             float alpha1, float eps, cudaStream_t st);
+cudaError_t launch_soft_cost_adj(const float* sF, const float* sM, const float* cbar, const float* cost, float* sFbar,
+                                 float* sMbar, double* dot, int m, int n, int o, int g, int hw, int q, float alpha1,
+                                 float eps, cudaStream_t st);
+size_t soft_tree_smem(int len);
+cudaError_t launch_soft_tree_forward(const SoftTreeDev& d, const int* h_level_start, int n_levels, const float* cost,
+                                     float* B, float* M, float* Mmin, float* logp, float* disp, cudaStream_t st);
+cudaError_t launch_soft_tree_backward(const SoftTreeDev& d, const int* h_level_start, int n_levels, const float* B,
+                                      const float* M, const float* logp, const float* gdisp, float* R, float* Bbar,
+                                      cudaStream_t st);
 cudaError_t launch_popc_probe(int blocks, int threads, int iters, unsigned long long* d_sink, cudaStream_t s);
 cudaError_t launch_jacobian(const float* u, const float* v, const float* w, int m, int n, int o, int g, double* d_acc,
                             cudaStream_t s);

@@ -1087,4 +1087,210 @@ deeds_status deeds_measure_popc_rate(deeds_ctx* ctx, double* rate) {
     return DEEDS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Soft-min form (soft.cu)
+
+void deeds_soft_default_params(deeds_soft_params* p) {
+    if (!p) return;
+    p->grid = 4;
+    p->radius = 3;
+    p->quant = 1;
+    p->mind_radius = 0;
+    p->alpha = 1.6f;
+    p->tau = 0.5f;
+    p->eps = 0.01f;
+}
+
+}  // extern "C"
+
+namespace {
+
+deeds_status soft_check(deeds_ctx* ctx, int m, int n, int o, const deeds_soft_params* p, int* qs) {
+    if (!p) return fail(ctx, DEEDS_ERR_INVALID, "params is NULL");
+    if (p->grid < 1 || p->radius < 0 || p->radius > 5 || p->quant < 1)
+        return fail(ctx, DEEDS_ERR_INVALID, "soft level: grid %d radius %d (0..5) quant %d", p->grid, p->radius,
+                    p->quant);
+    if (!(p->tau > 0.0f) || !(p->eps > 0.0f) || !(p->alpha > 0.0f))
+        return fail(ctx, DEEDS_ERR_INVALID, "soft level: tau, eps and alpha must be > 0");
+    *qs = p->mind_radius > 0 ? p->mind_radius : mind_step(p->quant);
+    if (*qs > 7) return fail(ctx, DEEDS_ERR_INVALID, "MIND radius %d > 7 unsupported", *qs);
+    if (m < 2 * *qs + 1 || n < 2 * *qs + 1 || o < 2 * *qs + 1)
+        return fail(ctx, DEEDS_ERR_INVALID, "volume %dx%dx%d too small for MIND radius %d", m, n, o, *qs);
+    if (m < p->grid || n < p->grid || o < p->grid)
+        return fail(ctx, DEEDS_ERR_INVALID, "volume %dx%dx%d smaller than grid %d", m, n, o, p->grid);
+    return DEEDS_OK;
+}
+
+float soft_alpha1(const deeds_soft_params* p) {
+    int sy, sx, sz;
+    float alpha1;
+    data_cost_params(p->grid, p->quant, p->alpha, &sy, &sx, &sz, &alpha1);
+    return alpha1;
+}
+
+}  // namespace
+
+extern "C" {
+
+deeds_status deeds_soft_descriptor_dev(deeds_ctx* ctx, const float* d_im, int m, int n, int o, int qs, float* d_desc,
+                                       void* stream) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!d_im || !d_desc || qs < 1 || qs > 7 || m < 2 * qs + 1 || n < 2 * qs + 1 || o < 2 * qs + 1)
+        return fail(ctx, DEEDS_ERR_INVALID, "deeds_soft_descriptor_dev: bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    deeds_status st = DEEDS_OK;
+    float* w6 = dbuf<float>(ctx, "soft_w6", (size_t)6 * m * n * o, &st);
+    float* w6b = dbuf<float>(ctx, "soft_w6b", (size_t)6 * m * n * o, &st);
+    if (st) return st;
+    CK(launch_soft_descriptor(d_im, w6, w6b, d_desc, m, n, o, qs, (cudaStream_t)stream));
+    return DEEDS_OK;
+}
+
+deeds_status deeds_soft_cost_dev(deeds_ctx* ctx, const float* d_F, const float* d_M, int m, int n, int o,
+                                 const deeds_soft_params* p, float* d_cost, void* stream) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!d_F || !d_M || !d_cost) return fail(ctx, DEEDS_ERR_INVALID, "null pointer");
+    int qs = 0;
+    if (deeds_status e = soft_check(ctx, m, n, o, p, &qs)) return e;
+    CK(cudaSetDevice(ctx->device));
+    CK(launch_soft_cost(d_F, d_M, d_cost, m, n, o, p->grid, p->radius, p->quant, soft_alpha1(p), p->eps,
+                        (cudaStream_t)stream));
+    return DEEDS_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Everything one soft level needs on the device, from the caller's host tree.
+struct SoftLevel {
+    int qs = 0, m1 = 0, n1 = 0, o1 = 0, sz1 = 0, len = 0;
+    size_t len3 = 0, sz = 0;
+    TreeSchedule sch;
+    SoftTreeDev tree{};
+    float *w6 = nullptr, *w6b = nullptr, *sF = nullptr, *sM = nullptr, *cost = nullptr, *B = nullptr, *M = nullptr, *Mmin = nullptr,
+          *logp = nullptr, *disp = nullptr;
+};
+
+deeds_status soft_setup(deeds_ctx* ctx, int m, int n, int o, const deeds_soft_params* p, const int* ordered,
+                        const int* parents, const float* edgemst, cudaStream_t s, SoftLevel& L) {
+    if (deeds_status e = soft_check(ctx, m, n, o, p, &L.qs)) return e;
+    if (!ordered || !parents || !edgemst) return fail(ctx, DEEDS_ERR_INVALID, "null tree array");
+    L.m1 = m / p->grid; L.n1 = n / p->grid; L.o1 = o / p->grid;
+    L.sz1 = L.m1 * L.n1 * L.o1;
+    L.len = 2 * p->radius + 1;
+    L.len3 = (size_t)L.len * L.len * L.len;
+    L.sz = (size_t)m * n * o;
+    for (int t = 0; t < L.sz1; t++)  // the root's parent entry is unused
+        if (ordered[t] < 0 || ordered[t] >= L.sz1 ||
+            (t > 0 && (parents[ordered[t]] < 0 || parents[ordered[t]] >= L.sz1)))
+            return fail(ctx, DEEDS_ERR_INVALID, "tree arrays out of range at %d", t);
+    build_schedule(ordered, parents, L.sz1, L.sch);
+    if (L.sch.level_start[L.sch.n_levels] != L.sz1 || L.sch.level_start[1] != 1)
+        return fail(ctx, DEEDS_ERR_INVALID, "ordered/parents do not form a breadth-ordered tree");
+    CK(cudaSetDevice(ctx->device));
+    deeds_status st = DEEDS_OK;
+    // packed tree: ordered | parents | edgemst | child_ptr | children
+    const size_t words = (size_t)L.sz1 * 4 + 1 + (L.sz1 > 0 ? L.sz1 - 1 : 0) + 1;
+    uint32_t* h = hbuf<uint32_t>(ctx, "soft_tree_h", words, &st);
+    uint32_t* d = dbuf<uint32_t>(ctx, "soft_tree_d", words, &st);
+    L.w6 = dbuf<float>(ctx, "soft_w6", 6 * L.sz, &st);
+    L.w6b = dbuf<float>(ctx, "soft_w6b", 6 * L.sz, &st);
+    L.sF = dbuf<float>(ctx, "soft_sF", 12 * L.sz, &st);
+    L.sM = dbuf<float>(ctx, "soft_sM", 12 * L.sz, &st);
+    L.cost = dbuf<float>(ctx, "soft_cost", L.sz1 * L.len3, &st);
+    L.B = dbuf<float>(ctx, "soft_B", L.sz1 * L.len3, &st);
+    L.M = dbuf<float>(ctx, "soft_M", L.sz1 * L.len3, &st);
+    L.Mmin = dbuf<float>(ctx, "soft_Mmin", L.sz1, &st);
+    L.logp = dbuf<float>(ctx, "soft_logp", L.sz1 * L.len3, &st);
+    L.disp = dbuf<float>(ctx, "soft_disp", 3 * (size_t)L.sz1, &st);
+    if (st) return st;
+    CK(cudaStreamSynchronize(s));  // the pinned staging block is reused across calls
+    const size_t o_par = L.sz1, o_edge = 2 * (size_t)L.sz1, o_cptr = 3 * (size_t)L.sz1,
+                 o_ch = 4 * (size_t)L.sz1 + 1;
+    std::memcpy(h, ordered, sizeof(int) * L.sz1);
+    std::memcpy(h + o_par, parents, sizeof(int) * L.sz1);
+    std::memcpy(h + o_edge, edgemst, sizeof(float) * L.sz1);
+    std::memcpy(h + o_cptr, L.sch.child_ptr.data(), sizeof(int) * (L.sz1 + 1));
+    if (!L.sch.children.empty()) std::memcpy(h + o_ch, L.sch.children.data(), sizeof(int) * L.sch.children.size());
+    CK(cudaMemcpyAsync(d, h, words * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    L.tree.len = L.len;
+    L.tree.sz = L.sz1;
+    L.tree.root = ordered[0];
+    L.tree.q = p->quant;
+    L.tree.tau = p->tau;
+    L.tree.ordered = reinterpret_cast<const int*>(d);
+    L.tree.parents = reinterpret_cast<const int*>(d + o_par);
+    L.tree.edgemst = reinterpret_cast<const float*>(d + o_edge);
+    L.tree.child_ptr = reinterpret_cast<const int*>(d + o_cptr);
+    L.tree.children = reinterpret_cast<const int*>(d + o_ch);
+    return DEEDS_OK;
+}
+
+deeds_status soft_run_forward(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, int m, int n, int o,
+                              const deeds_soft_params* p, SoftLevel& L, float* d_disp, cudaStream_t s) {
+    CK(launch_soft_descriptor(d_fixed, L.w6, L.w6b, L.sF, m, n, o, L.qs, s));
+    CK(launch_soft_descriptor(d_moving, L.w6, L.w6b, L.sM, m, n, o, L.qs, s));
+    CK(launch_soft_cost(L.sF, L.sM, L.cost, m, n, o, p->grid, p->radius, p->quant, soft_alpha1(p), p->eps, s));
+    CK(launch_soft_tree_forward(L.tree, L.sch.level_start.data(), L.sch.n_levels, L.cost, L.B, L.M, L.Mmin, L.logp,
+                                d_disp, s));
+    return DEEDS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+deeds_status deeds_soft_forward_dev(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, int m, int n, int o,
+                                    const deeds_soft_params* p, const int* ordered, const int* parents,
+                                    const float* edgemst, float* d_disp, void* stream) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!d_fixed || !d_moving || !d_disp) return fail(ctx, DEEDS_ERR_INVALID, "null pointer");
+    cudaStream_t s = (cudaStream_t)stream;
+    SoftLevel L;
+    if (deeds_status e = soft_setup(ctx, m, n, o, p, ordered, parents, edgemst, s, L)) return e;
+    return soft_run_forward(ctx, d_fixed, d_moving, m, n, o, p, L, d_disp, s);
+}
+
+deeds_status deeds_soft_backward_dev(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, int m, int n, int o,
+                                     const deeds_soft_params* p, const int* ordered, const int* parents,
+                                     const float* edgemst, const float* d_gdisp, float* d_gfixed, float* d_gmoving,
+                                     float* grad_alpha, void* stream) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!d_fixed || !d_moving || !d_gdisp) return fail(ctx, DEEDS_ERR_INVALID, "null pointer");
+    cudaStream_t s = (cudaStream_t)stream;
+    SoftLevel L;
+    if (deeds_status e = soft_setup(ctx, m, n, o, p, ordered, parents, edgemst, s, L)) return e;
+    deeds_status st = DEEDS_OK;
+    float* R = dbuf<float>(ctx, "soft_R", L.sz1 * L.len3, &st);
+    float* Bbar = dbuf<float>(ctx, "soft_Bbar", L.sz1 * L.len3, &st);
+    float* sFbar = dbuf<float>(ctx, "soft_sFbar", 12 * L.sz, &st);
+    float* sMbar = dbuf<float>(ctx, "soft_sMbar", 12 * L.sz, &st);
+    float* dbar6 = dbuf<float>(ctx, "soft_dbar6", 6 * L.sz, &st);
+    double* dot = dbuf<double>(ctx, "soft_dot", 1, &st);
+    if (st) return st;
+    // recompute the forward state (descriptors, cost, messages, marginals)
+    if (deeds_status e = soft_run_forward(ctx, d_fixed, d_moving, m, n, o, p, L, L.disp, s)) return e;
+    CK(launch_soft_tree_backward(L.tree, L.sch.level_start.data(), L.sch.n_levels, L.B, L.M, L.logp, d_gdisp, R, Bbar,
+                                 s));
+    // Bbar is now dL/dcost
+    CK(launch_soft_cost_adj(L.sF, L.sM, Bbar, L.cost, sFbar, sMbar, dot, m, n, o, p->grid, p->radius, p->quant,
+                            soft_alpha1(p), p->eps, s));
+    if (d_gfixed) {
+        CK(cudaMemsetAsync(d_gfixed, 0, sizeof(float) * L.sz, s));
+        CK(launch_soft_descriptor_adj(d_fixed, L.w6, L.w6b, sFbar, dbar6, d_gfixed, m, n, o, L.qs, s));
+    }
+    if (d_gmoving) {
+        CK(cudaMemsetAsync(d_gmoving, 0, sizeof(float) * L.sz, s));
+        CK(launch_soft_descriptor_adj(d_moving, L.w6, L.w6b, sMbar, dbar6, d_gmoving, m, n, o, L.qs, s));
+    }
+    if (grad_alpha) {
+        double hdot = 0.0;
+        CK(cudaMemcpyAsync(&hdot, dot, sizeof(double), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        *grad_alpha = (float)(-hdot / (double)p->alpha);
+    }
+    return DEEDS_OK;
+}
+
 }  // extern "C"

@@ -234,6 +234,58 @@ long long deeds_kernel_launches(void);
  * returns popc64 operations per second. Synchronous, ~0.2 s. */
 deeds_status deeds_measure_popc_rate(deeds_ctx* ctx, double* popc64_per_s);
 
+/* ---------------------------------------------------------------------------
+ * Soft-min form (no counterpart in the reference).  One deeds level
+ * (src/deedsBCV0.cpp:238-306) relaxed so that it is differentiable in both
+ * images and in alpha:
+ *   - descriptor: the continuous MIND-SSC level s = 6 exp(-mind1) per channel,
+ *     i.e. the quantity src/MINDSSCbox.h:175-224 thresholds into codes;
+ *   - cost: alpha1 * sum over the node's samples (src/dataCostD.h:141-200
+ *     sampling and clamping) and the 12 channels of sqrt(d^2 + eps^2) - eps;
+ *   - messages: src/regularisation.h:190-238 with min replaced by the soft-min
+ *     -tau log sum exp(-x/tau), over the MST given by primsGraph();
+ *   - output: the expected displacement sum_l p(l) d(l) per control point
+ *     (u|v|w, 3 x m1*n1*o1 floats), from soft root-to-leaf marginals.
+ * The prior field is zero (the level registers `moving` as given).
+ * tau -> 0 recovers the hard argmin of the min-sum tree.
+ */
+typedef struct deeds_soft_params {
+    int grid;        /* control-point spacing g */
+    int radius;      /* label half-width hw, 0..5: label set (2hw+1)^3 */
+    int quant;       /* label quantisation q */
+    int mind_radius; /* MIND-SSC radius; 0 = floor(q/2 + 1) as src/deedsBCV0.cpp:183-186 */
+    float alpha;     /* regularisation weight (-a) */
+    float tau;       /* soft-min temperature, > 0 */
+    float eps;       /* smoothing of |x| in the descriptor cost, > 0 */
+} deeds_soft_params;
+
+/* grid 4, radius 3, quant 1, mind_radius 0, alpha 1.6, tau 0.5, eps 0.01 */
+void deeds_soft_default_params(deeds_soft_params* p);
+
+/* Continuous MIND-SSC descriptor: 12 x m*n*o floats (channel-major). */
+deeds_status deeds_soft_descriptor_dev(deeds_ctx* ctx, const float* d_im, int m, int n, int o, int mind_radius,
+                                       float* d_desc, void* stream);
+
+/* Soft cost volume m1*n1*o1 x (2hw+1)^3 from two soft descriptors. */
+deeds_status deeds_soft_cost_dev(deeds_ctx* ctx, const float* d_desc_fixed, const float* d_desc_moving, int m, int n,
+                                 int o, const deeds_soft_params* p, float* d_cost, void* stream);
+
+/* Forward: expected displacement (u|v|w) of the soft level.  ordered/parents/
+ * edgemst are the host arrays of primsGraph() on the fixed image at this grid
+ * (deeds_prims_from_sad).  Synchronous with respect to the host arrays only. */
+deeds_status deeds_soft_forward_dev(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, int m, int n, int o,
+                                    const deeds_soft_params* p, const int* ordered, const int* parents,
+                                    const float* edgemst, float* d_disp, void* stream);
+
+/* Backward: given dL/d(displacement) (3 x m1*n1*o1), writes dL/dfixed and
+ * dL/dmoving (m*n*o each, overwritten; either may be NULL) and dL/dalpha
+ * (host float, may be NULL).  Recomputes the forward sweeps (no state is kept
+ * from deeds_soft_forward_dev).  Synchronous when grad_alpha is not NULL. */
+deeds_status deeds_soft_backward_dev(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, int m, int n, int o,
+                                     const deeds_soft_params* p, const int* ordered, const int* parents,
+                                     const float* edgemst, const float* d_grad_disp, float* d_grad_fixed,
+                                     float* d_grad_moving, float* grad_alpha, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
