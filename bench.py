@@ -50,6 +50,11 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the 16-pair batched measurement")
     ap.add_argument("--lanes", type=int, default=3, help="pairs in flight for the batched form")
     ap.add_argument("--no-soft", action="store_true", help="skip the soft-min (differentiable) measurement")
+    ap.add_argument("--soft-only", action="store_true",
+                    help="only the soft-min measurement (one JSON object; for profiling runs)")
+    ap.add_argument("--soft-pairs", type=int, default=4)
+    ap.add_argument("--soft-taus", default="0.1,0.5,2.0")
+    ap.add_argument("--soft-shape", default="160x160x192", help="soft-min pair shape (profiling runs use smaller)")
     return ap.parse_args()
 
 
@@ -175,7 +180,7 @@ SOFT_SHAPE = (160, 160, 192)
 SOFT_TAUS = (0.1, 0.5, 2.0)
 
 
-def measure_soft(api, ctx, n_pairs=4, grid=4, radius=3, quant=1):
+def measure_soft(api, ctx, n_pairs=4, grid=4, radius=3, quant=1, taus=SOFT_TAUS, shape=SOFT_SHAPE):
     """Differentiable soft-min level on 4 pairs at 160x160x192, label set 7^3,
     tau in {0.1, 0.5, 2.0}: forward (expected displacement) + backward (hand-written
     adjoint: gradients w.r.t. both images and alpha) of loss = MSE between the
@@ -184,12 +189,12 @@ def measure_soft(api, ctx, n_pairs=4, grid=4, radius=3, quant=1):
     before timing; device time with CUDA events over all pairs per tau."""
     import torch
     from deedsbcv_gb300 import phantom
-    m, n, o = SOFT_SHAPE
+    m, n, o = shape
     g = grid
     m1, n1, o1 = m // g, n // g, o // g
     data = []
     for i in range(n_pairs):
-        pr = phantom.make_pair(SOFT_SHAPE, seed=200 + i, max_disp=10.0)
+        pr = phantom.make_pair(shape, seed=200 + i, max_disp=10.0)
         fx = torch.from_numpy(pr["fixed"].ravel(order="F").astype(np.float32)).cuda()
         mv = torch.from_numpy(pr["moving"].ravel(order="F").astype(np.float32)).cuda()
         c = g // 2
@@ -202,7 +207,7 @@ def measure_soft(api, ctx, n_pairs=4, grid=4, radius=3, quant=1):
         F = fx.detach().requires_grad_(backward)
         M = mv.detach().requires_grad_(backward)
         a = torch.tensor(1.6, requires_grad=backward)
-        disp = api.soft_level(F, M, a, SOFT_SHAPE, grid=g, radius=radius, quant=quant, tau=tau, tree=tree, ctx=ctx)
+        disp = api.soft_level(F, M, a, shape, grid=g, radius=radius, quant=quant, tau=tau, tree=tree, ctx=ctx)
         loss = ((disp - gt) ** 2).mean()
         if backward:
             loss.backward()
@@ -211,7 +216,7 @@ def measure_soft(api, ctx, n_pairs=4, grid=4, radius=3, quant=1):
 
     out = {}
     launches0 = api.kernel_launches()
-    for tau in SOFT_TAUS:
+    for tau in taus:
         for fx, mv, gt, tree in data[:1]:
             step(fx, mv, gt, tree, tau)  # warm-up: buffers
         res = {}
@@ -314,6 +319,11 @@ def main():
     from deedsbcv_gb300 import api, phantom
 
     ctx = api.context(device)
+    if args.soft_only:
+        taus = tuple(float(t) for t in args.soft_taus.split(","))
+        shp = tuple(int(v) for v in args.soft_shape.split("x"))
+        print(json.dumps(measure_soft(api, ctx, n_pairs=args.soft_pairs, taus=taus, shape=shp)), flush=True)
+        return
     pair = make_workload(shape)
     m, n, o = shape
     sz = m * n * o

@@ -32,7 +32,8 @@ CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread", "-Wa
 
 CU_SOURCES = ["mind.cu", "datacost.cu", "mst.cu", "bp.cu", "transform.cu", "noalloc.cu", "soft.cu"]
 # soft.cu has no bit-exactness contract (its reference is a float64 definition),
-# so it may contract multiply-adds.
+# so it may contract multiply-adds and flush denormals (its operands never are:
+# every square root and reciprocal square root argument is >= eps^2).
 FMAD_SOURCES = {"soft.cu"}
 CPP_SOURCES = ["pipeline.cpp", "tree_host.cpp"]
 CLI_SOURCES = {"deedsBCV": ["deedsBCV.cpp", "cli_common.cpp"], "applyBCV": ["applyBCV.cpp", "cli_common.cpp"],
@@ -69,8 +70,8 @@ def build(verbose=False, force=False, cli=True):
         o = os.path.join(OUT, src + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            flags = [("--fmad=true" if f == "--fmad=false" else f) for f in NVCC_FLAGS] if src in FMAD_SOURCES \
-                else NVCC_FLAGS
+            flags = [("--fmad=true" if f == "--fmad=false" else f) for f in NVCC_FLAGS] + ["-ftz=true"] \
+                if src in FMAD_SOURCES else NVCC_FLAGS
             jobs.append(([NVCC] + flags + ["-c", s, "-o", o], o + ".log"))
     for src in CPP_SOURCES:
         s = os.path.join(CSRC, src)

@@ -89,11 +89,13 @@ cudaError_t launch_soft_cost_adj(const float* sF, const float* sM, const float* 
                                  float* sMbar, double* dot, int m, int n, int o, int g, int hw, int q, float alpha1,
                                  float eps, cudaStream_t st);
 size_t soft_tree_smem(int len);
-cudaError_t launch_soft_tree_forward(const SoftTreeDev& d, const int* h_level_start, int n_levels, const float* cost,
-                                     float* B, float* M, float* Mmin, float* logp, float* disp, cudaStream_t st);
-cudaError_t launch_soft_tree_backward(const SoftTreeDev& d, const int* h_level_start, int n_levels, const float* B,
-                                      const float* M, const float* logp, const float* gdisp, float* R, float* Bbar,
-                                      cudaStream_t st);
+// Tree sweeps are persistent kernels; sweep_mem holds sz + 2 ints (ticket, per-node
+// flags, error word).  The error word must be zeroed before the first sweep and is
+// non-zero afterwards if a bounded wait gave up.
+cudaError_t launch_soft_tree_forward(const SoftTreeDev& d, int* sweep_mem, const float* cost, float* B, float* M,
+                                     float* Mmin, float* logp, float* disp, cudaStream_t st);
+cudaError_t launch_soft_tree_backward(const SoftTreeDev& d, int* sweep_mem, const float* B, const float* M,
+                                      const float* logp, const float* gdisp, float* R, float* Bbar, cudaStream_t st);
 cudaError_t launch_popc_probe(int blocks, int threads, int iters, unsigned long long* d_sink, cudaStream_t s);
 cudaError_t launch_jacobian(const float* u, const float* v, const float* w, int m, int n, int o, int g, double* d_acc,
                             cudaStream_t s);

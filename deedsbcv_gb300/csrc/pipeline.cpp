@@ -1170,6 +1170,7 @@ struct SoftLevel {
     SoftTreeDev tree{};
     float *w6 = nullptr, *w6b = nullptr, *sF = nullptr, *sM = nullptr, *cost = nullptr, *B = nullptr, *M = nullptr, *Mmin = nullptr,
           *logp = nullptr, *disp = nullptr;
+    int* sweep = nullptr;  // persistent sweeps: ticket, per-node flags, error word
 };
 
 deeds_status soft_setup(deeds_ctx* ctx, int m, int n, int o, const deeds_soft_params* p, const int* ordered,
@@ -1185,9 +1186,18 @@ deeds_status soft_setup(deeds_ctx* ctx, int m, int n, int o, const deeds_soft_pa
         if (ordered[t] < 0 || ordered[t] >= L.sz1 ||
             (t > 0 && (parents[ordered[t]] < 0 || parents[ordered[t]] >= L.sz1)))
             return fail(ctx, DEEDS_ERR_INVALID, "tree arrays out of range at %d", t);
+    {
+        // every parent must precede its children in `ordered` (the sweeps' ticket order)
+        std::vector<int> pos(L.sz1, -1);
+        for (int t = 0; t < L.sz1; t++) {
+            if (pos[ordered[t]] >= 0) return fail(ctx, DEEDS_ERR_INVALID, "ordered repeats node %d", ordered[t]);
+            pos[ordered[t]] = t;
+        }
+        for (int t = 1; t < L.sz1; t++)
+            if (pos[parents[ordered[t]]] >= t)
+                return fail(ctx, DEEDS_ERR_INVALID, "parent of node %d does not precede it in ordered", ordered[t]);
+    }
     build_schedule(ordered, parents, L.sz1, L.sch);
-    if (L.sch.level_start[L.sch.n_levels] != L.sz1 || L.sch.level_start[1] != 1)
-        return fail(ctx, DEEDS_ERR_INVALID, "ordered/parents do not form a breadth-ordered tree");
     CK(cudaSetDevice(ctx->device));
     deeds_status st = DEEDS_OK;
     // packed tree: ordered | parents | edgemst | child_ptr | children
@@ -1204,7 +1214,9 @@ deeds_status soft_setup(deeds_ctx* ctx, int m, int n, int o, const deeds_soft_pa
     L.Mmin = dbuf<float>(ctx, "soft_Mmin", L.sz1, &st);
     L.logp = dbuf<float>(ctx, "soft_logp", L.sz1 * L.len3, &st);
     L.disp = dbuf<float>(ctx, "soft_disp", 3 * (size_t)L.sz1, &st);
+    L.sweep = dbuf<int>(ctx, "soft_sweep", (size_t)L.sz1 + 2, &st);
     if (st) return st;
+    CK(cudaMemsetAsync(L.sweep + L.sz1 + 1, 0, sizeof(int), s));
     CK(cudaStreamSynchronize(s));  // the pinned staging block is reused across calls
     const size_t o_par = L.sz1, o_edge = 2 * (size_t)L.sz1, o_cptr = 3 * (size_t)L.sz1,
                  o_ch = 4 * (size_t)L.sz1 + 1;
@@ -1232,8 +1244,16 @@ deeds_status soft_run_forward(deeds_ctx* ctx, const float* d_fixed, const float*
     CK(launch_soft_descriptor(d_fixed, L.w6, L.w6b, L.sF, m, n, o, L.qs, s));
     CK(launch_soft_descriptor(d_moving, L.w6, L.w6b, L.sM, m, n, o, L.qs, s));
     CK(launch_soft_cost(L.sF, L.sM, L.cost, m, n, o, p->grid, p->radius, p->quant, soft_alpha1(p), p->eps, s));
-    CK(launch_soft_tree_forward(L.tree, L.sch.level_start.data(), L.sch.n_levels, L.cost, L.B, L.M, L.Mmin, L.logp,
-                                d_disp, s));
+    CK(launch_soft_tree_forward(L.tree, L.sweep, L.cost, L.B, L.M, L.Mmin, L.logp, d_disp, s));
+    return DEEDS_OK;
+}
+
+// Reads the sweeps' error word (synchronises the stream).
+deeds_status soft_check_sweeps(deeds_ctx* ctx, const SoftLevel& L, cudaStream_t s) {
+    int herr = 0;
+    CK(cudaMemcpyAsync(&herr, L.sweep + L.sz1 + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (herr) return fail(ctx, DEEDS_ERR_TIMEOUT, "a tree sweep gave up waiting for a node's dependencies");
     return DEEDS_OK;
 }
 
@@ -1249,7 +1269,8 @@ deeds_status deeds_soft_forward_dev(deeds_ctx* ctx, const float* d_fixed, const 
     cudaStream_t s = (cudaStream_t)stream;
     SoftLevel L;
     if (deeds_status e = soft_setup(ctx, m, n, o, p, ordered, parents, edgemst, s, L)) return e;
-    return soft_run_forward(ctx, d_fixed, d_moving, m, n, o, p, L, d_disp, s);
+    if (deeds_status e = soft_run_forward(ctx, d_fixed, d_moving, m, n, o, p, L, d_disp, s)) return e;
+    return soft_check_sweeps(ctx, L, s);
 }
 
 deeds_status deeds_soft_backward_dev(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, int m, int n, int o,
@@ -1271,8 +1292,7 @@ deeds_status deeds_soft_backward_dev(deeds_ctx* ctx, const float* d_fixed, const
     if (st) return st;
     // recompute the forward state (descriptors, cost, messages, marginals)
     if (deeds_status e = soft_run_forward(ctx, d_fixed, d_moving, m, n, o, p, L, L.disp, s)) return e;
-    CK(launch_soft_tree_backward(L.tree, L.sch.level_start.data(), L.sch.n_levels, L.B, L.M, L.logp, d_gdisp, R, Bbar,
-                                 s));
+    CK(launch_soft_tree_backward(L.tree, L.sweep, L.B, L.M, L.logp, d_gdisp, R, Bbar, s));
     // Bbar is now dL/dcost
     CK(launch_soft_cost_adj(L.sF, L.sM, Bbar, L.cost, sFbar, sMbar, dot, m, n, o, p->grid, p->radius, p->quant,
                             soft_alpha1(p), p->eps, s));
@@ -1284,12 +1304,10 @@ deeds_status deeds_soft_backward_dev(deeds_ctx* ctx, const float* d_fixed, const
         CK(cudaMemsetAsync(d_gmoving, 0, sizeof(float) * L.sz, s));
         CK(launch_soft_descriptor_adj(d_moving, L.w6, L.w6b, sMbar, dbar6, d_gmoving, m, n, o, L.qs, s));
     }
-    if (grad_alpha) {
-        double hdot = 0.0;
-        CK(cudaMemcpyAsync(&hdot, dot, sizeof(double), cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
-        *grad_alpha = (float)(-hdot / (double)p->alpha);
-    }
+    double hdot = 0.0;
+    if (grad_alpha) CK(cudaMemcpyAsync(&hdot, dot, sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (deeds_status e = soft_check_sweeps(ctx, L, s)) return e;
+    if (grad_alpha) *grad_alpha = (float)(-hdot / (double)p->alpha);
     return DEEDS_OK;
 }
 

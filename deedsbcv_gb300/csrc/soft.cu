@@ -35,6 +35,8 @@
 // then the cost, descriptor, box-filter and squared-difference adjoints.  The min
 // subtracted from each message shifts B_parent by a constant to which the marginals
 // are invariant, so it carries no gradient.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -349,6 +351,440 @@ __global__ void k_soft_cost_adj_moving(const float* __restrict__ sF, const float
 }
 
 // ---------------------------------------------------------------------------
+// Halo form of the cost and its adjoint.  The moving descriptor values that one
+// node's samples reach under every label form one box (the node block grown by
+// hw*q on each side, clipped to the volume: the reference's clamp-to-edge maps
+// every displaced position into it).  The box of a group of channels is staged
+// in shared memory with coalesced loads, so the len^3 x samples x channels terms
+// read shared memory only.  For nodes whose box is not clipped the displaced
+// position is a per-sample base plus a per-label offset; clipped (border) nodes
+// clamp per axis.
+
+struct Halo {
+    int y0, x0, z0, HY, HX, HZ, H3;
+    bool interior;
+};
+
+__device__ __forceinline__ Halo node_halo(const SoftGeom& G, int y, int x, int z) {
+    const int R = G.hw * G.q;
+    const int ylo = y * G.g - R, yhi = y * G.g + G.g - 1 + R;
+    const int xlo = x * G.g - R, xhi = x * G.g + G.g - 1 + R;
+    const int zlo = z * G.g - R, zhi = z * G.g + G.g - 1 + R;
+    Halo h;
+    h.y0 = max(0, ylo); h.HY = min(G.m - 1, yhi) - h.y0 + 1;
+    h.x0 = max(0, xlo); h.HX = min(G.n - 1, xhi) - h.x0 + 1;
+    h.z0 = max(0, zlo); h.HZ = min(G.o - 1, zhi) - h.z0 + 1;
+    h.H3 = h.HY * h.HX * h.HZ;
+    h.interior = ylo >= 0 && yhi < G.m && xlo >= 0 && xhi < G.n && zlo >= 0 && zhi < G.o;
+    return h;
+}
+
+__device__ __forceinline__ int label_dy(const SoftGeom& G, int l) { return (l % G.len - G.hw) * G.q; }
+__device__ __forceinline__ int label_dx(const SoftGeom& G, int l) { return ((l / G.len) % G.len - G.hw) * G.q; }
+__device__ __forceinline__ int label_dz(const SoftGeom& G, int l) { return (l / (G.len * G.len) - G.hw) * G.q; }
+
+// sample s of node (y,x,z): voxel coordinates
+__device__ __forceinline__ void sample_pos(const SoftGeom& G, int y, int x, int z, int s, int& py, int& px, int& pz) {
+    py = y * G.g + s % G.g;
+    px = x * G.g + ((s / G.g) % G.nx) * G.S;
+    pz = z * G.g + (s / (G.g * G.nx)) * G.S;
+}
+
+__device__ __forceinline__ int halo_clamped(const SoftGeom& G, const Halo& h, int py, int px, int pz, int l) {
+    const int a = clampi(py + label_dy(G, l), 0, G.m - 1) - h.y0;
+    const int b = clampi(px + label_dx(G, l), 0, G.n - 1) - h.x0;
+    const int c = clampi(pz + label_dz(G, l), 0, G.o - 1) - h.z0;
+    return a + h.HY * (b + h.HX * c);
+}
+
+// Stage channels [c0, c0+CG) of the node's halo (coalesced along y).
+__device__ __forceinline__ void stage_halo(const SoftGeom& G, const Halo& h, const float* __restrict__ vol, int c0,
+                                           int CG, float* hv) {
+    const int64_t mn = (int64_t)G.m * G.n, sz = mn * G.o;
+    for (int e = threadIdx.x; e < CG * h.H3; e += blockDim.x) {
+        const int c = e / h.H3, r = e % h.H3;
+        const int a = r % h.HY, b = (r / h.HY) % h.HX, cc = r / (h.HY * h.HX);
+        hv[e] = vol[(int64_t)(c0 + c) * sz + (h.y0 + a) + (int64_t)(h.x0 + b) * G.m + (int64_t)(h.z0 + cc) * mn];
+    }
+}
+
+constexpr int kHaloLPT = 3;  // labels per thread in the halo cost kernel (len^3 <= 3 * 512)
+
+// C[node][l] from shared-memory halos; threads own labels, CG channels per stage.
+__global__ void __launch_bounds__(512) k_soft_cost_halo(const float* __restrict__ sF, const float* __restrict__ sM,
+                                                        float* __restrict__ cost, SoftGeom G, int CG, int H3max) {
+    extern __shared__ float sh[];
+    const int node = blockIdx.x;
+    const int y = node % G.m1, x = (node / G.m1) % G.n1, z = node / (G.m1 * G.n1);
+    const Halo h = node_halo(G, y, x, z);
+    const int64_t mn = (int64_t)G.m * G.n, sz = mn * G.o;
+    float* hv = sh;                                             // [CG][H3]
+    float* fsm = sh + (size_t)CG * H3max;                       // [CG][nsamp]
+    int* loff = reinterpret_cast<int*>(fsm + CG * G.nsamp);     // [len3]
+    int* sb = loff + G.len3;                                    // [nsamp]
+    for (int l = threadIdx.x; l < G.len3; l += blockDim.x)
+        loff[l] = label_dy(G, l) + h.HY * (label_dx(G, l) + h.HX * label_dz(G, l));
+    for (int s = threadIdx.x; s < G.nsamp; s += blockDim.x) {
+        int py, px, pz;
+        sample_pos(G, y, x, z, s, py, px, pz);
+        sb[s] = (py - h.y0) + h.HY * ((px - h.x0) + h.HX * (pz - h.z0));
+    }
+    float acc[kHaloLPT];
+#pragma unroll
+    for (int k = 0; k < kHaloLPT; k++) acc[k] = 0.0f;
+    const float eps2 = G.eps * G.eps;
+    for (int c0 = 0; c0 < 12; c0 += CG) {
+        __syncthreads();
+        stage_halo(G, h, sM, c0, CG, hv);
+        for (int e = threadIdx.x; e < CG * G.nsamp; e += blockDim.x) {
+            const int c = e / G.nsamp, s = e % G.nsamp;
+            int py, px, pz;
+            sample_pos(G, y, x, z, s, py, px, pz);
+            fsm[e] = sF[(int64_t)(c0 + c) * sz + py + (int64_t)px * G.m + (int64_t)pz * mn];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kHaloLPT; k++) {
+            const int l = threadIdx.x + k * blockDim.x;
+            if (l >= G.len3) break;
+            float a = acc[k];
+            if (h.interior) {
+                const int lo = loff[l];
+                for (int s = 0; s < G.nsamp; s++) {
+                    const int base = sb[s] + lo;
+                    for (int c = 0; c < CG; c++) {
+                        const float d = fsm[c * G.nsamp + s] - hv[c * h.H3 + base];
+                        const float x2 = d * d + eps2;
+                        a += x2 * rsqrtf(x2);
+                    }
+                }
+            } else {
+                for (int s = 0; s < G.nsamp; s++) {
+                    int py, px, pz;
+                    sample_pos(G, y, x, z, s, py, px, pz);
+                    const int base = halo_clamped(G, h, py, px, pz, l);
+                    for (int c = 0; c < CG; c++) {
+                        const float d = fsm[c * G.nsamp + s] - hv[c * h.H3 + base];
+                        const float x2 = d * d + eps2;
+                        a += x2 * rsqrtf(x2);
+                    }
+                }
+            }
+            acc[k] = a;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kHaloLPT; k++) {
+        const int l = threadIdx.x + k * blockDim.x;
+        if (l < G.len3) cost[(int64_t)node * G.len3 + l] = G.alpha1 * (acc[k] - (float)(12 * G.nsamp) * G.eps);
+    }
+}
+
+// Adjoint of the cost from shared-memory halos: threads own (channel, sample)
+// items and walk the labels; each term's gradient goes to the fixed sample (a
+// register) and, through a shared-memory atomic, to the halo position it read;
+// the halo gradients are then added to the moving descriptor's gradient
+// (neighbouring nodes' halos overlap).  Also dot = sum(cbar * C) for alpha.
+__global__ void __launch_bounds__(256) k_soft_cost_adj_halo(const float* __restrict__ sF,
+                                                            const float* __restrict__ sM,
+                                                            const float* __restrict__ cbar,
+                                                            const float* __restrict__ cost, float* __restrict__ sFbar,
+                                                            float* __restrict__ sMbar, double* __restrict__ dot,
+                                                            SoftGeom G, int CG, int H3max) {
+    extern __shared__ float sh[];
+    __shared__ double red[32];
+    const int node = blockIdx.x;
+    const int y = node % G.m1, x = (node / G.m1) % G.n1, z = node / (G.m1 * G.n1);
+    const Halo h = node_halo(G, y, x, z);
+    const int64_t mn = (int64_t)G.m * G.n, sz = mn * G.o;
+    float* hv = sh;                                        // [CG][H3]
+    float* hg = sh + (size_t)CG * H3max;                   // [CG][H3]
+    float* cb = hg + (size_t)CG * H3max;                   // [len3]
+    int* loff = reinterpret_cast<int*>(cb + G.len3);       // [len3]
+    int* sb = loff + G.len3;                               // [nsamp]
+    const float* cbn = cbar + (int64_t)node * G.len3;
+    const float* cn = cost + (int64_t)node * G.len3;
+    // alpha: centred dot product (the exact cbar sums to zero over labels)
+    double csum = 0.0;
+    for (int l = threadIdx.x; l < G.len3; l += blockDim.x) {
+        csum += (double)cn[l];
+        cb[l] = cbn[l];
+        loff[l] = label_dy(G, l) + h.HY * (label_dx(G, l) + h.HX * label_dz(G, l));
+    }
+    for (int off = 16; off > 0; off >>= 1) csum += __shfl_xor_sync(0xffffffffu, csum, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = csum;
+    for (int s = threadIdx.x; s < G.nsamp; s += blockDim.x) {
+        int py, px, pz;
+        sample_pos(G, y, x, z, s, py, px, pz);
+        sb[s] = (py - h.y0) + h.HY * ((px - h.x0) + h.HX * (pz - h.z0));
+    }
+    __syncthreads();
+    double cmean = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) cmean += red[w];
+    cmean /= (double)G.len3;
+    double part = 0.0;
+    for (int l = threadIdx.x; l < G.len3; l += blockDim.x) part += (double)cb[l] * ((double)cn[l] - cmean);
+    for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(dot, part);
+    const float eps2 = G.eps * G.eps;
+    for (int c0 = 0; c0 < 12; c0 += CG) {
+        __syncthreads();
+        stage_halo(G, h, sM, c0, CG, hv);
+        for (int e = threadIdx.x; e < CG * h.H3; e += blockDim.x) hg[e] = 0.0f;
+        __syncthreads();
+        for (int item = threadIdx.x; item < CG * G.nsamp; item += blockDim.x) {
+            const int c = item / G.nsamp, s = item % G.nsamp;
+            int py, px, pz;
+            sample_pos(G, y, x, z, s, py, px, pz);
+            const int64_t p = py + (int64_t)px * G.m + (int64_t)pz * mn;
+            const float f = sF[(int64_t)(c0 + c) * sz + p];
+            const float* hvc = hv + c * h.H3;
+            float* hgc = hg + c * h.H3;
+            float gF = 0.0f;
+            if (h.interior) {
+                const int base = sb[s];
+                for (int l = 0; l < G.len3; l++) {
+                    const int idx = base + loff[l];
+                    const float d = f - hvc[idx];
+                    const float gr = cb[l] * d * rsqrtf(d * d + eps2);
+                    gF += gr;
+                    atomicAdd(hgc + idx, -gr);
+                }
+            } else {
+                for (int l = 0; l < G.len3; l++) {
+                    const int idx = halo_clamped(G, h, py, px, pz, l);
+                    const float d = f - hvc[idx];
+                    const float gr = cb[l] * d * rsqrtf(d * d + eps2);
+                    gF += gr;
+                    atomicAdd(hgc + idx, -gr);
+                }
+            }
+            sFbar[(int64_t)(c0 + c) * sz + p] = G.alpha1 * gF;
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < CG * h.H3; e += blockDim.x) {
+            const float v = hg[e];
+            if (v == 0.0f) continue;
+            const int c = e / h.H3, r = e % h.H3;
+            const int a = r % h.HY, b = (r / h.HY) % h.HX, cc = r / (h.HY * h.HX);
+            atomicAdd(sMbar + (int64_t)(c0 + c) * sz + (h.y0 + a) + (int64_t)(h.x0 + b) * G.m +
+                          (int64_t)(h.z0 + cc) * mn,
+                      G.alpha1 * v);
+        }
+    }
+}
+
+// Column form of the two halo kernels, for compile-time grid spacing, label width
+// and quantisation.  Each node stages a full NA^3 box (NA = g + 2hw*q) of the
+// moving descriptor whose entry (a, b, c) holds the voxel at the clamped
+// coordinates (y*g - hw*q + a, ...): the reference's clamp-to-edge is baked into
+// the staged data, so every displaced sample position is plain box arithmetic.  A
+// thread owns one sampled column of the node (fixed x and z sample offsets, its g
+// samples along y) and one (lx, lz) label pair, and walks the len y-labels: the
+// displaced y positions i + ly*q of its g samples are NA consecutive box entries,
+// loaded once per channel; in the adjoint each entry's gradient is summed in a
+// register before one shared-memory atomic (instead of one per term).
+
+// Block size (whole warps, 128..256) that leaves the fewest idle item slots.
+constexpr int balanced_block(int items) {
+    int best = 256, waste = (items + 255) / 256 * 256 - items;
+    for (int b = 224; b >= 128; b -= 32) {
+        const int w = (items + b - 1) / b * b - items;
+        if (w * 256 < waste * b) { best = b; waste = w; }
+    }
+    return best;
+}
+
+template <int G_, int LEN_, int Q_>
+struct ColGeom {
+    static constexpr int GS = G_, HW = (LEN_ - 1) / 2, R = HW * Q_, NA = G_ + 2 * R, NA3 = NA * NA * NA;
+    static constexpr int S = G_ > 4 ? 2 : 1, NX = (G_ + S - 1) / S, NSAMP = NX * NX * G_;
+    static constexpr int ITEMS = NX * NX * LEN_ * LEN_, LEN3 = LEN_ * LEN_ * LEN_;
+    // forward items: (channel half, column, lx, lz); adjoint items per channel group: (channel, column, lx)
+    static constexpr int FWD_ITEMS = 2 * ITEMS, ADJ_ITEMS = 6 * NX * NX * LEN_;
+    static constexpr int FWD_BLOCK = balanced_block(FWD_ITEMS), ADJ_BLOCK = balanced_block(ADJ_ITEMS);
+};
+
+// Stage channels [c0, c0+CG) of the node's clamped box and, when fs is given, all
+// 12 channels of its fixed samples.
+template <class CGm>
+__device__ __forceinline__ void stage_box(const SoftGeom& G, int y, int x, int z, const float* __restrict__ sM, int c0,
+                                          int CG, float* hv, const float* __restrict__ sF, float* fs) {
+    const int64_t mn = (int64_t)G.m * G.n, sz = mn * G.o;
+    const int yb = y * G.g - CGm::R, xb = x * G.g - CGm::R, zb = z * G.g - CGm::R;
+    for (int e = threadIdx.x; e < CG * CGm::NA3; e += blockDim.x) {
+        const int c = e / CGm::NA3, r = e % CGm::NA3;
+        const int a = r % CGm::NA, b = (r / CGm::NA) % CGm::NA, cc = r / (CGm::NA * CGm::NA);
+        hv[e] = sM[(int64_t)(c0 + c) * sz + clampi(yb + a, 0, G.m - 1) + (int64_t)clampi(xb + b, 0, G.n - 1) * G.m +
+                   (int64_t)clampi(zb + cc, 0, G.o - 1) * mn];
+    }
+    if (fs)
+        for (int e = threadIdx.x; e < 12 * CGm::NSAMP; e += blockDim.x) {
+            const int c = e / CGm::NSAMP, s = e % CGm::NSAMP;
+            const int py = y * CGm::GS + s % CGm::GS, px = x * CGm::GS + ((s / CGm::GS) % CGm::NX) * CGm::S,
+                      pz = z * CGm::GS + (s / (CGm::GS * CGm::NX)) * CGm::S;
+            fs[e] = sF[(int64_t)c * sz + py + (int64_t)px * G.m + (int64_t)pz * mn];
+        }
+}
+
+template <int G_, int LEN_, int Q_>
+__global__ void __launch_bounds__(ColGeom<G_, LEN_, Q_>::FWD_BLOCK)
+    k_soft_cost_col(const float* __restrict__ sF, const float* __restrict__ sM, float* __restrict__ cost, SoftGeom G) {
+    using CGm = ColGeom<G_, LEN_, Q_>;
+    extern __shared__ float sh[];
+    const int node = blockIdx.x;
+    const int y = node % G.m1, x = (node / G.m1) % G.n1, z = node / (G.m1 * G.n1);
+    float* hv = sh;                      // [12][NA3]
+    float* fs = sh + 12 * CGm::NA3;      // [12][NSAMP]
+    float* acc = fs + 12 * CGm::NSAMP;   // [LEN3]
+    stage_box<CGm>(G, y, x, z, sM, 0, 12, hv, sF, fs);
+    for (int l = threadIdx.x; l < CGm::LEN3; l += blockDim.x) acc[l] = 0.0f;
+    __syncthreads();
+    const float eps2 = G.eps * G.eps;
+    for (int item = threadIdx.x; item < CGm::FWD_ITEMS; item += blockDim.x) {
+        const int col = item % (CGm::NX * CGm::NX), lab = (item / (CGm::NX * CGm::NX)) % (LEN_ * LEN_);
+        const int half = item / CGm::ITEMS;
+        const int jj = col % CGm::NX, kk = col / CGm::NX, lx = lab % LEN_, lz = lab / LEN_;
+        const int plane = CGm::NA * ((jj * CGm::S + lx * Q_) + CGm::NA * (kk * CGm::S + lz * Q_));
+        float sums[LEN_][2];
+#pragma unroll
+        for (int ly = 0; ly < LEN_; ly++) sums[ly][0] = sums[ly][1] = 0.0f;
+        for (int c = 6 * half; c < 6 * half + 6; c++) {
+            const float* hvc = hv + c * CGm::NA3 + plane;
+            const float* fsc = fs + c * CGm::NSAMP + G_ * col;
+            float v[CGm::NA], f[G_];
+#pragma unroll
+            for (int a = 0; a < CGm::NA; a++) v[a] = hvc[a];
+#pragma unroll
+            for (int i = 0; i < G_; i++) f[i] = fsc[i];
+#pragma unroll
+            for (int ly = 0; ly < LEN_; ly++)
+#pragma unroll
+                for (int i = 0; i < G_; i++) {
+                    const float d = f[i] - v[i + ly * Q_];
+                    const float x2 = d * d + eps2;
+                    sums[ly][i & 1] += x2 * rsqrtf(x2);
+                }
+        }
+#pragma unroll
+        for (int ly = 0; ly < LEN_; ly++) atomicAdd(acc + ly + LEN_ * lab, sums[ly][0] + sums[ly][1]);
+    }
+    __syncthreads();
+    for (int l = threadIdx.x; l < CGm::LEN3; l += blockDim.x)
+        cost[(int64_t)node * CGm::LEN3 + l] = G.alpha1 * (acc[l] - (float)(12 * CGm::NSAMP) * G.eps);
+}
+
+// Adjoint: an item is one (channel, column, lx) of a channel group; it walks lz
+// (different box rows) and, per row, the len y-labels x g samples: the row's
+// gradient sums are accumulated in registers and added to a shared row buffer with
+// one atomic per entry; the column's fixed-side gradients stay in registers across
+// lz and are added once per item.  Channels are processed in two groups of six so
+// that the shared footprint allows four CTAs per SM; items divide the block evenly.
+constexpr int kAdjCG = 6;
+
+template <int G_, int LEN_, int Q_>
+__global__ void __launch_bounds__(ColGeom<G_, LEN_, Q_>::ADJ_BLOCK)
+    k_soft_cost_adj_col(const float* __restrict__ sF, const float* __restrict__ sM, const float* __restrict__ cbar,
+                        const float* __restrict__ cost, float* __restrict__ sFbar, float* __restrict__ sMbar,
+                        double* __restrict__ dot, SoftGeom G) {
+    using CGm = ColGeom<G_, LEN_, Q_>;
+    extern __shared__ float sh[];
+    __shared__ double red[32];
+    const int node = blockIdx.x;
+    const int y = node % G.m1, x = (node / G.m1) % G.n1, z = node / (G.m1 * G.n1);
+    const int64_t mn = (int64_t)G.m * G.n, sz = mn * G.o;
+    float* hv = sh;                           // [CG][NA3]
+    float* hg = sh + kAdjCG * CGm::NA3;       // [CG][NA3]
+    float* fs = hg + kAdjCG * CGm::NA3;       // [12][NSAMP]
+    float* gfs = fs + 12 * CGm::NSAMP;        // [12][NSAMP]
+    float* cb = gfs + 12 * CGm::NSAMP;        // [LEN3]
+    const float* cbn = cbar + (int64_t)node * CGm::LEN3;
+    const float* cn = cost + (int64_t)node * CGm::LEN3;
+    // alpha: centred dot product (the exact cbar sums to zero over labels)
+    double csum = 0.0;
+    for (int l = threadIdx.x; l < CGm::LEN3; l += blockDim.x) {
+        csum += (double)cn[l];
+        cb[l] = cbn[l];
+    }
+    for (int off = 16; off > 0; off >>= 1) csum += __shfl_xor_sync(0xffffffffu, csum, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = csum;
+    for (int e = threadIdx.x; e < 12 * CGm::NSAMP; e += blockDim.x) gfs[e] = 0.0f;
+    __syncthreads();
+    double cmean = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) cmean += red[w];
+    cmean /= (double)CGm::LEN3;
+    double part = 0.0;
+    for (int l = threadIdx.x; l < CGm::LEN3; l += blockDim.x) part += (double)cb[l] * ((double)cn[l] - cmean);
+    for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(dot, part);
+    const float eps2 = G.eps * G.eps;
+    const int yb = y * G.g - CGm::R, xb = x * G.g - CGm::R, zb = z * G.g - CGm::R;
+    for (int c0 = 0; c0 < 12; c0 += kAdjCG) {
+        __syncthreads();
+        stage_box<CGm>(G, y, x, z, sM, c0, kAdjCG, hv, sF, c0 == 0 ? fs : nullptr);
+        for (int e = threadIdx.x; e < kAdjCG * CGm::NA3; e += blockDim.x) hg[e] = 0.0f;
+        __syncthreads();
+        for (int item = threadIdx.x; item < CGm::ADJ_ITEMS; item += blockDim.x) {
+            const int col = item % (CGm::NX * CGm::NX);
+            const int lx = (item / (CGm::NX * CGm::NX)) % LEN_;
+            const int cl = item / (CGm::NX * CGm::NX * LEN_);
+            const int jj = col % CGm::NX, kk = col / CGm::NX;
+            const float* fsc = fs + (c0 + cl) * CGm::NSAMP + G_ * col;
+            float f[G_], gf[G_];
+#pragma unroll
+            for (int i = 0; i < G_; i++) {
+                f[i] = fsc[i];
+                gf[i] = 0.0f;
+            }
+            for (int lz = 0; lz < LEN_; lz++) {
+                const int plane = CGm::NA * ((jj * CGm::S + lx * Q_) + CGm::NA * (kk * CGm::S + lz * Q_));
+                const float* hvr = hv + cl * CGm::NA3 + plane;
+                float* hgr = hg + cl * CGm::NA3 + plane;
+                const float* cbl = cb + LEN_ * (lx + LEN_ * lz);
+                float v[CGm::NA], gm[CGm::NA];
+#pragma unroll
+                for (int a = 0; a < CGm::NA; a++) {
+                    v[a] = hvr[a];
+                    gm[a] = 0.0f;
+                }
+#pragma unroll
+                for (int ly = 0; ly < LEN_; ly++) {
+                    const float w = cbl[ly];
+#pragma unroll
+                    for (int i = 0; i < G_; i++) {
+                        const float d = f[i] - v[i + ly * Q_];
+                        const float gr = w * d * rsqrtf(d * d + eps2);
+                        gf[i] += gr;
+                        gm[i + ly * Q_] -= gr;
+                    }
+                }
+#pragma unroll
+                for (int a = 0; a < CGm::NA; a++) atomicAdd(hgr + a, gm[a]);
+            }
+#pragma unroll
+            for (int i = 0; i < G_; i++) atomicAdd(gfs + (c0 + cl) * CGm::NSAMP + G_ * col + i, gf[i]);
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < kAdjCG * CGm::NA3; e += blockDim.x) {
+            const float gv = hg[e];
+            if (gv == 0.0f) continue;
+            const int cl = e / CGm::NA3, r = e % CGm::NA3;
+            const int a = r % CGm::NA, b = (r / CGm::NA) % CGm::NA, cc = r / (CGm::NA * CGm::NA);
+            atomicAdd(sMbar + (int64_t)(c0 + cl) * sz + clampi(yb + a, 0, G.m - 1) +
+                          (int64_t)clampi(xb + b, 0, G.n - 1) * G.m + (int64_t)clampi(zb + cc, 0, G.o - 1) * mn,
+                      G.alpha1 * gv);
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 12 * CGm::NSAMP; e += blockDim.x) {
+        const int c = e / CGm::NSAMP, s = e % CGm::NSAMP;
+        const int py = y * G_ + s % G_, px = x * G_ + ((s / G_) % CGm::NX) * CGm::S,
+                  pz = z * G_ + (s / (G_ * CGm::NX)) * CGm::S;
+        sFbar[(int64_t)c * sz + py + (int64_t)px * G.m + (int64_t)pz * mn] = G.alpha1 * gfs[e];
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Tree sweeps
 
 struct SoftTree {
@@ -396,9 +832,9 @@ __device__ void lse_axis(const float* in, float* out, int len, int len3, int s, 
         float acc = 0.0f;
         for (int a = 0; a < len; a++) {
             const float d = (float)(a - b);
-            acc += expf(line[a * s] - d * d * itau - mx);
+            acc += __expf(line[a * s] - d * d * itau - mx);
         }
-        out[o] = mx + logf(acc);
+        out[o] = mx + __logf(acc);
     }
     __syncthreads();
 }
@@ -413,7 +849,7 @@ __device__ void lse_axis_adj(const float* in, const float* out, const float* out
         float acc = 0.0f;
         for (int b = 0; b < len; b++) {
             const float d = (float)(a - b);
-            acc += outbar[base + b * s] * expf(x - d * d * itau - out[base + b * s]);
+            acc += outbar[base + b * s] * __expf(x - d * d * itau - out[base + b * s]);
         }
         inbar[o] = acc;
     }
@@ -437,16 +873,20 @@ __device__ __forceinline__ void sep_lse_adj(const float* in, const float* t1, co
     lse_axis_adj(in, t1, wb, inbar, len, len3, 1, itau);
 }
 
-// Upward sweep over one breadth level (one CTA per node).
-__global__ void k_soft_up_level(SoftTree t, const int* __restrict__ nodes, const float* __restrict__ cost,
-                                float* __restrict__ B, float* __restrict__ M, float* __restrict__ Mmin) {
-    extern __shared__ float sh[];
+// ---- per-node bodies (one CTA per node; data of other nodes written in the same
+// sweep is read with __ldcg, after the producer's release has been observed)
+
+// Upward: B_c = C_c + sum_children (M_k - min M_k), stored minus its minimum (the
+// marginals and the parent's (message - min) are invariant to a constant shift of
+// B_c, and the centred values keep the exponents of the label-space transforms
+// small where the probability mass is); M_c = -tau S(-e_c B_c / tau).
+__device__ void node_up(const SoftTree& t, int c, const float* __restrict__ cost, float* __restrict__ B,
+                        float* __restrict__ M, float* __restrict__ Mmin, float* sh) {
     const int L3 = t.len3;
     float* f = sh;
     float* t1 = sh + L3;
     float* t2 = sh + 2 * L3;
     float* red = sh + 3 * L3;
-    const int c = nodes[blockIdx.x];
     const float e = c == t.root ? 0.0f : t.edgemst[c];
     const int k0 = t.child_ptr[c], k1 = t.child_ptr[c + 1];
     float bmin = INFINITY;
@@ -454,15 +894,11 @@ __global__ void k_soft_up_level(SoftTree t, const int* __restrict__ nodes, const
         float v = cost[(int64_t)c * L3 + l];
         for (int ci = k0; ci < k1; ci++) {
             const int k = t.children[ci];
-            v += M[(int64_t)k * L3 + l] - Mmin[k];
+            v += __ldcg(M + (int64_t)k * L3 + l) - __ldcg(Mmin + k);
         }
         f[l] = v;
         bmin = fminf(bmin, v);
     }
-    // Beliefs are stored minus their minimum: the marginals and the parent's
-    // (message - min) are invariant to a constant shift of B_c, and the centred
-    // values keep the exponents of the label-space transforms small where the
-    // probability mass is.
     bmin = -block_max(-bmin, red);
     for (int l = threadIdx.x; l < L3; l += blockDim.x) {
         const float v = f[l] - bmin;
@@ -482,55 +918,42 @@ __global__ void k_soft_up_level(SoftTree t, const int* __restrict__ nodes, const
     if (threadIdx.x == 0) Mmin[c] = mn;
 }
 
-// Downward marginals over one breadth level; writes log p and the expected displacement.
-__global__ void k_soft_down_level(SoftTree t, const int* __restrict__ nodes, const float* __restrict__ B,
-                                  const float* __restrict__ M, float* __restrict__ logp, float* __restrict__ disp) {
-    extern __shared__ float sh[];
+// Downward marginals; writes log p_c and the expected displacement.  log p_c is
+// normalised in exact arithmetic; renormalising stops float rounding from drifting
+// along root-to-leaf paths (no effect on the exact gradient, whose parameter
+// derivatives are tangent to the normalised set).
+__device__ void node_down(const SoftTree& t, int c, const float* __restrict__ B, const float* __restrict__ M,
+                          float* __restrict__ logp, float* __restrict__ disp, float* sh) {
     const int L3 = t.len3, len = t.len;
     float* r = sh;
     float* t1 = sh + L3;
     float* t2 = sh + 2 * L3;
     float* red = sh + 3 * L3;
-    const int c = nodes[blockIdx.x];
     float* lc = logp + (int64_t)c * L3;
     const float* bc = B + (int64_t)c * L3;
     if (c == t.root) {
-        float mx = -INFINITY;
-        for (int l = threadIdx.x; l < L3; l += blockDim.x) mx = fmaxf(mx, -bc[l] * t.itau);
-        mx = block_max(mx, red);
-        float s = 0.0f;
-        for (int l = threadIdx.x; l < L3; l += blockDim.x) s += expf(-bc[l] * t.itau - mx);
-        s = block_sum(s, red);
-        const float lz = mx + logf(s);
-        for (int l = threadIdx.x; l < L3; l += blockDim.x) r[l] = -bc[l] * t.itau - lz;
-        __syncthreads();
+        for (int l = threadIdx.x; l < L3; l += blockDim.x) r[l] = -bc[l] * t.itau;
     } else {
         const int p = t.parents[c];
         const float e = t.edgemst[c];
         for (int lp = threadIdx.x; lp < L3; lp += blockDim.x)
-            r[lp] = logp[(int64_t)p * L3 + lp] + M[(int64_t)c * L3 + lp] * t.itau;
+            r[lp] = __ldcg(logp + (int64_t)p * L3 + lp) + M[(int64_t)c * L3 + lp] * t.itau;
         __syncthreads();
         sep_lse(r, t1, t2, r, len, L3, t.itau);
-        // log p_c is normalised in exact arithmetic; renormalising stops float
-        // rounding from drifting along root-to-leaf paths (no effect on the exact
-        // gradient, whose parameter derivatives are tangent to the normalised set)
-        float mx = -INFINITY;
-        for (int l = threadIdx.x; l < L3; l += blockDim.x) {
-            r[l] += -e * bc[l] * t.itau;
-            mx = fmaxf(mx, r[l]);
-        }
-        mx = block_max(mx, red);
-        float s = 0.0f;
-        for (int l = threadIdx.x; l < L3; l += blockDim.x) s += expf(r[l] - mx);
-        s = block_sum(s, red);
-        const float lz = mx + logf(s);
-        for (int l = threadIdx.x; l < L3; l += blockDim.x) r[l] -= lz;
-        __syncthreads();
+        for (int l = threadIdx.x; l < L3; l += blockDim.x) r[l] += -e * bc[l] * t.itau;
     }
+    float mx = -INFINITY;
+    for (int l = threadIdx.x; l < L3; l += blockDim.x) mx = fmaxf(mx, r[l]);
+    mx = block_max(mx, red);
+    float s = 0.0f;
+    for (int l = threadIdx.x; l < L3; l += blockDim.x) s += __expf(r[l] - mx);
+    s = block_sum(s, red);
+    const float lz = mx + __logf(s);
     float eu = 0.0f, ev = 0.0f, ew = 0.0f;
     for (int l = threadIdx.x; l < L3; l += blockDim.x) {
-        lc[l] = r[l];
-        const float pl = expf(r[l]);
+        const float lp = r[l] - lz;
+        lc[l] = lp;
+        const float pl = __expf(lp);
         eu += pl * (float)(((l / len) % len - t.hw) * t.q);
         ev += pl * (float)((l % len - t.hw) * t.q);
         ew += pl * (float)((l / (len * len) - t.hw) * t.q);
@@ -545,13 +968,12 @@ __global__ void k_soft_down_level(SoftTree t, const int* __restrict__ nodes, con
     }
 }
 
-// Adjoint of the marginals over one breadth level (run leaves to root).
+// Adjoint of the marginals (leaves to root):
 //   h(l) = gE_c . d(l) p_c(l) + sum_children R_k(l)    (= dL/dlog p_c)
-//   Bbar_c = -e h/tau (root: -(h - p sum h)/tau);  R_c = S^T h w.r.t. r
-__global__ void k_soft_down_adj_level(SoftTree t, const int* __restrict__ nodes, const float* __restrict__ M,
-                                      const float* __restrict__ logp, const float* __restrict__ gdisp,
-                                      float* __restrict__ R, float* __restrict__ Bbar) {
-    extern __shared__ float sh[];
+//   Bbar_c = -e h/tau (root: -(h - p sum h)/tau, projected to zero mean);  R_c = S^T h w.r.t. r
+__device__ void node_down_adj(const SoftTree& t, int c, const float* __restrict__ M, const float* __restrict__ logp,
+                              const float* __restrict__ gdisp, float* __restrict__ R, float* __restrict__ Bbar,
+                              float* sh) {
     const int L3 = t.len3, len = t.len;
     float* r = sh;
     float* t1 = sh + L3;
@@ -560,16 +982,15 @@ __global__ void k_soft_down_adj_level(SoftTree t, const int* __restrict__ nodes,
     float* h = sh + 4 * L3;
     float* wa = sh + 5 * L3;
     float* red = sh + 6 * L3;
-    const int c = nodes[blockIdx.x];
     const float* lc = logp + (int64_t)c * L3;
-    const float gu = gdisp[c], gv = gdisp[t.sz + c], gw = gdisp[2 * t.sz + c];
     const int k0 = t.child_ptr[c], k1 = t.child_ptr[c + 1];
+    const float gu = gdisp[c], gv = gdisp[t.sz + c], gw = gdisp[2 * t.sz + c];
     float tot = 0.0f;
     for (int l = threadIdx.x; l < L3; l += blockDim.x) {
         const float du = (float)(((l / len) % len - t.hw) * t.q), dv = (float)((l % len - t.hw) * t.q),
                     dw = (float)((l / (len * len) - t.hw) * t.q);
-        float v = (gu * du + gv * dv + gw * dw) * expf(lc[l]);
-        for (int ci = k0; ci < k1; ci++) v += R[(int64_t)t.children[ci] * L3 + l];
+        float v = (gu * du + gv * dv + gw * dw) * __expf(lc[l]);
+        for (int ci = k0; ci < k1; ci++) v += __ldcg(R + (int64_t)t.children[ci] * L3 + l);
         h[l] = v;
         tot += v;
     }
@@ -578,7 +999,7 @@ __global__ void k_soft_down_adj_level(SoftTree t, const int* __restrict__ nodes,
         tot = block_sum(tot, red);
         float mean = 0.0f;
         for (int l = threadIdx.x; l < L3; l += blockDim.x) {
-            wa[l] = -(h[l] - expf(lc[l]) * tot) * t.itau;
+            wa[l] = -(h[l] - __expf(lc[l]) * tot) * t.itau;
             mean += wa[l];
         }
         mean = block_sum(mean, red) / (float)L3;
@@ -598,12 +1019,14 @@ __global__ void k_soft_down_adj_level(SoftTree t, const int* __restrict__ nodes,
     for (int l = threadIdx.x; l < L3; l += blockDim.x) rc[l] = wa[l];
 }
 
-// Adjoint of the upward recursion over one breadth level (run root to leaves, root
-// excluded): Mbar_c = R_c/tau + Bbar_parent; M_c = -tau S(f), f = -e B_c/tau, so
-// dL/dB_c += -e/tau S^T(-tau Mbar_c) = e S^T(Mbar_c).  Bbar_c is final afterwards (= cbar_c).
-__global__ void k_soft_up_adj_level(SoftTree t, const int* __restrict__ nodes, const float* __restrict__ B,
-                                    const float* __restrict__ R, float* __restrict__ Bbar) {
-    extern __shared__ float sh[];
+// Adjoint of the upward recursion (root to leaves, root excluded):
+//   Mbar_c = R_c/tau + Bbar_parent; M_c = -tau S(f), f = -e B_c/tau, so
+//   dL/dB_c += -e/tau S^T(-tau Mbar_c) = e S^T(Mbar_c).  Bbar_c is final afterwards
+// (= dL/dC_c); the exact value sums to zero over labels (shift invariance), and
+// projecting keeps rounding from accumulating as a common mode down the tree.
+__device__ void node_up_adj(const SoftTree& t, int c, const float* __restrict__ B, const float* __restrict__ R,
+                            float* __restrict__ Bbar, float* sh) {
+    if (c == t.root) return;
     const int L3 = t.len3, len = t.len;
     float* f = sh;
     float* t1 = sh + L3;
@@ -612,18 +1035,15 @@ __global__ void k_soft_up_adj_level(SoftTree t, const int* __restrict__ nodes, c
     float* mb = sh + 4 * L3;
     float* wa = sh + 5 * L3;
     float* red = sh + 6 * L3;
-    const int c = nodes[blockIdx.x];
     const int p = t.parents[c];
     const float e = t.edgemst[c];
     for (int l = threadIdx.x; l < L3; l += blockDim.x) {
         f[l] = -e * B[(int64_t)c * L3 + l] * t.itau;
-        mb[l] = R[(int64_t)c * L3 + l] * t.itau + Bbar[(int64_t)p * L3 + l];
+        mb[l] = R[(int64_t)c * L3 + l] * t.itau + __ldcg(Bbar + (int64_t)p * L3 + l);
     }
     __syncthreads();
     sep_lse(f, t1, t2, out, len, L3, t.itau);
     sep_lse_adj(f, t1, t2, out, mb, wa, mb, wa, len, L3, t.itau);
-    // the exact dL/dB_c sums to zero over labels (shift invariance); projecting
-    // keeps rounding from accumulating as a common mode down the tree
     float* bb = Bbar + (int64_t)c * L3;
     float mean = 0.0f;
     for (int l = threadIdx.x; l < L3; l += blockDim.x) {
@@ -634,7 +1054,98 @@ __global__ void k_soft_up_adj_level(SoftTree t, const int* __restrict__ nodes, c
     for (int l = threadIdx.x; l < L3; l += blockDim.x) bb[l] = wa[l] - mean;
 }
 
+// ---- persistent sweeps
+//
+// One launch per sweep.  CTAs claim nodes with a global ticket in breadth order
+// (top-down sweeps) or reverse breadth order (bottom-up sweeps), wait until the
+// node's parent (top-down) or all of its children (bottom-up) are finished, run the
+// node body and release it.  A node only waits on nodes with smaller tickets,
+// which were claimed by CTAs that are running and wait only on smaller tickets
+// still, so the sweep always progresses; there are no per-level launches.  Each
+// wait is bounded: on expiry the sweep records an error (reported as a timeout by
+// the host) and carries on, so no CTA can hang.
+
+// Polls of >= 64 ns each (>= 0.13 s in all); a legitimate wait is at most the depth
+// of the tree times one node's latency (milliseconds).  After one wait has given up,
+// no further waits are made, so a failing sweep still ends quickly.
+constexpr long long kSweepSpinLimit = 1LL << 21;
+
+struct SweepState {
+    int* ticket;  // next ticket
+    int* done;    // top-down: 1 when the node is finished; bottom-up: children finished
+    int* err;     // set when a wait gave up
+};
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+enum SweepKind { kSweepUp = 0, kSweepDown = 1, kSweepDownAdj = 2, kSweepUpAdj = 3 };
+
+struct SweepArgs {
+    const float* cost;
+    float* B;
+    float* M;
+    float* Mmin;
+    float* logp;
+    float* disp;
+    const float* gdisp;
+    float* R;
+    float* Bbar;
+};
+
+template <int KIND>
+__global__ void k_soft_sweep(SoftTree t, const int* __restrict__ ordered, SweepArgs a, SweepState st) {
+    extern __shared__ float sh[];
+    __shared__ int s_tk;
+    constexpr bool kTopDown = KIND == kSweepDown || KIND == kSweepUpAdj;
+    for (;;) {
+        if (threadIdx.x == 0) s_tk = atomicAdd(st.ticket, 1);
+        __syncthreads();
+        const int tk = s_tk;
+        if (tk >= t.sz) break;
+        const int c = ordered[kTopDown ? tk : t.sz - 1 - tk];
+        if (threadIdx.x == 0) {
+            const int* flag;
+            int need;
+            if (kTopDown) {
+                flag = c == t.root ? nullptr : st.done + t.parents[c];
+                need = 1;
+            } else {
+                flag = st.done + c;
+                need = t.child_ptr[c + 1] - t.child_ptr[c];
+            }
+            if (flag && need > 0 && ld_acquire(st.err) == 0) {
+                long long it = 0;
+                while (ld_acquire(flag) < need) {
+                    if (++it > kSweepSpinLimit) {
+                        atomicExch(st.err, 1);
+                        break;
+                    }
+                    __nanosleep(64);
+                }
+            }
+        }
+        __syncthreads();
+        if (KIND == kSweepUp) node_up(t, c, a.cost, a.B, a.M, a.Mmin, sh);
+        else if (KIND == kSweepDown) node_down(t, c, a.B, a.M, a.logp, a.disp, sh);
+        else if (KIND == kSweepDownAdj) node_down_adj(t, c, a.M, a.logp, a.gdisp, a.R, a.Bbar, sh);
+        else node_up_adj(t, c, a.B, a.R, a.Bbar, sh);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            if (kTopDown) atomicExch(st.done + c, 1);
+            else if (c != t.root) atomicAdd(st.done + t.parents[c], 1);
+        }
+    }
+}
+
 int soft_threads(int len) { return len * len * len <= 343 ? 128 : 256; }
+
+// one thread per label (rounded to whole warps): the per-node passes are latency bound
+int tree_threads(int len) { return std::min(1024, (len * len * len + 31) / 32 * 32); }
 
 SoftGeom make_geom(int m, int n, int o, int g, int hw, int q, float alpha1, float eps) {
     SoftGeom G;
@@ -694,10 +1205,84 @@ cudaError_t launch_soft_descriptor_adj(const float* d_im, float* w6a, float* w6b
     return cudaGetLastError();
 }
 
+// Channels per halo stage so that the kernel's shared memory stays within ~110 KB
+// (two CTAs per SM); 0 when even one channel does not fit (generic kernels).
+static int halo_channels(const SoftGeom& G, int H3max, int arrays, size_t extra_bytes) {
+    static const int cands[6] = {12, 6, 4, 3, 2, 1};
+    for (int c : cands)
+        if ((size_t)arrays * c * H3max * sizeof(float) + extra_bytes + (arrays == 1 ? (size_t)c * G.nsamp * 4 : 0) <=
+            110 * 1024)
+            return c;
+    return 0;
+}
+
+static int halo_h3max(const SoftGeom& G) {
+    const int R = G.hw * G.q;
+    return std::min(G.g + 2 * R, G.m) * std::min(G.g + 2 * R, G.n) * std::min(G.g + 2 * R, G.o);
+}
+
+// Column kernels are instantiated for the finest-level shapes (grid 4, quant 1,
+// label widths 5/7/9); other shapes use the generic halo kernels.
+template <int G_, int LEN_, int Q_>
+static cudaError_t run_cost_col(const SoftGeom& G, const float* sF, const float* sM, float* cost, cudaStream_t st) {
+    using CGm = ColGeom<G_, LEN_, Q_>;
+    const size_t smem = sizeof(float) * (12 * (size_t)CGm::NA3 + 12 * CGm::NSAMP + CGm::LEN3);
+    if (smem > 200 * 1024) return cudaErrorNotSupported;
+    cudaError_t e = cudaFuncSetAttribute(k_soft_cost_col<G_, LEN_, Q_>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    k_soft_cost_col<G_, LEN_, Q_><<<G.m1 * G.n1 * G.o1, CGm::FWD_BLOCK, smem, st>>>(sF, sM, cost, G);
+    return cudaSuccess;
+}
+
+template <int G_, int LEN_, int Q_>
+static cudaError_t run_cost_adj_col(const SoftGeom& G, const float* sF, const float* sM, const float* cbar,
+                                    const float* cost, float* sFbar, float* sMbar, double* dot, cudaStream_t st) {
+    using CGm = ColGeom<G_, LEN_, Q_>;
+    const size_t smem = sizeof(float) * (2 * kAdjCG * (size_t)CGm::NA3 + 24 * CGm::NSAMP + CGm::LEN3);
+    if (smem > 200 * 1024) return cudaErrorNotSupported;
+    cudaError_t e = cudaFuncSetAttribute(k_soft_cost_adj_col<G_, LEN_, Q_>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_soft_cost_adj_col<G_, LEN_, Q_><<<G.m1 * G.n1 * G.o1, CGm::ADJ_BLOCK, smem, st>>>(sF, sM, cbar, cost, sFbar,
+                                                                                         sMbar, dot, G);
+    return cudaSuccess;
+}
+
+static int col_shape(const SoftGeom& G) {
+    if (G.g != 4 || G.q != 1) return 0;
+    return G.len == 5 || G.len == 7 || G.len == 9 ? G.len : 0;
+}
+
 cudaError_t launch_soft_cost(const float* sF, const float* sM, float* cost, int m, int n, int o, int g, int hw, int q,
                              float alpha1, float eps, cudaStream_t st) {
     const SoftGeom G = make_geom(m, n, o, g, hw, q, alpha1, eps);
-    k_soft_cost<<<G.m1 * G.n1 * G.o1, soft_threads(G.len), sizeof(float) * G.nsamp * 12, st>>>(sF, sM, cost, G);
+    const int H3max = halo_h3max(G);
+    {
+        cudaError_t e = cudaErrorNotSupported;
+        switch (col_shape(G)) {
+            case 5: e = run_cost_col<4, 5, 1>(G, sF, sM, cost, st); break;
+            case 7: e = run_cost_col<4, 7, 1>(G, sF, sM, cost, st); break;
+            case 9: e = run_cost_col<4, 9, 1>(G, sF, sM, cost, st); break;
+            default: break;
+        }
+        if (e == cudaSuccess) {
+            count_launches(1);
+            return cudaGetLastError();
+        }
+        if (e != cudaErrorNotSupported) return e;
+    }
+    const size_t extra = sizeof(int) * (size_t)(G.len3 + G.nsamp);
+    const int CG = G.len3 <= kHaloLPT * 512 ? halo_channels(G, H3max, 1, extra) : 0;
+    if (CG > 0) {
+        const size_t smem = sizeof(float) * ((size_t)CG * H3max + (size_t)CG * G.nsamp) + extra;
+        cudaError_t e = cudaFuncSetAttribute(k_soft_cost_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        const int threads = std::min(512, (G.len3 + 31) / 32 * 32);
+        k_soft_cost_halo<<<G.m1 * G.n1 * G.o1, threads, smem, st>>>(sF, sM, cost, G, CG, H3max);
+    } else {
+        k_soft_cost<<<G.m1 * G.n1 * G.o1, soft_threads(G.len), sizeof(float) * G.nsamp * 12, st>>>(sF, sM, cost, G);
+    }
     count_launches(1);
     return cudaGetLastError();
 }
@@ -710,47 +1295,83 @@ cudaError_t launch_soft_cost_adj(const float* sF, const float* sM, const float* 
     cudaError_t err = cudaMemsetAsync(sFbar, 0, sizeof(float) * 12 * sz, st);
     if (err == cudaSuccess) err = cudaMemsetAsync(dot, 0, sizeof(double), st);
     if (err != cudaSuccess) return err;
-    k_soft_cost_adj_fixed<<<G.m1 * G.n1 * G.o1, 256, 0, st>>>(sF, sM, cbar, cost, sFbar, dot, G);
-    k_soft_cost_adj_moving<<<blocks_for(sz, 128), 128, 0, st>>>(sF, sM, cbar, sMbar, G);
-    count_launches(2);
+    const int H3max = halo_h3max(G);
+    const size_t extra = sizeof(float) * (size_t)G.len3 + sizeof(int) * (size_t)(G.len3 + G.nsamp);
+    const int CG = halo_channels(G, H3max, 2, extra);
+    if (col_shape(G) || CG > 0) {
+        err = cudaMemsetAsync(sMbar, 0, sizeof(float) * 12 * sz, st);
+        if (err != cudaSuccess) return err;
+    }
+    {
+        cudaError_t e = cudaErrorNotSupported;
+        switch (col_shape(G)) {
+            case 5: e = run_cost_adj_col<4, 5, 1>(G, sF, sM, cbar, cost, sFbar, sMbar, dot, st); break;
+            case 7: e = run_cost_adj_col<4, 7, 1>(G, sF, sM, cbar, cost, sFbar, sMbar, dot, st); break;
+            case 9: e = run_cost_adj_col<4, 9, 1>(G, sF, sM, cbar, cost, sFbar, sMbar, dot, st); break;
+            default: break;
+        }
+        if (e == cudaSuccess) {
+            count_launches(1);
+            return cudaGetLastError();
+        }
+        if (e != cudaErrorNotSupported) return e;
+    }
+    if (CG > 0) {
+        const size_t smem = sizeof(float) * 2 * (size_t)CG * H3max + extra;
+        err = cudaFuncSetAttribute(k_soft_cost_adj_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (err != cudaSuccess) return err;
+        k_soft_cost_adj_halo<<<G.m1 * G.n1 * G.o1, 256, smem, st>>>(sF, sM, cbar, cost, sFbar, sMbar, dot, G, CG,
+                                                                     H3max);
+        count_launches(1);
+    } else {
+        k_soft_cost_adj_fixed<<<G.m1 * G.n1 * G.o1, 256, 0, st>>>(sF, sM, cbar, cost, sFbar, dot, G);
+        k_soft_cost_adj_moving<<<blocks_for(sz, 128), 128, 0, st>>>(sF, sM, cbar, sMbar, G);
+        count_launches(2);
+    }
     return cudaGetLastError();
 }
 
 size_t soft_tree_smem(int len) { return sizeof(float) * (6 * (size_t)len * len * len + 32); }
 
-cudaError_t launch_soft_tree_forward(const SoftTreeDev& d, const int* h_level_start, int n_levels, const float* cost,
-                                     float* B, float* M, float* Mmin, float* logp, float* disp, cudaStream_t st) {
-    const SoftTree t = make_tree(d);
-    const size_t smem = sizeof(float) * (3 * (size_t)t.len3 + 32);
-    const int nt = soft_threads(t.len);
-    for (int lev = n_levels - 1; lev >= 0; lev--) {
-        const int b = h_level_start[lev], e = h_level_start[lev + 1];
-        k_soft_up_level<<<e - b, nt, smem, st>>>(t, d.ordered + b, cost, B, M, Mmin);
-    }
-    for (int lev = 0; lev < n_levels; lev++) {
-        const int b = h_level_start[lev], e = h_level_start[lev + 1];
-        k_soft_down_level<<<e - b, nt, smem, st>>>(t, d.ordered + b, B, M, logp, disp);
-    }
-    count_launches(2 * n_levels);
+template <int KIND>
+static cudaError_t run_sweep(const SoftTree& t, const int* ordered, const SweepArgs& a, const SweepState& st,
+                             int* sweep_mem, cudaStream_t s) {
+    const int threads = tree_threads(t.len);
+    const size_t smem = sizeof(float) * ((KIND == kSweepUp || KIND == kSweepDown ? 3 : 6) * (size_t)t.len3 + 32);
+    cudaError_t e = cudaFuncSetAttribute(k_soft_sweep<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, per_sm = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_soft_sweep<KIND>, threads, smem)) != cudaSuccess)
+        return e;
+    const int grid = std::max(1, std::min(t.sz, sms * std::max(per_sm, 1)));
+    // ticket + per-node flags start at zero (the error word is cleared by the caller)
+    if ((e = cudaMemsetAsync(sweep_mem, 0, sizeof(int) * ((size_t)t.sz + 1), s)) != cudaSuccess) return e;
+    k_soft_sweep<KIND><<<grid, threads, smem, s>>>(t, ordered, a, st);
+    count_launches(1);
     return cudaGetLastError();
 }
 
-cudaError_t launch_soft_tree_backward(const SoftTreeDev& d, const int* h_level_start, int n_levels, const float* B,
-                                      const float* M, const float* logp, const float* gdisp, float* R, float* Bbar,
-                                      cudaStream_t st) {
+cudaError_t launch_soft_tree_forward(const SoftTreeDev& d, int* sweep_mem, const float* cost, float* B, float* M,
+                                     float* Mmin, float* logp, float* disp, cudaStream_t s) {
     const SoftTree t = make_tree(d);
-    const size_t smem = soft_tree_smem(t.len);
-    const int nt = soft_threads(t.len);
-    for (int lev = n_levels - 1; lev >= 0; lev--) {
-        const int b = h_level_start[lev], e = h_level_start[lev + 1];
-        k_soft_down_adj_level<<<e - b, nt, smem, st>>>(t, d.ordered + b, M, logp, gdisp, R, Bbar);
-    }
-    for (int lev = 1; lev < n_levels; lev++) {
-        const int b = h_level_start[lev], e = h_level_start[lev + 1];
-        k_soft_up_adj_level<<<e - b, nt, smem, st>>>(t, d.ordered + b, B, R, Bbar);
-    }
-    count_launches(2 * n_levels - 1);
-    return cudaGetLastError();
+    SweepArgs a{cost, B, M, Mmin, logp, disp, nullptr, nullptr, nullptr};
+    const SweepState st{sweep_mem, sweep_mem + 1, sweep_mem + t.sz + 1};
+    cudaError_t e = run_sweep<kSweepUp>(t, d.ordered, a, st, sweep_mem, s);
+    if (e == cudaSuccess) e = run_sweep<kSweepDown>(t, d.ordered, a, st, sweep_mem, s);
+    return e;
+}
+
+cudaError_t launch_soft_tree_backward(const SoftTreeDev& d, int* sweep_mem, const float* B, const float* M,
+                                      const float* logp, const float* gdisp, float* R, float* Bbar, cudaStream_t s) {
+    const SoftTree t = make_tree(d);
+    SweepArgs a{nullptr, const_cast<float*>(B), const_cast<float*>(M), nullptr, const_cast<float*>(logp), nullptr,
+                gdisp, R, Bbar};
+    const SweepState st{sweep_mem, sweep_mem + 1, sweep_mem + t.sz + 1};
+    cudaError_t e = run_sweep<kSweepDownAdj>(t, d.ordered, a, st, sweep_mem, s);
+    if (e == cudaSuccess) e = run_sweep<kSweepUpAdj>(t, d.ordered, a, st, sweep_mem, s);
+    return e;
 }
 
 }  // namespace deeds

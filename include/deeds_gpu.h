@@ -272,7 +272,9 @@ deeds_status deeds_soft_cost_dev(deeds_ctx* ctx, const float* d_desc_fixed, cons
 
 /* Forward: expected displacement (u|v|w) of the soft level.  ordered/parents/
  * edgemst are the host arrays of primsGraph() on the fixed image at this grid
- * (deeds_prims_from_sad).  Synchronous with respect to the host arrays only. */
+ * (deeds_prims_from_sad); every parent must precede its children in `ordered`.
+ * Synchronous (it reads back the tree sweeps' status; DEEDS_ERR_TIMEOUT if a
+ * bounded device-side wait gave up). */
 deeds_status deeds_soft_forward_dev(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, int m, int n, int o,
                                     const deeds_soft_params* p, const int* ordered, const int* parents,
                                     const float* edgemst, float* d_disp, void* stream);
@@ -280,7 +282,7 @@ deeds_status deeds_soft_forward_dev(deeds_ctx* ctx, const float* d_fixed, const 
 /* Backward: given dL/d(displacement) (3 x m1*n1*o1), writes dL/dfixed and
  * dL/dmoving (m*n*o each, overwritten; either may be NULL) and dL/dalpha
  * (host float, may be NULL).  Recomputes the forward sweeps (no state is kept
- * from deeds_soft_forward_dev).  Synchronous when grad_alpha is not NULL. */
+ * from deeds_soft_forward_dev).  Synchronous, like the forward. */
 deeds_status deeds_soft_backward_dev(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, int m, int n, int o,
                                      const deeds_soft_params* p, const int* ordered, const int* parents,
                                      const float* edgemst, const float* d_grad_disp, float* d_grad_fixed,

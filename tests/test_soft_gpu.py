@@ -54,7 +54,7 @@ def test_soft_descriptor_matches_float64(api):
         assert np.abs(s - ref).max() < 2e-4, (qs, np.abs(s - ref).max())
 
 
-@pytest.mark.parametrize("g,hw,q", [(4, 2, 1), (5, 1, 2), (3, 3, 1)])
+@pytest.mark.parametrize("g,hw,q", [(4, 2, 1), (4, 3, 1), (4, 4, 1), (5, 1, 2), (3, 3, 1)])
 def test_soft_cost_matches_float64(api, g, hw, q):
     m, n, o = DIMS
     f, mv = _pair(2)
@@ -87,10 +87,9 @@ def test_soft_forward_matches_float64(api, tau):
     assert torch.allclose(d.double(), ref, atol=2e-3), (d.double() - ref).abs().max()
 
 
-def _grads(api, tau, hw=2, seed=3):
+def _grads(api, tau, hw=2, seed=3, g=4, q=1):
     m, n, o = DIMS
-    g, q = 4, 1
-    f, mv, fd, md, tree = _case(api, seed=seed, hw=hw)
+    f, mv, fd, md, tree = _case(api, seed=seed, hw=hw, g=g)
     sz1 = (m // g) * (n // g) * (o // g)
     gt = torch.from_numpy(np.random.default_rng(seed).normal(0, 1, (3, sz1))).double()
     F = fd.clone().requires_grad_()
@@ -102,16 +101,29 @@ def _grads(api, tau, hw=2, seed=3):
     return f, mv, tree, gt, F.grad.cpu().double(), M.grad.cpu().double(), a.grad.double().item()
 
 
-@pytest.mark.parametrize("tau", [0.1, 0.5, 2.0])
-def test_soft_adjoint_matches_float64_autograd(api, tau):
-    g, hw, q = 4, 2, 1
-    f, mv, tree, gt, gF, gM, ga = _grads(api, tau, hw)
-    d, F, M, a = _ref_disp(f, mv, tree, 1.6, g, hw, q, tau, grad=True)
+@pytest.mark.parametrize("tau,g,hw,q", [(0.1, 4, 2, 1), (0.5, 4, 2, 1), (2.0, 4, 2, 1), (0.5, 4, 3, 1), (0.5, 3, 2, 1),
+                                        (0.5, 5, 1, 2)])
+def test_soft_adjoint_matches_float64_autograd(api, tau, g, hw, q):
+    # (4, *, 1): column kernels; (3, 2, 1) and (5, 1, 2): generic halo kernels
+    f, mv, tree, gt, gF, gM, ga = _grads(api, tau, hw, g=g, q=q)
+    qs = int(0.5 * q + 1.0)
+    F = _t64(f, DIMS).requires_grad_()
+    M = _t64(mv, DIMS).requires_grad_()
+    a = torch.tensor(1.6, dtype=torch.float64, requires_grad=True)
+    cost = sref.soft_cost(sref.soft_mind(F, qs), sref.soft_mind(M, qs), g, hw, q, a, 0.01)
+    cost.retain_grad()
+    d = sref.soft_tree(cost, *tree, hw, q, tau)
     ((d - gt) ** 2).mean().backward()
     for mine, ref in ((gF, F.grad.reshape(-1)), (gM, M.grad.reshape(-1))):
         err = (mine - ref).norm() / ref.norm()
         assert err < 2e-3, err.item()
-    assert abs(ga - a.grad.item()) <= 2e-3 * abs(a.grad.item()) + 1e-9
+    # dL/dalpha = -sum_c sum_l cbar (C - mean_l C) / alpha sums terms of both signs
+    # (cancellation up to ~30x here), so float32 rounding is bounded relative to the
+    # size of those terms rather than to the (small) sum
+    C = cost.detach()
+    terms = (cost.grad * (C - C.mean(dim=1, keepdim=True))).abs().sum().item() / 1.6
+    tol = max(2e-3 * abs(a.grad.item()), 2e-4 * terms)
+    assert abs(ga - a.grad.item()) <= tol, (ga, a.grad.item(), terms)
 
 
 def test_soft_adjoint_matches_central_differences(api):
@@ -174,3 +186,7 @@ def test_soft_invalid_arguments_raise(api):
     bad = (tree[0], np.full_like(tree[1], 10 ** 6), tree[2])
     with pytest.raises(api.DeedsError):
         api.soft_level(fd, md, 1.6, (m, n, o), tree=bad)
+    # a child listed before its parent (the sweeps' order requires parents first)
+    rev = (np.ascontiguousarray(tree[0][::-1]), tree[1], tree[2])
+    with pytest.raises(api.DeedsError):
+        api.soft_level(fd, md, 1.6, (m, n, o), tree=rev)
