@@ -75,11 +75,17 @@ __global__ void k_pad_codes(const uint64_t* __restrict__ M, uint64_t* __restrict
     Mp[y + (int64_t)x * mpp + (int64_t)z * mpp * np] = __ldg(M + src);
 }
 
-template <int G>
+// LEN_T/Q_T > 0: label width and quantisation fixed at compile time (the default
+// level schedule), so every label loop is exact and fully unrolled; 0: runtime
+// values, labels processed in chunks of 8 with guards.
+template <int G, int LEN_T, int Q_T>
 __global__ void __launch_bounds__(256) k_data_cost_tma(const __grid_constant__ CUtensorMap map,
                                                        const uint64_t* __restrict__ F, float* __restrict__ cost,
-                                                       int m, int n, int o, int len, int q, int ny_tile, int yb,
+                                                       int m, int n, int o, int len_rt, int q_rt, int ny_tile, int yb,
                                                        float alpha1, int* __restrict__ err) {
+    constexpr bool kFixed = LEN_T > 0;
+    const int len = kFixed ? LEN_T : len_rt;
+    const int q = kFixed ? Q_T : q_rt;
     constexpr int S = G > 4 ? 2 : 1;  // x and z sampling stride (RAND_SAMPLES=1, src/dataCostD.h:141-155)
     constexpr int NX = (G + S - 1) / S, NZ = (G + S - 1) / S;
     constexpr int NC = NX * NZ;       // sampled (x, z) columns per node
@@ -147,7 +153,20 @@ __global__ void __launch_bounds__(256) k_data_cost_tma(const __grid_constant__ C
         }
         __syncthreads();
         if (!s_ok) break;
-        if (active) {
+        if (kFixed && active) {
+            constexpr int LF = kFixed ? LEN_T : 1, QF = kFixed ? Q_T : 1;
+            int acc[LF];
+#pragma unroll
+            for (int u = 0; u < LF; u++) acc[u] = 0;
+#pragma unroll
+            for (int c = 0; c < NC; c++) {
+                const uint64_t* col = sb + c * yb + pos;
+#pragma unroll
+                for (int u = 0; u < LF; u++) acc[u] += __popcll(fr[c] ^ col[u * QF]);
+            }
+#pragma unroll
+            for (int u = 0; u < LF; u++) wred[u * 32 + lane] = acc[u];
+        } else if (active) {
             for (int ly0 = 0; ly0 < len; ly0 += CHUNK) {
                 int acc[CHUNK];
 #pragma unroll
@@ -256,7 +275,7 @@ size_t data_cost_tma_smem(int g, int hw, int q, int ny_tile) {
     return (size_t)2 * ((NX * NX * yb + 15) & ~15) * 8 + (size_t)warps * len * 32 * 4 + 128;
 }
 
-template <int G>
+template <int G, int LEN_T, int Q_T>
 cudaError_t launch_tma(const uint64_t* d_F, const uint64_t* d_Mp, int mpp, int np, int op, int m, int n, int o,
                        int hw, int q, int ny_tile, float alpha1, float* d_cost, int* d_err, cudaStream_t s) {
     constexpr int S = G > 4 ? 2 : 1;
@@ -277,12 +296,14 @@ cudaError_t launch_tma(const uint64_t* d_F, const uint64_t* d_Mp, int mpp, int n
         return cudaErrorInvalidValue;
     const int warps = (ny_tile + WN - 1) / WN;
     const size_t smem = data_cost_tma_smem(G, hw, q, ny_tile);
-    cudaError_t e = cudaFuncSetAttribute(k_data_cost_tma<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_data_cost_tma<G, LEN_T, Q_T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     const int m1 = m / G, n1 = n / G, o1 = o / G;
     const int tiles_y = (m1 + ny_tile - 1) / ny_tile;
     dim3 grid((unsigned)(tiles_y * n1 * o1), (unsigned)len);
-    k_data_cost_tma<G><<<grid, warps * 32, smem, s>>>(map, d_F, d_cost, m, n, o, len, q, ny_tile, yb, alpha1, d_err);
+    k_data_cost_tma<G, LEN_T, Q_T><<<grid, warps * 32, smem, s>>>(map, d_F, d_cost, m, n, o, len, q, ny_tile, yb,
+                                                                   alpha1, d_err);
     count_launches(1);
     return cudaGetLastError();
 }
@@ -314,16 +335,25 @@ cudaError_t launch_data_cost_tma(const uint64_t* d_F, const uint64_t* d_M, uint6
         k_pad_codes<<<grd, blk, 0, s>>>(d_M, d_Mpad, m, n, o, pad, mpp, np, op);
         count_launches(1);
     }
+    // the default level schedule (-G 8x7x6x5x4 -L 8x7x6x5x4 -Q 5x4x3x2x1) has its
+    // own compile-time instantiations; everything else runs the runtime-width kernel
+#define DEEDS_TMA_ARGS d_F, d_Mpad, mpp, np, op, m, n, o, hw, q, ny_tile, alpha1, d_cost, d_err, s
+    if (g == 8 && hw == 8 && q == 5) return launch_tma<8, 17, 5>(DEEDS_TMA_ARGS);
+    if (g == 7 && hw == 7 && q == 4) return launch_tma<7, 15, 4>(DEEDS_TMA_ARGS);
+    if (g == 6 && hw == 6 && q == 3) return launch_tma<6, 13, 3>(DEEDS_TMA_ARGS);
+    if (g == 5 && hw == 5 && q == 2) return launch_tma<5, 11, 2>(DEEDS_TMA_ARGS);
+    if (g == 4 && hw == 4 && q == 1) return launch_tma<4, 9, 1>(DEEDS_TMA_ARGS);
     switch (g) {
-        case 2: return launch_tma<2>(d_F, d_Mpad, mpp, np, op, m, n, o, hw, q, ny_tile, alpha1, d_cost, d_err, s);
-        case 3: return launch_tma<3>(d_F, d_Mpad, mpp, np, op, m, n, o, hw, q, ny_tile, alpha1, d_cost, d_err, s);
-        case 4: return launch_tma<4>(d_F, d_Mpad, mpp, np, op, m, n, o, hw, q, ny_tile, alpha1, d_cost, d_err, s);
-        case 5: return launch_tma<5>(d_F, d_Mpad, mpp, np, op, m, n, o, hw, q, ny_tile, alpha1, d_cost, d_err, s);
-        case 6: return launch_tma<6>(d_F, d_Mpad, mpp, np, op, m, n, o, hw, q, ny_tile, alpha1, d_cost, d_err, s);
-        case 7: return launch_tma<7>(d_F, d_Mpad, mpp, np, op, m, n, o, hw, q, ny_tile, alpha1, d_cost, d_err, s);
-        case 8: return launch_tma<8>(d_F, d_Mpad, mpp, np, op, m, n, o, hw, q, ny_tile, alpha1, d_cost, d_err, s);
+        case 2: return launch_tma<2, 0, 0>(DEEDS_TMA_ARGS);
+        case 3: return launch_tma<3, 0, 0>(DEEDS_TMA_ARGS);
+        case 4: return launch_tma<4, 0, 0>(DEEDS_TMA_ARGS);
+        case 5: return launch_tma<5, 0, 0>(DEEDS_TMA_ARGS);
+        case 6: return launch_tma<6, 0, 0>(DEEDS_TMA_ARGS);
+        case 7: return launch_tma<7, 0, 0>(DEEDS_TMA_ARGS);
+        case 8: return launch_tma<8, 0, 0>(DEEDS_TMA_ARGS);
         default: return cudaErrorInvalidValue;
     }
+#undef DEEDS_TMA_ARGS
 }
 
 cudaError_t launch_data_cost(const uint64_t* d_F, const uint64_t* d_M, int m, int n, int o, int g, int hw, int q,
