@@ -14,24 +14,84 @@
 #include <cstdint>
 #include <cstring>
 #include <stdexcept>
+#include <thread>
 #include <vector>
 
 #include "tree_host.h"
 
 namespace deeds {
 
+// The reference's statistics (src/primsMST.h:101-110) are sequential float sums:
+// mean += im[i], then var = float(double(var) + double(im[i]-mean)^2) -- a double
+// rounding per step.  The square of a float is exact in double, so each step
+// equals fmaf(d, d, var) (one rounding) except where the double rounding lands
+// on a float tie.  The variance chain is therefore run with fmaf (half the
+// dependency latency), keeping a checkpoint at the start of each of kChunks
+// chunks; the chunks are then replayed in parallel and every step is checked
+// against the reference's double-rounded formula.  From the first step where
+// the two differ (if any) the chain is recomputed with the reference formula,
+// so the result is always the reference's.
 void image_stats(const float* im, size_t sz, float* mean_out, float* std_out) {
     float mean = 0.0f;
     for (size_t i = 0; i < sz; i++) mean += im[i];
     mean /= (float)sz;
+    constexpr int kChunks = 8;
+    float check[kChunks + 1];
+    size_t bound[kChunks + 1];
+    for (int c = 0; c <= kChunks; c++) bound[c] = sz * (size_t)c / kChunks;
     float var = 0.0f;
-    for (size_t i = 0; i < sz; i++) {
-        const double d = (double)(im[i] - mean);
-        var = (float)((double)var + d * d);  // float += pow(float,2) in double
+    for (int c = 0; c < kChunks; c++) {
+        check[c] = var;
+        for (size_t i = bound[c]; i < bound[c + 1]; i++) {
+            const float d = im[i] - mean;
+            var = std::fma(d, d, var);
+        }
+    }
+    check[kChunks] = var;
+    size_t first_bad[kChunks];
+    auto verify = [&](int c) {
+        first_bad[c] = sz;
+        float v = check[c];
+        for (size_t i = bound[c]; i < bound[c + 1]; i++) {
+            const float d = im[i] - mean;
+            const float fast = std::fma(d, d, v);
+            if ((float)((double)v + (double)d * (double)d) != fast) {
+                first_bad[c] = i;
+                return;
+            }
+            v = fast;
+        }
+    };
+    if (sz >= ((size_t)1 << 20)) {
+        std::vector<std::thread> th;
+        for (int c = 1; c < kChunks; c++) th.emplace_back(verify, c);
+        verify(0);
+        for (auto& t : th) t.join();
+    } else {
+        for (int c = 0; c < kChunks; c++) verify(c);
+    }
+    for (int c = 0; c < kChunks; c++) {
+        if (first_bad[c] == sz) continue;
+        // replay the chunk's fast steps up to the first difference, then the reference formula
+        float v = check[c];
+        for (size_t i = bound[c]; i < first_bad[c]; i++) {
+            const float d = im[i] - mean;
+            v = std::fma(d, d, v);
+        }
+        for (size_t i = first_bad[c]; i < sz; i++) {
+            const double d = (double)(im[i] - mean);
+            v = (float)((double)v + d * d);  // float += pow(float,2) in double
+        }
+        var = v;
+        break;
     }
     *mean_out = mean;
     *std_out = std::sqrt(var / (float)sz);
 }
+
+#ifndef DEEDS_HEAP_LOOKAHEAD
+#define DEEDS_HEAP_LOOKAHEAD 3
+#endif
 
 namespace {
 // A candidate edge: weight and (from vertex, direction).  The reference stores
@@ -73,6 +133,17 @@ class EdgeHeap {
         QueuedEdge* d = a_.data();
         size_t hole = 0, child = 0;
         while (child < (len - 1) / 2) {
+            // The descendants of the hole k levels down are the 2^k contiguous
+            // entries from 2^k (hole + 1) - 1: prefetch those DEEDS_HEAP_LOOKAHEAD
+            // levels ahead so the misses of a root-to-leaf walk overlap.
+            {
+                const size_t k = DEEDS_HEAP_LOOKAHEAD;
+                const size_t first = ((hole + 1) << k) - 1;
+                if (first < len) {
+                    __builtin_prefetch(d + first);
+                    if (k >= 4 && first + 8 < len) __builtin_prefetch(d + first + 8);
+                }
+            }
             child = 2 * (child + 1);  // right child
             const size_t gc = 2 * child + 1;
             if (gc < len) __builtin_prefetch(d + gc);
