@@ -12,6 +12,20 @@ namespace deeds {
 
 __host__ __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
+// Exact float -> double widening with integer operations: on GB300 the FP64
+// pipe (which also executes F2F conversions) is the bound of the trilinear
+// warps, and widening a float is exact.  Normal numbers re-bias the exponent
+// and shift the mantissa; zeros keep their sign; subnormals, infinities and NaNs
+// (not expected in images or displacement fields) take the hardware conversion.
+__device__ __forceinline__ double f2d(float f) {
+    const uint32_t b = __float_as_uint(f);
+    const uint32_t e = (b >> 23) & 0xffu;
+    if (e == 0xffu || (e == 0u && (b & 0x7fffffu) != 0u)) return (double)f;
+    const uint64_t sign = (uint64_t)(b & 0x80000000u) << 32;
+    const uint64_t mag = e == 0u ? 0ull : ((uint64_t)(e + 896u) << 52) | ((uint64_t)(b & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)(sign | mag));
+}
+
 // Trilinear 8-term blend with the reference's evaluation types and order
 // (src/transformations.h:15-22, src/dataCostD.h:288-295): terms touching the
 // double literal 1.0 are double, dx*dy and dx*dy*dz*v are float, the sum is
@@ -24,31 +38,32 @@ struct Blend8Weights {
 
 __device__ __forceinline__ Blend8Weights blend8_weights(float dx, float dy, float dz) {
     Blend8Weights b;
-    const double a = 1.0 - (double)dx, bb = 1.0 - (double)dy, c = 1.0 - (double)dz;
-    const double ab = a * bb;             // (1-dx)(1-dy)
-    const double ady = a * (double)dy;    // (1-dx)dy
-    const double dxb = (double)dx * bb;   // dx(1-dy)
+    const double ddx = f2d(dx), ddy = f2d(dy), ddz = f2d(dz);
+    const double a = 1.0 - ddx, bb = 1.0 - ddy, c = 1.0 - ddz;
+    const double ab = a * bb;     // (1-dx)(1-dy)
+    const double ady = a * ddy;   // (1-dx)dy
+    const double dxb = ddx * bb;  // dx(1-dy)
     b.w000 = ab * c;
     b.w100 = ady * c;
     b.w010 = dxb * c;
-    b.w001 = ab * (double)dz;
-    b.w110 = (double)(dx * dy) * c;
-    b.w101 = ady * (double)dz;
-    b.w011 = dxb * (double)dz;
+    b.w001 = ab * ddz;
+    b.w110 = f2d(dx * dy) * c;
+    b.w101 = ady * ddz;
+    b.w011 = dxb * ddz;
     b.dxdydz = dx * dy * dz;
     return b;
 }
 
 __device__ __forceinline__ float blend8_apply(const Blend8Weights& b, float c000, float c100, float c010,
                                               float c001, float c110, float c101, float c011, float c111) {
-    double acc = b.w000 * (double)c000;
-    acc = acc + b.w100 * (double)c100;
-    acc = acc + b.w010 * (double)c010;
-    acc = acc + b.w001 * (double)c001;
-    acc = acc + b.w110 * (double)c110;
-    acc = acc + b.w101 * (double)c101;
-    acc = acc + b.w011 * (double)c011;
-    acc = acc + (double)(b.dxdydz * c111);
+    double acc = b.w000 * f2d(c000);
+    acc = acc + b.w100 * f2d(c100);
+    acc = acc + b.w010 * f2d(c010);
+    acc = acc + b.w001 * f2d(c001);
+    acc = acc + b.w110 * f2d(c110);
+    acc = acc + b.w101 * f2d(c101);
+    acc = acc + b.w011 * f2d(c011);
+    acc = acc + f2d(b.dxdydz * c111);
     return (float)acc;
 }
 
