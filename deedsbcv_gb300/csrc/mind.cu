@@ -37,30 +37,37 @@ __constant__ int c_sz[12] = {0, 0, 0, 0, -1, 0, -1, 0, -1, 0, -1, 0};
 // is staged in shared memory with coalesced loads; each thread streams one
 // (channel, line) through the sequential box sum; outputs go through a shared
 // tile so that the six channel planes are written with coalesced stores.
+// The radius QS is a compile-time constant and chunks start at multiples of 16,
+// so every index into the ring of prefix values is static after unrolling and the
+// ring lives in registers (a runtime index would place it in local memory); the
+// tail outputs are emitted at the line's last step for the same reason.
 constexpr int TJ = 32;  // lines per CTA
-constexpr int CH = 32;  // i samples per chunk
+constexpr int CH = 32;  // i samples per chunk (a multiple of kRing)
 
+template <int QS>
 __global__ void __launch_bounds__(6 * TJ) k_pass_i(const float* __restrict__ im, float* __restrict__ D, int m, int n,
-                                                   int o, int qs) {
+                                                   int o) {
     extern __shared__ float sm[];
-    const int W = CH + 2 * qs + 1;         // padded row length of the image tile
-    const int R = TJ + 2 * qs;             // image rows per k slice
+    constexpr int W = CH + 2 * QS + 1;     // padded row length of the image tile
+    constexpr int WL = CH + 2 * QS;        // loaded row length
+    constexpr int R = TJ + 2 * QS;         // image rows per k slice
     float* T = sm;                         // [2][R][W]
     float* O = sm + 2 * R * W;             // [6][TJ][CH+1]
     const int k = blockIdx.y, j0 = blockIdx.x * TJ;
     const int l = threadIdx.x / TJ, jj = threadIdx.x % TJ, j = j0 + jj;
     const int64_t mn = (int64_t)m * n, sz = mn * o;
-    const int dx = c_dx[l] * qs, dy = c_dy[l] * qs, dz = c_dz[l] * qs;
+    const int dx = c_dx[l] * QS, dy = c_dy[l] * QS, dz = c_dz[l] * QS;
     const bool line_ok = j < n;
     const bool other_ok = j + dx >= 0 && j + dx < n && k + dz < o;
     const int kk = dz ? 1 : 0;
+    float* gout = D + l * sz + (int64_t)j * m + (int64_t)k * mn;
     float ring[kRing];
     float P = 0.0f;
     for (int i0 = 0; i0 < m; i0 += CH) {
         __syncthreads();  // previous chunk's tiles are consumed
-        for (int e = threadIdx.x; e < 2 * R * (CH + 2 * qs); e += blockDim.x) {
-            const int ip = e % (CH + 2 * qs), r = (e / (CH + 2 * qs)) % R, z = e / ((CH + 2 * qs) * R);
-            const int ii = i0 - qs + ip, jr = j0 - qs + r, kz = k + z * qs;
+        for (int e = threadIdx.x; e < 2 * R * WL; e += blockDim.x) {
+            const int ip = e % WL, r = (e / WL) % R, z = e / (WL * R);
+            const int ii = i0 - QS + ip, jr = j0 - QS + r, kz = k + z * QS;
             float v = 0.0f;
             if (ii >= 0 && ii < m && jr >= 0 && jr < n && kz < o) v = im[ii + (int64_t)jr * m + (int64_t)kz * mn];
             T[(z * R + r) * W + ip] = v;
@@ -68,42 +75,47 @@ __global__ void __launch_bounds__(6 * TJ) k_pass_i(const float* __restrict__ im,
         __syncthreads();
         const int cend = min(CH, m - i0);
         if (line_ok) {
-            const float* self = T + (jj + qs) * W + qs;
-            const float* oth = T + (kk * R + jj + qs + dx) * W + qs + dy;
+            const float* self = T + (jj + QS) * W + QS;
+            const float* oth = T + (kk * R + jj + QS + dx) * W + QS + dy;
             float* out = O + (l * TJ + jj) * (CH + 1);
-            for (int u = 0; u < cend; u++) {
-                const int t = i0 + u;
-                const float s = self[u];
-                const float v = (other_ok && t + dy >= 0 && t + dy < m) ? oth[u] : s;
-                const float d = v - s;
-                const float x = d * d;
-                P = (t == 0) ? x : P + x;
-                ring[t & (kRing - 1)] = P;
-                const int i = t - qs;  // output position (lag r = qs)
-                if (i >= 0) out[u] = (i <= qs) ? P : P - ring[(t - 2 * qs - 1) & (kRing - 1)];
+#pragma unroll
+            for (int u = 0; u < CH; u++) {
+                if (u < cend) {
+                    const int t = i0 + u;
+                    const float s = self[u];
+                    const float v = (other_ok && t + dy >= 0 && t + dy < m) ? oth[u] : s;
+                    const float d = v - s;
+                    const float x = d * d;
+                    P = (t == 0) ? x : P + x;
+                    ring[u & (kRing - 1)] = P;  // i0 is a multiple of kRing
+                    const int i = t - QS;       // output position (lag r = QS)
+                    if (i >= 0) out[u] = (i <= QS) ? P : P - ring[(u - 2 * QS - 1) & (kRing - 1)];
+                    if (t == m - 1) {
+                        // tail: i in [m-QS, m): P[m-1] - P[i-QS-1]
+#pragma unroll
+                        for (int s2 = 0; s2 < QS; s2++) gout[m - QS + s2] = P - ring[(u - 2 * QS + s2) & (kRing - 1)];
+                    }
+                }
             }
         }
         __syncthreads();
-        // coalesced store of outputs i0-qs .. i0+cend-1-qs
+        // coalesced store of outputs i0-QS .. i0+cend-1-QS
         for (int e = threadIdx.x; e < 6 * TJ * cend; e += blockDim.x) {
             const int u = e % cend, line = e / cend;
             const int ll = line / TJ, jl = line % TJ, jg = j0 + jl;
-            const int i = i0 + u - qs;
+            const int i = i0 + u - QS;
             if (i >= 0 && jg < n) D[ll * sz + i + (int64_t)jg * m + (int64_t)k * mn] = O[(ll * TJ + jl) * (CH + 1) + u];
         }
-    }
-    // tail: i in [m-qs, m): P[m-1] - P[i-qs-1]
-    if (line_ok) {
-        float* out = D + l * sz + (int64_t)j * m + (int64_t)k * mn;
-        for (int i = (m - qs > 0 ? m - qs : 0); i < m; i++) out[i] = P - ring[(i - qs - 1) & (kRing - 1)];
     }
 }
 
 // In-place box pass along j (axis=1) or k (axis=2); threads over consecutive i.
 // Samples are loaded CHUNK at a time before any of the chunk's outputs (which
-// lag by r) are stored, so the loads of a chunk are independent.
-template <int CHUNK>
-__global__ void k_pass_jk(float* __restrict__ D, int m, int n, int o, int qs, int axis) {
+// lag by r) are stored, so the loads of a chunk are independent; with CHUNK a
+// multiple of kRing and QS fixed at compile time the ring stays in registers.
+template <int QS>
+__global__ void k_pass_jk(float* __restrict__ D, int m, int n, int o, int axis) {
+    constexpr int CHUNK = kRing;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int b = blockIdx.y;  // the other coordinate: k for axis 1, j for axis 2
     const int l = blockIdx.z;
@@ -125,13 +137,17 @@ __global__ void k_pass_jk(float* __restrict__ D, int m, int n, int o, int qs, in
             const int t = c0 + u;
             if (t < L) {
                 P = (t == 0) ? x[u] : P + x[u];
-                ring[t & (kRing - 1)] = P;
-                const int io = t - qs;
-                if (io >= 0) base[io * stride] = (io <= qs) ? P : P - ring[(t - 2 * qs - 1) & (kRing - 1)];
+                ring[u] = P;  // c0 is a multiple of kRing
+                const int io = t - QS;
+                if (io >= 0) base[io * stride] = (io <= QS) ? P : P - ring[(u - 2 * QS - 1) & (kRing - 1)];
+                if (t == L - 1) {
+#pragma unroll
+                    for (int s2 = 0; s2 < QS; s2++)
+                        base[(L - QS + s2) * stride] = P - ring[(u - 2 * QS + s2) & (kRing - 1)];
+                }
             }
         }
     }
-    for (int io = (L - qs > 0 ? L - qs : 0); io < L; io++) base[io * stride] = P - ring[(io - qs - 1) & (kRing - 1)];
 }
 
 __global__ void k_quantise(const float* __restrict__ D, uint64_t* __restrict__ codes, int m, int n, int o, int qs,
@@ -169,24 +185,26 @@ __global__ void k_quantise(const float* __restrict__ D, uint64_t* __restrict__ c
 
 }  // namespace
 
+template <int QS>
+static void mind_passes(const float* d_im, int m, int n, int o, float* d_scratch, cudaStream_t s) {
+    const size_t smem = (size_t)(2 * (TJ + 2 * QS) * (CH + 2 * QS + 1) + 6 * TJ * (CH + 1)) * sizeof(float);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_pass_i<QS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_pass_i<QS><<<dim3((n + TJ - 1) / TJ, o), 6 * TJ, smem, s>>>(d_im, d_scratch, m, n, o);
+    k_pass_jk<QS><<<dim3((m + 127) / 128, o, 6), 128, 0, s>>>(d_scratch, m, n, o, 1);
+    k_pass_jk<QS><<<dim3((m + 127) / 128, n, 6), 128, 0, s>>>(d_scratch, m, n, o, 2);
+}
+
 cudaError_t launch_mind_ssc(const float* d_im, int m, int n, int o, int qs, const float thr[5], float* d_scratch,
                             uint64_t* d_codes, cudaStream_t s) {
-    {
-        const size_t smem = (size_t)(2 * (TJ + 2 * qs) * (CH + 2 * qs + 1) + 6 * TJ * (CH + 1)) * sizeof(float);
-        if (smem > 48 * 1024) {
-            cudaError_t e = cudaFuncSetAttribute(k_pass_i, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess) return e;
-        }
-        dim3 grd((n + TJ - 1) / TJ, o);
-        k_pass_i<<<grd, 6 * TJ, smem, s>>>(d_im, d_scratch, m, n, o, qs);
-    }
-    {
-        dim3 blk(128), grd((m + 127) / 128, o, 6);
-        k_pass_jk<8><<<grd, blk, 0, s>>>(d_scratch, m, n, o, qs, 1);
-    }
-    {
-        dim3 blk(128), grd((m + 127) / 128, n, 6);
-        k_pass_jk<8><<<grd, blk, 0, s>>>(d_scratch, m, n, o, qs, 2);
+    switch (qs) {
+        case 1: mind_passes<1>(d_im, m, n, o, d_scratch, s); break;
+        case 2: mind_passes<2>(d_im, m, n, o, d_scratch, s); break;
+        case 3: mind_passes<3>(d_im, m, n, o, d_scratch, s); break;
+        case 4: mind_passes<4>(d_im, m, n, o, d_scratch, s); break;
+        case 5: mind_passes<5>(d_im, m, n, o, d_scratch, s); break;
+        case 6: mind_passes<6>(d_im, m, n, o, d_scratch, s); break;
+        case 7: mind_passes<7>(d_im, m, n, o, d_scratch, s); break;
+        default: return cudaErrorInvalidValue;
     }
     {
         dim3 blk(128), grd((m + 127) / 128, n, o);
