@@ -1201,7 +1201,7 @@ deeds_status soft_setup(deeds_ctx* ctx, int m, int n, int o, const deeds_soft_pa
     CK(cudaSetDevice(ctx->device));
     deeds_status st = DEEDS_OK;
     // packed tree: ordered | parents | edgemst | child_ptr | children
-    const size_t words = (size_t)L.sz1 * 4 + 1 + (L.sz1 > 0 ? L.sz1 - 1 : 0) + 1;
+    const size_t words = (size_t)L.sz1 * 5 + 2;
     uint32_t* h = hbuf<uint32_t>(ctx, "soft_tree_h", words, &st);
     uint32_t* d = dbuf<uint32_t>(ctx, "soft_tree_d", words, &st);
     L.w6 = dbuf<float>(ctx, "soft_w6", 6 * L.sz, &st);
