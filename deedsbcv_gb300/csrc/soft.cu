@@ -612,12 +612,18 @@ __device__ __forceinline__ void stage_box(const SoftGeom& G, int y, int x, int z
                                           int CG, float* hv, const float* __restrict__ sF, float* fs) {
     const int64_t mn = (int64_t)G.m * G.n, sz = mn * G.o;
     const int yb = y * G.g - CGm::R, xb = x * G.g - CGm::R, zb = z * G.g - CGm::R;
-    for (int e = threadIdx.x; e < CG * CGm::NA3; e += blockDim.x) {
-        const int c = e / CGm::NA3, r = e % CGm::NA3;
-        const int a = r % CGm::NA, b = (r / CGm::NA) % CGm::NA, cc = r / (CGm::NA * CGm::NA);
-        hv[e] = sM[(int64_t)(c0 + c) * sz + clampi(yb + a, 0, G.m - 1) + (int64_t)clampi(xb + b, 0, G.n - 1) * G.m +
-                   (int64_t)clampi(zb + cc, 0, G.o - 1) * mn];
-    }
+    // a warp stages 32/NA box rows at a time: lane -> (row within the group, y offset)
+    constexpr int RPW = 32 / CGm::NA;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int sub = lane / CGm::NA, a = lane - sub * CGm::NA;
+    const int ya = clampi(yb + a, 0, G.m - 1);
+    const int nrows = CG * CGm::NA * CGm::NA;
+    if (sub < RPW)
+        for (int r = warp * RPW + sub; r < nrows; r += nw * RPW) {
+            const int b = r % CGm::NA, t = r / CGm::NA, cc = t % CGm::NA, c = t / CGm::NA;
+            hv[r * CGm::NA + a] = sM[(int64_t)(c0 + c) * sz + ya + (int64_t)clampi(xb + b, 0, G.n - 1) * G.m +
+                                     (int64_t)clampi(zb + cc, 0, G.o - 1) * mn];
+        }
     if (fs)
         for (int e = threadIdx.x; e < 12 * CGm::NSAMP; e += blockDim.x) {
             const int c = e / CGm::NSAMP, s = e % CGm::NSAMP;
@@ -628,7 +634,7 @@ __device__ __forceinline__ void stage_box(const SoftGeom& G, int y, int x, int z
 }
 
 template <int G_, int LEN_, int Q_>
-__global__ void __launch_bounds__(ColGeom<G_, LEN_, Q_>::FWD_BLOCK)
+__global__ void __launch_bounds__(ColGeom<G_, LEN_, Q_>::FWD_BLOCK, 4)
     k_soft_cost_col(const float* __restrict__ sF, const float* __restrict__ sM, float* __restrict__ cost, SoftGeom G) {
     using CGm = ColGeom<G_, LEN_, Q_>;
     extern __shared__ float sh[];
@@ -641,33 +647,47 @@ __global__ void __launch_bounds__(ColGeom<G_, LEN_, Q_>::FWD_BLOCK)
     for (int l = threadIdx.x; l < CGm::LEN3; l += blockDim.x) acc[l] = 0.0f;
     __syncthreads();
     const float eps2 = G.eps * G.eps;
-    for (int item = threadIdx.x; item < CGm::FWD_ITEMS; item += blockDim.x) {
-        const int col = item % (CGm::NX * CGm::NX), lab = (item / (CGm::NX * CGm::NX)) % (LEN_ * LEN_);
-        const int half = item / CGm::ITEMS;
+    // items are (column, lab, channel half) with the column fastest: the NX^2 = 16
+    // columns of one (lab, half) are the 16 lanes of a half-warp (the block is a
+    // multiple of 16 threads), whose label sums are reduced with shuffles before
+    // one shared-memory add per label
+    static_assert(CGm::NX * CGm::NX == 16, "column kernels assume 16 sampled columns per node");
+    for (int base = 0; base < CGm::FWD_ITEMS; base += blockDim.x) {
+        const int item = base + threadIdx.x;
+        const bool valid = item < CGm::FWD_ITEMS;
+        const int it = valid ? item : 0;
+        const int col = it % 16, lab = (it / 16) % (LEN_ * LEN_);
+        const int half = it / CGm::ITEMS;
         const int jj = col % CGm::NX, kk = col / CGm::NX, lx = lab % LEN_, lz = lab / LEN_;
         const int plane = CGm::NA * ((jj * CGm::S + lx * Q_) + CGm::NA * (kk * CGm::S + lz * Q_));
         float sums[LEN_][2];
 #pragma unroll
         for (int ly = 0; ly < LEN_; ly++) sums[ly][0] = sums[ly][1] = 0.0f;
-        for (int c = 6 * half; c < 6 * half + 6; c++) {
-            const float* hvc = hv + c * CGm::NA3 + plane;
-            const float* fsc = fs + c * CGm::NSAMP + G_ * col;
-            float v[CGm::NA], f[G_];
+        if (valid)
+            for (int c = 6 * half; c < 6 * half + 6; c++) {
+                const float* hvc = hv + c * CGm::NA3 + plane;
+                const float* fsc = fs + c * CGm::NSAMP + G_ * col;
+                float v[CGm::NA], f[G_];
 #pragma unroll
-            for (int a = 0; a < CGm::NA; a++) v[a] = hvc[a];
+                for (int a = 0; a < CGm::NA; a++) v[a] = hvc[a];
 #pragma unroll
-            for (int i = 0; i < G_; i++) f[i] = fsc[i];
+                for (int i = 0; i < G_; i++) f[i] = fsc[i];
 #pragma unroll
-            for (int ly = 0; ly < LEN_; ly++)
+                for (int ly = 0; ly < LEN_; ly++)
 #pragma unroll
-                for (int i = 0; i < G_; i++) {
-                    const float d = f[i] - v[i + ly * Q_];
-                    const float x2 = d * d + eps2;
-                    sums[ly][i & 1] += x2 * rsqrtf(x2);
-                }
+                    for (int i = 0; i < G_; i++) {
+                        const float d = f[i] - v[i + ly * Q_];
+                        const float x2 = d * d + eps2;
+                        sums[ly][i & 1] += x2 * rsqrtf(x2);
+                    }
+            }
+#pragma unroll
+        for (int ly = 0; ly < LEN_; ly++) {
+            float v = sums[ly][0] + sums[ly][1];
+#pragma unroll
+            for (int off = 8; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+            if (valid && col == 0) atomicAdd(acc + ly + LEN_ * lab, v);
         }
-#pragma unroll
-        for (int ly = 0; ly < LEN_; ly++) atomicAdd(acc + ly + LEN_ * lab, sums[ly][0] + sums[ly][1]);
     }
     __syncthreads();
     for (int l = threadIdx.x; l < CGm::LEN3; l += blockDim.x)
@@ -683,7 +703,7 @@ __global__ void __launch_bounds__(ColGeom<G_, LEN_, Q_>::FWD_BLOCK)
 constexpr int kAdjCG = 6;
 
 template <int G_, int LEN_, int Q_>
-__global__ void __launch_bounds__(ColGeom<G_, LEN_, Q_>::ADJ_BLOCK)
+__global__ void __launch_bounds__(ColGeom<G_, LEN_, Q_>::ADJ_BLOCK, 4)
     k_soft_cost_adj_col(const float* __restrict__ sF, const float* __restrict__ sM, const float* __restrict__ cbar,
                         const float* __restrict__ cost, float* __restrict__ sFbar, float* __restrict__ sMbar,
                         double* __restrict__ dot, SoftGeom G) {
@@ -724,10 +744,13 @@ __global__ void __launch_bounds__(ColGeom<G_, LEN_, Q_>::ADJ_BLOCK)
         stage_box<CGm>(G, y, x, z, sM, c0, kAdjCG, hv, sF, c0 == 0 ? fs : nullptr);
         for (int e = threadIdx.x; e < kAdjCG * CGm::NA3; e += blockDim.x) hg[e] = 0.0f;
         __syncthreads();
+        // items (column, channel, lx) with the column fastest: a half-warp holds the 16
+        // columns of one (channel, lx), whose box rows (jj + lx, kk + lz) are distinct,
+        // so the row atomics of a warp never collide on an address
         for (int item = threadIdx.x; item < CGm::ADJ_ITEMS; item += blockDim.x) {
             const int col = item % (CGm::NX * CGm::NX);
-            const int lx = (item / (CGm::NX * CGm::NX)) % LEN_;
-            const int cl = item / (CGm::NX * CGm::NX * LEN_);
+            const int cl = (item / (CGm::NX * CGm::NX)) % kAdjCG;
+            const int lx = item / (CGm::NX * CGm::NX * kAdjCG);
             const int jj = col % CGm::NX, kk = col / CGm::NX;
             const float* fsc = fs + (c0 + cl) * CGm::NSAMP + G_ * col;
             float f[G_], gf[G_];
