@@ -1118,6 +1118,8 @@ deeds_status soft_check(deeds_ctx* ctx, int m, int n, int o, const deeds_soft_pa
         return fail(ctx, DEEDS_ERR_INVALID, "volume %dx%dx%d too small for MIND radius %d", m, n, o, *qs);
     if (m < p->grid || n < p->grid || o < p->grid)
         return fail(ctx, DEEDS_ERR_INVALID, "volume %dx%dx%d smaller than grid %d", m, n, o, p->grid);
+    if (n > 65535 || 6LL * o > 65535)  // launch grid limits of the descriptor kernels
+        return fail(ctx, DEEDS_ERR_INVALID, "volume %dx%dx%d too large for the soft descriptor", m, n, o);
     return DEEDS_OK;
 }
 
@@ -1135,7 +1137,8 @@ extern "C" {
 deeds_status deeds_soft_descriptor_dev(deeds_ctx* ctx, const float* d_im, int m, int n, int o, int qs, float* d_desc,
                                        void* stream) {
     if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
-    if (!d_im || !d_desc || qs < 1 || qs > 7 || m < 2 * qs + 1 || n < 2 * qs + 1 || o < 2 * qs + 1)
+    if (!d_im || !d_desc || qs < 1 || qs > 7 || m < 2 * qs + 1 || n < 2 * qs + 1 || o < 2 * qs + 1 || n > 65535 ||
+        6LL * o > 65535)
         return fail(ctx, DEEDS_ERR_INVALID, "deeds_soft_descriptor_dev: bad arguments");
     CK(cudaSetDevice(ctx->device));
     deeds_status st = DEEDS_OK;

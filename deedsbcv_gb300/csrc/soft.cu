@@ -80,22 +80,25 @@ __global__ void k_soft_sqdiff(const float* __restrict__ im, float* __restrict__ 
 // Windowed sum over [max(0,i-r), min(L-1,i+r)] along one axis, out of place, summed
 // directly (no prefix-sum differences, whose cancellation would cost the soft
 // descriptor its float32 accuracy).  The operator is symmetric, so the same
-// kernel is its own adjoint.
+// kernel is its own adjoint.  Grid: x over i, y over j (32 x 8 blocks), z over
+// (k, channel): no index divisions by runtime sizes.
 __global__ void k_soft_box(const float* __restrict__ in, float* __restrict__ out, int m, int n, int o, int r, int axis) {
-    const int64_t mn = (int64_t)m * n, sz = mn * o;
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= 6 * sz) return;
-    const int64_t p = t % sz;
-    int L, i;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= m || j >= n) return;
+    const int k = blockIdx.z % o, ch = blockIdx.z / o;
+    const int64_t mn = (int64_t)m * n;
+    const int64_t p = (int64_t)ch * mn * o + i + (int64_t)j * m + (int64_t)k * mn;
+    int L, c;
     int64_t stride;
-    if (axis == 0) { L = m; stride = 1; i = (int)(p % m); }
-    else if (axis == 1) { L = n; stride = m; i = (int)((p / m) % n); }
-    else { L = o; stride = mn; i = (int)(p / mn); }
-    const float* x = in + (t - (int64_t)i * stride);
-    const int a0 = max(0, i - r), a1 = min(L - 1, i + r);
+    if (axis == 0) { L = m; stride = 1; c = i; }
+    else if (axis == 1) { L = n; stride = m; c = j; }
+    else { L = o; stride = mn; c = k; }
+    const float* x = in + (p - (int64_t)c * stride);
+    const int a0 = max(0, c - r), a1 = min(L - 1, c + r);
     float acc = 0.0f;
     for (int a = a0; a <= a1; a++) acc += x[a * stride];
-    out[t] = acc;
+    out[p] = acc;
 }
 
 struct DescPoint {
@@ -1240,10 +1243,10 @@ SoftTree make_tree(const SoftTreeDev& d) {
 
 // three box passes a -> b -> a -> b; the result is in b
 static void box3(float* a, float* b, int m, int n, int o, int r, cudaStream_t st) {
-    const int64_t n6 = (int64_t)6 * m * n * o;
-    k_soft_box<<<blocks_for(n6, 256), 256, 0, st>>>(a, b, m, n, o, r, 0);
-    k_soft_box<<<blocks_for(n6, 256), 256, 0, st>>>(b, a, m, n, o, r, 1);
-    k_soft_box<<<blocks_for(n6, 256), 256, 0, st>>>(a, b, m, n, o, r, 2);
+    const dim3 blk(32, 8), grid(blocks_for(m, 32), blocks_for(n, 8), 6 * o);
+    k_soft_box<<<grid, blk, 0, st>>>(a, b, m, n, o, r, 0);
+    k_soft_box<<<grid, blk, 0, st>>>(b, a, m, n, o, r, 1);
+    k_soft_box<<<grid, blk, 0, st>>>(a, b, m, n, o, r, 2);
 }
 
 cudaError_t launch_soft_descriptor(const float* d_im, float* w6a, float* w6b, float* s12, int m, int n, int o, int qs,
