@@ -65,6 +65,21 @@ def dist_env():
     return ws, rank, local
 
 
+def replica_rate(local_s, steps, device=None):
+    """Pairs/s of the whole job: every rank (one replica per GPU, no collective on
+    the data path) registers `steps` pairs; the job's time is the slowest rank's
+    (max over ranks), so value = ranks * steps / max time.  Returns (value, time)."""
+    import torch
+    import torch.distributed as dist
+    ws = dist.get_world_size() if dist.is_available() and dist.is_initialized() else 1
+    t = float(local_s)
+    if ws > 1:
+        x = torch.tensor([t], dtype=torch.float64, device=device)
+        dist.all_reduce(x, op=dist.ReduceOp.MAX)
+        t = float(x.item())
+    return ws * steps / t, t
+
+
 def popc64_per_pair(shape):
     """Algorithmic 64-bit Hamming operations of one pair (both directions)."""
     m, n, o = shape
@@ -392,12 +407,8 @@ def main():
         barrier()
     launches = api.kernel_launches() - launches0
     ctx.set_profiling(False)
-    ms = ev0.elapsed_time(ev1)
-    if ws > 1:
-        t = torch.tensor([ms], device=f"cuda:{device}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * args.steps / (ms / 1000.0)
+    value, secs = replica_rate(ev0.elapsed_time(ev1) / 1000.0, args.steps, f"cuda:{device}")
+    ms = secs * 1000.0
     stages = ctx.stage_times()
     clk = clocks.summary()
 
@@ -408,12 +419,8 @@ def main():
     t0 = time.perf_counter()
     for _ in range(args.steps):
         flow_h, _ = api.register(fixed_h, moving_h, dims=shape, params=params, want_warped=False, ctx=ctx)
-    e2e_s = time.perf_counter() - t0
-    if ws > 1:
-        t = torch.tensor([e2e_s], device=f"cuda:{device}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": ws * args.steps / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": 2 * sz * 4,
+    e2e_value, _ = replica_rate(time.perf_counter() - t0, args.steps, f"cuda:{device}")
+    e2e = {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": 2 * sz * 4,
            "d2h_bytes_per_step": 3 * sz1 * 4}
 
     # ---- roofline of the dominant stage
