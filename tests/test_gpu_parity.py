@@ -9,6 +9,7 @@ Tolerances (the contract for this path):
   * warped-label Dice: within 0.1 points (0.001) of the oracle's.
 """
 import hashlib
+import os
 
 import numpy as np
 import pytest
@@ -86,7 +87,7 @@ def test_data_cost_golden(api, golden):
         assert same_bits(cost, g[f"cost_{gs}_{hw}_{q}"]), (gs, hw, q)
 
 
-@pytest.mark.parametrize("gs,hw,q", [(8, 8, 5), (6, 6, 3), (4, 4, 1)])
+@pytest.mark.parametrize("gs,hw,q", [(8, 8, 5), (7, 7, 4), (6, 6, 3), (5, 5, 2), (4, 4, 1), (4, 3, 2)])
 def test_data_cost_phantom_vs_oracle(api, gs, hw, q):
     from deedsbcv_gb300 import phantom
     shape = (64, 48, 72)
@@ -311,3 +312,54 @@ def test_constant_images_follow_reference_nan_semantics(api):
     f = flat.ravel(order="F") + np.float32(1024)
     ref = orc.register(f, f, *shape, G=(6, 4), L=(3, 2), Q=(2, 1))
     assert same_bits(flow, ref)
+
+
+def test_cli_deedsbcv_and_applybcv_match_reference_outputs(api, golden, tmp_path):
+    """The drop-in boundary end to end: the deedsBCV binary on NIfTI files with the
+    reference's flags writes the reference's displacement file and deformed images;
+    applyBCV re-applies the .dat to the labels."""
+    import subprocess
+    from deedsbcv_gb300 import build, nifti, phantom
+    e = golden("e2e")
+    f, mv = tmp_path / "f.nii.gz", tmp_path / "m.nii.gz"
+    seg = tmp_path / "seg.nii.gz"
+    nifti.write(str(f), e["fixed"])
+    nifti.write(str(mv), e["moving"])
+    nifti.write(str(seg), e["moving_labels"].astype(np.int16))
+    stem = str(tmp_path / "out")
+    exe = os.path.join(build.OUT, "deedsBCV")
+    r = subprocess.run([exe, "-F", str(f), "-M", str(mv), "-O", stem, "-G", "6x5x4", "-L", "5x4x3", "-Q", "3x2x1",
+                        "-S", str(seg)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    flow = nifti.read_dat(stem + "_displacements.dat")
+    assert flow.size == e["flow"].size
+    agree = np.mean(flow == e["flow"])
+    assert agree >= ARGMIN_AGREE, agree
+    wseg, _ = nifti.read(stem + "_deformed_seg.nii.gz")
+    lab = e["fixed_labels"].ravel(order="F")
+    assert abs(phantom.dice(lab, wseg.ravel(order="F")) - phantom.dice(lab, e["warped_seg"])) <= DICE_TOL
+    if agree == 1.0:
+        warped, _ = nifti.read(stem + "_deformed.nii.gz")
+        assert np.array_equal(warped.ravel(order="F").astype(np.float32), e["warped"])
+        assert np.array_equal(wseg.ravel(order="F"), e["warped_seg"])
+    # applyBCV: the same labels through the written displacement file
+    out = str(tmp_path / "applied.nii.gz")
+    r = subprocess.run([os.path.join(build.OUT, "applyBCV"), "-M", str(seg), "-O", stem, "-D", out],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    applied, _ = nifti.read(out)
+    assert np.array_equal(applied.ravel(order="F"), wseg.ravel(order="F"))
+
+
+def test_register_cross_contrast_vs_oracle(api):
+    """The cross-contrast workload (per-organ intensity remap, inverted background,
+    bias field, Rician noise) at 64x64x72: GPU against the oracle."""
+    from deedsbcv_gb300 import phantom
+    shape = (64, 64, 72)
+    pair = phantom.make_pair(shape, seed=31, max_disp=5.0, contrast="cross")
+    flow, _ = api.register(pair["fixed"], pair["moving"])
+    f = pair["fixed"].ravel(order="F") + np.float32(1024)
+    mv = pair["moving"].ravel(order="F") + np.float32(1024)
+    rflow, ux, vx, wx, rwarped = orc.register(f, mv, *shape, want_full=True)
+    agree = np.mean(flow == rflow)
+    assert agree >= ARGMIN_AGREE, agree
