@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--soft-pairs", type=int, default=4)
     ap.add_argument("--soft-taus", default="0.1,0.5,2.0")
     ap.add_argument("--soft-shape", default="160x160x192", help="soft-min pair shape (profiling runs use smaller)")
+    ap.add_argument("--soft-single", action="store_true", help="--soft-only: the finest soft level alone")
     return ap.parse_args()
 
 
@@ -246,19 +247,25 @@ def measure_batched(api, ctx, lanes):
 
 SOFT_SHAPE = (160, 160, 192)
 SOFT_TAUS = (0.1, 0.5, 2.0)
+# (grid, radius, quant, MIND radius) per level, coarse to fine: label set 7^3 at
+# every level, displacement range +-9, +-6 and +-3 voxels
+SOFT_LEVELS = ((6, 3, 3, 2), (5, 3, 2, 2), (4, 3, 1, 1))
 
 
-def measure_soft(api, ctx, n_pairs=4, grid=4, radius=3, quant=1, taus=SOFT_TAUS, shape=SOFT_SHAPE):
-    """Differentiable soft-min level on 4 pairs at 160x160x192, label set 7^3,
-    tau in {0.1, 0.5, 2.0}: forward (expected displacement) + backward (hand-written
-    adjoint: gradients w.r.t. both images and alpha) of loss = MSE between the
-    expected displacement and the seeded ground-truth field at the control points.
-    Each pair's MST is built once from its fixed image (a constant of the level)
-    before timing; device time with CUDA events over all pairs per tau."""
+def measure_soft(api, ctx, n_pairs=4, levels=SOFT_LEVELS, taus=SOFT_TAUS, shape=SOFT_SHAPE):
+    """Differentiable soft-min registration on 4 pairs at 160x160x192, label set 7^3
+    at the finest level, tau in {0.1, 0.5, 2.0}: forward (expected displacement
+    after the last level) + backward (hand-written adjoints: gradients w.r.t. both
+    images and alpha) of loss = MSE between that field and the seeded ground-truth
+    field at the finest control points.  With several levels each level's prior is
+    the previous field upsampled, the moving image is warped by it and the
+    pairwise term is taken relative to it.  Each pair's MSTs are built once from
+    its fixed image (constants of the levels) before timing; device time with CUDA
+    events over all pairs per tau."""
     import torch
     from deedsbcv_gb300 import phantom
     m, n, o = shape
-    g = grid
+    g = levels[-1][0]
     m1, n1, o1 = m // g, n // g, o // g
     data = []
     for i in range(n_pairs):
@@ -268,14 +275,14 @@ def measure_soft(api, ctx, n_pairs=4, grid=4, radius=3, quant=1, taus=SOFT_TAUS,
         c = g // 2
         d = pr["disp"][:, c::g, c::g, c::g][:, :m1, :n1, :o1]  # (y, x, z) components at node voxels
         gt = -np.stack([d[1], d[0], d[2]]).reshape(3, -1, order="F")  # u (x), v (y), w (z), node order y fastest
-        tree = api.soft_tree(fx, m, n, o, g, ctx)
-        data.append((fx, mv, torch.from_numpy(gt.astype(np.float32)).cuda(), tree))
+        trees = [api.soft_tree(fx, m, n, o, lv[0], ctx) for lv in levels]
+        data.append((fx, mv, torch.from_numpy(gt.astype(np.float32)).cuda(), trees))
 
-    def step(fx, mv, gt, tree, tau, backward=True):
+    def step(fx, mv, gt, trees, tau, backward=True):
         F = fx.detach().requires_grad_(backward)
         M = mv.detach().requires_grad_(backward)
         a = torch.tensor(1.6, requires_grad=backward)
-        disp = api.soft_level(F, M, a, shape, grid=g, radius=radius, quant=quant, tau=tau, tree=tree, ctx=ctx)
+        disp = api.soft_register_levels(F, M, a, shape, levels, tau=tau, trees=trees, ctx=ctx)
         loss = ((disp - gt) ** 2).mean()
         if backward:
             loss.backward()
@@ -307,9 +314,10 @@ def measure_soft(api, ctx, n_pairs=4, grid=4, radius=3, quant=1, taus=SOFT_TAUS,
                                                "alpha": float(ga)}
             res["mean_loss"] = float(torch.stack(losses).mean())
         out[str(tau)] = res
-    return {"workload": f"{n_pairs} pairs {m}x{n}x{o} (seeds 200..{199 + n_pairs}), soft level grid {g}, "
-                        f"label set {2 * radius + 1}^3, quant {quant}, alpha 1.6, eps 0.01; loss = MSE(expected "
-                        f"displacement, ground-truth field at control points); MST per pair built before timing",
+    lv = " ".join(f"G{a}L{b}Q{c}" for a, b, c, _ in levels)
+    return {"workload": f"{n_pairs} pairs {m}x{n}x{o} (seeds 200..{199 + n_pairs}), soft levels {lv}, label set "
+                        f"{2 * levels[-1][1] + 1}^3 at the finest, alpha 1.6, eps 0.01; loss = MSE(expected "
+                        f"displacement, ground-truth field at control points); MSTs per pair built before timing",
             "per_tau": out, "gpu_launches": api.kernel_launches() - launches0}
 
 
@@ -390,7 +398,9 @@ def main():
     if args.soft_only:
         taus = tuple(float(t) for t in args.soft_taus.split(","))
         shp = tuple(int(v) for v in args.soft_shape.split("x"))
-        print(json.dumps(measure_soft(api, ctx, n_pairs=args.soft_pairs, taus=taus, shape=shp)), flush=True)
+        lv = SOFT_LEVELS[-1:] if args.soft_single else SOFT_LEVELS
+        print(json.dumps(measure_soft(api, ctx, n_pairs=args.soft_pairs, levels=lv, taus=taus, shape=shp)),
+              flush=True)
         return
     pair = make_workload(shape)
     m, n, o = shape
@@ -506,6 +516,7 @@ def main():
     soft = None
     if rank == 0 and not args.no_soft and not args.small:
         soft = measure_soft(api, ctx)
+        soft["finest_level_alone"] = measure_soft(api, ctx, levels=SOFT_LEVELS[-1:])
 
     # ---- CPU baseline and full-size parity (rank 0, N=1)
     cpu = None

@@ -26,7 +26,8 @@ EXPORTS = [
     "deeds_set_profiling", "deeds_stage_times", "deeds_reset_stage_times", "deeds_kernel_launches",
     "deeds_measure_popc_rate", "deeds_register_batch", "deeds_consistent_noalloc_dev",
     "deeds_soft_default_params", "deeds_soft_descriptor_dev", "deeds_soft_cost_dev", "deeds_soft_forward_dev",
-    "deeds_soft_backward_dev",
+    "deeds_soft_backward_dev", "deeds_soft_upsample_dev", "deeds_soft_upsample_backward_dev", "deeds_soft_warp_dev",
+    "deeds_soft_warp_backward_dev",
 ]
 NOALLOC_MAX_NODES = 131072
 STAGES = ["mind", "datacost", "mst_edges", "bp_up", "bp_down", "transform", "consistent", "tree_wait"]
@@ -123,8 +124,12 @@ def load():
     L.deeds_soft_default_params.restype = None
     L.deeds_soft_descriptor_dev.argtypes = [P, P, I, I, I, I, P, P]
     L.deeds_soft_cost_dev.argtypes = [P, P, P, I, I, I, SP, P, P]
-    L.deeds_soft_forward_dev.argtypes = [P, P, P, I, I, I, SP, P, P, P, P, P]
-    L.deeds_soft_backward_dev.argtypes = [P, P, P, I, I, I, SP, P, P, P, P, P, P, P, P]
+    L.deeds_soft_forward_dev.argtypes = [P, P, P, I, I, I, SP, P, P, P, P, P, P]
+    L.deeds_soft_backward_dev.argtypes = [P, P, P, I, I, I, SP, P, P, P, P, P, P, P, P, P, P]
+    L.deeds_soft_upsample_dev.argtypes = [P, P, I, I, I, P, I, I, I, P]
+    L.deeds_soft_upsample_backward_dev.argtypes = [P, P, I, I, I, P, I, I, I, P]
+    L.deeds_soft_warp_dev.argtypes = [P, P, I, I, I, P, I, I, I, P, P]
+    L.deeds_soft_warp_backward_dev.argtypes = [P, P, I, I, I, P, I, I, I, P, P, P, P]
     for name in EXPORTS:
         fn = getattr(L, name)
         if name not in ("deeds_default_params", "deeds_destroy", "deeds_last_error", "deeds_version",

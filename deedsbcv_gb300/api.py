@@ -432,17 +432,23 @@ def _soft_call(ctx, fn, fixed, moving, dims, params, tree, *rest):
                  m, n, o, C.byref(params), p(ordered), p(parents), p(edgemst), *rest, _stream()))
 
 
+def _ptr(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
 class SoftDeedsLevel(torch.autograd.Function if torch is not None else object):
     """Expected displacement (3, sz1) [u, v, w] of one soft-min deeds level.
 
-    forward(fixed, moving, alpha, dims, params, tree, ctx): fixed/moving are flat
-    float32 CUDA tensors (i fastest), alpha a 0-d tensor (its value replaces
-    params.alpha), tree = (ordered, parents, edgemst) host arrays of the fixed
-    image's MST at params.grid.  Backward runs the library's adjoint kernels,
-    which recompute the forward sweeps instead of keeping message tensors."""
+    forward(fixed, moving, alpha, prior, dims, params, tree, ctx): fixed/moving are
+    flat float32 CUDA tensors (i fastest), alpha a 0-d tensor (its value replaces
+    params.alpha), prior None or the current grid field (3, sz1) that the pairwise
+    term is taken relative to (src/regularisation.h:205-208), tree = (ordered,
+    parents, edgemst) host arrays of the fixed image's MST at params.grid.  Backward
+    runs the library's adjoint kernels, which recompute the forward sweeps instead
+    of keeping message tensors."""
 
     @staticmethod
-    def forward(fctx, fixed, moving, alpha, dims, params, tree, dctx):
+    def forward(fctx, fixed, moving, alpha, prior, dims, params, tree, dctx):
         params = soft_params(params.grid, params.radius, params.quant, float(alpha.detach()), params.tau, params.eps,
                              params.mind_radius)
         tree = _tree_arrays(tree)
@@ -451,28 +457,88 @@ class SoftDeedsLevel(torch.autograd.Function if torch is not None else object):
         sz1 = (m // g) * (n // g) * (o // g)
         out = torch.empty(3 * sz1, dtype=torch.float32, device=fixed.device)
         fixed_c, moving_c = fixed.detach().contiguous(), moving.detach().contiguous()
-        _soft_call(dctx, dctx._L.deeds_soft_forward_dev, fixed_c, moving_c, dims, params, tree,
-                   C.c_void_p(out.data_ptr()))
-        fctx.save_for_backward(fixed_c, moving_c)
+        prior_c = None
+        if prior is not None:
+            prior_c = prior.detach().contiguous()
+            _dev(prior_c, torch.float32, 3 * sz1, "prior")
+        _soft_call(dctx, dctx._L.deeds_soft_forward_dev, fixed_c, moving_c, dims, params, tree, _ptr(prior_c),
+                   _ptr(out))
+        fctx.save_for_backward(fixed_c, moving_c, prior_c)
         fctx.soft = (dims, params, tree, dctx)
         fctx.alpha_like = (alpha.dtype, alpha.device) if isinstance(alpha, torch.Tensor) else (torch.float32, "cpu")
         return out.view(3, sz1)
 
     @staticmethod
     def backward(fctx, gdisp):
-        fixed, moving = fctx.saved_tensors
+        fixed, moving, prior = fctx.saved_tensors
         dims, params, tree, dctx = fctx.soft
         gdisp = gdisp.detach().contiguous().to(torch.float32)
-        need_f, need_m, need_a = fctx.needs_input_grad[:3]
+        need_f, need_m, need_a, need_p = fctx.needs_input_grad[:4]
         gf = torch.empty_like(fixed) if need_f else None
         gm = torch.empty_like(moving) if need_m else None
+        gp = torch.empty_like(prior) if (need_p and prior is not None) else None
         ga = C.c_float(0.0)
-        _soft_call(dctx, dctx._L.deeds_soft_backward_dev, fixed, moving, dims, params, tree,
-                   C.c_void_p(gdisp.data_ptr()), C.c_void_p(gf.data_ptr()) if gf is not None else None,
-                   C.c_void_p(gm.data_ptr()) if gm is not None else None, C.byref(ga) if need_a else None)
+        _soft_call(dctx, dctx._L.deeds_soft_backward_dev, fixed, moving, dims, params, tree, _ptr(prior),
+                   _ptr(gdisp), _ptr(gf), _ptr(gm), _ptr(gp), C.byref(ga) if need_a else None)
         adt, adev = fctx.alpha_like
         galpha = torch.tensor(ga.value, dtype=adt, device=adev) if need_a else None
-        return gf, gm, galpha, None, None, None, None
+        return gf, gm, galpha, gp, None, None, None, None
+
+
+class SoftUpsample(torch.autograd.Function if torch is not None else object):
+    """Trilinear upsampling of a grid field (3, mA*nA*oA) to (3, m*n*o) with the
+    coordinates of upsampleDeformationsCL (src/transformations.h:245-279)."""
+
+    @staticmethod
+    def forward(fctx, field, src_dims, dst_dims, dctx):
+        mA, nA, oA = src_dims
+        m, n, o = dst_dims
+        f = _dev(field.detach().contiguous(), torch.float32, 3 * mA * nA * oA, "field")
+        out = torch.empty(3 * m * n * o, dtype=torch.float32, device=field.device)
+        dctx.check(dctx._L.deeds_soft_upsample_dev(dctx.handle, f, mA, nA, oA, _ptr(out), m, n, o, _stream()))
+        fctx.dims = (tuple(src_dims), tuple(dst_dims), dctx)
+        return out.view(3, m * n * o)
+
+    @staticmethod
+    def backward(fctx, gout):
+        (mA, nA, oA), (m, n, o), dctx = fctx.dims
+        gout = gout.detach().contiguous().to(torch.float32)
+        gin = torch.empty(3 * mA * nA * oA, dtype=torch.float32, device=gout.device)
+        dctx.check(dctx._L.deeds_soft_upsample_backward_dev(dctx.handle, _ptr(gout), m, n, o, _ptr(gin), mA, nA, oA,
+                                                             _stream()))
+        return gin.view(3, mA * nA * oA), None, None, None
+
+
+class SoftWarp(torch.autograd.Function if torch is not None else object):
+    """The moving image (flat, m*n*o) sampled at p + field(p), field = the grid
+    field (3, mA*nA*oA) upsampled to full resolution on the fly (warpAffine with the
+    identity, src/dataCostD.h:267-295); differentiable in the image and the grid."""
+
+    @staticmethod
+    def forward(fctx, moving, grid, dims, grid_dims, dctx):
+        m, n, o = dims
+        mA, nA, oA = grid_dims
+        mov = moving.detach().contiguous()
+        gr = grid.detach().contiguous()
+        out = torch.empty(m * n * o, dtype=torch.float32, device=moving.device)
+        dctx.check(dctx._L.deeds_soft_warp_dev(dctx.handle, _dev(mov, torch.float32, m * n * o, "moving"), m, n, o,
+                                               _dev(gr, torch.float32, 3 * mA * nA * oA, "grid"), mA, nA, oA,
+                                               _ptr(out), _stream()))
+        fctx.save_for_backward(mov, gr)
+        fctx.dims = (tuple(dims), tuple(grid_dims), dctx)
+        return out
+
+    @staticmethod
+    def backward(fctx, gout):
+        mov, gr = fctx.saved_tensors
+        (m, n, o), (mA, nA, oA), dctx = fctx.dims
+        need_m, need_g = fctx.needs_input_grad[:2]
+        gout = gout.detach().contiguous().to(torch.float32)
+        gm = torch.empty_like(mov) if need_m else None
+        gg = torch.empty_like(gr) if need_g else None
+        dctx.check(dctx._L.deeds_soft_warp_backward_dev(dctx.handle, _ptr(mov), m, n, o, _ptr(gr), mA, nA, oA,
+                                                         _ptr(gout), _ptr(gm), _ptr(gg), _stream()))
+        return gm, gg, None, None, None
 
 
 def soft_tree(fixed, m, n, o, g, ctx=None):
@@ -493,4 +559,35 @@ def soft_level(fixed, moving, alpha, dims, grid=4, radius=3, quant=1, tau=0.5, e
     if not isinstance(alpha, torch.Tensor):
         alpha = torch.tensor(float(alpha), dtype=torch.float32)
     params = soft_params(grid, radius, quant, float(alpha.detach()), tau, eps, mind_radius)
-    return SoftDeedsLevel.apply(fixed, moving, alpha, tuple(dims), params, tree, ctx)
+    return SoftDeedsLevel.apply(fixed, moving, alpha, None, tuple(dims), params, tree, ctx)
+
+
+def soft_register_levels(fixed, moving, alpha, dims, levels, tau=0.5, eps=0.01, trees=None, ctx=None):
+    """Differentiable multi-level soft-min registration (the level loop of
+    src/deedsBCV0.cpp:222-306, forward direction).
+
+    levels: [(grid, radius, quant, mind_radius)], coarse to fine.  At each level the
+    prior grid field U is the previous level's field upsampled to this grid
+    (zero at the first level), the moving image is warped by U at full resolution,
+    and the soft level's expected displacement E is taken relative to U; the level
+    returns U + E.  Returns the last grid field (3, sz1) [u, v, w].  trees: the
+    fixed image's MST per level (computed when None)."""
+    m, n, o = dims
+    ctx = ctx or context(fixed.device.index or 0)
+    if not isinstance(alpha, torch.Tensor):
+        alpha = torch.tensor(float(alpha), dtype=torch.float32)
+    prev, prev_dims = None, None
+    for li, (g, hw, q, qs) in enumerate(levels):
+        gdims = (m // g, n // g, o // g)
+        tree = trees[li] if trees is not None else soft_tree(fixed, m, n, o, g, ctx)
+        params = soft_params(g, hw, q, float(alpha.detach()), tau, eps, qs)
+        if prev is None:
+            E = SoftDeedsLevel.apply(fixed, moving, alpha, None, tuple(dims), params, tree, ctx)
+            prev = E
+        else:
+            U = SoftUpsample.apply(prev, prev_dims, gdims, ctx)
+            warped = SoftWarp.apply(moving, U, tuple(dims), gdims, ctx)
+            E = SoftDeedsLevel.apply(fixed, warped, alpha, U, tuple(dims), params, tree, ctx)
+            prev = U + E
+        prev_dims = gdims
+    return prev

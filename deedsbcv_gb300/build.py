@@ -30,11 +30,11 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompil
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread", "-Wall", "-Wno-unused-function",
              f"-I{CUDA_HOME}/include"]
 
-CU_SOURCES = ["mind.cu", "datacost.cu", "mst.cu", "bp.cu", "transform.cu", "noalloc.cu", "soft.cu"]
+CU_SOURCES = ["mind.cu", "datacost.cu", "mst.cu", "bp.cu", "transform.cu", "noalloc.cu", "soft.cu", "soft_warp.cu"]
 # soft.cu has no bit-exactness contract (its reference is a float64 definition),
 # so it may contract multiply-adds and flush denormals (its operands never are:
 # every square root and reciprocal square root argument is >= eps^2).
-FMAD_SOURCES = {"soft.cu"}
+FMAD_SOURCES = {"soft.cu", "soft_warp.cu"}
 CPP_SOURCES = ["pipeline.cpp", "tree_host.cpp"]
 CLI_SOURCES = {"deedsBCV": ["deedsBCV.cpp", "cli_common.cpp"], "applyBCV": ["applyBCV.cpp", "cli_common.cpp"],
                "applyBCVfloat": ["applyBCV.cpp", "cli_common.cpp"]}

@@ -78,7 +78,21 @@ struct SoftTreeDev {
     const float* edgemst;
     const int* child_ptr;
     const int* children;
+    const float* off;  // nullable: (3, sz) x|y|z label-unit offsets of each node's edge
+    float* offbar;     // nullable (backward): dL/doff, (3, sz), zeroed by the caller
 };
+cudaError_t launch_soft_offsets(const float* prior, const int* parents, int root, int sz, float q, float* off,
+                                cudaStream_t st);
+cudaError_t launch_soft_offbar_to_prior(const float* offbar, const int* parents, int root, int sz, float q,
+                                        float* gprior, cudaStream_t st);
+cudaError_t launch_soft_upsample(const float* in, int mA, int nA, int oA, float* out, int m, int n, int o,
+                                 cudaStream_t s);
+cudaError_t launch_soft_upsample_adj(const float* gout, int m, int n, int o, float* gin, int mA, int nA, int oA,
+                                     cudaStream_t s);
+cudaError_t launch_soft_warp(const float* mov, const float* grid, int mA, int nA, int oA, float* out, int m, int n,
+                             int o, cudaStream_t s);
+cudaError_t launch_soft_warp_adj(const float* mov, const float* grid, int mA, int nA, int oA, const float* gout,
+                                 float* gmov, float* gfull, int m, int n, int o, cudaStream_t s);
 cudaError_t launch_soft_descriptor(const float* d_im, float* w6a, float* w6b, float* s12, int m, int n, int o, int qs,
                                    cudaStream_t st);
 cudaError_t launch_soft_descriptor_adj(const float* d_im, float* w6a, float* w6b, const float* sbar12, float* dbar6,

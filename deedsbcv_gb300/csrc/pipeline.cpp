@@ -1177,7 +1177,8 @@ struct SoftLevel {
 };
 
 deeds_status soft_setup(deeds_ctx* ctx, int m, int n, int o, const deeds_soft_params* p, const int* ordered,
-                        const int* parents, const float* edgemst, cudaStream_t s, SoftLevel& L) {
+                        const int* parents, const float* edgemst, const float* d_prior, cudaStream_t s,
+                        SoftLevel& L) {
     if (deeds_status e = soft_check(ctx, m, n, o, p, &L.qs)) return e;
     if (!ordered || !parents || !edgemst) return fail(ctx, DEEDS_ERR_INVALID, "null tree array");
     L.m1 = m / p->grid; L.n1 = n / p->grid; L.o1 = o / p->grid;
@@ -1239,6 +1240,14 @@ deeds_status soft_setup(deeds_ctx* ctx, int m, int n, int o, const deeds_soft_pa
     L.tree.edgemst = reinterpret_cast<const float*>(d + o_edge);
     L.tree.child_ptr = reinterpret_cast<const int*>(d + o_cptr);
     L.tree.children = reinterpret_cast<const int*>(d + o_ch);
+    L.tree.off = nullptr;
+    L.tree.offbar = nullptr;
+    if (d_prior) {
+        float* off = dbuf<float>(ctx, "soft_off", 3 * (size_t)L.sz1, &st);
+        if (st) return st;
+        CK(launch_soft_offsets(d_prior, L.tree.parents, L.tree.root, L.sz1, (float)p->quant, off, s));
+        L.tree.off = off;
+    }
     return DEEDS_OK;
 }
 
@@ -1266,26 +1275,34 @@ extern "C" {
 
 deeds_status deeds_soft_forward_dev(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, int m, int n, int o,
                                     const deeds_soft_params* p, const int* ordered, const int* parents,
-                                    const float* edgemst, float* d_disp, void* stream) {
+                                    const float* edgemst, const float* d_prior, float* d_disp, void* stream) {
     if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
     if (!d_fixed || !d_moving || !d_disp) return fail(ctx, DEEDS_ERR_INVALID, "null pointer");
     cudaStream_t s = (cudaStream_t)stream;
     SoftLevel L;
-    if (deeds_status e = soft_setup(ctx, m, n, o, p, ordered, parents, edgemst, s, L)) return e;
+    if (deeds_status e = soft_setup(ctx, m, n, o, p, ordered, parents, edgemst, d_prior, s, L)) return e;
     if (deeds_status e = soft_run_forward(ctx, d_fixed, d_moving, m, n, o, p, L, d_disp, s)) return e;
     return soft_check_sweeps(ctx, L, s);
 }
 
 deeds_status deeds_soft_backward_dev(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, int m, int n, int o,
                                      const deeds_soft_params* p, const int* ordered, const int* parents,
-                                     const float* edgemst, const float* d_gdisp, float* d_gfixed, float* d_gmoving,
-                                     float* grad_alpha, void* stream) {
+                                     const float* edgemst, const float* d_prior, const float* d_gdisp,
+                                     float* d_gfixed, float* d_gmoving, float* d_gprior, float* grad_alpha,
+                                     void* stream) {
     if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
     if (!d_fixed || !d_moving || !d_gdisp) return fail(ctx, DEEDS_ERR_INVALID, "null pointer");
+    if (d_gprior && !d_prior) return fail(ctx, DEEDS_ERR_INVALID, "grad_prior needs a prior field");
     cudaStream_t s = (cudaStream_t)stream;
     SoftLevel L;
-    if (deeds_status e = soft_setup(ctx, m, n, o, p, ordered, parents, edgemst, s, L)) return e;
+    if (deeds_status e = soft_setup(ctx, m, n, o, p, ordered, parents, edgemst, d_prior, s, L)) return e;
     deeds_status st = DEEDS_OK;
+    if (d_gprior) {
+        float* offbar = dbuf<float>(ctx, "soft_offbar", 3 * (size_t)L.sz1, &st);
+        if (st) return st;
+        CK(cudaMemsetAsync(offbar, 0, sizeof(float) * 3 * L.sz1, s));
+        L.tree.offbar = offbar;
+    }
     float* R = dbuf<float>(ctx, "soft_R", L.sz1 * L.len3, &st);
     float* Bbar = dbuf<float>(ctx, "soft_Bbar", L.sz1 * L.len3, &st);
     float* sFbar = dbuf<float>(ctx, "soft_sFbar", 12 * L.sz, &st);
@@ -1296,6 +1313,11 @@ deeds_status deeds_soft_backward_dev(deeds_ctx* ctx, const float* d_fixed, const
     // recompute the forward state (descriptors, cost, messages, marginals)
     if (deeds_status e = soft_run_forward(ctx, d_fixed, d_moving, m, n, o, p, L, L.disp, s)) return e;
     CK(launch_soft_tree_backward(L.tree, L.sweep, L.B, L.M, L.logp, d_gdisp, R, Bbar, s));
+    if (d_gprior) {
+        CK(cudaMemsetAsync(d_gprior, 0, sizeof(float) * 3 * L.sz1, s));
+        CK(launch_soft_offbar_to_prior(L.tree.offbar, L.tree.parents, L.tree.root, L.sz1, (float)p->quant, d_gprior,
+                                       s));
+    }
     // Bbar is now dL/dcost
     CK(launch_soft_cost_adj(L.sF, L.sM, Bbar, L.cost, sFbar, sMbar, dot, m, n, o, p->grid, p->radius, p->quant,
                             soft_alpha1(p), p->eps, s));
@@ -1311,6 +1333,56 @@ deeds_status deeds_soft_backward_dev(deeds_ctx* ctx, const float* d_fixed, const
     if (grad_alpha) CK(cudaMemcpyAsync(&hdot, dot, sizeof(double), cudaMemcpyDeviceToHost, s));
     if (deeds_status e = soft_check_sweeps(ctx, L, s)) return e;
     if (grad_alpha) *grad_alpha = (float)(-hdot / (double)p->alpha);
+    return DEEDS_OK;
+}
+
+deeds_status deeds_soft_upsample_dev(deeds_ctx* ctx, const float* d_in, int mA, int nA, int oA, float* d_out, int m,
+                                     int n, int o, void* stream) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!d_in || !d_out || mA < 1 || nA < 1 || oA < 1 || m < 1 || n < 1 || o < 1 || n > 65535 || o > 65535)
+        return fail(ctx, DEEDS_ERR_INVALID, "deeds_soft_upsample_dev: bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    CK(launch_soft_upsample(d_in, mA, nA, oA, d_out, m, n, o, (cudaStream_t)stream));
+    return DEEDS_OK;
+}
+
+deeds_status deeds_soft_upsample_backward_dev(deeds_ctx* ctx, const float* d_gout, int m, int n, int o, float* d_gin,
+                                              int mA, int nA, int oA, void* stream) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!d_gout || !d_gin || mA < 1 || nA < 1 || oA < 1 || m < 1 || n < 1 || o < 1)
+        return fail(ctx, DEEDS_ERR_INVALID, "deeds_soft_upsample_backward_dev: bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    CK(launch_soft_upsample_adj(d_gout, m, n, o, d_gin, mA, nA, oA, (cudaStream_t)stream));
+    return DEEDS_OK;
+}
+
+deeds_status deeds_soft_warp_dev(deeds_ctx* ctx, const float* d_moving, int m, int n, int o, const float* d_grid,
+                                 int mA, int nA, int oA, float* d_out, void* stream) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!d_moving || !d_grid || !d_out || mA < 1 || nA < 1 || oA < 1 || m < 1 || n < 1 || o < 1 || n > 65535 ||
+        o > 65535)
+        return fail(ctx, DEEDS_ERR_INVALID, "deeds_soft_warp_dev: bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    CK(launch_soft_warp(d_moving, d_grid, mA, nA, oA, d_out, m, n, o, (cudaStream_t)stream));
+    return DEEDS_OK;
+}
+
+deeds_status deeds_soft_warp_backward_dev(deeds_ctx* ctx, const float* d_moving, int m, int n, int o,
+                                          const float* d_grid, int mA, int nA, int oA, const float* d_gout,
+                                          float* d_gmoving, float* d_ggrid, void* stream) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!d_moving || !d_grid || !d_gout || mA < 1 || nA < 1 || oA < 1 || m < 1 || n < 1 || o < 1 || n > 65535 ||
+        o > 65535)
+        return fail(ctx, DEEDS_ERR_INVALID, "deeds_soft_warp_backward_dev: bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t sz = (size_t)m * n * o;
+    deeds_status st = DEEDS_OK;
+    float* gfull = d_ggrid ? dbuf<float>(ctx, "soft_gfull", 3 * sz, &st) : nullptr;
+    if (st) return st;
+    if (d_gmoving) CK(cudaMemsetAsync(d_gmoving, 0, sizeof(float) * sz, s));
+    CK(launch_soft_warp_adj(d_moving, d_grid, mA, nA, oA, d_gout, d_gmoving, gfull, m, n, o, s));
+    if (d_ggrid) CK(launch_soft_upsample_adj(gfull, m, n, o, d_ggrid, mA, nA, oA, s));
     return DEEDS_OK;
 }
 

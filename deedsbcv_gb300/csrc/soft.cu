@@ -820,7 +820,16 @@ struct SoftTree {
     const float* edgemst;
     const int* child_ptr;
     const int* children;
+    const float* off;  // nullable: (3, sz) label-unit offsets x|y|z of each node's edge, (prior[parent]-prior[node])/q
+    float* offbar;     // nullable (backward): dL/doff, (3, sz)
 };
+
+// The offset of node c's edge along label axis s (stride 1 = y, len = x, len^2 = z).
+__device__ __forceinline__ float edge_off(const SoftTree& t, int c, int axis) {
+    if (!t.off) return 0.0f;
+    const int comp = axis == 0 ? 1 : (axis == 1 ? 0 : 2);  // off is stored x|y|z
+    return t.off[comp * t.sz + c];
+}
 
 __device__ float block_max(float v, float* red) {
     for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -891,20 +900,22 @@ __device__ float block_sum(float v, float* red) {
     return r;
 }
 
-// out(o) = LSE_a in(line(o), a) - (a - b)^2/tau along the axis of stride s (b = o's
-// coordinate on that axis).  Ends with a barrier.
-__device__ void lse_axis(const float* in, float* out, int len, int len3, int s, float itau) {
+// out(o) = LSE_a in(line(o), a) - d(a, b)^2/tau along the axis of stride s, with b =
+// o's coordinate on that axis and d = sgn (b - a) + off (the prior field's offset of
+// the edge; sgn = +1 when b indexes the parent label, -1 when it indexes the child's).
+// Ends with a barrier.
+__device__ void lse_axis(const float* in, float* out, int len, int len3, int s, float itau, float off, float sgn) {
     for (int o = threadIdx.x; o < len3; o += blockDim.x) {
         const int b = (o / s) % len;
         const float* line = in + (o - b * s);
         float mx = -INFINITY;
         for (int a = 0; a < len; a++) {
-            const float d = (float)(a - b);
+            const float d = sgn * (float)(b - a) + off;
             mx = fmaxf(mx, line[a * s] - d * d * itau);
         }
         float acc = 0.0f;
         for (int a = 0; a < len; a++) {
-            const float d = (float)(a - b);
+            const float d = sgn * (float)(b - a) + off;
             acc += __expf(line[a * s] - d * d * itau - mx);
         }
         out[o] = mx + __logf(acc);
@@ -912,38 +923,56 @@ __device__ void lse_axis(const float* in, float* out, int len, int len3, int s, 
     __syncthreads();
 }
 
-// adjoint of one pass: inbar(a) = sum_b outbar(b) exp(in(a) - (a-b)^2/tau - out(b))
-__device__ void lse_axis_adj(const float* in, const float* out, const float* outbar, float* inbar, int len, int len3,
-                             int s, float itau) {
+// adjoint of one pass: inbar(a) = sum_b outbar(b) w(a, b), w = exp(in(a) - d^2/tau - out(b));
+// returns this thread's part of dL/doff = sum_{a,b} outbar(b) w(a, b) (-2 d / tau).
+__device__ float lse_axis_adj(const float* in, const float* out, const float* outbar, float* inbar, int len, int len3,
+                              int s, float itau, float off, float sgn) {
+    float dof = 0.0f;
     for (int o = threadIdx.x; o < len3; o += blockDim.x) {
         const int a = (o / s) % len;
         const int base = o - a * s;
         const float x = in[o];
         float acc = 0.0f;
         for (int b = 0; b < len; b++) {
-            const float d = (float)(a - b);
-            acc += outbar[base + b * s] * __expf(x - d * d * itau - out[base + b * s]);
+            const float d = sgn * (float)(b - a) + off;
+            const float wb = outbar[base + b * s] * __expf(x - d * d * itau - out[base + b * s]);
+            acc += wb;
+            dof += wb * d;
         }
         inbar[o] = acc;
     }
     __syncthreads();
+    return -2.0f * itau * dof;
 }
 
-// S = pass z o pass x o pass y; keeps t1, t2 for the adjoint (out may alias in)
+// S = pass z o pass x o pass y; keeps t1, t2 for the adjoint (out may alias in).
+// off3 = (y, x, z) offsets of the node's edge.
 __device__ __forceinline__ void sep_lse(const float* in, float* t1, float* t2, float* out, int len, int len3,
-                                        float itau) {
-    lse_axis(in, t1, len, len3, 1, itau);
-    lse_axis(t1, t2, len, len3, len, itau);
-    lse_axis(t2, out, len, len3, len * len, itau);
+                                        float itau, const float* off3, float sgn) {
+    lse_axis(in, t1, len, len3, 1, itau, off3[0], sgn);
+    lse_axis(t1, t2, len, len3, len, itau, off3[1], sgn);
+    lse_axis(t2, out, len, len3, len * len, itau, off3[2], sgn);
 }
 
 // inbar = S^T outbar.  wa is scratch; wb may alias outbar and inbar may alias wa.
+// dof3 (y, x, z) receives this thread's parts of dL/doff.
 __device__ __forceinline__ void sep_lse_adj(const float* in, const float* t1, const float* t2, const float* out,
                                             const float* outbar, float* wa, float* wb, float* inbar, int len,
-                                            int len3, float itau) {
-    lse_axis_adj(t2, out, outbar, wa, len, len3, len * len, itau);
-    lse_axis_adj(t1, t2, wa, wb, len, len3, len, itau);
-    lse_axis_adj(in, t1, wb, inbar, len, len3, 1, itau);
+                                            int len3, float itau, const float* off3, float sgn, float* dof3) {
+    dof3[2] = lse_axis_adj(t2, out, outbar, wa, len, len3, len * len, itau, off3[2], sgn);
+    dof3[1] = lse_axis_adj(t1, t2, wa, wb, len, len3, len, itau, off3[1], sgn);
+    dof3[0] = lse_axis_adj(in, t1, wb, inbar, len, len3, 1, itau, off3[0], sgn);
+}
+
+// Adds this block's dL/doff of node c (scaled) into t.offbar (x|y|z layout); red: 96 floats.
+__device__ void add_offbar(const SoftTree& t, int c, float* dof3, float scale, float* red) {
+    if (!t.offbar) return;
+    block_sum3(dof3[0], dof3[1], dof3[2], red);
+    if (threadIdx.x == 0) {
+        t.offbar[t.sz + c] += scale * dof3[0];      // y
+        t.offbar[c] += scale * dof3[1];             // x
+        t.offbar[2 * t.sz + c] += scale * dof3[2];  // z
+    }
 }
 
 // ---- per-node bodies (one CTA per node; data of other nodes written in the same
@@ -980,7 +1009,8 @@ __device__ void node_up(const SoftTree& t, int c, const float* __restrict__ cost
     }
     __syncthreads();
     if (c == t.root) return;
-    sep_lse(f, t1, t2, f, t.len, L3, t.itau);
+    const float off3[3] = {edge_off(t, c, 0), edge_off(t, c, 1), edge_off(t, c, 2)};
+    sep_lse(f, t1, t2, f, t.len, L3, t.itau, off3, 1.0f);  // output index = parent label
     float mn = INFINITY;
     for (int lp = threadIdx.x; lp < L3; lp += blockDim.x) {
         const float msg = -t.tau * f[lp];
@@ -1012,7 +1042,8 @@ __device__ void node_down(const SoftTree& t, int c, const float* __restrict__ B,
         for (int lp = threadIdx.x; lp < L3; lp += blockDim.x)
             r[lp] = __ldcg(logp + (int64_t)p * L3 + lp) + M[(int64_t)c * L3 + lp] * t.itau;
         __syncthreads();
-        sep_lse(r, t1, t2, r, len, L3, t.itau);
+        const float off3[3] = {edge_off(t, c, 0), edge_off(t, c, 1), edge_off(t, c, 2)};
+        sep_lse(r, t1, t2, r, len, L3, t.itau, off3, -1.0f);  // output index = child label
         for (int l = threadIdx.x; l < L3; l += blockDim.x) r[l] += -e * bc[l] * t.itau;
     }
     float mx = -INFINITY;
@@ -1082,10 +1113,13 @@ __device__ void node_down_adj(const SoftTree& t, int c, const float* __restrict_
         r[l] = logp[(int64_t)p * L3 + l] + M[(int64_t)c * L3 + l] * t.itau;
     }
     __syncthreads();
-    sep_lse(r, t1, t2, G, len, L3, t.itau);
-    sep_lse_adj(r, t1, t2, G, h, wa, h, wa, len, L3, t.itau);
+    const float off3[3] = {edge_off(t, c, 0), edge_off(t, c, 1), edge_off(t, c, 2)};
+    float dof3[3];
+    sep_lse(r, t1, t2, G, len, L3, t.itau, off3, -1.0f);
+    sep_lse_adj(r, t1, t2, G, h, wa, h, wa, len, L3, t.itau, off3, -1.0f, dof3);
     float* rc = R + (int64_t)c * L3;
     for (int l = threadIdx.x; l < L3; l += blockDim.x) rc[l] = wa[l];
+    add_offbar(t, c, dof3, 1.0f, red);
 }
 
 // Adjoint of the upward recursion (root to leaves, root excluded):
@@ -1111,8 +1145,12 @@ __device__ void node_up_adj(const SoftTree& t, int c, const float* __restrict__ 
         mb[l] = R[(int64_t)c * L3 + l] * t.itau + __ldcg(Bbar + (int64_t)p * L3 + l);
     }
     __syncthreads();
-    sep_lse(f, t1, t2, out, len, L3, t.itau);
-    sep_lse_adj(f, t1, t2, out, mb, wa, mb, wa, len, L3, t.itau);
+    const float off3[3] = {edge_off(t, c, 0), edge_off(t, c, 1), edge_off(t, c, 2)};
+    float dof3[3];
+    sep_lse(f, t1, t2, out, len, L3, t.itau, off3, 1.0f);
+    sep_lse_adj(f, t1, t2, out, mb, wa, mb, wa, len, L3, t.itau, off3, 1.0f, dof3);
+    // M = -tau out: dL/dout = -tau Mbar, so the offset gradient computed with Mbar scales by -tau
+    add_offbar(t, c, dof3, -t.tau, red);
     float* bb = Bbar + (int64_t)c * L3;
     float mean = 0.0f;
     for (int l = threadIdx.x; l < L3; l += blockDim.x) {
@@ -1233,10 +1271,35 @@ SoftTree make_tree(const SoftTreeDev& d) {
     t.len = d.len; t.len3 = d.len * d.len * d.len; t.hw = (d.len - 1) / 2; t.sz = d.sz; t.root = d.root;
     t.q = d.q; t.tau = d.tau; t.itau = 1.0f / d.tau;
     t.parents = d.parents; t.edgemst = d.edgemst; t.child_ptr = d.child_ptr; t.children = d.children;
+    t.off = d.off; t.offbar = d.offbar;
     return t;
 }
 
 }  // namespace
+
+// off (x|y|z) of node c's edge = (prior[parent] - prior[c]) / q; the root has none
+__global__ void k_soft_offsets(const float* __restrict__ prior, const int* __restrict__ parents, int root, int sz,
+                               float q, float* __restrict__ off) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= sz) return;
+    const int p = c == root ? c : parents[c];
+#pragma unroll
+    for (int a = 0; a < 3; a++) off[a * sz + c] = (prior[a * sz + p] - prior[a * sz + c]) / q;
+}
+
+// dL/dprior from dL/doff: each edge's offset depends on its two end nodes
+__global__ void k_soft_offbar_to_prior(const float* __restrict__ offbar, const int* __restrict__ parents, int root,
+                                       int sz, float q, float* __restrict__ gprior) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= sz || c == root) return;
+    const int p = parents[c];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float g = offbar[a * sz + c] / q;
+        atomicAdd(gprior + a * sz + p, g);
+        atomicAdd(gprior + a * sz + c, -g);
+    }
+}
 
 // ---------------------------------------------------------------------------
 // Host drivers
@@ -1247,6 +1310,20 @@ static void box3(float* a, float* b, int m, int n, int o, int r, cudaStream_t st
     k_soft_box<<<grid, blk, 0, st>>>(a, b, m, n, o, r, 0);
     k_soft_box<<<grid, blk, 0, st>>>(b, a, m, n, o, r, 1);
     k_soft_box<<<grid, blk, 0, st>>>(a, b, m, n, o, r, 2);
+}
+
+cudaError_t launch_soft_offsets(const float* prior, const int* parents, int root, int sz, float q, float* off,
+                                cudaStream_t st) {
+    k_soft_offsets<<<blocks_for(sz, 256), 256, 0, st>>>(prior, parents, root, sz, q, off);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_soft_offbar_to_prior(const float* offbar, const int* parents, int root, int sz, float q,
+                                        float* gprior, cudaStream_t st) {
+    k_soft_offbar_to_prior<<<blocks_for(sz, 256), 256, 0, st>>>(offbar, parents, root, sz, q, gprior);
+    count_launches(1);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_soft_descriptor(const float* d_im, float* w6a, float* w6b, float* s12, int m, int n, int o, int qs,

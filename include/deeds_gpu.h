@@ -270,23 +270,48 @@ deeds_status deeds_soft_descriptor_dev(deeds_ctx* ctx, const float* d_im, int m,
 deeds_status deeds_soft_cost_dev(deeds_ctx* ctx, const float* d_desc_fixed, const float* d_desc_moving, int m, int n,
                                  int o, const deeds_soft_params* p, float* d_cost, void* stream);
 
-/* Forward: expected displacement (u|v|w) of the soft level.  ordered/parents/
- * edgemst are the host arrays of primsGraph() on the fixed image at this grid
- * (deeds_prims_from_sad); every parent must precede its children in `ordered`.
- * Synchronous (it reads back the tree sweeps' status; DEEDS_ERR_TIMEOUT if a
- * bounded device-side wait gave up). */
+/* Forward: expected displacement (u|v|w) of the soft level, relative to the
+ * prior field when d_prior is given.  ordered/parents/edgemst are the host arrays
+ * of primsGraph() on the fixed image at this grid (deeds_prims_from_sad); every
+ * parent must precede its children in `ordered`.  d_prior (nullable): the current
+ * grid field u|v|w (3 x m1*n1*o1), which enters the pairwise term as in
+ * regularisationCL (src/regularisation.h:205-208): |lab(child) - lab(parent) - off|^2,
+ * off = (prior[parent] - prior[child]) / q; `moving` is then expected to be
+ * warped by the prior already (deeds_soft_warp_dev).  Synchronous (it reads back
+ * the tree sweeps' status; DEEDS_ERR_TIMEOUT if a bounded device-side wait gave
+ * up). */
 deeds_status deeds_soft_forward_dev(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, int m, int n, int o,
                                     const deeds_soft_params* p, const int* ordered, const int* parents,
-                                    const float* edgemst, float* d_disp, void* stream);
+                                    const float* edgemst, const float* d_prior, float* d_disp, void* stream);
 
 /* Backward: given dL/d(displacement) (3 x m1*n1*o1), writes dL/dfixed and
- * dL/dmoving (m*n*o each, overwritten; either may be NULL) and dL/dalpha
- * (host float, may be NULL).  Recomputes the forward sweeps (no state is kept
- * from deeds_soft_forward_dev).  Synchronous, like the forward. */
+ * dL/dmoving (m*n*o each, overwritten; either may be NULL), dL/dprior through the
+ * pairwise offsets (3 x m1*n1*o1, overwritten; NULL unless d_prior is given) and
+ * dL/dalpha (host float, may be NULL).  Recomputes the forward sweeps (no state is
+ * kept from deeds_soft_forward_dev).  Synchronous, like the forward. */
 deeds_status deeds_soft_backward_dev(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, int m, int n, int o,
                                      const deeds_soft_params* p, const int* ordered, const int* parents,
-                                     const float* edgemst, const float* d_grad_disp, float* d_grad_fixed,
-                                     float* d_grad_moving, float* grad_alpha, void* stream);
+                                     const float* edgemst, const float* d_prior, const float* d_grad_disp,
+                                     float* d_grad_fixed, float* d_grad_moving, float* d_grad_prior,
+                                     float* grad_alpha, void* stream);
+
+/* Differentiable trilinear upsampling of a field u|v|w from an mA x nA x oA grid to
+ * m x n x o (the coordinates of upsampleDeformationsCL, src/transformations.h:245-279,
+ * in float arithmetic), and its adjoint (gin overwritten). */
+deeds_status deeds_soft_upsample_dev(deeds_ctx* ctx, const float* d_in, int mA, int nA, int oA, float* d_out, int m,
+                                     int n, int o, void* stream);
+deeds_status deeds_soft_upsample_backward_dev(deeds_ctx* ctx, const float* d_grad_out, int m, int n, int o,
+                                              float* d_grad_in, int mA, int nA, int oA, void* stream);
+
+/* Differentiable warp of an m x n x o image by a grid field u|v|w (mA x nA x oA,
+ * upsampled on the fly): warpAffine with the identity (src/dataCostD.h:267-295) in
+ * float arithmetic; its adjoint writes dL/dmoving and dL/dgrid (each nullable,
+ * overwritten). */
+deeds_status deeds_soft_warp_dev(deeds_ctx* ctx, const float* d_moving, int m, int n, int o, const float* d_grid,
+                                 int mA, int nA, int oA, float* d_out, void* stream);
+deeds_status deeds_soft_warp_backward_dev(deeds_ctx* ctx, const float* d_moving, int m, int n, int o,
+                                          const float* d_grid, int mA, int nA, int oA, const float* d_grad_out,
+                                          float* d_grad_moving, float* d_grad_grid, void* stream);
 
 #ifdef __cplusplus
 }

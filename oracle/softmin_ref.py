@@ -139,11 +139,33 @@ def label_grid(hw):
     return torch.stack([lx, ly, lz], dim=1).to(torch.float64)  # (len3, 3): x, y, z label coords
 
 
-def soft_tree(cost, ordered, parents, edgemst, hw, q, tau):
-    """Expected displacement (3, sz1) as [u(x), v(y), w(z)] from the soft recursion."""
+def edge_offsets(prior, parents, root, q):
+    """(sz1, 3) label-unit offsets (x, y, z) of each node's edge to its parent from a
+    prior grid field (3, sz1) [u, v, w]: (prior[parent] - prior[node]) / q, as the
+    reference's regularisationCL (src/regularisation.h:205-208); zero at the root."""
+    par = torch.as_tensor(np.asarray(parents, np.int64)).clone()
+    par[int(root)] = int(root)
+    off = (prior[:, par] - prior) / q  # (3, sz1)
+    return off.T
+
+
+def soft_tree(cost, ordered, parents, edgemst, hw, q, tau, prior=None):
+    """Expected displacement (3, sz1) as [u(x), v(y), w(z)] from the soft recursion,
+    relative to the prior field (3, sz1) when one is given: the pairwise term of an
+    edge is |lab(l_child) - lab(l_parent) - off|^2 with off the prior's difference
+    parent - child in label units."""
     sz1, len3 = cost.shape
     lab = label_grid(hw)
     Q = ((lab[:, None, :] - lab[None, :, :]) ** 2).sum(-1)  # (l, lp)
+    offs = None
+    if prior is not None:
+        offs = edge_offsets(prior, parents, int(ordered[0]), q)  # (sz1, 3)
+
+    def Qc(c):
+        if offs is None:
+            return Q
+        d = lab[None, :, :] - lab[:, None, :] + offs[c][None, None, :]  # (l, lp, 3): lp - l + off
+        return (d ** 2).sum(-1)
     children = [[] for _ in range(sz1)]
     for t in range(1, sz1):
         c = int(ordered[t])
@@ -158,7 +180,7 @@ def soft_tree(cost, ordered, parents, edgemst, hw, q, tau):
         B[c] = b
         if t > 0:
             e = float(edgemst[c])
-            M[c] = -tau * torch.logsumexp(-(e * b[:, None] + Q) / tau, dim=0)  # over l, for each lp
+            M[c] = -tau * torch.logsumexp(-(e * b[:, None] + Qc(c)) / tau, dim=0)  # over l, for each lp
     logp = [None] * sz1
     root = int(ordered[0])
     logp[root] = torch.log_softmax(-B[root] / tau, dim=0)
@@ -167,7 +189,7 @@ def soft_tree(cost, ordered, parents, edgemst, hw, q, tau):
         p = int(parents[c])
         e = float(edgemst[c])
         r = logp[p] + M[c] / tau
-        G = torch.logsumexp(r[None, :] - Q / tau, dim=1)  # over lp, for each l
+        G = torch.logsumexp(r[None, :] - Qc(c) / tau, dim=1)  # over lp, for each l
         logp[c] = -e * B[c] / tau + G
     P = torch.stack([torch.exp(lp) for lp in logp])  # (sz1, len3)
     disp = (lab - hw) * q  # (len3, 3) x, y, z
@@ -181,3 +203,84 @@ def soft_register(fixed, moving, alpha, tree, g, hw, q, tau, eps, qs):
     sM = soft_mind(moving, qs)
     cost = soft_cost(sF, sM, g, hw, q, alpha, eps)
     return soft_tree(cost, ordered, parents, edgemst, hw, q, tau)
+
+
+def upsample(field, src_dims, dst_dims):
+    """Trilinear upsampling of a (3, o2, n2, m2) field to (3, o, n, m) with the
+    reference's coordinates (src/transformations.h:245-279): node (i, j, k) reads the
+    source at (i / (m/m2), j / (n/n2), k / (o/o2)), corners clamped to the grid."""
+    m2, n2, o2 = src_dims
+    m, n, o = dst_dims
+    dt = field.dtype
+    y = torch.arange(m, dtype=dt) / (m / m2)
+    x = torch.arange(n, dtype=dt) / (n / n2)
+    z = torch.arange(o, dtype=dt) / (o / o2)
+    return _trilinear(field, z[:, None, None], x[None, :, None], y[None, None, :])
+
+
+def _trilinear(vol, zc, xc, yc):
+    """Trilinear interpolation of vol (..., o, n, m) at coordinates zc, xc, yc
+    (broadcastable, voxel units), clamp-to-edge corners; differentiable in vol
+    and in the coordinates (piecewise)."""
+    o, n, m = vol.shape[-3:]
+    z0f, x0f, y0f = torch.floor(zc), torch.floor(xc), torch.floor(yc)
+    dz, dx, dy = zc - z0f, xc - x0f, yc - y0f
+    z0, x0, y0 = z0f.long(), x0f.long(), y0f.long()
+    zc0, zc1 = z0.clamp(0, o - 1), (z0 + 1).clamp(0, o - 1)
+    xc0, xc1 = x0.clamp(0, n - 1), (x0 + 1).clamp(0, n - 1)
+    yc0, yc1 = y0.clamp(0, m - 1), (y0 + 1).clamp(0, m - 1)
+    shape = torch.broadcast_shapes(zc.shape, xc.shape, yc.shape)
+    zc0, zc1, xc0, xc1, yc0, yc1 = (t.expand(shape) for t in (zc0, zc1, xc0, xc1, yc0, yc1))
+    dz, dx, dy = (t.expand(shape) for t in (dz, dx, dy))
+
+    def at(zz, xx, yy):
+        return vol[..., zz, xx, yy]
+
+    return (at(zc0, xc0, yc0) * (1 - dz) * (1 - dx) * (1 - dy) + at(zc0, xc0, yc1) * (1 - dz) * (1 - dx) * dy
+            + at(zc0, xc1, yc0) * (1 - dz) * dx * (1 - dy) + at(zc0, xc1, yc1) * (1 - dz) * dx * dy
+            + at(zc1, xc0, yc0) * dz * (1 - dx) * (1 - dy) + at(zc1, xc0, yc1) * dz * (1 - dx) * dy
+            + at(zc1, xc1, yc0) * dz * dx * (1 - dy) + at(zc1, xc1, yc1) * dz * dx * dy)
+
+
+def warp(moving, full):
+    """moving (o, n, m) sampled at p + field, field (3, o, n, m) [u(x), v(y), w(z)]
+    (warpAffine with the identity, src/dataCostD.h:267-295, in float arithmetic)."""
+    o, n, m = moving.shape
+    dt = moving.dtype
+    zz = torch.arange(o, dtype=dt)[:, None, None] + full[2]
+    xx = torch.arange(n, dtype=dt)[None, :, None] + full[0]
+    yy = torch.arange(m, dtype=dt)[None, None, :] + full[1]
+    return _trilinear(moving, zz, xx, yy)
+
+
+def soft_register_levels(fixed, moving, alpha, trees, levels, tau, eps, perturb=None):
+    """Multi-level soft registration in float64 (the deeds level loop,
+    src/deedsBCV0.cpp:222-306, forward direction only): per level the prior grid
+    field is the previous level's result upsampled to this grid, the moving image is
+    warped by the prior upsampled to full resolution, and the soft level returns the
+    displacement relative to the prior.  levels: [(g, hw, q, qs)], trees: per level
+    (ordered, parents, edgemst).  perturb (tests only): callable (level, E) -> E
+    applied to each level's expected displacement, to measure how far rounding-size
+    changes of the forward move the gradients.  Returns the last grid field
+    (3, o1, n1, m1)."""
+    o, n, m = fixed.shape
+    prev = None
+    prev_dims = None
+    for li, ((g, hw, q, qs), tree) in enumerate(zip(levels, trees)):
+        m1, n1, o1 = m // g, n // g, o // g
+        if prev is None:
+            U = torch.zeros(3, o1, n1, m1, dtype=fixed.dtype)
+            warped = moving
+        else:
+            U = upsample(prev, prev_dims, (m1, n1, o1))
+            warped = warp(moving, upsample(U, (m1, n1, o1), (m, n, o)))
+        sF = soft_mind(fixed, qs)
+        sM = soft_mind(warped, qs)
+        cost = soft_cost(sF, sM, g, hw, q, alpha, eps)
+        # node order y fastest = the (o1, n1, m1) C order of U
+        E = soft_tree(cost, tree[0], tree[1], tree[2], hw, q, tau, prior=U.reshape(3, -1))
+        if perturb is not None:
+            E = perturb(li, E)
+        prev = U + E.reshape(3, o1, n1, m1)
+        prev_dims = (m1, n1, o1)
+    return prev
