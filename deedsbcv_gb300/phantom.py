@@ -9,6 +9,11 @@ on volumes from this generator.  A pair is built from one label map:
 * moving: the same anatomy resampled through a smooth random displacement field
   (cubic B-spline on a control grid of spacing 16 voxels, scaled to a given
   maximum displacement), with its own noise draw.
+* ``affine=(max_degrees, max_scale, max_shift)`` composes a seeded affine map
+  (rotations about the three axes, per-axis scaling and a translation about the
+  volume centre) with the displacement field: moving(p) = anatomy(A p + disp(p));
+  the 4x4 map is returned in the deeds matrix layout (X[0..3] gives y, X[4..7] x,
+  X[8..11] z, src/linearBCV.cpp:289-296).
 * ``contrast="cross"`` re-maps the moving anatomy's intensities per organ into
   [0, 1000] with an inverted background, multiplies a smooth bias field in
   [0.7, 1.3] and adds Rician noise (sigma 15).
@@ -93,11 +98,29 @@ def _render(body, labels, organ_hu, background, body_hu):
     return img
 
 
-def make_pair(shape, seed=0, n_organs=None, max_disp=6.0, spacing=16, contrast="same"):
-    """Return dict(fixed, moving, fixed_labels, moving_labels, disp) for one pair.
+def _affine(shape, max_degrees, max_scale, max_shift, rng):
+    """4x4 float64 map of (y, x, z, 1) about the volume centre."""
+    ang = np.deg2rad(rng.uniform(-max_degrees, max_degrees, 3))
+    ca, sa = np.cos(ang), np.sin(ang)
+    rx = np.array([[1, 0, 0], [0, ca[0], -sa[0]], [0, sa[0], ca[0]]])
+    ry = np.array([[ca[1], 0, sa[1]], [0, 1, 0], [-sa[1], 0, ca[1]]])
+    rz = np.array([[ca[2], -sa[2], 0], [sa[2], ca[2], 0], [0, 0, 1]])
+    lin = rz @ ry @ rx @ np.diag(1.0 + rng.uniform(-max_scale, max_scale, 3))
+    c = (np.array(shape, np.float64) - 1) / 2
+    t = c - lin @ c + rng.uniform(-max_shift, max_shift, 3)
+    A = np.eye(4)
+    A[:3, :3] = lin
+    A[:3, 3] = t
+    return A
+
+
+def make_pair(shape, seed=0, n_organs=None, max_disp=6.0, spacing=16, contrast="same", affine=None):
+    """Return dict(fixed, moving, fixed_labels, moving_labels, disp[, affine]) for one pair.
 
     ``disp`` (3, m, n, o) float32 maps fixed to moving: moving(p) = anatomy(p + disp(p))
-    with components ordered (y, x, z) = (dim 1, dim 2, dim 3).
+    with components ordered (y, x, z) = (dim 1, dim 2, dim 3).  With ``affine``
+    the map is moving(p) = anatomy(A p + disp(p)) and ``affine`` in the result
+    holds A as 16 float32 values in the deeds matrix layout.
     """
     shape = tuple(int(s) for s in shape)
     rng = np.random.default_rng(seed)
@@ -108,7 +131,13 @@ def make_pair(shape, seed=0, n_organs=None, max_disp=6.0, spacing=16, contrast="
     fixed = _render(body, labels, organ_hu, -1000.0, 0.0)
     disp = _bspline_field(shape, spacing, max_disp, rng)
     grid = np.meshgrid(*[np.arange(s, dtype=np.float32) for s in shape], indexing="ij")
-    coords = [grid[d] + disp[d] for d in range(3)]
+    A = None
+    if affine is not None:
+        A = _affine(shape, *affine, rng)
+        pos = [sum(A[d, e] * grid[e] for e in range(3)) + A[d, 3] for d in range(3)]
+        coords = [(pos[d] + disp[d]).astype(np.float32) for d in range(3)]
+    else:
+        coords = [grid[d] + disp[d] for d in range(3)]
     mov_labels = ndimage.map_coordinates(labels, coords, order=0, mode="nearest").astype(np.uint8)
     mov_body = ndimage.map_coordinates(body.astype(np.uint8), coords, order=0, mode="nearest").astype(bool)
     if contrast == "same":
@@ -126,13 +155,17 @@ def make_pair(shape, seed=0, n_organs=None, max_disp=6.0, spacing=16, contrast="
     else:
         raise ValueError(f"unknown contrast {contrast!r}")
     fixed = fixed + rng.normal(0.0, 20.0, shape).astype(np.float32)
-    return {
+    out = {
         "fixed": np.asfortranarray(fixed.astype(np.float32)),
         "moving": np.asfortranarray(moving.astype(np.float32)),
         "fixed_labels": np.asfortranarray(labels),
         "moving_labels": np.asfortranarray(mov_labels),
         "disp": disp,
     }
+    if A is not None:
+        out["affine"] = A[:3, :].ravel().astype(np.float32).tolist() + [0.0, 0.0, 0.0, 1.0]
+        out["affine"] = np.array(out["affine"], np.float32)
+    return out
 
 
 def dice(a, b):

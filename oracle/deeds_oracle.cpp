@@ -738,4 +738,349 @@ int orc_register(const float* fixed, const float* moving, int m, int n, int o, c
     return (int)sz1;
 }
 
+// ---------------------------------------------------------------------------
+// linearBCV (src/linearBCV.cpp:163-262): affine / rigid pre-registration from the
+// per-node best labels of two smoothed cost volumes, fitted by least trimmed
+// squares.  pow(x, 2) of a float is exact in double and sqrt of a float is the
+// float overload (the reference's `using namespace std` with <cmath>).
+
+// warpAffine of src/affineLTS1.h:39-68: trilinear with the affine map only, zero
+// where the floor corner leaves [0, dim-2].
+void orc_lin_warp(float* out, const float* in, const float* X, int m, int n, int o) {
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < o; k++)
+        for (int j = 0; j < n; j++)
+            for (int i = 0; i < m; i++) {
+                const size_t p = i + (size_t)j * m + (size_t)k * m * n;
+                const float y1 = (float)i * X[0] + (float)j * X[1] + (float)k * X[2] + X[3];
+                const float x1 = (float)i * X[4] + (float)j * X[5] + (float)k * X[6] + X[7];
+                const float z1 = (float)i * X[8] + (float)j * X[9] + (float)k * X[10] + X[11];
+                const int x = (int)std::floor(x1), y = (int)std::floor(y1), z = (int)std::floor(z1);
+                const float dx = x1 - x, dy = y1 - y, dz = z1 - z;
+                if (y < 0 || y >= m - 1 || x < 0 || x >= n - 1 || z < 0 || z >= o - 1) out[p] = 0.0f;
+                else out[p] = sample_trilinear(in, m, n, o, y, x, z, dx, dy, dz);
+            }
+}
+
+}  // extern "C"
+
+namespace {
+
+float lin_norm(const float* v, int len) {  // src/QRsolve.h:2-8
+    float s = 0;
+    for (int i = 0; i < len; i++) s = (float)((double)s + (double)v[i] * (double)v[i]);
+    return std::sqrt(s);
+}
+
+float lin_dot(const float* a, const float* b, int len) {  // src/QRsolve.h:10-16
+    float d = 0;
+    for (int i = 0; i < len; i++) d += a[i] * b[i];
+    return d;
+}
+
+// Classical Gram-Schmidt QR of A (len x 4, column c at A + c*len) and the
+// back-substitution for len2 right-hand sides (src/QRsolve.h:18-84).
+void lin_qrsolve(float* X, const float* A, const float* b, int len, int len2) {
+    std::vector<float> Q(4 * (size_t)len);
+    const float r11 = lin_norm(A, len);
+    for (int i = 0; i < len; i++) Q[i] = A[i] / r11;
+    const float r12 = lin_dot(Q.data(), A + len, len);
+    const float r13 = lin_dot(Q.data(), A + 2 * len, len);
+    const float r14 = lin_dot(Q.data(), A + 3 * len, len);
+    for (int i = 0; i < len; i++) {
+        Q[i + len] = A[i + len] - Q[i] * r12;
+        Q[i + 2 * len] = A[i + 2 * len] - Q[i] * r13;
+        Q[i + 3 * len] = A[i + 3 * len] - Q[i] * r14;
+    }
+    const float r22 = lin_norm(Q.data() + len, len);
+    for (int i = 0; i < len; i++) Q[i + len] = Q[i + len] / r22;
+    const float r23 = lin_dot(Q.data() + len, A + 2 * len, len);
+    const float r24 = lin_dot(Q.data() + len, A + 3 * len, len);
+    for (int i = 0; i < len; i++) {
+        Q[i + 2 * len] = A[i + 2 * len] - Q[i] * r13 - Q[i + len] * r23;
+        Q[i + 3 * len] = A[i + 3 * len] - Q[i] * r14 - Q[i + len] * r24;
+    }
+    const float r33 = lin_norm(Q.data() + 2 * len, len);
+    for (int i = 0; i < len; i++) Q[i + 2 * len] = Q[i + 2 * len] / r33;
+    const float r34 = lin_dot(Q.data() + 2 * len, A + 3 * len, len);
+    for (int i = 0; i < len; i++) Q[i + 3 * len] = A[i + 3 * len] - Q[i] * r14 - Q[i + len] * r24 - Q[i + 2 * len] * r34;
+    const float r44 = lin_norm(Q.data() + 3 * len, len);
+    for (int i = 0; i < len; i++) Q[i + 3 * len] = Q[i + 3 * len] / r44;
+    for (int j = 0; j < len2; j++) {
+        const float d1 = lin_dot(Q.data(), b + (size_t)j * len, len);
+        const float d2 = lin_dot(Q.data() + len, b + (size_t)j * len, len);
+        const float d3 = lin_dot(Q.data() + 2 * len, b + (size_t)j * len, len);
+        const float d4 = lin_dot(Q.data() + 3 * len, b + (size_t)j * len, len);
+        const float x4 = d4 / r44;
+        const float x3 = (d3 - r34 * x4) / r33;
+        const float x2 = (d2 - r23 * x3 - r24 * x4) / r22;
+        const float x1 = (d1 - r12 * x2 - r13 * x3 - r14 * x4) / r11;
+        X[0 + j * 4] = x1; X[1 + j * 4] = x2; X[2 + j * 4] = x3; X[3 + j * 4] = x4;
+    }
+}
+
+// One-sided Jacobi SVD of a 3x3 matrix, 4 sweeps (src/QRsolve.h:86-141).
+void lin_jacobi3(const float* A, float* U, float* V) {
+    for (int i = 0; i < 9; i++) { U[i] = A[i]; V[i] = 0; }
+    V[0] = 1; V[4] = 1; V[8] = 1;
+    float T[3];
+    for (int iter = 0; iter < 4; iter++)
+        for (int j = 1; j < 3; j++)
+            for (int i = 0; i < j; i++) {
+                const float al = lin_dot(U + i * 3, U + i * 3, 3);
+                const float be = lin_dot(U + j * 3, U + j * 3, 3);
+                const float ga = lin_dot(U + i * 3, U + j * 3, 3);
+                const float zeta = (float)((double)(be - al) / (2.0 * (double)ga));
+                const float t = (float)((zeta > 0 ? 1.0 : -1.0) /
+                                        ((double)std::fabs(zeta) + std::sqrt(1.0 + (double)(zeta * zeta))));
+                const float c = (float)(1.0 / (double)std::sqrt(1.0f + t * t));
+                const float sn = c * t;
+                for (int k = 0; k < 3; k++) T[k] = U[k + i * 3];
+                for (int k = 0; k < 3; k++) U[k + i * 3] = c * T[k] - sn * U[k + j * 3];
+                for (int k = 0; k < 3; k++) U[k + j * 3] = sn * T[k] + c * U[k + j * 3];
+                for (int k = 0; k < 3; k++) T[k] = V[k + i * 3];
+                for (int k = 0; k < 3; k++) V[k + i * 3] = c * T[k] - sn * V[k + j * 3];
+                for (int k = 0; k < 3; k++) V[k + j * 3] = sn * T[k] + c * V[k + j * 3];
+            }
+    for (int j = 0; j < 3; j++) {
+        const float sv = lin_norm(U + j * 3, 3);
+        for (int i = 0; i < 3; i++) U[i + j * 3] /= sv;
+    }
+}
+
+// Rigid fit (rotation from the SVD of the cross-covariance, translation from the
+// means) of point sets in column layout (src/QRsolve.h:143-254).
+void lin_find_rigid(float* RT, const float* p1t, const float* p2t, int len) {
+    std::vector<float> p1(4 * (size_t)len), p2(4 * (size_t)len);
+    for (int i = 0; i < 4; i++)
+        for (int k = 0; k < len; k++) {
+            p1[i + k * 4] = p1t[k + (size_t)i * len];
+            p2[i + k * 4] = p2t[k + (size_t)i * len];
+        }
+    float m1[3] = {0, 0, 0}, m2[3] = {0, 0, 0};
+    for (int k = 0; k < len; k++)
+        for (int c = 0; c < 3; c++) { m1[c] += p1[c + k * 4]; m2[c] += p2[c + k * 4]; }
+    for (int c = 0; c < 3; c++) { m1[c] /= (float)len; m2[c] /= (float)len; }
+    float K[9] = {0}, U[9], V[9], R[16] = {0};
+    for (int k = 0; k < len; k++)
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) K[i + j * 3] += (p1[j + k * 4] - m1[j]) * (p2[i + k * 4] - m2[i]);
+    lin_jacobi3(K, U, V);
+    for (int i = 0; i < 16; i++) RT[i] = 0.0f;
+    R[15] = 1.0f;
+    RT[15] = 1.0f;
+    for (int k = 0; k < 3; k++)
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) R[j + i * 4] += U[j + k * 3] * V[i + k * 3];
+    std::vector<float> Rp2(4 * (size_t)len);
+    lin_qrsolve(Rp2.data(), R, p2.data(), 4, len);
+    float t1[3] = {0, 0, 0};
+    for (int i = 0; i < len; i++)
+        for (int c = 0; c < 3; c++) t1[c] += Rp2[c + i * 4];
+    for (int c = 0; c < 3; c++) t1[c] = t1[c] / (float)len - m1[c];
+    float t0[3] = {0, 0, 0};
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) t0[i] += R[i + j * 4] * t1[j];
+    for (int i = 0; i < 3; i++) {
+        for (int j = 0; j < 3; j++) RT[i + j * 4] += R[j + i * 4];
+        RT[3 + i * 4] = t0[i];
+    }
+}
+
+void lin_fit(float* RT, const float* p1, const float* p2, int len, bool rigid) {
+    if (rigid) lin_find_rigid(RT, p1, p2, len);
+    else lin_qrsolve(RT, p1, p2, len, 4);
+}
+
+}  // namespace
+
+extern "C" {
+
+// affineRobust (src/QRsolve.h:258-296): a fit to all points, then 15 rounds of
+// refitting to the half with the smallest squared residuals.
+void orc_affine_robust(float* RT, const float* p1, const float* p2, int len, int rigid) {
+    lin_fit(RT, p1, p2, len, rigid != 0);
+    const int lenh = len / 2;
+    std::vector<float> err(len), err2(len), p1b(4 * (size_t)lenh, 1.0f), p2b(4 * (size_t)lenh, 1.0f);
+    for (int iter = 0; iter < 15; iter++) {
+        for (int l = 0; l < len; l++) {
+            float x = 0, y = 0, z = 0;
+            for (int i = 0; i < 3; i++) {
+                y += p1[l + (size_t)i * len] * RT[i];
+                x += p1[l + (size_t)i * len] * RT[i + 4];
+                z += p1[l + (size_t)i * len] * RT[i + 8];
+            }
+            y += p1[l + 3 * (size_t)len] * RT[3];
+            x += p1[l + 3 * (size_t)len] * RT[7];
+            z += p1[l + 3 * (size_t)len] * RT[11];
+            const double ey = (double)(y - p2[l]), ex = (double)(x - p2[l + len]), ez = (double)(z - p2[l + 2 * (size_t)len]);
+            err[l] = (float)(ey * ey + ex * ex + ez * ez);
+            err2[l] = err[l];
+        }
+        std::nth_element(err.begin(), err.begin() + len / 2, err.end());
+        const float median = err[len / 2];
+        int count = 0;
+        for (int i = 0; i < len; i++) {
+            const int l = std::min(count, lenh - 1);
+            if (err2[i] <= median) {
+                for (int c = 0; c < 3; c++) {
+                    p1b[l + (size_t)c * lenh] = p1[i + (size_t)c * len];
+                    p2b[l + (size_t)c * lenh] = p2[i + (size_t)c * len];
+                }
+                count++;
+            }
+        }
+        lin_fit(RT, p1b.data(), p2b.data(), lenh, rigid != 0);
+    }
+}
+
+void orc_qrsolve(float* X, const float* A, const float* b, int len, int len2) { lin_qrsolve(X, A, b, len, len2); }
+
+// The three in-place smoothing passes of estimateAffine2 (src/affineLTS1.h:124-158):
+// along y, then x, then z, each node gets half its two neighbours added, the
+// lower neighbour already updated by the same pass (sequential node order).
+void orc_lin_smooth(float* cost, int m1, int n1, int o1, int len3) {
+    const int sz1 = m1 * n1 * o1;
+    for (int axis = 0; axis < 3; axis++)
+        for (int i = 0; i < sz1; i++) {
+            const int z1 = i / (m1 * n1), x1 = (i - z1 * m1 * n1) / m1, y1 = i - z1 * m1 * n1 - x1 * m1;
+            int i1, i2;
+            if (axis == 0) {
+                i1 = std::min(y1 + 1, m1 - 1) + x1 * m1 + z1 * m1 * n1;
+                i2 = std::max(y1 - 1, 0) + x1 * m1 + z1 * m1 * n1;
+            } else if (axis == 1) {
+                i1 = y1 + std::min(x1 + 1, n1 - 1) * m1 + z1 * m1 * n1;
+                i2 = y1 + std::max(x1 - 1, 0) * m1 + z1 * m1 * n1;
+            } else {
+                i1 = y1 + x1 * m1 + std::min(z1 + 1, o1 - 1) * m1 * n1;
+                i2 = y1 + x1 * m1 + std::max(z1 - 1, 0) * m1 * n1;
+            }
+            for (int l = 0; l < len3; l++) {
+                const double add = 0.5 * (double)cost[(size_t)i1 * len3 + l] + 0.5 * (double)cost[(size_t)i2 * len3 + l];
+                cost[(size_t)i * len3 + l] = (float)((double)cost[(size_t)i * len3 + l] + add);
+            }
+        }
+}
+
+// estimateAffine2 (src/affineLTS1.h:91-236) on the two cost volumes of a level
+// (smoothed in place), the +1024-shifted fixed and moving images and the previous
+// matrix; X = fit * Xprev.  Returns the number of points used.
+int orc_estimate_affine(float* X, const float* Xprev, const float* fixed, const float* moving, float* cost,
+                        float* cost2, int m, int n, int o, int g, float q, int hw, int rigid) {
+    const int m1 = m / g, n1 = n / g, o1 = o / g, sz1 = m1 * n1 * o1;
+    const int len = 2 * hw + 1, len3 = len * len * len, stephw = (g - 1) / 2;
+    std::vector<float> xs(len3), ys(len3), zs(len3);
+    for (int l = 0; l < len3; l++) {
+        const int i = l % len, j = (l / len) % len, k = l / (len * len);
+        xs[l] = (j - hw) * q; ys[l] = (i - hw) * q; zs[l] = (k - hw) * q;
+    }
+    orc_lin_smooth(cost, m1, n1, o1, len3);
+    orc_lin_smooth(cost2, m1, n1, o1, len3);
+    std::vector<float> minval(sz1), minval2(sz1);
+    std::vector<int> minind(sz1), minind2(sz1);
+    int allcount = 0;
+    for (int i = 0; i < sz1; i++) {
+        const float* c1 = cost + (size_t)i * len3;
+        const float* c2 = cost2 + (size_t)i * len3;
+        minind[i] = (int)(std::min_element(c1, c1 + len3) - c1);
+        minval[i] = c1[minind[i]];
+        minind2[i] = (int)(std::min_element(c2, c2 + len3) - c2);
+        minval2[i] = c2[minind2[i]];
+        const int z1 = i / (m1 * n1), x1 = (i - z1 * m1 * n1) / m1, y1 = i - z1 * m1 * n1 - x1 * m1;
+        float mean1 = 0.0f, mean2 = 0.0f;
+        for (int k1 = 0; k1 < g; k1++)
+            for (int j1 = 0; j1 < g; j1++)
+                for (int i1 = 0; i1 < g; i1++) {
+                    const size_t ind = y1 * g + i1 + (size_t)(x1 * g + j1) * m + (size_t)(z1 * g + k1) * m * n;
+                    mean1 += fixed[ind];
+                    mean2 += moving[ind];
+                }
+        mean1 /= (float)(g * g * g);
+        mean2 /= (float)(g * g * g);
+        if (mean1 < 5.0f) minval[i] = 1e20f;
+        if (mean2 < 5.0f) minval2[i] = 1e20f;
+        if (z1 < 2 || z1 > o1 - 2 || x1 < 2 || x1 > n1 - 2 || y1 < 2 || y1 > m1 - 2) {
+            minval[i] = 1e20f;
+            minval2[i] = 1e20f;
+        }
+        if (minval[i] < 1e19f) allcount++;
+        if (minval2[i] < 1e19f) allcount++;
+    }
+    // quantile() of src/linearBCV.cpp:36-46 at 0.5*allcount/sz1/2
+    const float qf = (float)(0.5 * (double)allcount / (double)(float)sz1 / 2.0);
+    auto quantile = [&](const std::vector<float>& v) {
+        std::vector<float> c(v);
+        const int qi = (int)((float)sz1 * std::min(std::max(qf, 0.01f), 0.99f));
+        std::nth_element(c.begin(), c.begin() + qi, c.end());
+        return c[qi];
+    };
+    const float med1 = quantile(minval), med2 = quantile(minval2);
+    int valsz = 0;
+    for (int i = 0; i < sz1; i++) valsz += (minval[i] < med1) + (minval2[i] < med2);
+    std::vector<float> p1(4 * (size_t)valsz), p2(4 * (size_t)valsz);
+    int cur = 0;
+    for (int i = 0; i < sz1; i++) {
+        const int k1 = i / (m1 * n1), j1 = (i - k1 * (m1 * n1)) / m1, i1 = i - j1 * m1 - k1 * m1 * n1;
+        const int y1 = i1 * g + stephw, x1 = j1 * g + stephw, z1 = k1 * g + stephw;
+        if (minval[i] < med1) {
+            const int ind = minind[i];
+            p1[cur + 3 * (size_t)valsz] = 1.0f; p2[cur + 3 * (size_t)valsz] = 1.0f;
+            p1[cur] = y1; p1[cur + valsz] = x1; p1[cur + 2 * (size_t)valsz] = z1;
+            p2[cur] = y1 + ys[ind]; p2[cur + valsz] = x1 + xs[ind]; p2[cur + 2 * (size_t)valsz] = z1 + zs[ind];
+            cur++;
+        }
+        if (minval2[i] < med2) {
+            const int ind = minind2[i];
+            p1[cur + 3 * (size_t)valsz] = 1.0f; p2[cur + 3 * (size_t)valsz] = 1.0f;
+            p2[cur] = y1; p2[cur + valsz] = x1; p2[cur + 2 * (size_t)valsz] = z1;
+            p1[cur] = y1 + ys[ind]; p1[cur + valsz] = x1 + xs[ind]; p1[cur + 2 * (size_t)valsz] = z1 + zs[ind];
+            cur++;
+        }
+    }
+    float X1[16];
+    orc_affine_robust(X1, p1.data(), p2.data(), valsz, rigid);
+    for (int i = 0; i < 4; i++)  // matmult (src/affineLTS1.h:1-12)
+        for (int j = 0; j < 4; j++) {
+            float acc = 0.0f;
+            for (int k = 0; k < 4; k++) acc += X1[i + k * 4] * Xprev[k + j * 4];
+            X[i + j * 4] = acc;
+        }
+    return valsz;
+}
+
+// The linearBCV level loop (src/linearBCV.cpp:163-262) on +1024-shifted images:
+// per level both images are warped by the current matrix (moving forwards,
+// fixed by its QR inverse), both cost volumes are built with alpha 1 and the
+// matrix is re-estimated.  X: 16 floats out.
+void orc_linear_register(const float* fixed, const float* moving, int m, int n, int o, int levels, const int* G,
+                         const int* Lr, const int* Q, int rigid, float* X) {
+    const size_t sz = (size_t)m * n * o;
+    float Xprev[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    std::copy(Xprev, Xprev + 16, X);
+    const float ident[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    std::vector<float> w1(sz), w2(sz);
+    std::vector<uint64_t> mov_mind(sz), fix_mind(sz), warped_mind(sz);
+    for (int level = 0; level < levels; level++) {
+        const int g = G[level], hw = Lr[level], q = Q[level];
+        float Xinv[16];
+        lin_qrsolve(Xinv, Xprev, ident, 4, 4);
+        orc_lin_warp(w2.data(), fixed, Xinv, m, n, o);
+        orc_lin_warp(w1.data(), moving, Xprev, m, n, o);
+        const int prev = orc_mind_step(Q[std::max(level - 1, 0)]), curr = orc_mind_step(q);
+        if (level == 0 || prev != curr) {
+            orc_descriptor(mov_mind.data(), moving, m, n, o, curr);
+            orc_descriptor(fix_mind.data(), fixed, m, n, o, curr);
+        }
+        const int len = 2 * hw + 1, len3 = len * len * len;
+        const size_t sz1 = (size_t)(m / g) * (n / g) * (o / g);
+        std::vector<float> cost(sz1 * len3), cost2(sz1 * len3);
+        orc_descriptor(warped_mind.data(), w1.data(), m, n, o, curr);
+        orc_data_cost(fix_mind.data(), warped_mind.data(), cost.data(), m, n, o, g, hw, q, 1.0f);
+        orc_descriptor(warped_mind.data(), w2.data(), m, n, o, curr);
+        orc_data_cost(mov_mind.data(), warped_mind.data(), cost2.data(), m, n, o, g, hw, q, 1.0f);
+        orc_estimate_affine(X, Xprev, fixed, moving, cost.data(), cost2.data(), m, n, o, g, (float)q, hw, rigid);
+        std::copy(X, X + 16, Xprev);
+    }
+}
+
 }  // extern "C"

@@ -63,6 +63,13 @@ def _declare(L):
     L.orc_jacobian.argtypes = [P, P, P, I, I, I, I, P]; L.orc_jacobian.restype = F
     L.orc_register.argtypes = [P, P, I, I, I, P, I, P, P, P, F, P, P, P, P, P, I]
     L.orc_register.restype = I
+    L.orc_lin_warp.argtypes = [P, P, P, I, I, I]
+    L.orc_qrsolve.argtypes = [P, P, P, I, I]
+    L.orc_affine_robust.argtypes = [P, P, P, I, I]
+    L.orc_lin_smooth.argtypes = [P, I, I, I, I]
+    L.orc_estimate_affine.argtypes = [P, P, P, P, P, P, I, I, I, I, F, I, I]
+    L.orc_estimate_affine.restype = I
+    L.orc_linear_register.argtypes = [P, P, I, I, I, I, P, P, P, I, P]
 
 
 def _flat(a, dtype):
@@ -227,3 +234,57 @@ def register(fixed, moving, m, n, o, X=None, G=(8, 7, 6, 5, 4), L=(8, 7, 6, 5, 4
     lib().orc_register(_p(fixed), _p(moving), m, n, o, _p(X), lv, _p(Ga), _p(La), _p(Qa), float(alpha),
                        _p(flow), None, None, None, None, int(verbose))
     return flow
+
+
+# ---- linearBCV (src/linearBCV.cpp, src/affineLTS1.h, src/QRsolve.h)
+
+LINEAR_DEFAULTS = dict(G=(7, 6, 5, 4), L=(5, 4, 3, 2), Q=(4, 3, 2, 1))  # src/linearBCV.cpp:86-89
+
+
+def lin_warp(inp, X, m, n, o):
+    """warpAffine of src/affineLTS1.h:39-68 (affine only, zero outside)."""
+    inp = _flat(inp, np.float32); X = _flat(X, np.float32)
+    out = np.zeros(m * n * o, np.float32)
+    lib().orc_lin_warp(_p(out), _p(inp), _p(X), m, n, o)
+    return out
+
+
+def qrsolve(A, b, length, nrhs):
+    A = _flat(A, np.float32); b = _flat(b, np.float32)
+    X = np.zeros(4 * nrhs, np.float32)
+    lib().orc_qrsolve(_p(X), _p(A), _p(b), int(length), int(nrhs))
+    return X
+
+
+def affine_robust(p1, p2, length, rigid=False):
+    p1 = _flat(p1, np.float32); p2 = _flat(p2, np.float32)
+    RT = np.zeros(16, np.float32)
+    lib().orc_affine_robust(_p(RT), _p(p1), _p(p2), int(length), int(bool(rigid)))
+    return RT
+
+
+def lin_smooth(cost, m1, n1, o1, len3):
+    cost = _flat(cost, np.float32).copy()
+    lib().orc_lin_smooth(_p(cost), m1, n1, o1, len3)
+    return cost
+
+
+def estimate_affine(Xprev, fixed, moving, cost, cost2, m, n, o, g, q, hw, rigid=False):
+    """estimateAffine2: returns (X, smoothed cost, smoothed cost2, points used)."""
+    Xprev = _flat(Xprev, np.float32); fixed = _flat(fixed, np.float32); moving = _flat(moving, np.float32)
+    c1 = _flat(cost, np.float32).copy(); c2 = _flat(cost2, np.float32).copy()
+    X = np.zeros(16, np.float32)
+    used = lib().orc_estimate_affine(_p(X), _p(Xprev), _p(fixed), _p(moving), _p(c1), _p(c2), m, n, o, g, float(q),
+                                     hw, int(bool(rigid)))
+    return X, c1, c2, used
+
+
+def linear_register(fixed, moving, m, n, o, G=LINEAR_DEFAULTS["G"], L=LINEAR_DEFAULTS["L"], Q=LINEAR_DEFAULTS["Q"],
+                    rigid=False):
+    """The linearBCV level loop on +1024-shifted images: the 16-float matrix."""
+    fixed = _flat(fixed, np.float32); moving = _flat(moving, np.float32)
+    Ga = np.asarray(G, np.int32); La = np.asarray(L, np.int32); Qa = np.asarray(Q, np.int32)
+    X = np.zeros(16, np.float32)
+    lib().orc_linear_register(_p(fixed), _p(moving), m, n, o, len(G), _p(Ga), _p(La), _p(Qa), int(bool(rigid)),
+                              _p(X))
+    return X

@@ -7,7 +7,8 @@ inputs and stores inputs and outputs under tests/golden/*.npz.  It needs the
 reference sources, so it runs only where they are present; the fixtures it
 writes are committed and travel with the tests.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py                 # every fixture
+    python tests/golden/make_golden.py --linear-only   # linear.npz alone
 """
 from __future__ import annotations
 
@@ -63,9 +64,109 @@ def shifted_phantom(shape, seed, **kw):
     return pair, f.astype(np.float32), mv.astype(np.float32)
 
 
+def lin(name, *args):
+    return run(os.path.join(REF, "ref_linear"), name, *args)
+
+
+def make_linear(d, rng):
+    """linearBCV (src/linearBCV.cpp, src/affineLTS1.h, src/QRsolve.h): each stage of
+    the reference through oracle/_ref/ref_linear, and the reference binary end to
+    end (affine and rigid) on a phantom pair with a seeded affine misalignment."""
+    lg = {}
+    # affine-only warp (zero outside) and the QR inverse of a near-identity matrix
+    m, n, o = 24, 20, 28
+    _, fim, _ = shifted_phantom((m, n, o), seed=1, n_organs=6, max_disp=3.0)
+    Xw = np.array([0.97, 0.04, -0.03, 1.6, -0.02, 1.03, 0.05, -2.2, 0.03, -0.04, 0.99, 0.9,
+                   0.0, 0.0, 0.0, 1.0], np.float32)
+    lin("warp", tofile(d, "im", fim), tofile(d, "X", Xw), m, n, o, os.path.join(d, "w"))
+    lg["warp_dims"] = np.array([m, n, o]); lg["warp_image"] = fim; lg["warp_X"] = Xw
+    lg["warp_out"] = np.fromfile(os.path.join(d, "w"), np.float32)
+    lin("qrinv", tofile(d, "X", Xw), os.path.join(d, "xi"))
+    lg["qrinv"] = np.fromfile(os.path.join(d, "xi"), np.float32)
+    # affineRobust on seeded point sets with 20% outliers (affine and rigid fits)
+    npts = 301
+    p1 = np.ones((4, npts), np.float32)
+    p1[:3] = rng.uniform(0, 60, (3, npts)).astype(np.float32)
+    A = np.array([[0.98, 0.05, -0.02, 2.0], [-0.04, 1.02, 0.03, -1.5], [0.02, -0.03, 0.99, 3.0]])
+    p2 = np.ones((4, npts), np.float32)
+    p2[:3] = (A[:, :3] @ p1[:3] + A[:, 3:]).astype(np.float32) + rng.normal(0, 0.3, (3, npts)).astype(np.float32)
+    out_idx = rng.choice(npts, npts // 5, replace=False)
+    p2[:3, out_idx] += rng.uniform(-15, 15, (3, out_idx.size)).astype(np.float32)
+    lg["robust_p1"] = p1.ravel(); lg["robust_p2"] = p2.ravel()
+    for rigid in (0, 1):
+        lin("robust", tofile(d, "p1", p1.ravel()), tofile(d, "p2", p2.ravel()), npts, rigid, os.path.join(d, "rt"))
+        lg[f"robust_{rigid}"] = np.fromfile(os.path.join(d, "rt"), np.float32)
+    # estimateAffine2 on the two cost volumes of a misaligned pair
+    em, en, eo = 48, 40, 48
+    pair = phantom.make_pair((em, en, eo), seed=5, n_organs=7, max_disp=1.5, affine=(5.0, 0.05, 3.0))
+    # whole-HU images (stored as int16), +1024 as the reference shifts them
+    fi = np.round(pair["fixed"].ravel(order="F")).astype(np.int16)
+    mi = np.round(pair["moving"].ravel(order="F")).astype(np.int16)
+    f = fi.astype(np.float32) + np.float32(1024)
+    mv = mi.astype(np.float32) + np.float32(1024)
+    lg["est_dims"] = np.array([em, en, eo]); lg["est_fixed"] = fi; lg["est_moving"] = mi
+    Xp = np.array([1.01, -0.02, 0.01, 0.5, 0.02, 0.99, -0.01, -0.4, -0.01, 0.02, 1.0, 0.3,
+                   0.0, 0.0, 0.0, 1.0], np.float32)
+    lg["est_Xprev"] = Xp
+    for (g, hw, q) in [(5, 3, 2), (4, 2, 1)]:
+        qs = int(np.floor(0.5 * q + 1.0))
+        for name, img in (("cf", f), ("cm", mv)):
+            stage("mind", tofile(d, name + ".f32", img), em, en, eo, qs, os.path.join(d, name + ".u64"))
+        cost = {}
+        for tag, a, b in (("1", "cf", "cm"), ("2", "cm", "cf")):
+            stage("datacost", os.path.join(d, a + ".u64"), os.path.join(d, b + ".u64"), em, en, eo, g, hw, q, "1",
+                  os.path.join(d, "cost" + tag))
+            cost[tag] = np.fromfile(os.path.join(d, "cost" + tag), np.float32)
+        key = f"{g}_{hw}_{q}"
+        for tag in ("1", "2"):
+            counts, alpha1 = _as_counts(cost[tag], g, q, alpha=1.0)
+            lg[f"est_counts{tag}_{key}"] = counts
+            lg[f"est_alpha1_{key}"] = alpha1
+        for rigid in (0, 1):
+            out = lin("estimate", tofile(d, "f", f), tofile(d, "mv", mv), os.path.join(d, "cost1"),
+                      os.path.join(d, "cost2"), tofile(d, "xp", Xp), em, en, eo, g, hw, q, rigid,
+                      *(os.path.join(d, x) for x in ("X", "s1", "s2")))
+            lg[f"est_X_{key}_{rigid}"] = np.fromfile(os.path.join(d, "X"), np.float32)
+            lg[f"est_used_{key}_{rigid}"] = np.int32(int(out.split("# points used:")[1].split("/")[0]))
+            if rigid == 0:
+                for tag, fn in (("1", "s1"), ("2", "s2")):
+                    sm = np.fromfile(os.path.join(d, fn), np.float32)
+                    lg[f"est_smooth{tag}_sha256_{key}"] = np.frombuffer(hashlib.sha256(sm.tobytes()).digest(), np.uint8)
+    # the reference binary end to end (default 4 levels), with a label map
+    lm, ln, lo = 64, 48, 64
+    pair = phantom.make_pair((lm, ln, lo), seed=8, n_organs=8, max_disp=1.5, affine=(6.0, 0.05, 4.0))
+    fpath, mpath, spath = (os.path.join(d, x) for x in ("lf.nii.gz", "lm.nii.gz", "ls.nii.gz"))
+    fi = np.round(pair["fixed"]).astype(np.int16)
+    mi = np.round(pair["moving"]).astype(np.int16)
+    nifti.write(fpath, fi)
+    nifti.write(mpath, mi)
+    nifti.write(spath, pair["moving_labels"].astype(np.int16))
+    lg["e2e_dims"] = np.array([lm, ln, lo])
+    lg["e2e_fixed"] = fi.ravel(order="F"); lg["e2e_moving"] = mi.ravel(order="F")
+    lg["e2e_moving_labels"] = pair["moving_labels"].ravel(order="F")
+    lg["e2e_fixed_labels"] = pair["fixed_labels"].ravel(order="F")
+    lg["e2e_true_affine"] = pair["affine"]
+    logs = []
+    for rigid in (0, 1):
+        stem = os.path.join(d, f"lin{rigid}")
+        args = ["-F", fpath, "-M", mpath, "-O", stem, "-S", spath] + (["-R", "1"] if rigid else [])
+        logs.append(run(os.path.join(REF, "linearBCV"), *args))
+        with open(stem + "_matrix.txt") as fh:
+            lg[f"e2e_matrix_txt_{rigid}"] = np.frombuffer(fh.read().encode(), np.uint8)
+        wseg, _ = nifti.read(stem + "_deformed_seg.nii.gz")
+        lg[f"e2e_seg_{rigid}"] = wseg.ravel(order="F").astype(np.int16)
+    np.savez_compressed(os.path.join(HERE, "linear.npz"), **lg)
+    with open(os.path.join(HERE, "linear_ref_log.txt"), "w") as fh:
+        fh.write("\n".join(logs))
+
+
 def main():
-    if not os.path.exists(os.path.join(REF, "ref_stages")):
+    if not os.path.exists(os.path.join(REF, "ref_linear")):
         run("make", "-C", os.path.join(ROOT, "oracle"), "ref")
+    if "--linear-only" in sys.argv:  # regenerate linear.npz alone
+        with tempfile.TemporaryDirectory() as d:
+            make_linear(d, np.random.default_rng(20241204))
+        return
     rng = np.random.default_rng(20241203)
     out = {}
     with tempfile.TemporaryDirectory() as d:
@@ -187,6 +288,8 @@ def main():
                             flow=flow, warped=warped.ravel(order="F"), warped_seg=wseg.ravel(order="F"))
         with open(os.path.join(HERE, "e2e_ref_log.txt"), "w") as f:
             f.write(log)
+    with tempfile.TemporaryDirectory() as d:
+        make_linear(d, np.random.default_rng(20241204))
     for fn in sorted(os.listdir(HERE)):
         if fn.endswith(".npz"):
             print(fn, os.path.getsize(os.path.join(HERE, fn)))
