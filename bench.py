@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--soft-taus", default="0.1,0.5,2.0")
     ap.add_argument("--soft-shape", default="160x160x192", help="soft-min pair shape (profiling runs use smaller)")
     ap.add_argument("--soft-single", action="store_true", help="--soft-only: the finest soft level alone")
+    ap.add_argument("--no-linear", action="store_true", help="skip the linearBCV measurement")
+    ap.add_argument("--linear-only", action="store_true", help="only the linearBCV measurement (one JSON object)")
     return ap.parse_args()
 
 
@@ -321,6 +323,61 @@ def measure_soft(api, ctx, n_pairs=4, levels=SOFT_LEVELS, taus=SOFT_TAUS, shape=
             "per_tau": out, "gpu_launches": api.kernel_launches() - launches0}
 
 
+def measure_linear(api, ctx, shape, steps=5, warmup=3, cpu=True):
+    """linearBCV (4 default levels, affine fit) on one 192x160x256 pair with a seeded
+    affine misalignment (up to 6 degrees, 6% scaling, 5 voxels) plus a 2-voxel
+    B-spline field.  e2e: through the public host-buffer call (copies in, matrix
+    out; the call returns after the work), wall clock.  value: the device-pointer
+    call on resident inputs, CUDA events on its stream.  The oracle restatement of
+    the same registration gives the CPU baseline and the bit-parity check."""
+    import torch
+    from deedsbcv_gb300 import phantom
+    pair = phantom.make_pair(shape, seed=21, max_disp=2.0, affine=(6.0, 0.06, 5.0))
+    f = np.ascontiguousarray(pair["fixed"].ravel(order="F"), np.float32)
+    mv = np.ascontiguousarray(pair["moving"].ravel(order="F"), np.float32)
+    params = api.linear_params()
+    for _ in range(warmup):
+        X = api.linear_register(f, mv, shape, params, ctx)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        X = api.linear_register(f, mv, shape, params, ctx)
+    e2e_s = (time.perf_counter() - t0) / steps
+    df, dm = torch.from_numpy(f).cuda(), torch.from_numpy(mv).cuda()
+    launches0 = api.kernel_launches()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        Xd = api.linear_register(df, dm, shape, params, ctx)
+    e1.record()
+    torch.cuda.synchronize()
+    dev_s = e0.elapsed_time(e1) / 1000.0 / steps
+    launches = (api.kernel_launches() - launches0) // steps
+    A = pair["affine"].reshape(4, 4).astype(np.float64)
+    Xm = np.array([[X[i * 4 + j] for j in range(4)] for i in range(3)] + [[0, 0, 0, 1]], np.float64)
+    corners = np.array([[a, b, c, 1.0] for a in (0, shape[0] - 1) for b in (0, shape[1] - 1) for c in (0, shape[2] - 1)])
+    out = {"workload": f"linearBCV affine, 4 levels G7x6x5x4 L5x4x3x2 Q4x3x2x1, one {shape[0]}x{shape[1]}x{shape[2]} "
+                       "pair (seed 21, affine up to 6 deg / 6% / 5 voxels + 2-voxel B-spline field)",
+           "pairs_per_s": 1.0 / dev_s, "ms_per_pair": dev_s * 1000.0,
+           "e2e": {"value": 1.0 / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": 2 * f.nbytes,
+                   "d2h_bytes_per_step": 64},
+           "gpu_launches_per_pair": int(launches),
+           "device_and_host_calls_agree": bool(np.array_equal(X.view(np.uint32), Xd.view(np.uint32))),
+           "max_corner_error_vs_truth_voxels": float(np.abs((A @ Xm) @ corners.T - corners.T)[:3].max())}
+    if cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle as orc
+        t0 = time.perf_counter()
+        ref = orc.linear_register(f + np.float32(1024), mv + np.float32(1024), *shape)
+        secs = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 1.0 / secs, "unit": "pairs/s",
+                               "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count())), "kind": "port",
+                               "sample": f"one full linear registration of the same pair ({secs:.1f} s), oracle/ "
+                                         "restatement with OpenMP"}
+        out["matrix_identical_to_oracle"] = bool(np.array_equal(X.view(np.uint32), ref.view(np.uint32)))
+    return out
+
+
 def cpu_reference_pair(pair, shape):
     """The oracle registration of one pair on all host cores: (seconds, flow, ux, vx, wx)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -395,6 +452,9 @@ def main():
     from deedsbcv_gb300 import api, phantom
 
     ctx = api.context(device)
+    if args.linear_only:
+        print(json.dumps(measure_linear(api, ctx, shape, cpu=not args.no_cpu_baseline)), flush=True)
+        return
     if args.soft_only:
         taus = tuple(float(t) for t in args.soft_taus.split(","))
         shp = tuple(int(v) for v in args.soft_shape.split("x"))
@@ -518,6 +578,11 @@ def main():
         soft = measure_soft(api, ctx)
         soft["finest_level_alone"] = measure_soft(api, ctx, levels=SOFT_LEVELS[-1:])
 
+    # ---- linearBCV affine pre-registration (rank 0)
+    linear = None
+    if rank == 0 and not args.no_linear:
+        linear = measure_linear(api, ctx, shape, cpu=(ws == 1 and not args.no_cpu_baseline))
+
     # ---- CPU baseline and full-size parity (rank 0, N=1)
     cpu = None
     parity = None
@@ -557,6 +622,7 @@ def main():
             "parity": parity,
             "batched": batched,
             "soft": soft,
+            "linear": linear,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:

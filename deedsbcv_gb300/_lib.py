@@ -28,6 +28,8 @@ EXPORTS = [
     "deeds_soft_default_params", "deeds_soft_descriptor_dev", "deeds_soft_cost_dev", "deeds_soft_forward_dev",
     "deeds_soft_backward_dev", "deeds_soft_upsample_dev", "deeds_soft_upsample_backward_dev", "deeds_soft_warp_dev",
     "deeds_soft_warp_backward_dev",
+    "deeds_linear_default_params", "deeds_linear_register", "deeds_linear_register_dev", "deeds_lin_warp_dev",
+    "deeds_lin_smooth_dev", "deeds_estimate_affine_dev", "deeds_affine_robust", "deeds_affine_warp_segmentation",
 ]
 NOALLOC_MAX_NODES = 131072
 STAGES = ["mind", "datacost", "mst_edges", "bp_up", "bp_down", "transform", "consistent", "tree_wait"]
@@ -40,6 +42,18 @@ class DeedsParams(C.Structure):
         ("radius", C.c_int * MAX_LEVELS),
         ("quant", C.c_int * MAX_LEVELS),
         ("alpha", C.c_float),
+        ("intensity_shift", C.c_float),
+        ("verbose", C.c_int),
+    ]
+
+
+class DeedsLinearParams(C.Structure):
+    _fields_ = [
+        ("levels", C.c_int),
+        ("grid", C.c_int * MAX_LEVELS),
+        ("radius", C.c_int * MAX_LEVELS),
+        ("quant", C.c_int * MAX_LEVELS),
+        ("rigid", C.c_int),
         ("intensity_shift", C.c_float),
         ("verbose", C.c_int),
     ]
@@ -130,10 +144,20 @@ def load():
     L.deeds_soft_upsample_backward_dev.argtypes = [P, P, I, I, I, P, I, I, I, P]
     L.deeds_soft_warp_dev.argtypes = [P, P, I, I, I, P, I, I, I, P, P]
     L.deeds_soft_warp_backward_dev.argtypes = [P, P, I, I, I, P, I, I, I, P, P, P, P]
+    LP = C.POINTER(DeedsLinearParams)
+    L.deeds_linear_default_params.argtypes = [LP]
+    L.deeds_linear_default_params.restype = None
+    L.deeds_linear_register.argtypes = [P, P, P, I, I, I, LP, P]
+    L.deeds_linear_register_dev.argtypes = [P, P, P, I, I, I, LP, P, P]
+    L.deeds_lin_warp_dev.argtypes = [P, P, I, I, I, P, P]
+    L.deeds_lin_smooth_dev.argtypes = [P, I, I, I, I, P]
+    L.deeds_estimate_affine_dev.argtypes = [P, P, P, P, P, I, I, I, I, I, I, I, P, P, P, P]
+    L.deeds_affine_robust.argtypes = [P, P, I, I, P]
+    L.deeds_affine_warp_segmentation.argtypes = [P, P, I, I, I, P, P]
     for name in EXPORTS:
         fn = getattr(L, name)
         if name not in ("deeds_default_params", "deeds_destroy", "deeds_last_error", "deeds_version",
-                        "deeds_soft_default_params"):
+                        "deeds_soft_default_params", "deeds_linear_default_params"):
             fn.restype = I
     L.deeds_kernel_launches.restype = C.c_longlong
     _lib = L

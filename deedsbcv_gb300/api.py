@@ -21,7 +21,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import DeedsError, DeedsParams, DeedsSoftParams  # noqa: F401
+from ._lib import DeedsError, DeedsLinearParams, DeedsParams, DeedsSoftParams  # noqa: F401
 
 try:  # torch is plumbing for device memory and streams only
     import torch
@@ -591,3 +591,99 @@ def soft_register_levels(fixed, moving, alpha, dims, levels, tau=0.5, eps=0.01, 
             prev = U + E
         prev_dims = gdims
     return prev
+
+
+# ---------------------------------------------------------------------------
+# linearBCV (src/linearBCV.cpp): affine / rigid pre-registration.
+
+def linear_params(grid=(7, 6, 5, 4), radius=(5, 4, 3, 2), quant=(4, 3, 2, 1), rigid=False, verbose=False):
+    p = DeedsLinearParams()
+    _lib.load().deeds_linear_default_params(C.byref(p))
+    if not (len(grid) == len(radius) == len(quant)):
+        raise ValueError("grid, radius and quant need the same number of levels")
+    p.levels = len(grid)
+    for i in range(len(grid)):
+        p.grid[i], p.radius[i], p.quant[i] = int(grid[i]), int(radius[i]), int(quant[i])
+    p.rigid = int(bool(rigid))
+    p.verbose = int(bool(verbose))
+    return p
+
+
+def linear_register(fixed, moving, dims, params=None, ctx=None):
+    """The linearBCV matrix (16 float32, deeds layout) of two volumes in HU.
+
+    fixed/moving: float32 arrays (flat, i fastest, or (m, n, o) Fortran-ordered)
+    on the host, or flat float32 CUDA tensors; +1024 is applied inside."""
+    m, n, o = dims
+    params = params or linear_params()
+    X = np.zeros(16, np.float32)
+    if torch is not None and isinstance(fixed, torch.Tensor) and fixed.is_cuda:
+        ctx = ctx or context(fixed.device.index or 0)
+        sz = m * n * o
+        ctx.check(ctx._L.deeds_linear_register_dev(ctx.handle, _dev(fixed, torch.float32, sz, "fixed"),
+                                                   _dev(moving, torch.float32, sz, "moving"), m, n, o,
+                                                   C.byref(params), X.ctypes.data_as(C.c_void_p), _stream()))
+        return X
+    ctx = ctx or context(0)
+    f = np.ascontiguousarray(np.asarray(fixed, np.float32).ravel(order="F"))
+    mv = np.ascontiguousarray(np.asarray(moving, np.float32).ravel(order="F"))
+    ctx.check(ctx._L.deeds_linear_register(ctx.handle, f.ctypes.data_as(C.c_void_p), mv.ctypes.data_as(C.c_void_p),
+                                           m, n, o, C.byref(params), X.ctypes.data_as(C.c_void_p)))
+    return X
+
+
+def warpAffineLinear(im, X, m, n, o):
+    """warpAffine of src/affineLTS1.h:39-68 (affine only, zero outside) on a CUDA tensor."""
+    sz = m * n * o
+    X = _affine(X)
+    out = torch.empty(sz, dtype=torch.float32, device=im.device)
+    _lib.check(_lib.load().deeds_lin_warp_dev(_dev(im, torch.float32, sz, "im"), X.ctypes.data_as(C.c_void_p),
+                                              m, n, o, C.c_void_p(out.data_ptr()), _stream()))
+    return out
+
+
+def smoothCosts(cost, m1, n1, o1, len3):
+    """The in-place smoothing passes of estimateAffine2 on one cost volume (CUDA tensor)."""
+    _lib.check(_lib.load().deeds_lin_smooth_dev(_dev(cost, torch.float32, m1 * n1 * o1 * len3, "cost"), m1, n1, o1,
+                                                int(len3), _stream()))
+    return cost
+
+
+def estimateAffine2(Xprev, fixed, moving, cost, cost2, m, n, o, g, q, hw, rigid=False, ctx=None):
+    """estimateAffine2 on CUDA tensors (+1024-shifted images; the cost volumes are
+    smoothed in place): (X, points used)."""
+    ctx = ctx or context(fixed.device.index or 0)
+    sz = m * n * o
+    len3 = (2 * hw + 1) ** 3
+    sz1 = (m // g) * (n // g) * (o // g)
+    Xp = _affine(Xprev)
+    X = np.zeros(16, np.float32)
+    used = C.c_int(0)
+    ctx.check(ctx._L.deeds_estimate_affine_dev(
+        ctx.handle, _dev(fixed, torch.float32, sz, "fixed"), _dev(moving, torch.float32, sz, "moving"),
+        _dev(cost, torch.float32, sz1 * len3, "cost"), _dev(cost2, torch.float32, sz1 * len3, "cost2"), m, n, o,
+        int(g), int(hw), int(q), int(bool(rigid)), Xp.ctypes.data_as(C.c_void_p), X.ctypes.data_as(C.c_void_p),
+        C.byref(used), _stream()))
+    return X, used.value
+
+
+def affineRobust(pts1, pts2, length, rigid=False):
+    """affineRobust (src/QRsolve.h:258-296) on host point sets (column layout)."""
+    p1 = np.ascontiguousarray(pts1, np.float32)
+    p2 = np.ascontiguousarray(pts2, np.float32)
+    RT = np.zeros(16, np.float32)
+    _lib.check(_lib.load().deeds_affine_robust(p1.ctypes.data_as(C.c_void_p), p2.ctypes.data_as(C.c_void_p),
+                                               int(length), int(bool(rigid)), RT.ctypes.data_as(C.c_void_p)), None)
+    return RT
+
+
+def affine_warp_segmentation(seg, dims, X, ctx=None):
+    """The -S output of linearBCV: int16 labels warped by X alone (host arrays)."""
+    m, n, o = dims
+    ctx = ctx or context(0)
+    sg = np.ascontiguousarray(np.asarray(seg, np.int16).ravel(order="F"))
+    out = np.zeros_like(sg)
+    Xa = _affine(X)
+    ctx.check(ctx._L.deeds_affine_warp_segmentation(ctx.handle, sg.ctypes.data_as(C.c_void_p), m, n, o,
+                                                    Xa.ctypes.data_as(C.c_void_p), out.ctypes.data_as(C.c_void_p)))
+    return out

@@ -1,4 +1,4 @@
-"""Build libdeeds_gpu.so and the deedsBCV / applyBCV command-line drivers in-tree.
+"""Build libdeeds_gpu.so and the deedsBCV / applyBCV / linearBCV command-line drivers in-tree.
 
     python -m deedsbcv_gb300.build          # or deedsbcv_gb300.build.build()
 
@@ -30,14 +30,15 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompil
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread", "-Wall", "-Wno-unused-function",
              f"-I{CUDA_HOME}/include"]
 
-CU_SOURCES = ["mind.cu", "datacost.cu", "mst.cu", "bp.cu", "transform.cu", "noalloc.cu", "soft.cu", "soft_warp.cu"]
+CU_SOURCES = ["mind.cu", "datacost.cu", "mst.cu", "bp.cu", "transform.cu", "noalloc.cu", "soft.cu", "soft_warp.cu",
+              "linear.cu"]
 # soft.cu has no bit-exactness contract (its reference is a float64 definition),
 # so it may contract multiply-adds and flush denormals (its operands never are:
 # every square root and reciprocal square root argument is >= eps^2).
 FMAD_SOURCES = {"soft.cu", "soft_warp.cu"}
-CPP_SOURCES = ["pipeline.cpp", "tree_host.cpp"]
+CPP_SOURCES = ["pipeline.cpp", "tree_host.cpp", "linear_host.cpp"]
 CLI_SOURCES = {"deedsBCV": ["deedsBCV.cpp", "cli_common.cpp"], "applyBCV": ["applyBCV.cpp", "cli_common.cpp"],
-               "applyBCVfloat": ["applyBCV.cpp", "cli_common.cpp"]}
+               "applyBCVfloat": ["applyBCV.cpp", "cli_common.cpp"], "linearBCV": ["linearBCV.cpp", "cli_common.cpp"]}
 
 
 def _run(cmd, log):
@@ -91,7 +92,7 @@ def build(verbose=False, force=False, cli=True):
 
 
 def build_cli(force=False):
-    """The deedsBCV / applyBCV / applyBCVfloat executables (need zlib)."""
+    """The deedsBCV / applyBCV / applyBCVfloat / linearBCV executables (need zlib)."""
     lib_deps = [LIB]
     for exe, srcs in CLI_SOURCES.items():
         target = os.path.join(OUT, exe)

@@ -110,6 +110,12 @@ cudaError_t launch_soft_tree_forward(const SoftTreeDev& d, int* sweep_mem, const
                                      float* Mmin, float* logp, float* disp, cudaStream_t st);
 cudaError_t launch_soft_tree_backward(const SoftTreeDev& d, int* sweep_mem, const float* B, const float* M,
                                       const float* logp, const float* gdisp, float* R, float* Bbar, cudaStream_t st);
+// linearBCV (linear.cu)
+cudaError_t launch_lin_warp(const float* d_in, const float* X, int m, int n, int o, float* d_out, cudaStream_t s);
+cudaError_t launch_lin_smooth(float* d_c0, float* d_c1, int m1, int n1, int o1, int len3, cudaStream_t s);
+cudaError_t launch_lin_node_stats(const float* d_c0, const float* d_c1, const float* d_fixed, const float* d_moving,
+                                  int m, int n, int o, int g, int len3, float* d_minval, int* d_minind,
+                                  cudaStream_t s);
 cudaError_t launch_popc_probe(int blocks, int threads, int iters, unsigned long long* d_sink, cudaStream_t s);
 cudaError_t launch_jacobian(const float* u, const float* v, const float* w, int m, int n, int o, int g, double* d_acc,
                             cudaStream_t s);

@@ -30,6 +30,7 @@
 #include "../../include/deeds_gpu.h"
 #include "kernels.h"
 #include "tree_host.h"
+#include "linear_host.h"
 
 using namespace deeds;
 
@@ -1384,6 +1385,242 @@ deeds_status deeds_soft_warp_backward_dev(deeds_ctx* ctx, const float* d_moving,
     CK(launch_soft_warp_adj(d_moving, d_grid, mA, nA, oA, d_gout, d_gmoving, gfull, m, n, o, s));
     if (d_ggrid) CK(launch_soft_upsample_adj(gfull, m, n, o, d_ggrid, mA, nA, oA, s));
     return DEEDS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// linearBCV (src/linearBCV.cpp:163-262)
+
+void deeds_linear_default_params(deeds_linear_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    const int G[4] = {7, 6, 5, 4}, L[4] = {5, 4, 3, 2}, Q[4] = {4, 3, 2, 1};  // src/linearBCV.cpp:86-89
+    p->levels = 4;
+    for (int l = 0; l < 4; l++) { p->grid[l] = G[l]; p->radius[l] = L[l]; p->quant[l] = Q[l]; }
+    p->rigid = 0;
+    p->intensity_shift = 1024.0f;
+    p->verbose = 0;
+}
+
+}  // extern "C"
+
+namespace {
+
+deeds_status check_linear_params(deeds_ctx* ctx, const deeds_linear_params* p, int m, int n, int o) {
+    if (!p) return fail(ctx, DEEDS_ERR_INVALID, "params is NULL");
+    deeds_params d;
+    deeds_default_params(&d);
+    d.levels = p->levels;
+    if (p->levels < 1 || p->levels > DEEDS_MAX_LEVELS)
+        return fail(ctx, DEEDS_ERR_INVALID, "levels=%d outside 1..%d", p->levels, DEEDS_MAX_LEVELS);
+    for (int l = 0; l < p->levels; l++) {
+        d.grid[l] = p->grid[l]; d.radius[l] = p->radius[l]; d.quant[l] = p->quant[l];
+        // estimateAffine2 needs interior nodes (two from each border) to fit anything
+        const int g = p->grid[l];
+        if (g >= 1 && (m / g < 5 || n / g < 5 || o / g < 5))
+            return fail(ctx, DEEDS_ERR_INVALID, "level %d: grid %d leaves fewer than 5 control points on an axis", l, g);
+    }
+    return check_params(ctx, &d, m, n, o);
+}
+
+// One linearBCV level after the cost volumes: smoothing, node statistics (GPU),
+// then the fit on the host.  Returns the number of points used.
+deeds_status linear_estimate(deeds_ctx* ctx, const float* fix, const float* mov, float* cost0, float* cost1, int m,
+                             int n, int o, int g, int hw, int q, bool rigid, const float Xprev[16], float X[16],
+                             int* used, int* allcount, float* quantile, cudaStream_t s, cudaStream_t s2) {
+    const int m1 = m / g, n1 = n / g, o1 = o / g, sz1 = m1 * n1 * o1;
+    const int len = 2 * hw + 1, len3 = len * len * len;
+    deeds_status st = DEEDS_OK;
+    float* d_minval = dbuf<float>(ctx, "lin_minval", 2 * (size_t)sz1, &st);
+    int* d_minind = dbuf<int>(ctx, "lin_minind", 2 * (size_t)sz1, &st);
+    float* h_minval = hbuf<float>(ctx, "lin_h_minval", 2 * (size_t)sz1, &st);
+    int* h_minind = hbuf<int>(ctx, "lin_h_minind", 2 * (size_t)sz1, &st);
+    if (st) return st;
+    if (s2 && s2 != s) {
+        // each volume smoothed on the stream that built it, then joined
+        CK(launch_lin_smooth(cost1, nullptr, m1, n1, o1, len3, s2));
+        CK(cudaEventRecord(ctx->ev_d, s2));
+        CK(launch_lin_smooth(cost0, nullptr, m1, n1, o1, len3, s));
+        CK(cudaStreamWaitEvent(s, ctx->ev_d, 0));
+    } else {
+        CK(launch_lin_smooth(cost0, cost1, m1, n1, o1, len3, s));
+    }
+    CK(launch_lin_node_stats(cost0, cost1, fix, mov, m, n, o, g, len3, d_minval, d_minind, s));
+    CK(cudaMemcpyAsync(h_minval, d_minval, 2 * (size_t)sz1 * sizeof(float), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(h_minind, d_minind, 2 * (size_t)sz1 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    int ac = 0;
+    float qf = 0.0f;
+    const int u = lin_estimate_from_stats(X, Xprev, h_minval, h_minind, m1, n1, o1, g, (float)q, hw, rigid, &ac, &qf);
+    if (u < kMinFitPoints)
+        return fail(ctx, DEEDS_ERR_INVALID,
+                    "grid %d: %d of %d control-point votes fall below the selection quantile (at least %d needed)", g,
+                    u, ac, kMinFitPoints);
+    if (used) *used = u;
+    if (allcount) *allcount = ac;
+    if (quantile) *quantile = qf;
+    return DEEDS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+deeds_status deeds_lin_warp_dev(const float* d_in, const float X[16], int m, int n, int o, float* d_out, void* stream) {
+    deeds_ctx* ctx = nullptr;
+    if (!d_in || !X || !d_out || m < 1 || n < 1 || o < 1 || n > 65535 || o > 65535)
+        return fail(nullptr, DEEDS_ERR_INVALID, "deeds_lin_warp_dev: bad arguments");
+    CK(launch_lin_warp(d_in, X, m, n, o, d_out, (cudaStream_t)stream));
+    return DEEDS_OK;
+}
+
+deeds_status deeds_lin_smooth_dev(float* d_cost, int m1, int n1, int o1, int len3, void* stream) {
+    deeds_ctx* ctx = nullptr;
+    if (!d_cost || m1 < 1 || n1 < 1 || o1 < 1 || len3 < 1)
+        return fail(nullptr, DEEDS_ERR_INVALID, "deeds_lin_smooth_dev: bad arguments");
+    CK(launch_lin_smooth(d_cost, nullptr, m1, n1, o1, len3, (cudaStream_t)stream));
+    return DEEDS_OK;
+}
+
+deeds_status deeds_estimate_affine_dev(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, float* d_cost,
+                                       float* d_cost2, int m, int n, int o, int g, int hw, int q, int rigid,
+                                       const float Xprev[16], float X[16], int* points_used, void* stream) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!d_fixed || !d_moving || !d_cost || !d_cost2 || !Xprev || !X) return fail(ctx, DEEDS_ERR_INVALID, "null pointer");
+    if (m < 1 || n < 1 || o < 1 || g < 1 || hw < 0 || q < 1 || m / g < 1 || n / g < 1 || o / g < 1)
+        return fail(ctx, DEEDS_ERR_INVALID, "bad dims or level parameters");
+    CK(cudaSetDevice(ctx->device));
+    return linear_estimate(ctx, d_fixed, d_moving, d_cost, d_cost2, m, n, o, g, hw, q, rigid != 0, Xprev, X,
+                           points_used, nullptr, nullptr, (cudaStream_t)stream, nullptr);
+}
+
+deeds_status deeds_affine_robust(const float* pts1, const float* pts2, int len, int rigid, float RT[16]) {
+    deeds_ctx* ctx = nullptr;
+    if (!pts1 || !pts2 || !RT || len < kMinFitPoints)
+        return fail(ctx, DEEDS_ERR_INVALID, "deeds_affine_robust: bad arguments (len %d, at least %d)", len, kMinFitPoints);
+    lin_affine_robust(RT, pts1, pts2, len, rigid != 0);
+    return DEEDS_OK;
+}
+
+deeds_status deeds_linear_register_dev(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, int m, int n,
+                                       int o, const deeds_linear_params* P, float X_out[16], void* stream) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!d_fixed || !d_moving || !X_out) return fail(ctx, DEEDS_ERR_INVALID, "null pointer");
+    deeds_status st = check_linear_params(ctx, P, m, n, o);
+    if (st) return st;
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = (cudaStream_t)stream, sb = ctx->stream_b;
+    const size_t sz = (size_t)m * n * o;
+    size_t max_cost = 0, max_pad = 0;
+    for (int l = 0; l < P->levels; l++) {
+        const int g = P->grid[l], len = 2 * P->radius[l] + 1;
+        max_cost = std::max(max_cost, (size_t)(m / g) * (n / g) * (o / g) * len * len * len);
+        max_pad = std::max(max_pad, padded_codes_count(m, n, o, P->quant[l] * P->radius[l]));
+    }
+    float* fix = dbuf<float>(ctx, "lin_fix", sz, &st);
+    float* mov = dbuf<float>(ctx, "lin_mov", sz, &st);
+    float* warped[2] = {dbuf<float>(ctx, "lin_w1", sz, &st), dbuf<float>(ctx, "lin_w2", sz, &st)};
+    uint64_t* c_fix = dbuf<uint64_t>(ctx, "lin_c_fix", sz, &st);
+    uint64_t* c_mov = dbuf<uint64_t>(ctx, "lin_c_mov", sz, &st);
+    uint64_t* c_warp[2] = {dbuf<uint64_t>(ctx, "lin_c_w1", sz, &st), dbuf<uint64_t>(ctx, "lin_c_w2", sz, &st)};
+    float* scr[2] = {dbuf<float>(ctx, "lin_mind1", 6 * sz, &st), dbuf<float>(ctx, "lin_mind2", 6 * sz, &st)};
+    float* cost[2] = {dbuf<float>(ctx, "lin_cost1", max_cost, &st), dbuf<float>(ctx, "lin_cost2", max_cost, &st)};
+    uint64_t* mpad[2] = {dbuf<uint64_t>(ctx, "lin_mpad1", max_pad, &st), dbuf<uint64_t>(ctx, "lin_mpad2", max_pad, &st)};
+    int* d_err = dbuf<int>(ctx, "lin_err", 2, &st);
+    if (st) return st;
+    float thr[5];
+    mind_thresholds(thr);
+    CK(cudaMemsetAsync(d_err, 0, 2 * sizeof(int), s));
+    CK(launch_shift(d_fixed, fix, (int64_t)sz, P->intensity_shift, s));
+    CK(launch_shift(d_moving, mov, (int64_t)sz, P->intensity_shift, s));
+    float Xprev[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    const float ident[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    float X[16];
+    std::memcpy(X, Xprev, sizeof(X));
+    int prev_step = -1;
+    for (int l = 0; l < P->levels; l++) {
+        const int g = P->grid[l], hw = P->radius[l], q = P->quant[l];
+        const int qs = mind_step(q);
+        float Xinv[16];
+        lin_qrsolve(Xinv, Xprev, ident, 4, 4);  // src/linearBCV.cpp:186-187
+        if (l == 0 || qs != prev_step) {
+            StageScope sc(ctx, DEEDS_STAGE_MIND, s);
+            CK(launch_mind_ssc(mov, m, n, o, qs, thr, scr[0], c_mov, s));
+            CK(launch_mind_ssc(fix, m, n, o, qs, thr, scr[0], c_fix, s));
+        }
+        prev_step = qs;
+        CK(cudaEventRecord(ctx->ev_d, s));
+        CK(cudaStreamWaitEvent(sb, ctx->ev_d, 0));
+        // direction 1: fixed codes against the moving image warped by X; direction 2:
+        // moving codes against the fixed image warped by the inverse
+        for (int d = 0; d < 2; d++) {
+            cudaStream_t sd = d == 0 ? s : sb;
+            {
+                StageScope sc(ctx, DEEDS_STAGE_TRANSFORM, sd);
+                CK(launch_lin_warp(d == 0 ? mov : fix, d == 0 ? Xprev : Xinv, m, n, o, warped[d], sd));
+            }
+            {
+                StageScope sc(ctx, DEEDS_STAGE_MIND, sd);
+                CK(launch_mind_ssc(warped[d], m, n, o, qs, thr, scr[d], c_warp[d], sd));
+            }
+            {
+                StageScope sc(ctx, DEEDS_STAGE_DATACOST, sd);
+                CK(data_cost_auto(ctx, d == 0 ? c_fix : c_mov, c_warp[d], mpad[d], m, n, o, g, hw, q, 1.0f, cost[d],
+                                  d_err + d, sd));
+            }
+        }
+        int used = 0, allcount = 0;
+        float quant = 0.0f;
+        st = linear_estimate(ctx, fix, mov, cost[0], cost[1], m, n, o, g, hw, q, P->rigid != 0, Xprev, X, &used,
+                             &allcount, &quant, s, sb);
+        if (st) return st;
+        if (P->verbose) printf("# points used: %d/%d, quantile: %f\n", used, allcount, quant);
+        std::memcpy(Xprev, X, sizeof(X));
+    }
+    int herr[2] = {0, 0};
+    CK(cudaMemcpyAsync(herr, d_err, sizeof(herr), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (ctx->prof) collect_marks(ctx);
+    if (herr[0] == 3 || herr[1] == 3) return fail(ctx, DEEDS_ERR_TIMEOUT, "cost volume: a bounded wait for a TMA copy expired");
+    if (herr[0] || herr[1]) return fail(ctx, DEEDS_ERR_INTERNAL, "cost volume kernel reported error %d", herr[0] | herr[1]);
+    std::memcpy(X_out, X, sizeof(X));
+    return DEEDS_OK;
+}
+
+deeds_status deeds_affine_warp_segmentation(deeds_ctx* ctx, const int16_t* seg, int m, int n, int o, const float X[16],
+                                           int16_t* seg_out) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!seg || !seg_out || !X || m < 1 || n < 1 || o < 1 || n > 65535 || o > 65535)
+        return fail(ctx, DEEDS_ERR_INVALID, "deeds_affine_warp_segmentation: bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    const size_t sz = (size_t)m * n * o;
+    deeds_status st = DEEDS_OK;
+    short* d_in = dbuf<short>(ctx, "seg_in", sz, &st);
+    short* d_out = dbuf<short>(ctx, "seg_out", sz, &st);
+    if (st) return st;
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(d_in, seg, sz * sizeof(short), cudaMemcpyHostToDevice, s));
+    FieldRef zero{0, nullptr, nullptr, nullptr, 0, 0, 0};
+    CK(launch_warp_seg(d_in, X, zero, m, n, o, d_out, s));
+    CK(cudaMemcpyAsync(seg_out, d_out, sz * sizeof(short), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return DEEDS_OK;
+}
+
+deeds_status deeds_linear_register(deeds_ctx* ctx, const float* fixed, const float* moving, int m, int n, int o,
+                                   const deeds_linear_params* params, float X_out[16]) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!fixed || !moving || !X_out) return fail(ctx, DEEDS_ERR_INVALID, "null pointer");
+    deeds_status st = check_linear_params(ctx, params, m, n, o);
+    if (st) return st;
+    CK(cudaSetDevice(ctx->device));
+    const size_t sz = (size_t)m * n * o;
+    float* d_f = dbuf<float>(ctx, "in_fixed", sz, &st);
+    float* d_m = dbuf<float>(ctx, "in_moving", sz, &st);
+    if (st) return st;
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(d_f, fixed, sz * sizeof(float), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_m, moving, sz * sizeof(float), cudaMemcpyHostToDevice, s));
+    return deeds_linear_register_dev(ctx, d_f, d_m, m, n, o, params, X_out, s);
 }
 
 }  // extern "C"

@@ -313,6 +313,55 @@ deeds_status deeds_soft_warp_backward_dev(deeds_ctx* ctx, const float* d_moving,
                                           const float* d_grid, int mA, int nA, int oA, const float* d_grad_out,
                                           float* d_grad_moving, float* d_grad_grid, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * linearBCV: affine / rigid pre-registration (src/linearBCV.cpp:163-262).  Per
+ * level both images are warped by the current matrix (the moving image forwards,
+ * the fixed image by its QR inverse), MIND-SSC codes and Hamming cost volumes are
+ * built in both directions (alpha 1), the volumes are smoothed along y, x and z,
+ * each control point votes with its best label, and a least-trimmed-squares fit
+ * of the best half of the votes updates the matrix.  The matrix uses the deeds
+ * layout (X[0..3] gives y, X[4..7] x, X[8..11] z) and maps fixed voxels to moving
+ * voxels; the linearBCV CLI writes it as stem_matrix.txt for deedsBCV -A. */
+typedef struct deeds_linear_params {
+    int levels;                      /* -l (default 4) */
+    int grid[DEEDS_MAX_LEVELS];      /* -G (default 7x6x5x4) */
+    int radius[DEEDS_MAX_LEVELS];    /* -L (default 5x4x3x2) */
+    int quant[DEEDS_MAX_LEVELS];     /* -Q (default 4x3x2x1) */
+    int rigid;                       /* -R: 6-parameter rigid fit instead of affine */
+    float intensity_shift;           /* added to both images (1024, src/linearBCV.cpp:146-153) */
+    int verbose;                     /* print "# points used" per level like the reference */
+} deeds_linear_params;
+
+void deeds_linear_default_params(deeds_linear_params* p);
+
+/* Whole linearBCV registration on host buffers (copied to the device inside);
+ * X_out: 16 floats.  Replaces main of src/linearBCV.cpp:163-262. */
+deeds_status deeds_linear_register(deeds_ctx* ctx, const float* fixed, const float* moving, int m, int n, int o,
+                                   const deeds_linear_params* params, float X_out[16]);
+/* The same on device buffers and the caller's stream (synchronises it once per level). */
+deeds_status deeds_linear_register_dev(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, int m, int n,
+                                       int o, const deeds_linear_params* params, float X_out[16], void* stream);
+
+/* The -S output of linearBCV (src/linearBCV.cpp:301-317): a label map warped by X
+ * alone (nearest neighbour, warpAffineS with a zero field); host buffers. */
+deeds_status deeds_affine_warp_segmentation(deeds_ctx* ctx, const int16_t* seg, int m, int n, int o, const float X[16],
+                                           int16_t* seg_out);
+
+/* warpAffine of src/affineLTS1.h:39-68: affine map only, 0 outside the volume. */
+deeds_status deeds_lin_warp_dev(const float* d_in, const float X[16], int m, int n, int o, float* d_out, void* stream);
+/* The three in-place smoothing passes of estimateAffine2 (src/affineLTS1.h:124-158)
+ * on one cost volume (m1 x n1 x o1 nodes x len3 labels). */
+deeds_status deeds_lin_smooth_dev(float* d_cost, int m1, int n1, int o1, int len3, void* stream);
+/* estimateAffine2 (src/affineLTS1.h:91-236): smooths both cost volumes in place
+ * and returns X = fit * Xprev; d_fixed/d_moving are the shifted (+1024) images.
+ * *points_used (nullable) receives the number of points fitted. */
+deeds_status deeds_estimate_affine_dev(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, float* d_cost,
+                                       float* d_cost2, int m, int n, int o, int g, int hw, int q, int rigid,
+                                       const float Xprev[16], float X[16], int* points_used, void* stream);
+/* affineRobust (src/QRsolve.h:258-296) on host point sets in column layout
+ * (y | x | z | 1, len points each). */
+deeds_status deeds_affine_robust(const float* pts1, const float* pts2, int len, int rigid, float RT[16]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -899,6 +899,7 @@ extern "C" {
 // affineRobust (src/QRsolve.h:258-296): a fit to all points, then 15 rounds of
 // refitting to the half with the smallest squared residuals.
 void orc_affine_robust(float* RT, const float* p1, const float* p2, int len, int rigid) {
+    if (len < 8) return;  // the reference indexes an empty trimmed half here (undefined); not fitted
     lin_fit(RT, p1, p2, len, rigid != 0);
     const int lenh = len / 2;
     std::vector<float> err(len), err2(len), p1b(4 * (size_t)lenh, 1.0f), p2b(4 * (size_t)lenh, 1.0f);
@@ -1037,6 +1038,7 @@ int orc_estimate_affine(float* X, const float* Xprev, const float* fixed, const 
             cur++;
         }
     }
+    if (valsz < 8) return valsz;  // too few points to fit (X not written)
     float X1[16];
     orc_affine_robust(X1, p1.data(), p2.data(), valsz, rigid);
     for (int i = 0; i < 4; i++)  // matmult (src/affineLTS1.h:1-12)

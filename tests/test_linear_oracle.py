@@ -74,3 +74,14 @@ def test_linear_register_matches_reference_binary(golden, rigid):
     Xm = np.array([[X[i * 4 + j] for j in range(4)] for i in range(3)] + [[0, 0, 0, 1]], np.float64)
     centre = np.array([m / 2, n / 2, o / 2, 1.0])
     assert np.abs((A @ Xm) @ centre - centre)[:3].max() < 1.5
+
+
+@pytest.mark.parametrize("rigid", [0, 1])
+def test_library_host_fit_bit_exact(golden, rigid):
+    """The library's own least-trimmed-squares fit (host code, no device calls)
+    against the reference's affineRobust."""
+    from deedsbcv_gb300 import api
+    g = golden("linear")
+    npts = g["robust_p1"].size // 4
+    RT = api.affineRobust(g["robust_p1"], g["robust_p2"], npts, rigid)
+    assert np.array_equal(RT.view(np.uint32), g[f"robust_{rigid}"].view(np.uint32))
