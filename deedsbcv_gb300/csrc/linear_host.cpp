@@ -8,6 +8,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstddef>
+#include <cstdint>
+#include <cstring>
 
 namespace deeds {
 
@@ -115,6 +117,37 @@ void find_rigid(float* RT, Cols a, Cols b) {
     }
 }
 
+// The k-th smallest of non-negative floats (squared residuals): their bit
+// patterns order like the values, so two 16-bit radix passes find it exactly, in
+// place of nth_element (whose answer is the same value).
+float kth_smallest_nonneg(const std::vector<float>& v, int k, std::vector<uint32_t>& scratch) {
+    static thread_local std::vector<uint32_t> hist(65536);
+    std::fill(hist.begin(), hist.end(), 0u);
+    const size_t n = v.size();
+    const uint32_t* bits = reinterpret_cast<const uint32_t*>(v.data());
+    for (size_t i = 0; i < n; i++) hist[bits[i] >> 16]++;
+    uint32_t hi = 0, below = 0;
+    for (;; hi++) {
+        if (below + hist[hi] > (uint32_t)k) break;
+        below += hist[hi];
+    }
+    scratch.clear();
+    for (size_t i = 0; i < n; i++)
+        if ((bits[i] >> 16) == hi) scratch.push_back(bits[i] & 0xffffu);
+    std::fill(hist.begin(), hist.end(), 0u);
+    for (uint32_t lo : scratch) hist[lo]++;
+    const uint32_t want = (uint32_t)k - below;
+    uint32_t lo = 0, acc = 0;
+    for (;; lo++) {
+        if (acc + hist[lo] > want) break;
+        acc += hist[lo];
+    }
+    const uint32_t r = (hi << 16) | lo;
+    float out;
+    std::memcpy(&out, &r, sizeof(out));
+    return out;
+}
+
 void fit(float* RT, Cols a, Cols b, bool rigid) {
     if (rigid) find_rigid(RT, a, b);
     else lin_qrsolve(RT, a.p, b.p, a.len, 4);
@@ -122,6 +155,11 @@ void fit(float* RT, Cols a, Cols b, bool rigid) {
 
 }  // namespace
 
+// The Gram-Schmidt QR with every sum kept in its own sequential accumulator, in
+// index order, exactly as the reference evaluates it; what changes is only that
+// independent sums (and the vector updates feeding them) share one pass over
+// the points, so their dependency chains overlap instead of running one after
+// another.  Same bits, several times fewer passes.
 void lin_qrsolve(float* X, const float* A, const float* b, int len, int nrhs) {
     std::vector<float> Qv(4 * (size_t)len);
     float* q0 = Qv.data();
@@ -132,38 +170,101 @@ void lin_qrsolve(float* X, const float* A, const float* b, int len, int nrhs) {
     const float* a1 = A + len;
     const float* a2 = A + 2 * (size_t)len;
     const float* a3 = A + 3 * (size_t)len;
-    const float r11 = sq_norm_sqrt(a0, len);
-    for (int i = 0; i < len; i++) q0[i] = a0[i] / r11;
-    const float r12 = dotf(q0, a1, len), r13 = dotf(q0, a2, len), r14 = dotf(q0, a3, len);
+    auto norm_step = [](float acc, float v) { return (float)((double)acc + (double)v * (double)v); };
+    // column 1
+    float n0 = 0.0f;
+    for (int i = 0; i < len; i++) n0 = norm_step(n0, a0[i]);
+    const float r11 = std::sqrt(n0);
+    float r12 = 0.0f, r13 = 0.0f, r14 = 0.0f;
     for (int i = 0; i < len; i++) {
-        q1[i] = a1[i] - q0[i] * r12;
+        const float q = a0[i] / r11;
+        q0[i] = q;
+        r12 += q * a1[i];
+        r13 += q * a2[i];
+        r14 += q * a3[i];
+    }
+    // column 2 (q2, q3 hold the partially orthogonalised columns 3 and 4)
+    float n1 = 0.0f;
+    for (int i = 0; i < len; i++) {
+        const float v = a1[i] - q0[i] * r12;
+        q1[i] = v;
         q2[i] = a2[i] - q0[i] * r13;
         q3[i] = a3[i] - q0[i] * r14;
+        n1 = norm_step(n1, v);
     }
-    const float r22 = sq_norm_sqrt(q1, len);
-    for (int i = 0; i < len; i++) q1[i] = q1[i] / r22;
-    const float r23 = dotf(q1, a2, len), r24 = dotf(q1, a3, len);
+    const float r22 = std::sqrt(n1);
+    float r23 = 0.0f, r24 = 0.0f;
     for (int i = 0; i < len; i++) {
-        q2[i] = a2[i] - q0[i] * r13 - q1[i] * r23;
-        q3[i] = a3[i] - q0[i] * r14 - q1[i] * r24;
+        const float q = q1[i] / r22;
+        q1[i] = q;
+        r23 += q * a2[i];
+        r24 += q * a3[i];
     }
-    const float r33 = sq_norm_sqrt(q2, len);
-    for (int i = 0; i < len; i++) q2[i] = q2[i] / r33;
-    const float r34 = dotf(q2, a3, len);
-    for (int i = 0; i < len; i++) q3[i] = a3[i] - q0[i] * r14 - q1[i] * r24 - q2[i] * r34;
-    const float r44 = sq_norm_sqrt(q3, len);
+    // column 3
+    float n2 = 0.0f;
+    for (int i = 0; i < len; i++) {
+        const float v = a2[i] - q0[i] * r13 - q1[i] * r23;
+        q2[i] = v;
+        q3[i] = a3[i] - q0[i] * r14 - q1[i] * r24;
+        n2 = norm_step(n2, v);
+    }
+    const float r33 = std::sqrt(n2);
+    float r34 = 0.0f;
+    for (int i = 0; i < len; i++) {
+        const float q = q2[i] / r33;
+        q2[i] = q;
+        r34 += q * a3[i];
+    }
+    // column 4
+    float n3 = 0.0f;
+    for (int i = 0; i < len; i++) {
+        const float v = a3[i] - q0[i] * r14 - q1[i] * r24 - q2[i] * r34;
+        q3[i] = v;
+        n3 = norm_step(n3, v);
+    }
+    const float r44 = std::sqrt(n3);
     for (int i = 0; i < len; i++) q3[i] = q3[i] / r44;
-    for (int j = 0; j < nrhs; j++) {
-        const float* bj = b + (size_t)j * len;
-        const float d1 = dotf(q0, bj, len), d2 = dotf(q1, bj, len), d3 = dotf(q2, bj, len), d4 = dotf(q3, bj, len);
-        const float x4 = d4 / r44;
-        const float x3 = (d3 - r34 * x4) / r33;
-        const float x2 = (d2 - r23 * x3 - r24 * x4) / r22;
-        const float x1 = (d1 - r12 * x2 - r13 * x3 - r14 * x4) / r11;
-        X[4 * j] = x1;
-        X[4 * j + 1] = x2;
-        X[4 * j + 2] = x3;
-        X[4 * j + 3] = x4;
+    // right-hand sides: 4 dot products each, up to four right-hand sides per pass
+    for (int j0 = 0; j0 < nrhs; j0 += 4) {
+        const int nj = std::min(4, nrhs - j0);
+        float d[4][4] = {{0.0f}};
+        if (nj == 4) {
+            const float* b0 = b + (size_t)j0 * len;
+            const float* b1 = b0 + len;
+            const float* b2 = b1 + len;
+            const float* b3 = b2 + len;
+            for (int i = 0; i < len; i++) {
+                const float qa = q0[i], qb = q1[i], qc = q2[i], qd = q3[i];
+                const float bb[4] = {b0[i], b1[i], b2[i], b3[i]};
+                for (int j = 0; j < 4; j++) {
+                    d[j][0] += qa * bb[j];
+                    d[j][1] += qb * bb[j];
+                    d[j][2] += qc * bb[j];
+                    d[j][3] += qd * bb[j];
+                }
+            }
+        } else {
+            for (int j = 0; j < nj; j++) {
+                const float* bj = b + (size_t)(j0 + j) * len;
+                for (int i = 0; i < len; i++) {
+                    d[j][0] += q0[i] * bj[i];
+                    d[j][1] += q1[i] * bj[i];
+                    d[j][2] += q2[i] * bj[i];
+                    d[j][3] += q3[i] * bj[i];
+                }
+            }
+        }
+        for (int j = 0; j < nj; j++) {
+            const float x4 = d[j][3] / r44;
+            const float x3 = (d[j][2] - r34 * x4) / r33;
+            const float x2 = (d[j][1] - r23 * x3 - r24 * x4) / r22;
+            const float x1 = (d[j][0] - r12 * x2 - r13 * x3 - r14 * x4) / r11;
+            float* Xj = X + 4 * (size_t)(j0 + j);
+            Xj[0] = x1;
+            Xj[1] = x2;
+            Xj[2] = x3;
+            Xj[3] = x4;
+        }
     }
 }
 
@@ -172,7 +273,9 @@ void lin_affine_robust(float* RT, const float* p1, const float* p2, int len, boo
     const Cols A{p1, len}, B{p2, len};
     fit(RT, A, B, rigid);
     const int half = len / 2;
-    std::vector<float> err(len), err_sorted(len);
+    std::vector<float> err(len);
+    std::vector<uint32_t> scratch;
+    scratch.reserve(len);
     std::vector<float> ha(4 * (size_t)half, 1.0f), hb(4 * (size_t)half, 1.0f);  // the kept half; column 3 stays 1
     for (int iter = 0; iter < 15; iter++) {
         for (int l = 0; l < len; l++) {
@@ -190,9 +293,7 @@ void lin_affine_robust(float* RT, const float* p1, const float* p2, int len, boo
             const double ey = (double)(y - B.col(0)[l]), ex = (double)(x - B.col(1)[l]), ez = (double)(z - B.col(2)[l]);
             err[l] = (float)(ey * ey + ex * ex + ez * ez);
         }
-        err_sorted = err;
-        std::nth_element(err_sorted.begin(), err_sorted.begin() + len / 2, err_sorted.end());
-        const float median = err_sorted[len / 2];
+        const float median = kth_smallest_nonneg(err, len / 2, scratch);
         // points at or below the median, in order; any beyond the half overwrite the last slot
         int count = 0;
         for (int i = 0; i < len; i++) {
@@ -230,10 +331,10 @@ int lin_estimate_from_stats(float* X, const float* Xprev, const float* minval, c
     const int qi = (int)((float)sz1 * std::min(std::max(qf, 0.01f), 0.99f));
     float med[2];
     std::vector<float> tmp(sz1);
-    for (int v = 0; v < 2; v++) {
+    std::vector<uint32_t> scratch;
+    for (int v = 0; v < 2; v++) {  // cost volumes are non-negative, the exclusion value is 1e20
         std::copy(mv[v], mv[v] + sz1, tmp.begin());
-        std::nth_element(tmp.begin(), tmp.begin() + qi, tmp.end());
-        med[v] = tmp[qi];
+        med[v] = kth_smallest_nonneg(tmp, qi, scratch);
     }
     int valsz = 0;
     for (int i = 0; i < sz1; i++) valsz += (mv[0][i] < med[0]) + (mv[1][i] < med[1]);

@@ -85,3 +85,20 @@ def test_library_host_fit_bit_exact(golden, rigid):
     npts = g["robust_p1"].size // 4
     RT = api.affineRobust(g["robust_p1"], g["robust_p2"], npts, rigid)
     assert np.array_equal(RT.view(np.uint32), g[f"robust_{rigid}"].view(np.uint32))
+
+
+@pytest.mark.parametrize("npts,rigid", [(40001, 0), (40001, 1), (9, 0), (9, 1)])
+def test_library_host_fit_matches_oracle_large(npts, rigid):
+    """The library's fit (fused Gram-Schmidt passes, radix median) against the
+    oracle's plain restatement on seeded point sets with 20% outliers."""
+    from deedsbcv_gb300 import api
+    rng = np.random.default_rng(npts + rigid)
+    p1 = np.ones((4, npts), np.float32)
+    p1[:3] = rng.uniform(0, 200, (3, npts))
+    p2 = p1.copy()
+    p2[:3] += rng.normal(0, 1, (3, npts)).astype(np.float32)
+    out = rng.choice(npts, npts // 5, replace=False)
+    p2[:3, out] += rng.uniform(-20, 20, (3, out.size)).astype(np.float32)
+    RT = api.affineRobust(p1.ravel(), p2.ravel(), npts, rigid)
+    ref = orc.affine_robust(p1.ravel(), p2.ravel(), npts, rigid)
+    assert np.array_equal(RT.view(np.uint32), ref.view(np.uint32))
