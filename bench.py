@@ -353,6 +353,17 @@ def measure_linear(api, ctx, shape, steps=5, warmup=3, cpu=True):
     torch.cuda.synchronize()
     dev_s = e0.elapsed_time(e1) / 1000.0 / steps
     launches = (api.kernel_launches() - launches0) // steps
+    # one more registration with per-stage CUDA events: the GPU stages; the rest of
+    # the pair time is cost smoothing, node statistics and the host fit
+    ctx.reset_stage_times()
+    ctx.set_profiling(True)
+    t0 = time.perf_counter()
+    api.linear_register(df, dm, shape, params, ctx)
+    prof_s = time.perf_counter() - t0
+    ctx.set_profiling(False)
+    st = ctx.stage_times()
+    ctx.reset_stage_times()
+    gpu_stages = {k: round(v[0], 3) for k, v in st.items() if v[1] > 0}
     A = pair["affine"].reshape(4, 4).astype(np.float64)
     Xm = np.array([[X[i * 4 + j] for j in range(4)] for i in range(3)] + [[0, 0, 0, 1]], np.float64)
     corners = np.array([[a, b, c, 1.0] for a in (0, shape[0] - 1) for b in (0, shape[1] - 1) for c in (0, shape[2] - 1)])
@@ -362,6 +373,8 @@ def measure_linear(api, ctx, shape, steps=5, warmup=3, cpu=True):
            "e2e": {"value": 1.0 / e2e_s, "unit": "pairs/s", "h2d_bytes_per_step": 2 * f.nbytes,
                    "d2h_bytes_per_step": 64},
            "gpu_launches_per_pair": int(launches),
+           "stages_ms": {"gpu (both direction streams summed)": gpu_stages,
+                         "profiled pair wall ms": round(prof_s * 1000.0, 3)},
            "device_and_host_calls_agree": bool(np.array_equal(X.view(np.uint32), Xd.view(np.uint32))),
            "max_corner_error_vs_truth_voxels": float(np.abs((A @ Xm) @ corners.T - corners.T)[:3].max())}
     if cpu:
