@@ -811,6 +811,216 @@ __global__ void __launch_bounds__(ColGeom<G_, LEN_, Q_>::ADJ_BLOCK, 4)
 }
 
 // ---------------------------------------------------------------------------
+// Box form for the coarser levels (grid > 4: nine sampled columns per node, and
+// label quantisation > 1, whose boxes NA = g + (len-1) q no longer fit twelve
+// channels in shared memory).  A node's clamped box of the moving descriptor is
+// staged one channel group at a time in a padded layout [c][bz][bx][a] (row pitch
+// PY, plane pitch PZ, chosen on the host so that the rows a warp reads start in
+// different banks); a thread owns one item (label pair (lx, lz), sampled
+// column) for the whole launch and keeps its len sums (forward) or its g
+// fixed-sample gradients (adjoint) in registers across the channel groups.
+// The moving-side gradient is the gather kernel k_soft_cost_adj_moving.
+
+struct BoxPitch {
+    int PY, PZ, CG;  // row pitch, plane pitch (floats), channels per stage
+};
+
+template <int G_, int LEN_, int Q_>
+struct BoxGeom {
+    static constexpr int S = G_ > 4 ? 2 : 1, NX = (G_ + S - 1) / S, NCOL = NX * NX, NSAMP = NCOL * G_;
+    static constexpr int NA = G_ + (LEN_ - 1) * Q_, LEN2 = LEN_ * LEN_, LEN3 = LEN2 * LEN_;
+    static constexpr int ITEMS = LEN2 * NCOL;
+    static constexpr int IPT = (ITEMS + 511) / 512;
+    static constexpr int BLOCK = ((ITEMS + IPT - 1) / IPT + 31) / 32 * 32;
+};
+
+// Stage channels [c0, c0+CG) of node (y,x,z)'s clamped box into hv (padded).
+template <class BG>
+__device__ __forceinline__ void stage_box_padded(const SoftGeom& G, int y, int x, int z, const float* __restrict__ sM,
+                                                 int c0, int CG, BoxPitch P, float* hv) {
+    const int64_t mn = (int64_t)G.m * G.n, sz = mn * G.o;
+    const int R = (BG::NA - G.g) / 2;
+    const int yb = y * G.g - R, xb = x * G.g - R, zb = z * G.g - R;
+    const int total = CG * BG::NA * BG::NA * BG::NA;
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+        const int a = e % BG::NA, r = e / BG::NA;
+        const int bx = r % BG::NA, t = r / BG::NA;
+        const int bz = t % BG::NA, c = t / BG::NA;
+        hv[c * (P.PZ * BG::NA) + bz * P.PZ + bx * P.PY + a] =
+            __ldg(sM + (int64_t)(c0 + c) * sz + clampi(yb + a, 0, G.m - 1) +
+                  (int64_t)clampi(xb + bx, 0, G.n - 1) * G.m + (int64_t)clampi(zb + bz, 0, G.o - 1) * mn);
+    }
+}
+
+template <class BG>
+__device__ __forceinline__ void stage_fixed_samples(const SoftGeom& G, int y, int x, int z,
+                                                    const float* __restrict__ sF, float* fs) {
+    const int64_t mn = (int64_t)G.m * G.n, sz = mn * G.o;
+    for (int e = threadIdx.x; e < 12 * BG::NSAMP; e += blockDim.x) {
+        const int c = e / BG::NSAMP, s = e % BG::NSAMP;
+        const int col = s / G.g, i = s % G.g;
+        const int py = y * G.g + i, px = x * G.g + (col % BG::NX) * BG::S, pz = z * G.g + (col / BG::NX) * BG::S;
+        fs[e] = __ldg(sF + (int64_t)c * sz + py + (int64_t)px * G.m + (int64_t)pz * mn);
+    }
+}
+
+template <int G_, int LEN_, int Q_>
+__global__ void __launch_bounds__(BoxGeom<G_, LEN_, Q_>::BLOCK, 2)
+    k_soft_cost_box(const float* __restrict__ sF, const float* __restrict__ sM, float* __restrict__ cost, SoftGeom G,
+                    BoxPitch P) {
+    using BG = BoxGeom<G_, LEN_, Q_>;
+    extern __shared__ float sh[];
+    const int node = blockIdx.x;
+    const int y = node % G.m1, x = (node / G.m1) % G.n1, z = node / (G.m1 * G.n1);
+    float* hv = sh;                               // [CG][NA][PZ]
+    float* fs = sh + P.CG * P.PZ * BG::NA;        // [12][NSAMP]
+    float* acc = fs + 12 * BG::NSAMP;             // [LEN3]
+    stage_fixed_samples<BG>(G, y, x, z, sF, fs);
+    for (int l = threadIdx.x; l < BG::LEN3; l += blockDim.x) acc[l] = 0.0f;
+    const float eps2 = G.eps * G.eps;
+    int rowoff[BG::IPT], fcol[BG::IPT];
+    float sums[BG::IPT][LEN_];
+#pragma unroll
+    for (int k = 0; k < BG::IPT; k++) {
+        const int t = min((int)threadIdx.x + k * (int)blockDim.x, BG::ITEMS - 1);
+        const int lab = t % BG::LEN2, col = t / BG::LEN2;
+        const int lx = lab % LEN_, lz = lab / LEN_, jj = col % BG::NX, kk = col / BG::NX;
+        rowoff[k] = (kk * BG::S + lz * Q_) * P.PZ + (jj * BG::S + lx * Q_) * P.PY;
+        fcol[k] = col * G_;
+#pragma unroll
+        for (int ly = 0; ly < LEN_; ly++) sums[k][ly] = 0.0f;
+    }
+    for (int c0 = 0; c0 < 12; c0 += P.CG) {
+        __syncthreads();
+        stage_box_padded<BG>(G, y, x, z, sM, c0, P.CG, P, hv);
+        __syncthreads();
+        for (int c = 0; c < P.CG; c++) {
+            const float* hvc = hv + c * (P.PZ * BG::NA);
+            const float* fsc = fs + (c0 + c) * BG::NSAMP;
+#pragma unroll
+            for (int k = 0; k < BG::IPT; k++) {
+                if ((int)threadIdx.x + k * (int)blockDim.x >= BG::ITEMS) break;
+                float v[BG::NA], f[G_];
+#pragma unroll
+                for (int a = 0; a < BG::NA; a++) v[a] = hvc[rowoff[k] + a];
+#pragma unroll
+                for (int i = 0; i < G_; i++) f[i] = fsc[fcol[k] + i];
+#pragma unroll
+                for (int ly = 0; ly < LEN_; ly++)
+#pragma unroll
+                    for (int i = 0; i < G_; i++) {
+                        const float d = f[i] - v[i + ly * Q_];
+                        const float x2 = d * d + eps2;
+                        sums[k][ly] += x2 * rsqrtf(x2);
+                    }
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < BG::IPT; k++) {
+        const int t = (int)threadIdx.x + k * (int)blockDim.x;
+        if (t >= BG::ITEMS) break;
+        const int lab = t % BG::LEN2;
+#pragma unroll
+        for (int ly = 0; ly < LEN_; ly++) atomicAdd(acc + ly + LEN_ * lab, sums[k][ly]);
+    }
+    __syncthreads();
+    for (int l = threadIdx.x; l < BG::LEN3; l += blockDim.x)
+        cost[(int64_t)node * BG::LEN3 + l] = G.alpha1 * (acc[l] - (float)(12 * BG::NSAMP) * G.eps);
+}
+
+// Fixed-side adjoint and the alpha dot product in box form: an item's len
+// label weights stay in registers, its g sample gradients are summed over the
+// item's labels per channel and added to the node's shared sample gradients.
+template <int G_, int LEN_, int Q_>
+__global__ void __launch_bounds__(BoxGeom<G_, LEN_, Q_>::BLOCK, 2)
+    k_soft_cost_adjF_box(const float* __restrict__ sF, const float* __restrict__ sM, const float* __restrict__ cbar,
+                         const float* __restrict__ cost, float* __restrict__ sFbar, double* __restrict__ dot,
+                         SoftGeom G, BoxPitch P) {
+    using BG = BoxGeom<G_, LEN_, Q_>;
+    extern __shared__ float sh[];
+    __shared__ double red[32];
+    const int node = blockIdx.x;
+    const int y = node % G.m1, x = (node / G.m1) % G.n1, z = node / (G.m1 * G.n1);
+    const int64_t mn = (int64_t)G.m * G.n, sz = mn * G.o;
+    float* hv = sh;                               // [CG][NA][PZ]
+    float* fs = sh + P.CG * P.PZ * BG::NA;        // [12][NSAMP]
+    float* gfs = fs + 12 * BG::NSAMP;             // [12][NSAMP]
+    float* cb = gfs + 12 * BG::NSAMP;             // [LEN3]
+    const float* cbn = cbar + (int64_t)node * BG::LEN3;
+    const float* cn = cost + (int64_t)node * BG::LEN3;
+    // alpha: centred dot product (the exact cbar sums to zero over labels)
+    double csum = 0.0;
+    for (int l = threadIdx.x; l < BG::LEN3; l += blockDim.x) {
+        csum += (double)cn[l];
+        cb[l] = cbn[l];
+    }
+    for (int off = 16; off > 0; off >>= 1) csum += __shfl_xor_sync(0xffffffffu, csum, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = csum;
+    for (int e = threadIdx.x; e < 12 * BG::NSAMP; e += blockDim.x) gfs[e] = 0.0f;
+    stage_fixed_samples<BG>(G, y, x, z, sF, fs);
+    __syncthreads();
+    double cmean = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) cmean += red[w];
+    cmean /= (double)BG::LEN3;
+    double part = 0.0;
+    for (int l = threadIdx.x; l < BG::LEN3; l += blockDim.x) part += (double)cb[l] * ((double)cn[l] - cmean);
+    for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+    if ((threadIdx.x & 31) == 0) atomicAdd(dot, part);
+    const float eps2 = G.eps * G.eps;
+    int rowoff[BG::IPT], fcol[BG::IPT];
+    float w[BG::IPT][LEN_];
+#pragma unroll
+    for (int k = 0; k < BG::IPT; k++) {
+        const int t = min((int)threadIdx.x + k * (int)blockDim.x, BG::ITEMS - 1);
+        const int lab = t % BG::LEN2, col = t / BG::LEN2;
+        const int lx = lab % LEN_, lz = lab / LEN_, jj = col % BG::NX, kk = col / BG::NX;
+        rowoff[k] = (kk * BG::S + lz * Q_) * P.PZ + (jj * BG::S + lx * Q_) * P.PY;
+        fcol[k] = col * G_;
+#pragma unroll
+        for (int ly = 0; ly < LEN_; ly++) w[k][ly] = cb[ly + LEN_ * lab];
+    }
+    for (int c0 = 0; c0 < 12; c0 += P.CG) {
+        __syncthreads();
+        stage_box_padded<BG>(G, y, x, z, sM, c0, P.CG, P, hv);
+        __syncthreads();
+        for (int c = 0; c < P.CG; c++) {
+            const float* hvc = hv + c * (P.PZ * BG::NA);
+            const float* fsc = fs + (c0 + c) * BG::NSAMP;
+            float* gfc = gfs + (c0 + c) * BG::NSAMP;
+#pragma unroll
+            for (int k = 0; k < BG::IPT; k++) {
+                if ((int)threadIdx.x + k * (int)blockDim.x >= BG::ITEMS) break;
+                float v[BG::NA], f[G_], gf[G_];
+#pragma unroll
+                for (int a = 0; a < BG::NA; a++) v[a] = hvc[rowoff[k] + a];
+#pragma unroll
+                for (int i = 0; i < G_; i++) {
+                    f[i] = fsc[fcol[k] + i];
+                    gf[i] = 0.0f;
+                }
+#pragma unroll
+                for (int ly = 0; ly < LEN_; ly++)
+#pragma unroll
+                    for (int i = 0; i < G_; i++) {
+                        const float d = f[i] - v[i + ly * Q_];
+                        gf[i] += w[k][ly] * d * rsqrtf(d * d + eps2);
+                    }
+#pragma unroll
+                for (int i = 0; i < G_; i++) atomicAdd(gfc + fcol[k] + i, gf[i]);
+            }
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 12 * BG::NSAMP; e += blockDim.x) {
+        const int c = e / BG::NSAMP, s = e % BG::NSAMP;
+        const int col = s / G.g, i = s % G.g;
+        const int py = y * G.g + i, px = x * G.g + (col % BG::NX) * BG::S, pz = z * G.g + (col / BG::NX) * BG::S;
+        sFbar[(int64_t)c * sz + py + (int64_t)px * G.m + (int64_t)pz * mn] = G.alpha1 * gfs[e];
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Tree sweeps
 
 struct SoftTree {
@@ -1394,6 +1604,87 @@ static cudaError_t run_cost_adj_col(const SoftGeom& G, const float* sF, const fl
     return cudaSuccess;
 }
 
+// Pitches of the padded box: rows of NA floats at pitch PY, planes at pitch PZ,
+// chosen to minimise, over the block's warps, the largest number of item rows
+// that start in one bank; then as many channels per stage as fit in 60 KB (three
+// CTAs per SM).
+template <int G_, int LEN_, int Q_>
+static BoxPitch box_pitch() {
+    using BG = BoxGeom<G_, LEN_, Q_>;
+    static BoxPitch cached{0, 0, 0};
+    if (cached.PY) return cached;
+    BoxPitch best{BG::NA, BG::NA * BG::NA, 1};
+    int best_cost = 1 << 30;
+    for (int py = BG::NA; py < BG::NA + 8; py++)
+        for (int pz = py * BG::NA; pz < py * BG::NA + 32; pz++) {
+            int cost = 0;
+            for (int w0 = 0; w0 < BG::ITEMS; w0 += 32) {
+                int cnt[32] = {0}, mx = 0;
+                for (int t = w0; t < std::min(w0 + 32, BG::ITEMS); t++) {
+                    const int lab = t % BG::LEN2, col = t / BG::LEN2;
+                    const int lx = lab % LEN_, lz = lab / LEN_, jj = col % BG::NX, kk = col / BG::NX;
+                    const int off = (kk * BG::S + lz * Q_) * pz + (jj * BG::S + lx * Q_) * py;
+                    mx = std::max(mx, ++cnt[off & 31]);
+                }
+                cost += mx;
+            }
+            // prefer the smaller footprint on ties
+            if (cost < best_cost || (cost == best_cost && pz * BG::NA < best.PZ * BG::NA)) {
+                best_cost = cost;
+                best = BoxPitch{py, pz, 1};
+            }
+        }
+    static const int cands[6] = {12, 6, 4, 3, 2, 1};
+    for (int c : cands)
+        if ((size_t)c * best.PZ * BG::NA * sizeof(float) <= 60 * 1024) { best.CG = c; break; }
+    cached = best;
+    return best;
+}
+
+template <int G_, int LEN_, int Q_>
+static cudaError_t run_cost_box(const SoftGeom& G, const float* sF, const float* sM, float* cost, cudaStream_t st) {
+    using BG = BoxGeom<G_, LEN_, Q_>;
+    const BoxPitch P = box_pitch<G_, LEN_, Q_>();
+    const size_t smem = sizeof(float) * ((size_t)P.CG * P.PZ * BG::NA + 12 * BG::NSAMP + BG::LEN3);
+    cudaError_t e = cudaFuncSetAttribute(k_soft_cost_box<G_, LEN_, Q_>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    k_soft_cost_box<G_, LEN_, Q_><<<G.m1 * G.n1 * G.o1, BG::BLOCK, smem, st>>>(sF, sM, cost, G, P);
+    return cudaSuccess;
+}
+
+template <int G_, int LEN_, int Q_>
+static cudaError_t run_cost_adjF_box(const SoftGeom& G, const float* sF, const float* sM, const float* cbar,
+                                     const float* cost, float* sFbar, double* dot, cudaStream_t st) {
+    using BG = BoxGeom<G_, LEN_, Q_>;
+    const BoxPitch P = box_pitch<G_, LEN_, Q_>();
+    const size_t smem = sizeof(float) * ((size_t)P.CG * P.PZ * BG::NA + 24 * BG::NSAMP + BG::LEN3);
+    cudaError_t e = cudaFuncSetAttribute(k_soft_cost_adjF_box<G_, LEN_, Q_>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_soft_cost_adjF_box<G_, LEN_, Q_><<<G.m1 * G.n1 * G.o1, BG::BLOCK, smem, st>>>(sF, sM, cbar, cost, sFbar, dot,
+                                                                                     G, P);
+    return cudaSuccess;
+}
+
+// Box kernels are instantiated for the coarse soft levels in use (grid 6 / quant
+// 3 and grid 5 / quant 2 with label widths 5 and 7).
+static int box_shape(const SoftGeom& G) {
+    if (G.len != 5 && G.len != 7) return 0;
+    if (G.g == 6 && G.q == 3) return 60 + G.len;
+    if (G.g == 6 && G.q == 2) return 600 + G.len;
+    if (G.g == 5 && G.q == 2) return 50 + G.len;
+    return 0;
+}
+
+#define DEEDS_BOX_CASES(FN, ...)                                                   \
+    case 65: e = FN<6, 5, 3>(__VA_ARGS__); break;                                  \
+    case 67: e = FN<6, 7, 3>(__VA_ARGS__); break;                                  \
+    case 605: e = FN<6, 5, 2>(__VA_ARGS__); break;                                 \
+    case 607: e = FN<6, 7, 2>(__VA_ARGS__); break;                                 \
+    case 55: e = FN<5, 5, 2>(__VA_ARGS__); break;                                  \
+    case 57: e = FN<5, 7, 2>(__VA_ARGS__); break;
+
 static int col_shape(const SoftGeom& G) {
     if (G.g != 4 || G.q != 1) return 0;
     return G.len == 5 || G.len == 7 || G.len == 9 ? G.len : 0;
@@ -1416,6 +1707,13 @@ cudaError_t launch_soft_cost(const float* sF, const float* sM, float* cost, int 
             return cudaGetLastError();
         }
         if (e != cudaErrorNotSupported) return e;
+    }
+    if (const int bs = box_shape(G)) {
+        cudaError_t e = cudaErrorNotSupported;
+        switch (bs) { DEEDS_BOX_CASES(run_cost_box, G, sF, sM, cost, st) default: break; }
+        if (e != cudaSuccess) return e;
+        count_launches(1);
+        return cudaGetLastError();
     }
     const size_t extra = sizeof(int) * (size_t)(G.len3 + G.nsamp);
     const int CG = G.len3 <= kHaloLPT * 512 ? halo_channels(G, H3max, 1, extra) : 0;
@@ -1440,6 +1738,14 @@ cudaError_t launch_soft_cost_adj(const float* sF, const float* sM, const float* 
     cudaError_t err = cudaMemsetAsync(sFbar, 0, sizeof(float) * 12 * sz, st);
     if (err == cudaSuccess) err = cudaMemsetAsync(dot, 0, sizeof(double), st);
     if (err != cudaSuccess) return err;
+    if (const int bs = box_shape(G)) {  // fixed side in box form, moving side as a gather (no atomics)
+        cudaError_t e = cudaErrorNotSupported;
+        switch (bs) { DEEDS_BOX_CASES(run_cost_adjF_box, G, sF, sM, cbar, cost, sFbar, dot, st) default: break; }
+        if (e != cudaSuccess) return e;
+        k_soft_cost_adj_moving<<<blocks_for(sz, 128), 128, 0, st>>>(sF, sM, cbar, sMbar, G);
+        count_launches(2);
+        return cudaGetLastError();
+    }
     const int H3max = halo_h3max(G);
     const size_t extra = sizeof(float) * (size_t)G.len3 + sizeof(int) * (size_t)(G.len3 + G.nsamp);
     const int CG = halo_channels(G, H3max, 2, extra);
