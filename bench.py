@@ -391,6 +391,36 @@ def measure_linear(api, ctx, shape, steps=5, warmup=3, cpu=True):
     return out
 
 
+def measure_gzio(pair, shape):
+    """NIfTI-gz IO of one volume of the workload (the fixed image, 352-byte header +
+    float32 data) through the library's parallel gzip writer/reader: one thread
+    (the reference's single-threaded zlib rate) against all host threads."""
+    import ctypes as C
+    import tempfile
+    from deedsbcv_gb300 import _lib
+    L = _lib.load()
+    data = np.ascontiguousarray(pair["fixed"].ravel(order="F"), np.float32)
+    head = np.zeros(352, np.uint8)
+    out = np.zeros(352 + data.nbytes, np.uint8)
+    res = {"volume": f"{shape[0]}x{shape[1]}x{shape[2]} float32 ({data.nbytes / 1e6:.1f} MB)", "level": 6}
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "v.nii.gz").encode()
+        for label, th in (("1_thread", 1), ("all_threads", 0)):
+            t0 = time.perf_counter()
+            st = L.deeds_gz_write(path, head.ctypes.data_as(C.c_void_p), 352, data.ctypes.data_as(C.c_void_p),
+                                  data.nbytes, -1, th)
+            w = time.perf_counter() - t0
+            tot = C.c_size_t(0)
+            t0 = time.perf_counter()
+            st2 = L.deeds_gz_read(path, out.ctypes.data_as(C.c_void_p), out.size, C.byref(tot), th)
+            r = time.perf_counter() - t0
+            ok = st == 0 and st2 == 0 and bool(np.array_equal(out[352:].view(np.float32), data))
+            res[label] = {"write_s": round(w, 4), "read_s": round(r, 4), "roundtrip_identical": ok,
+                          "compressed_MB": round(os.path.getsize(path) / 1e6, 2)}
+    res["threads"] = os.cpu_count()
+    return res
+
+
 def cpu_reference_pair(pair, shape):
     """The oracle registration of one pair on all host cores: (seconds, flow, ux, vx, wx)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -591,6 +621,9 @@ def main():
         soft = measure_soft(api, ctx)
         soft["finest_level_alone"] = measure_soft(api, ctx, levels=SOFT_LEVELS[-1:])
 
+    # ---- NIfTI-gz IO of one volume (rank 0)
+    gzio = measure_gzio(pair, shape) if rank == 0 else None
+
     # ---- linearBCV affine pre-registration (rank 0)
     linear = None
     if rank == 0 and not args.no_linear:
@@ -636,6 +669,7 @@ def main():
             "batched": batched,
             "soft": soft,
             "linear": linear,
+            "gzip_io": gzio,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:

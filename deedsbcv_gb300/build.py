@@ -36,7 +36,7 @@ CU_SOURCES = ["mind.cu", "datacost.cu", "mst.cu", "bp.cu", "transform.cu", "noal
 # so it may contract multiply-adds and flush denormals (its operands never are:
 # every square root and reciprocal square root argument is >= eps^2).
 FMAD_SOURCES = {"soft.cu", "soft_warp.cu"}
-CPP_SOURCES = ["pipeline.cpp", "tree_host.cpp", "linear_host.cpp"]
+CPP_SOURCES = ["pipeline.cpp", "tree_host.cpp", "linear_host.cpp", "gzio.cpp"]
 CLI_SOURCES = {"deedsBCV": ["deedsBCV.cpp", "cli_common.cpp"], "applyBCV": ["applyBCV.cpp", "cli_common.cpp"],
                "applyBCVfloat": ["applyBCV.cpp", "cli_common.cpp"], "linearBCV": ["linearBCV.cpp", "cli_common.cpp"]}
 
@@ -83,7 +83,7 @@ def build(verbose=False, force=False, cli=True):
     with ThreadPoolExecutor(max_workers=max(2, min(len(jobs), os.cpu_count() or 4))) as ex:
         list(ex.map(lambda j: _run(*j), jobs))
     if force or jobs or not os.path.exists(LIB):
-        _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread"], LIB + ".log")
+        _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread", "-lz"], LIB + ".log")
     if cli:
         build_cli(force=force)
     if verbose:

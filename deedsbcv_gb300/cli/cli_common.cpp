@@ -1,5 +1,7 @@
 #include "cli_common.h"
 
+#include "deeds_gpu.h"
+
 #include <zlib.h>
 
 #include <cstdio>
@@ -80,37 +82,68 @@ bool parse_args(int argc, char** argv, Args& a) {
 
 namespace {
 
-struct GzReader {
-    gzFile f = nullptr;
-    explicit GzReader(const std::string& p) { f = gzopen(p.c_str(), "rb"); }
-    ~GzReader() { if (f) gzclose(f); }
-};
+// Worker threads for gzip IO: DEEDS_GZ_THREADS, else every core.
+int gz_threads() {
+    const char* e = std::getenv("DEEDS_GZ_THREADS");
+    return e ? std::atoi(e) : 0;
+}
 
-bool read_header(GzReader& r, const std::string& path, Volume& v, short& dtype, short& bitpix, std::string& err) {
-    if (!r.f) { err = "gzopen of '" + path + "' failed."; return false; }
-    v.header.assign(352, 0);
-    if (gzread(r.f, v.header.data(), 352) != 352) { err = path + ": truncated header"; return false; }
+// The whole decompressed file (gzip or plain) through the library's parallel
+// reader; the buffer is sized from the gzip ISIZE trailer, so a single-member
+// file is inflated once.
+bool slurp(const std::string& path, std::vector<char>& raw, std::string& err) {
+    size_t hint = 0;
+    if (FILE* f = std::fopen(path.c_str(), "rb")) {
+        unsigned char mag[2] = {0, 0}, tr[4] = {0, 0, 0, 0};
+        std::fseek(f, 0, SEEK_END);
+        const long n = std::ftell(f);
+        std::fseek(f, 0, SEEK_SET);
+        const bool gz = std::fread(mag, 1, 2, f) == 2 && mag[0] == 0x1f && mag[1] == 0x8b;
+        if (gz && n >= 4 && std::fseek(f, n - 4, SEEK_SET) == 0 && std::fread(tr, 1, 4, f) == 4)
+            hint = (size_t)tr[0] | ((size_t)tr[1] << 8) | ((size_t)tr[2] << 16) | ((size_t)tr[3] << 24);
+        if (!gz || hint > (size_t)n * 64 + (1u << 20)) hint = (size_t)std::max<long>(n, 0) * (gz ? 4 : 1);
+        std::fclose(f);
+    } else {
+        err = "gzopen of '" + path + "' failed.";
+        return false;
+    }
+    raw.resize(std::max<size_t>(hint, 352));
+    size_t total = 0;
+    deeds_status st = deeds_gz_read(path.c_str(), raw.data(), raw.size(), &total, gz_threads());
+    if (st != DEEDS_OK && total > raw.size()) {  // more than the trailer said (several members)
+        raw.resize(total);
+        st = deeds_gz_read(path.c_str(), raw.data(), raw.size(), &total, gz_threads());
+    }
+    if (st != DEEDS_OK) {
+        err = path + ": " + deeds_gz_last_error();
+        return false;
+    }
+    raw.resize(total);
+    return true;
+}
+
+bool parse_header(const std::vector<char>& raw, const std::string& path, Volume& v, short& dtype, size_t& data_off,
+                  std::string& err) {
+    if (raw.size() < 352) { err = path + ": truncated header"; return false; }
+    v.header.assign(raw.begin(), raw.begin() + 352);
     short dims[8];
     std::memcpy(dims, v.header.data() + 40, sizeof(dims));
     std::memcpy(&dtype, v.header.data() + 70, 2);
-    std::memcpy(&bitpix, v.header.data() + 72, 2);
     v.m = dims[1]; v.n = dims[2]; v.o = dims[3]; v.p = dims[4] > 0 ? dims[4] : 1;
     if (v.m < 1 || v.n < 1 || v.o < 1) { err = path + ": bad dimensions"; return false; }
     float vox_offset = 352.0f;
     std::memcpy(&vox_offset, v.header.data() + 108, 4);
-    const long skip = (long)vox_offset - 352;
-    if (skip > 0) {
-        std::vector<char> tmp(skip);
-        if (gzread(r.f, tmp.data(), (unsigned)skip) != skip) { err = path + ": truncated extension"; return false; }
-    }
+    data_off = std::max<size_t>(352, (size_t)vox_offset);
     return true;
 }
 
 template <class T>
 bool read_nifti(const std::string& path, Volume& v, std::vector<T>& out, std::string& err) {
-    GzReader r(path);
-    short dtype = 0, bitpix = 0;
-    if (!read_header(r, path, v, dtype, bitpix, err)) return false;
+    std::vector<char> raw;
+    if (!slurp(path, raw, err)) return false;
+    short dtype = 0;
+    size_t off = 0;
+    if (!parse_header(raw, path, v, dtype, off, err)) return false;
     const size_t count = (size_t)v.m * v.n * v.o * v.p;
     size_t esz;
     switch (dtype) {
@@ -120,18 +153,10 @@ bool read_nifti(const std::string& path, Volume& v, std::vector<T>& out, std::st
         case 64: esz = 8; break;
         default: err = "Datatype " + std::to_string(dtype) + " not supported."; return false;
     }
-    std::vector<char> raw(count * esz);
-    size_t got = 0;
-    while (got < raw.size()) {
-        const unsigned chunk = (unsigned)std::min<size_t>(raw.size() - got, 1u << 30);
-        const int rd = gzread(r.f, raw.data() + got, chunk);
-        if (rd <= 0) break;
-        got += (size_t)rd;
-    }
-    if (got != raw.size()) { err = path + ": truncated data"; return false; }
+    if (raw.size() < off + count * esz) { err = path + ": truncated data"; return false; }
     out.resize(count);
     for (size_t i = 0; i < count; i++) {
-        const char* p = raw.data() + i * esz;
+        const char* p = raw.data() + off + i * esz;
         switch (dtype) {
             case 2: out[i] = (T)(*(const uint8_t*)p); break;
             case 4: { int16_t x; std::memcpy(&x, p, 2); out[i] = (T)x; } break;
@@ -157,19 +182,11 @@ bool write_nifti(const std::string& path, const Volume& like, const void* data, 
     const float off = 352.0f;
     std::memcpy(h.data() + 108, &off, 4);
     if (ends_with_gz(path)) {
-        gzFile f = gzopen(path.c_str(), "wb");
-        if (!f) { err = "File error. Could not write " + path; return false; }
-        bool ok = gzwrite(f, h.data(), 352) == 352;
-        size_t done = 0;
-        const char* p = static_cast<const char*>(data);
-        while (ok && done < bytes) {
-            const unsigned chunk = (unsigned)std::min<size_t>(bytes - done, 1u << 30);
-            ok = gzwrite(f, p + done, chunk) == (int)chunk;
-            done += chunk;
+        if (deeds_gz_write(path.c_str(), h.data(), 352, data, bytes, Z_DEFAULT_COMPRESSION, gz_threads()) != DEEDS_OK) {
+            err = "File error. Could not write " + path + ": " + deeds_gz_last_error();
+            return false;
         }
-        if (gzclose(f) != Z_OK) ok = false;
-        if (!ok) err = "write error on " + path;
-        return ok;
+        return true;
     }
     std::ofstream f(path, std::ios::binary);
     if (!f) { err = "File error. Could not write " + path; return false; }

@@ -198,6 +198,17 @@ __global__ void k_soft_sqdiff_adj(const float* __restrict__ im, const float* __r
 // ---------------------------------------------------------------------------
 // Cost
 
+// 4-byte asynchronous global->shared copies (cp.async, sm_80+): a thread issues all
+// its staging copies back to back and waits once, instead of one load latency per
+// element.  The caller waits with cp_async_wait_all() and then a block barrier.
+__device__ __forceinline__ void cp_async4(float* smem_dst, const float* gsrc) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
 struct SoftGeom {
     int m, n, o, g, hw, q, len, len3, m1, n1, o1, S, nx, nsamp;
     float alpha1, eps;
@@ -624,16 +635,17 @@ __device__ __forceinline__ void stage_box(const SoftGeom& G, int y, int x, int z
     if (sub < RPW)
         for (int r = warp * RPW + sub; r < nrows; r += nw * RPW) {
             const int b = r % CGm::NA, t = r / CGm::NA, cc = t % CGm::NA, c = t / CGm::NA;
-            hv[r * CGm::NA + a] = sM[(int64_t)(c0 + c) * sz + ya + (int64_t)clampi(xb + b, 0, G.n - 1) * G.m +
-                                     (int64_t)clampi(zb + cc, 0, G.o - 1) * mn];
+            cp_async4(hv + r * CGm::NA + a, sM + (int64_t)(c0 + c) * sz + ya + (int64_t)clampi(xb + b, 0, G.n - 1) * G.m +
+                                                (int64_t)clampi(zb + cc, 0, G.o - 1) * mn);
         }
     if (fs)
         for (int e = threadIdx.x; e < 12 * CGm::NSAMP; e += blockDim.x) {
             const int c = e / CGm::NSAMP, s = e % CGm::NSAMP;
             const int py = y * CGm::GS + s % CGm::GS, px = x * CGm::GS + ((s / CGm::GS) % CGm::NX) * CGm::S,
                       pz = z * CGm::GS + (s / (CGm::GS * CGm::NX)) * CGm::S;
-            fs[e] = sF[(int64_t)c * sz + py + (int64_t)px * G.m + (int64_t)pz * mn];
+            cp_async4(fs + e, sF + (int64_t)c * sz + py + (int64_t)px * G.m + (int64_t)pz * mn);
         }
+    cp_async_wait_all();
 }
 
 template <int G_, int LEN_, int Q_>
@@ -834,22 +846,29 @@ struct BoxGeom {
     static constexpr int BLOCK = ((ITEMS + IPT - 1) / IPT + 31) / 32 * 32;
 };
 
-// Stage channels [c0, c0+CG) of node (y,x,z)'s clamped box into hv (padded).
+// Stage channels [c0, c0+CG) of node (y,x,z)'s clamped box into hv (padded): a
+// warp copies one box row (NA consecutive voxels along y, coalesced) per step,
+// with the row's clamped x/z address formed once and each lane's clamped y
+// offset formed once per call.
 template <class BG>
 __device__ __forceinline__ void stage_box_padded(const SoftGeom& G, int y, int x, int z, const float* __restrict__ sM,
                                                  int c0, int CG, BoxPitch P, float* hv) {
+    static_assert(BG::NA <= 32, "box rows are staged one per warp");
     const int64_t mn = (int64_t)G.m * G.n, sz = mn * G.o;
     const int R = (BG::NA - G.g) / 2;
     const int yb = y * G.g - R, xb = x * G.g - R, zb = z * G.g - R;
-    const int total = CG * BG::NA * BG::NA * BG::NA;
-    for (int e = threadIdx.x; e < total; e += blockDim.x) {
-        const int a = e % BG::NA, r = e / BG::NA;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int ya = clampi(yb + lane, 0, G.m - 1);
+    const int rows = CG * BG::NA * BG::NA;
+    for (int r = warp; r < rows; r += nw) {
         const int bx = r % BG::NA, t = r / BG::NA;
         const int bz = t % BG::NA, c = t / BG::NA;
-        hv[c * (P.PZ * BG::NA) + bz * P.PZ + bx * P.PY + a] =
-            __ldg(sM + (int64_t)(c0 + c) * sz + clampi(yb + a, 0, G.m - 1) +
-                  (int64_t)clampi(xb + bx, 0, G.n - 1) * G.m + (int64_t)clampi(zb + bz, 0, G.o - 1) * mn);
+        if (lane < BG::NA)
+            cp_async4(hv + c * (P.PZ * BG::NA) + bz * P.PZ + bx * P.PY + lane,
+                      sM + (int64_t)(c0 + c) * sz + ya + (int64_t)clampi(xb + bx, 0, G.n - 1) * G.m +
+                          (int64_t)clampi(zb + bz, 0, G.o - 1) * mn);
     }
+    cp_async_wait_all();
 }
 
 template <class BG>
@@ -860,8 +879,9 @@ __device__ __forceinline__ void stage_fixed_samples(const SoftGeom& G, int y, in
         const int c = e / BG::NSAMP, s = e % BG::NSAMP;
         const int col = s / G.g, i = s % G.g;
         const int py = y * G.g + i, px = x * G.g + (col % BG::NX) * BG::S, pz = z * G.g + (col / BG::NX) * BG::S;
-        fs[e] = __ldg(sF + (int64_t)c * sz + py + (int64_t)px * G.m + (int64_t)pz * mn);
+        cp_async4(fs + e, sF + (int64_t)c * sz + py + (int64_t)px * G.m + (int64_t)pz * mn);
     }
+    cp_async_wait_all();
 }
 
 template <int G_, int LEN_, int Q_>

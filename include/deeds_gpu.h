@@ -362,6 +362,20 @@ deeds_status deeds_estimate_affine_dev(deeds_ctx* ctx, const float* d_fixed, con
  * (y | x | z | 1, len points each). */
 deeds_status deeds_affine_robust(const float* pts1, const float* pts2, int len, int rigid, float RT[16]);
 
+/* ---------------------------------------------------------------------------
+ * Parallel gzip IO for NIfTI volumes (host only; the reference uses single-
+ * threaded zlib, src/imageIOgzType.h:14-26, 212-218).  deeds_gz_write deflates
+ * head ++ data in 4 MiB chunks on `threads` threads (0 = all cores) into
+ * concatenated gzip members that any gzip reader accepts; level as zlib
+ * (-1 = default 6).  deeds_gz_read inflates such files in parallel and any
+ * other gzip or plain file through zlib; *total receives the decompressed size
+ * (out = NULL only asks for it; a too small cap returns DEEDS_ERR_INVALID with
+ * *total set). */
+deeds_status deeds_gz_write(const char* path, const void* head, size_t head_bytes, const void* data,
+                            size_t data_bytes, int level, int threads);
+deeds_status deeds_gz_read(const char* path, void* out, size_t cap, size_t* total, int threads);
+const char* deeds_gz_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif
