@@ -823,200 +823,201 @@ __global__ void __launch_bounds__(ColGeom<G_, LEN_, Q_>::ADJ_BLOCK, 4)
 }
 
 // ---------------------------------------------------------------------------
-// Box form for the coarser levels (grid > 4: nine sampled columns per node, and
-// label quantisation > 1, whose boxes NA = g + (len-1) q no longer fit twelve
-// channels in shared memory).  A node's clamped box of the moving descriptor is
-// staged one channel group at a time in a padded layout [c][bz][bx][a] (row pitch
-// PY, plane pitch PZ, chosen on the host so that the rows a warp reads start in
-// different banks); a thread owns one item (label pair (lx, lz), sampled
-// column) for the whole launch and keeps its len sums (forward) or its g
-// fixed-sample gradients (adjoint) in registers across the channel groups.
-// The moving-side gradient is the gather kernel k_soft_cost_adj_moving.
+// Row form for the coarser levels (grid > 4: nine sampled columns per node, and
+// label quantisation > 1).  An item is one label pair (lx, lz) of one sampled
+// column; its displaced samples read one row of the moving descriptor: NA = g +
+// (len-1) q consecutive voxels along y at clamped (x, z).  At these shapes no
+// two items of a node read the same row, so a node's rows are staged compactly,
+// row t at slot t with an odd pitch: the staging copies are coalesced along y
+// (a warp per row, cp.async) and each thread then reads its own row from shared
+// memory without bank conflicts (consecutive threads, rows PY apart, PY odd).  A thread keeps its item's len sums (forward)
+// or the label weights (adjoint) in registers across all channel groups.  The
+// moving-side gradient is the gather kernel k_soft_cost_adj_moving.
 
-struct BoxPitch {
-    int PY, PZ, CG;  // row pitch, plane pitch (floats), channels per stage
+struct RowPlan {
+    int PY, CG;  // row pitch (floats, odd), channels per stage
 };
 
 template <int G_, int LEN_, int Q_>
-struct BoxGeom {
+struct RowGeom {
     static constexpr int S = G_ > 4 ? 2 : 1, NX = (G_ + S - 1) / S, NCOL = NX * NX, NSAMP = NCOL * G_;
     static constexpr int NA = G_ + (LEN_ - 1) * Q_, LEN2 = LEN_ * LEN_, LEN3 = LEN2 * LEN_;
     static constexpr int ITEMS = LEN2 * NCOL;
-    static constexpr int IPT = (ITEMS + 511) / 512;
-    static constexpr int BLOCK = ((ITEMS + IPT - 1) / IPT + 31) / 32 * 32;
+    static constexpr int BLOCK = (ITEMS + 31) / 32 * 32;
+    static constexpr int PY = NA | 1;
+    static_assert(ITEMS <= 1024 && NA <= 32, "one item per thread, one row per warp");
 };
 
-// Stage channels [c0, c0+CG) of node (y,x,z)'s clamped box into hv (padded): a
-// warp copies one box row (NA consecutive voxels along y, coalesced) per step,
-// with the row's clamped x/z address formed once and each lane's clamped y
-// offset formed once per call.
-template <class BG>
-__device__ __forceinline__ void stage_box_padded(const SoftGeom& G, int y, int x, int z, const float* __restrict__ sM,
-                                                 int c0, int CG, BoxPitch P, float* hv) {
-    static_assert(BG::NA <= 32, "box rows are staged one per warp");
-    const int64_t mn = (int64_t)G.m * G.n, sz = mn * G.o;
-    const int R = (BG::NA - G.g) / 2;
-    const int yb = y * G.g - R, xb = x * G.g - R, zb = z * G.g - R;
+// Item t of a node: label pair (lab = lx + len*lz) and sampled column (jj, kk).
+template <class RG, int LEN_, int Q_>
+__device__ __forceinline__ void row_item(int t, int& lab, int& col, int& bx, int& bz) {
+    lab = t % RG::LEN2;
+    col = t / RG::LEN2;
+    const int lx = lab % LEN_, lz = lab / LEN_, jj = col % RG::NX, kk = col / RG::NX;
+    bx = jj * RG::S + lx * Q_;
+    bz = kk * RG::S + lz * Q_;
+}
+
+// Stage channels [c0, c0+CG) of the node's item rows: rows[c][t][a], pitch PY.
+// goff[t] holds item t's clamped (x, z) offset in one channel.
+template <class RG>
+__device__ __forceinline__ void stage_rows(const SoftGeom& G, int yb, const float* __restrict__ sM, int c0, int CG,
+                                           const int* goff, float* rows) {
+    const int64_t sz = (int64_t)G.m * G.n * G.o;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int ya = clampi(yb + lane, 0, G.m - 1);
-    const int rows = CG * BG::NA * BG::NA;
-    for (int r = warp; r < rows; r += nw) {
-        const int bx = r % BG::NA, t = r / BG::NA;
-        const int bz = t % BG::NA, c = t / BG::NA;
-        if (lane < BG::NA)
-            cp_async4(hv + c * (P.PZ * BG::NA) + bz * P.PZ + bx * P.PY + lane,
-                      sM + (int64_t)(c0 + c) * sz + ya + (int64_t)clampi(xb + bx, 0, G.n - 1) * G.m +
-                          (int64_t)clampi(zb + bz, 0, G.o - 1) * mn);
-    }
+    if (lane < RG::NA)
+        for (int c = 0; c < CG; c++) {
+            const float* src = sM + (int64_t)(c0 + c) * sz + ya;
+            float* dst = rows + c * (RG::ITEMS * RG::PY) + lane;
+            for (int r = warp; r < RG::ITEMS; r += nw) cp_async4(dst + r * RG::PY, src + goff[r]);
+        }
     cp_async_wait_all();
 }
 
-template <class BG>
+template <class RG>
 __device__ __forceinline__ void stage_fixed_samples(const SoftGeom& G, int y, int x, int z,
                                                     const float* __restrict__ sF, float* fs) {
     const int64_t mn = (int64_t)G.m * G.n, sz = mn * G.o;
-    for (int e = threadIdx.x; e < 12 * BG::NSAMP; e += blockDim.x) {
-        const int c = e / BG::NSAMP, s = e % BG::NSAMP;
+    for (int e = threadIdx.x; e < 12 * RG::NSAMP; e += blockDim.x) {
+        const int c = e / RG::NSAMP, s = e % RG::NSAMP;
         const int col = s / G.g, i = s % G.g;
-        const int py = y * G.g + i, px = x * G.g + (col % BG::NX) * BG::S, pz = z * G.g + (col / BG::NX) * BG::S;
+        const int py = y * G.g + i, px = x * G.g + (col % RG::NX) * RG::S, pz = z * G.g + (col / RG::NX) * RG::S;
         cp_async4(fs + e, sF + (int64_t)c * sz + py + (int64_t)px * G.m + (int64_t)pz * mn);
     }
     cp_async_wait_all();
 }
 
+// Each thread writes its item's clamped (x, z) row offset; returns the box's y origin.
+template <class RG, int LEN_, int Q_>
+__device__ __forceinline__ int row_offsets(const SoftGeom& G, int y, int x, int z, int* goff) {
+    const int R = (RG::NA - G.g) / 2;
+    const int t = threadIdx.x;
+    if (t < RG::ITEMS) {
+        int lab, col, bx, bz;
+        row_item<RG, LEN_, Q_>(t, lab, col, bx, bz);
+        goff[t] = clampi(x * G.g - R + bx, 0, G.n - 1) * G.m + clampi(z * G.g - R + bz, 0, G.o - 1) * G.m * G.n;
+    }
+    return y * G.g - R;
+}
+
 template <int G_, int LEN_, int Q_>
-__global__ void __launch_bounds__(BoxGeom<G_, LEN_, Q_>::BLOCK, 2)
-    k_soft_cost_box(const float* __restrict__ sF, const float* __restrict__ sM, float* __restrict__ cost, SoftGeom G,
-                    BoxPitch P) {
-    using BG = BoxGeom<G_, LEN_, Q_>;
+__global__ void __launch_bounds__(RowGeom<G_, LEN_, Q_>::BLOCK, 2)
+    k_soft_cost_rows(const float* __restrict__ sF, const float* __restrict__ sM, float* __restrict__ cost, SoftGeom G,
+                     RowPlan P) {
+    using RG = RowGeom<G_, LEN_, Q_>;
     extern __shared__ float sh[];
     const int node = blockIdx.x;
     const int y = node % G.m1, x = (node / G.m1) % G.n1, z = node / (G.m1 * G.n1);
-    float* hv = sh;                               // [CG][NA][PZ]
-    float* fs = sh + P.CG * P.PZ * BG::NA;        // [12][NSAMP]
-    float* acc = fs + 12 * BG::NSAMP;             // [LEN3]
-    stage_fixed_samples<BG>(G, y, x, z, sF, fs);
-    for (int l = threadIdx.x; l < BG::LEN3; l += blockDim.x) acc[l] = 0.0f;
+    float* rows = sh;                                  // [CG][ITEMS][PY]
+    float* fs = rows + P.CG * RG::ITEMS * RG::PY;      // [12][NSAMP]
+    float* acc = fs + 12 * RG::NSAMP;                  // [LEN3]
+    int* goff = reinterpret_cast<int*>(acc + RG::LEN3);  // [ITEMS]
+    const int yb = row_offsets<RG, LEN_, Q_>(G, y, x, z, goff);
+    for (int l = threadIdx.x; l < RG::LEN3; l += blockDim.x) acc[l] = 0.0f;
+    stage_fixed_samples<RG>(G, y, x, z, sF, fs);
     const float eps2 = G.eps * G.eps;
-    int rowoff[BG::IPT], fcol[BG::IPT];
-    float sums[BG::IPT][LEN_];
+    const int t = threadIdx.x;
+    const bool active = t < RG::ITEMS;
+    int lab = 0, col = 0, bx, bz;
+    row_item<RG, LEN_, Q_>(active ? t : 0, lab, col, bx, bz);
+    float sums[LEN_];
 #pragma unroll
-    for (int k = 0; k < BG::IPT; k++) {
-        const int t = min((int)threadIdx.x + k * (int)blockDim.x, BG::ITEMS - 1);
-        const int lab = t % BG::LEN2, col = t / BG::LEN2;
-        const int lx = lab % LEN_, lz = lab / LEN_, jj = col % BG::NX, kk = col / BG::NX;
-        rowoff[k] = (kk * BG::S + lz * Q_) * P.PZ + (jj * BG::S + lx * Q_) * P.PY;
-        fcol[k] = col * G_;
-#pragma unroll
-        for (int ly = 0; ly < LEN_; ly++) sums[k][ly] = 0.0f;
-    }
+    for (int ly = 0; ly < LEN_; ly++) sums[ly] = 0.0f;
     for (int c0 = 0; c0 < 12; c0 += P.CG) {
+        __syncthreads();  // goff written / previous rows consumed
+        stage_rows<RG>(G, yb, sM, c0, P.CG, goff, rows);
         __syncthreads();
-        stage_box_padded<BG>(G, y, x, z, sM, c0, P.CG, P, hv);
-        __syncthreads();
-        for (int c = 0; c < P.CG; c++) {
-            const float* hvc = hv + c * (P.PZ * BG::NA);
-            const float* fsc = fs + (c0 + c) * BG::NSAMP;
+        if (active)
+            for (int c = 0; c < P.CG; c++) {
+                const float* row = rows + (c * RG::ITEMS + t) * RG::PY;
+                const float* fc = fs + (c0 + c) * RG::NSAMP + col * G_;
+                float v[RG::NA], f[G_];
 #pragma unroll
-            for (int k = 0; k < BG::IPT; k++) {
-                if ((int)threadIdx.x + k * (int)blockDim.x >= BG::ITEMS) break;
-                float v[BG::NA], f[G_];
+                for (int a = 0; a < RG::NA; a++) v[a] = row[a];
 #pragma unroll
-                for (int a = 0; a < BG::NA; a++) v[a] = hvc[rowoff[k] + a];
-#pragma unroll
-                for (int i = 0; i < G_; i++) f[i] = fsc[fcol[k] + i];
+                for (int i = 0; i < G_; i++) f[i] = fc[i];
 #pragma unroll
                 for (int ly = 0; ly < LEN_; ly++)
 #pragma unroll
                     for (int i = 0; i < G_; i++) {
                         const float d = f[i] - v[i + ly * Q_];
                         const float x2 = d * d + eps2;
-                        sums[k][ly] += x2 * rsqrtf(x2);
+                        sums[ly] += x2 * rsqrtf(x2);
                     }
             }
-        }
     }
+    if (active)
 #pragma unroll
-    for (int k = 0; k < BG::IPT; k++) {
-        const int t = (int)threadIdx.x + k * (int)blockDim.x;
-        if (t >= BG::ITEMS) break;
-        const int lab = t % BG::LEN2;
-#pragma unroll
-        for (int ly = 0; ly < LEN_; ly++) atomicAdd(acc + ly + LEN_ * lab, sums[k][ly]);
-    }
+        for (int ly = 0; ly < LEN_; ly++) atomicAdd(acc + ly + LEN_ * lab, sums[ly]);
     __syncthreads();
-    for (int l = threadIdx.x; l < BG::LEN3; l += blockDim.x)
-        cost[(int64_t)node * BG::LEN3 + l] = G.alpha1 * (acc[l] - (float)(12 * BG::NSAMP) * G.eps);
+    for (int l = threadIdx.x; l < RG::LEN3; l += blockDim.x)
+        cost[(int64_t)node * RG::LEN3 + l] = G.alpha1 * (acc[l] - (float)(12 * RG::NSAMP) * G.eps);
 }
 
-// Fixed-side adjoint and the alpha dot product in box form: an item's len
-// label weights stay in registers, its g sample gradients are summed over the
-// item's labels per channel and added to the node's shared sample gradients.
+// Fixed-side adjoint and the alpha dot product in row form: an item's len label
+// weights stay in registers, its g sample gradients are summed over its labels
+// per channel and added to the node's shared sample gradients.
 template <int G_, int LEN_, int Q_>
-__global__ void __launch_bounds__(BoxGeom<G_, LEN_, Q_>::BLOCK, 2)
-    k_soft_cost_adjF_box(const float* __restrict__ sF, const float* __restrict__ sM, const float* __restrict__ cbar,
-                         const float* __restrict__ cost, float* __restrict__ sFbar, double* __restrict__ dot,
-                         SoftGeom G, BoxPitch P) {
-    using BG = BoxGeom<G_, LEN_, Q_>;
+__global__ void __launch_bounds__(RowGeom<G_, LEN_, Q_>::BLOCK, 2)
+    k_soft_cost_adjF_rows(const float* __restrict__ sF, const float* __restrict__ sM, const float* __restrict__ cbar,
+                          const float* __restrict__ cost, float* __restrict__ sFbar, double* __restrict__ dot,
+                          SoftGeom G, RowPlan P) {
+    using RG = RowGeom<G_, LEN_, Q_>;
     extern __shared__ float sh[];
     __shared__ double red[32];
     const int node = blockIdx.x;
     const int y = node % G.m1, x = (node / G.m1) % G.n1, z = node / (G.m1 * G.n1);
     const int64_t mn = (int64_t)G.m * G.n, sz = mn * G.o;
-    float* hv = sh;                               // [CG][NA][PZ]
-    float* fs = sh + P.CG * P.PZ * BG::NA;        // [12][NSAMP]
-    float* gfs = fs + 12 * BG::NSAMP;             // [12][NSAMP]
-    float* cb = gfs + 12 * BG::NSAMP;             // [LEN3]
-    const float* cbn = cbar + (int64_t)node * BG::LEN3;
-    const float* cn = cost + (int64_t)node * BG::LEN3;
+    float* rows = sh;                                  // [CG][ITEMS][PY]
+    float* fs = rows + P.CG * RG::ITEMS * RG::PY;      // [12][NSAMP]
+    float* gfs = fs + 12 * RG::NSAMP;                  // [12][NSAMP]
+    float* cb = gfs + 12 * RG::NSAMP;                  // [LEN3]
+    int* goff = reinterpret_cast<int*>(cb + RG::LEN3);  // [ITEMS]
+    const float* cbn = cbar + (int64_t)node * RG::LEN3;
+    const float* cn = cost + (int64_t)node * RG::LEN3;
+    const int yb = row_offsets<RG, LEN_, Q_>(G, y, x, z, goff);
     // alpha: centred dot product (the exact cbar sums to zero over labels)
     double csum = 0.0;
-    for (int l = threadIdx.x; l < BG::LEN3; l += blockDim.x) {
+    for (int l = threadIdx.x; l < RG::LEN3; l += blockDim.x) {
         csum += (double)cn[l];
         cb[l] = cbn[l];
     }
     for (int off = 16; off > 0; off >>= 1) csum += __shfl_xor_sync(0xffffffffu, csum, off);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = csum;
-    for (int e = threadIdx.x; e < 12 * BG::NSAMP; e += blockDim.x) gfs[e] = 0.0f;
-    stage_fixed_samples<BG>(G, y, x, z, sF, fs);
+    for (int e = threadIdx.x; e < 12 * RG::NSAMP; e += blockDim.x) gfs[e] = 0.0f;
+    stage_fixed_samples<RG>(G, y, x, z, sF, fs);
     __syncthreads();
     double cmean = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); w++) cmean += red[w];
-    cmean /= (double)BG::LEN3;
+    cmean /= (double)RG::LEN3;
     double part = 0.0;
-    for (int l = threadIdx.x; l < BG::LEN3; l += blockDim.x) part += (double)cb[l] * ((double)cn[l] - cmean);
+    for (int l = threadIdx.x; l < RG::LEN3; l += blockDim.x) part += (double)cb[l] * ((double)cn[l] - cmean);
     for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
     if ((threadIdx.x & 31) == 0) atomicAdd(dot, part);
     const float eps2 = G.eps * G.eps;
-    int rowoff[BG::IPT], fcol[BG::IPT];
-    float w[BG::IPT][LEN_];
+    const int t = threadIdx.x;
+    const bool active = t < RG::ITEMS;
+    int lab = 0, col = 0, bx, bz;
+    row_item<RG, LEN_, Q_>(active ? t : 0, lab, col, bx, bz);
+    float w[LEN_];
 #pragma unroll
-    for (int k = 0; k < BG::IPT; k++) {
-        const int t = min((int)threadIdx.x + k * (int)blockDim.x, BG::ITEMS - 1);
-        const int lab = t % BG::LEN2, col = t / BG::LEN2;
-        const int lx = lab % LEN_, lz = lab / LEN_, jj = col % BG::NX, kk = col / BG::NX;
-        rowoff[k] = (kk * BG::S + lz * Q_) * P.PZ + (jj * BG::S + lx * Q_) * P.PY;
-        fcol[k] = col * G_;
-#pragma unroll
-        for (int ly = 0; ly < LEN_; ly++) w[k][ly] = cb[ly + LEN_ * lab];
-    }
+    for (int ly = 0; ly < LEN_; ly++) w[ly] = cb[ly + LEN_ * lab];
     for (int c0 = 0; c0 < 12; c0 += P.CG) {
         __syncthreads();
-        stage_box_padded<BG>(G, y, x, z, sM, c0, P.CG, P, hv);
+        stage_rows<RG>(G, yb, sM, c0, P.CG, goff, rows);
         __syncthreads();
-        for (int c = 0; c < P.CG; c++) {
-            const float* hvc = hv + c * (P.PZ * BG::NA);
-            const float* fsc = fs + (c0 + c) * BG::NSAMP;
-            float* gfc = gfs + (c0 + c) * BG::NSAMP;
+        if (active)
+            for (int c = 0; c < P.CG; c++) {
+                const float* row = rows + (c * RG::ITEMS + t) * RG::PY;
+                const float* fc = fs + (c0 + c) * RG::NSAMP + col * G_;
+                float* gfc = gfs + (c0 + c) * RG::NSAMP + col * G_;
+                float v[RG::NA], f[G_], gf[G_];
 #pragma unroll
-            for (int k = 0; k < BG::IPT; k++) {
-                if ((int)threadIdx.x + k * (int)blockDim.x >= BG::ITEMS) break;
-                float v[BG::NA], f[G_], gf[G_];
-#pragma unroll
-                for (int a = 0; a < BG::NA; a++) v[a] = hvc[rowoff[k] + a];
+                for (int a = 0; a < RG::NA; a++) v[a] = row[a];
 #pragma unroll
                 for (int i = 0; i < G_; i++) {
-                    f[i] = fsc[fcol[k] + i];
+                    f[i] = fc[i];
                     gf[i] = 0.0f;
                 }
 #pragma unroll
@@ -1024,18 +1025,17 @@ __global__ void __launch_bounds__(BoxGeom<G_, LEN_, Q_>::BLOCK, 2)
 #pragma unroll
                     for (int i = 0; i < G_; i++) {
                         const float d = f[i] - v[i + ly * Q_];
-                        gf[i] += w[k][ly] * d * rsqrtf(d * d + eps2);
+                        gf[i] += w[ly] * d * rsqrtf(d * d + eps2);
                     }
 #pragma unroll
-                for (int i = 0; i < G_; i++) atomicAdd(gfc + fcol[k] + i, gf[i]);
+                for (int i = 0; i < G_; i++) atomicAdd(gfc + i, gf[i]);
             }
-        }
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < 12 * BG::NSAMP; e += blockDim.x) {
-        const int c = e / BG::NSAMP, s = e % BG::NSAMP;
-        const int col = s / G.g, i = s % G.g;
-        const int py = y * G.g + i, px = x * G.g + (col % BG::NX) * BG::S, pz = z * G.g + (col / BG::NX) * BG::S;
+    for (int e = threadIdx.x; e < 12 * RG::NSAMP; e += blockDim.x) {
+        const int c = e / RG::NSAMP, s = e % RG::NSAMP;
+        const int cl = s / G.g, i = s % G.g;
+        const int py = y * G.g + i, px = x * G.g + (cl % RG::NX) * RG::S, pz = z * G.g + (cl / RG::NX) * RG::S;
         sFbar[(int64_t)c * sz + py + (int64_t)px * G.m + (int64_t)pz * mn] = G.alpha1 * gfs[e];
     }
 }
@@ -1624,72 +1624,50 @@ static cudaError_t run_cost_adj_col(const SoftGeom& G, const float* sF, const fl
     return cudaSuccess;
 }
 
-// Pitches of the padded box: rows of NA floats at pitch PY, planes at pitch PZ,
-// chosen to minimise, over the block's warps, the largest number of item rows
-// that start in one bank; then as many channels per stage as fit in 60 KB (three
-// CTAs per SM).
+// Channels per stage of the row kernels: as many as fit in 64 KB of rows.
 template <int G_, int LEN_, int Q_>
-static BoxPitch box_pitch() {
-    using BG = BoxGeom<G_, LEN_, Q_>;
-    static BoxPitch cached{0, 0, 0};
-    if (cached.PY) return cached;
-    BoxPitch best{BG::NA, BG::NA * BG::NA, 1};
-    int best_cost = 1 << 30;
-    for (int py = BG::NA; py < BG::NA + 8; py++)
-        for (int pz = py * BG::NA; pz < py * BG::NA + 32; pz++) {
-            int cost = 0;
-            for (int w0 = 0; w0 < BG::ITEMS; w0 += 32) {
-                int cnt[32] = {0}, mx = 0;
-                for (int t = w0; t < std::min(w0 + 32, BG::ITEMS); t++) {
-                    const int lab = t % BG::LEN2, col = t / BG::LEN2;
-                    const int lx = lab % LEN_, lz = lab / LEN_, jj = col % BG::NX, kk = col / BG::NX;
-                    const int off = (kk * BG::S + lz * Q_) * pz + (jj * BG::S + lx * Q_) * py;
-                    mx = std::max(mx, ++cnt[off & 31]);
-                }
-                cost += mx;
-            }
-            // prefer the smaller footprint on ties
-            if (cost < best_cost || (cost == best_cost && pz * BG::NA < best.PZ * BG::NA)) {
-                best_cost = cost;
-                best = BoxPitch{py, pz, 1};
-            }
-        }
+static RowPlan row_plan() {
+    using RG = RowGeom<G_, LEN_, Q_>;
     static const int cands[6] = {12, 6, 4, 3, 2, 1};
+    RowPlan P{RG::PY, 1};
     for (int c : cands)
-        if ((size_t)c * best.PZ * BG::NA * sizeof(float) <= 60 * 1024) { best.CG = c; break; }
-    cached = best;
-    return best;
+        if ((size_t)c * RG::ITEMS * RG::PY * sizeof(float) <= 64 * 1024) { P.CG = c; break; }
+    return P;
 }
 
 template <int G_, int LEN_, int Q_>
-static cudaError_t run_cost_box(const SoftGeom& G, const float* sF, const float* sM, float* cost, cudaStream_t st) {
-    using BG = BoxGeom<G_, LEN_, Q_>;
-    const BoxPitch P = box_pitch<G_, LEN_, Q_>();
-    const size_t smem = sizeof(float) * ((size_t)P.CG * P.PZ * BG::NA + 12 * BG::NSAMP + BG::LEN3);
-    cudaError_t e = cudaFuncSetAttribute(k_soft_cost_box<G_, LEN_, Q_>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+static cudaError_t run_cost_rows(const SoftGeom& G, const float* sF, const float* sM, float* cost, cudaStream_t st) {
+    using RG = RowGeom<G_, LEN_, Q_>;
+    const RowPlan P = row_plan<G_, LEN_, Q_>();
+    const size_t smem = sizeof(float) * ((size_t)P.CG * RG::ITEMS * RG::PY + 12 * RG::NSAMP + RG::LEN3) +
+                        sizeof(int) * RG::ITEMS;
+    cudaError_t e = cudaFuncSetAttribute(k_soft_cost_rows<G_, LEN_, Q_>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    k_soft_cost_box<G_, LEN_, Q_><<<G.m1 * G.n1 * G.o1, BG::BLOCK, smem, st>>>(sF, sM, cost, G, P);
+    k_soft_cost_rows<G_, LEN_, Q_><<<G.m1 * G.n1 * G.o1, RG::BLOCK, smem, st>>>(sF, sM, cost, G, P);
     return cudaSuccess;
 }
 
 template <int G_, int LEN_, int Q_>
-static cudaError_t run_cost_adjF_box(const SoftGeom& G, const float* sF, const float* sM, const float* cbar,
-                                     const float* cost, float* sFbar, double* dot, cudaStream_t st) {
-    using BG = BoxGeom<G_, LEN_, Q_>;
-    const BoxPitch P = box_pitch<G_, LEN_, Q_>();
-    const size_t smem = sizeof(float) * ((size_t)P.CG * P.PZ * BG::NA + 24 * BG::NSAMP + BG::LEN3);
-    cudaError_t e = cudaFuncSetAttribute(k_soft_cost_adjF_box<G_, LEN_, Q_>,
+static cudaError_t run_cost_adjF_rows(const SoftGeom& G, const float* sF, const float* sM, const float* cbar,
+                                      const float* cost, float* sFbar, double* dot, cudaStream_t st) {
+    using RG = RowGeom<G_, LEN_, Q_>;
+    const RowPlan P = row_plan<G_, LEN_, Q_>();
+    const size_t smem = sizeof(float) * ((size_t)P.CG * RG::ITEMS * RG::PY + 24 * RG::NSAMP + RG::LEN3) +
+                        sizeof(int) * RG::ITEMS;
+    cudaError_t e = cudaFuncSetAttribute(k_soft_cost_adjF_rows<G_, LEN_, Q_>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_soft_cost_adjF_box<G_, LEN_, Q_><<<G.m1 * G.n1 * G.o1, BG::BLOCK, smem, st>>>(sF, sM, cbar, cost, sFbar, dot,
-                                                                                     G, P);
+    k_soft_cost_adjF_rows<G_, LEN_, Q_><<<G.m1 * G.n1 * G.o1, RG::BLOCK, smem, st>>>(sF, sM, cbar, cost, sFbar,
+                                                                                      dot, G, P);
     return cudaSuccess;
 }
 
-// Box kernels are instantiated for the coarse soft levels in use (grid 6 / quant
-// 3 and grid 5 / quant 2 with label widths 5 and 7).
-static int box_shape(const SoftGeom& G) {
+// Row kernels are instantiated for the coarse soft levels in use (grid 6 / quant
+// 3 or 2, grid 5 / quant 2, label widths 5 and 7).  Every item stages its own
+// row; where two items of a node read the same row (quant 2: x offsets 2jj + 2lx
+// repeat) that row is simply staged twice.
+static int row_shape(const SoftGeom& G) {
     if (G.len != 5 && G.len != 7) return 0;
     if (G.g == 6 && G.q == 3) return 60 + G.len;
     if (G.g == 6 && G.q == 2) return 600 + G.len;
@@ -1697,7 +1675,7 @@ static int box_shape(const SoftGeom& G) {
     return 0;
 }
 
-#define DEEDS_BOX_CASES(FN, ...)                                                   \
+#define DEEDS_ROW_CASES(FN, ...)                                                   \
     case 65: e = FN<6, 5, 3>(__VA_ARGS__); break;                                  \
     case 67: e = FN<6, 7, 3>(__VA_ARGS__); break;                                  \
     case 605: e = FN<6, 5, 2>(__VA_ARGS__); break;                                 \
@@ -1728,9 +1706,9 @@ cudaError_t launch_soft_cost(const float* sF, const float* sM, float* cost, int 
         }
         if (e != cudaErrorNotSupported) return e;
     }
-    if (const int bs = box_shape(G)) {
+    if (const int rs = row_shape(G)) {
         cudaError_t e = cudaErrorNotSupported;
-        switch (bs) { DEEDS_BOX_CASES(run_cost_box, G, sF, sM, cost, st) default: break; }
+        switch (rs) { DEEDS_ROW_CASES(run_cost_rows, G, sF, sM, cost, st) default: break; }
         if (e != cudaSuccess) return e;
         count_launches(1);
         return cudaGetLastError();
@@ -1758,9 +1736,9 @@ cudaError_t launch_soft_cost_adj(const float* sF, const float* sM, const float* 
     cudaError_t err = cudaMemsetAsync(sFbar, 0, sizeof(float) * 12 * sz, st);
     if (err == cudaSuccess) err = cudaMemsetAsync(dot, 0, sizeof(double), st);
     if (err != cudaSuccess) return err;
-    if (const int bs = box_shape(G)) {  // fixed side in box form, moving side as a gather (no atomics)
+    if (const int rs = row_shape(G)) {  // fixed side in row form, moving side as a gather (no atomics)
         cudaError_t e = cudaErrorNotSupported;
-        switch (bs) { DEEDS_BOX_CASES(run_cost_adjF_box, G, sF, sM, cbar, cost, sFbar, dot, st) default: break; }
+        switch (rs) { DEEDS_ROW_CASES(run_cost_adjF_rows, G, sF, sM, cbar, cost, sFbar, dot, st) default: break; }
         if (e != cudaSuccess) return e;
         k_soft_cost_adj_moving<<<blocks_for(sz, 128), 128, 0, st>>>(sF, sM, cbar, sMbar, G);
         count_launches(2);

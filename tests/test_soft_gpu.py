@@ -57,7 +57,7 @@ def test_soft_descriptor_matches_float64(api):
 @pytest.mark.parametrize("g,hw,q", [(4, 2, 1), (4, 3, 1), (4, 4, 1), (5, 1, 2), (3, 3, 1),
                                     (5, 2, 2), (5, 3, 2), (6, 2, 3), (6, 3, 3), (6, 2, 2), (6, 3, 2)])
 def test_soft_cost_matches_float64(api, g, hw, q):
-    # (4, *, 1): column kernels; (5|6, 2|3, 2|3): box kernels; the rest generic halo kernels
+    # (4, *, 1): column kernels; (5|6, 2|3, 2|3): row kernels; the rest generic halo kernels
     m, n, o = DIMS
     f, mv = _pair(2)
     qs = 1
@@ -107,7 +107,7 @@ def _grads(api, tau, hw=2, seed=3, g=4, q=1):
                                         (0.5, 5, 1, 2), (0.5, 5, 3, 2), (0.1, 6, 3, 3), (0.5, 6, 2, 2)])
 def test_soft_adjoint_matches_float64_autograd(api, tau, g, hw, q):
     # (4, *, 1): column kernels; (3, 2, 1) and (5, 1, 2): generic halo kernels; (5, 3, 2), (6, 3, 3)
-    # and (6, 2, 2): box kernels with the moving side gathered
+    # and (6, 2, 2): row kernels with the moving side gathered
     f, mv, tree, gt, gF, gM, ga = _grads(api, tau, hw, g=g, q=q)
     qs = int(0.5 * q + 1.0)
     F = _t64(f, DIMS).requires_grad_()
