@@ -849,10 +849,13 @@ struct RowGeom {
 };
 
 // Item t of a node: label pair (lab = lx + len*lz) and sampled column (jj, kk).
-template <class RG, int LEN_, int Q_>
+// Label-fastest order (forward: a warp's items share a column, its label sums go
+// to distinct addresses) or column-fastest order (adjoint: a warp's items spread
+// over the nine columns, so its sample-gradient atomics hit a column <= 4 times).
+template <class RG, int LEN_, int Q_, bool COL_FAST>
 __device__ __forceinline__ void row_item(int t, int& lab, int& col, int& bx, int& bz) {
-    lab = t % RG::LEN2;
-    col = t / RG::LEN2;
+    lab = COL_FAST ? t / RG::NCOL : t % RG::LEN2;
+    col = COL_FAST ? t % RG::NCOL : t / RG::LEN2;
     const int lx = lab % LEN_, lz = lab / LEN_, jj = col % RG::NX, kk = col / RG::NX;
     bx = jj * RG::S + lx * Q_;
     bz = kk * RG::S + lz * Q_;
@@ -889,13 +892,13 @@ __device__ __forceinline__ void stage_fixed_samples(const SoftGeom& G, int y, in
 }
 
 // Each thread writes its item's clamped (x, z) row offset; returns the box's y origin.
-template <class RG, int LEN_, int Q_>
+template <class RG, int LEN_, int Q_, bool COL_FAST>
 __device__ __forceinline__ int row_offsets(const SoftGeom& G, int y, int x, int z, int* goff) {
     const int R = (RG::NA - G.g) / 2;
     const int t = threadIdx.x;
     if (t < RG::ITEMS) {
         int lab, col, bx, bz;
-        row_item<RG, LEN_, Q_>(t, lab, col, bx, bz);
+        row_item<RG, LEN_, Q_, COL_FAST>(t, lab, col, bx, bz);
         goff[t] = clampi(x * G.g - R + bx, 0, G.n - 1) * G.m + clampi(z * G.g - R + bz, 0, G.o - 1) * G.m * G.n;
     }
     return y * G.g - R;
@@ -913,14 +916,14 @@ __global__ void __launch_bounds__(RowGeom<G_, LEN_, Q_>::BLOCK, 2)
     float* fs = rows + P.CG * RG::ITEMS * RG::PY;      // [12][NSAMP]
     float* acc = fs + 12 * RG::NSAMP;                  // [LEN3]
     int* goff = reinterpret_cast<int*>(acc + RG::LEN3);  // [ITEMS]
-    const int yb = row_offsets<RG, LEN_, Q_>(G, y, x, z, goff);
+    const int yb = row_offsets<RG, LEN_, Q_, false>(G, y, x, z, goff);
     for (int l = threadIdx.x; l < RG::LEN3; l += blockDim.x) acc[l] = 0.0f;
     stage_fixed_samples<RG>(G, y, x, z, sF, fs);
     const float eps2 = G.eps * G.eps;
     const int t = threadIdx.x;
     const bool active = t < RG::ITEMS;
     int lab = 0, col = 0, bx, bz;
-    row_item<RG, LEN_, Q_>(active ? t : 0, lab, col, bx, bz);
+    row_item<RG, LEN_, Q_, false>(active ? t : 0, lab, col, bx, bz);
     float sums[LEN_];
 #pragma unroll
     for (int ly = 0; ly < LEN_; ly++) sums[ly] = 0.0f;
@@ -976,7 +979,7 @@ __global__ void __launch_bounds__(RowGeom<G_, LEN_, Q_>::BLOCK, 2)
     int* goff = reinterpret_cast<int*>(cb + RG::LEN3);  // [ITEMS]
     const float* cbn = cbar + (int64_t)node * RG::LEN3;
     const float* cn = cost + (int64_t)node * RG::LEN3;
-    const int yb = row_offsets<RG, LEN_, Q_>(G, y, x, z, goff);
+    const int yb = row_offsets<RG, LEN_, Q_, true>(G, y, x, z, goff);
     // alpha: centred dot product (the exact cbar sums to zero over labels)
     double csum = 0.0;
     for (int l = threadIdx.x; l < RG::LEN3; l += blockDim.x) {
@@ -999,7 +1002,7 @@ __global__ void __launch_bounds__(RowGeom<G_, LEN_, Q_>::BLOCK, 2)
     const int t = threadIdx.x;
     const bool active = t < RG::ITEMS;
     int lab = 0, col = 0, bx, bz;
-    row_item<RG, LEN_, Q_>(active ? t : 0, lab, col, bx, bz);
+    row_item<RG, LEN_, Q_, true>(active ? t : 0, lab, col, bx, bz);
     float w[LEN_];
 #pragma unroll
     for (int ly = 0; ly < LEN_; ly++) w[ly] = cb[ly + LEN_ * lab];
