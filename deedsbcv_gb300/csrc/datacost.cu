@@ -335,14 +335,20 @@ cudaError_t launch_data_cost_tma(const uint64_t* d_F, const uint64_t* d_M, uint6
         k_pad_codes<<<grd, blk, 0, s>>>(d_M, d_Mpad, m, n, o, pad, mpp, np, op);
         count_launches(1);
     }
-    // the default level schedule (-G 8x7x6x5x4 -L 8x7x6x5x4 -Q 5x4x3x2x1) has its
-    // own compile-time instantiations; everything else runs the runtime-width kernel
+    // deedsBCV's default level schedule (-G 8x7x6x5x4 -L 8x7x6x5x4 -Q 5x4x3x2x1) and
+    // linearBCV's have their own compile-time instantiations; everything else runs
+    // the runtime-width kernel
 #define DEEDS_TMA_ARGS d_F, d_Mpad, mpp, np, op, m, n, o, hw, q, ny_tile, alpha1, d_cost, d_err, s
     if (g == 8 && hw == 8 && q == 5) return launch_tma<8, 17, 5>(DEEDS_TMA_ARGS);
     if (g == 7 && hw == 7 && q == 4) return launch_tma<7, 15, 4>(DEEDS_TMA_ARGS);
     if (g == 6 && hw == 6 && q == 3) return launch_tma<6, 13, 3>(DEEDS_TMA_ARGS);
     if (g == 5 && hw == 5 && q == 2) return launch_tma<5, 11, 2>(DEEDS_TMA_ARGS);
     if (g == 4 && hw == 4 && q == 1) return launch_tma<4, 9, 1>(DEEDS_TMA_ARGS);
+    // linearBCV's default schedule (src/linearBCV.cpp:86-89)
+    if (g == 7 && hw == 5 && q == 4) return launch_tma<7, 11, 4>(DEEDS_TMA_ARGS);
+    if (g == 6 && hw == 4 && q == 3) return launch_tma<6, 9, 3>(DEEDS_TMA_ARGS);
+    if (g == 5 && hw == 3 && q == 2) return launch_tma<5, 7, 2>(DEEDS_TMA_ARGS);
+    if (g == 4 && hw == 2 && q == 1) return launch_tma<4, 5, 1>(DEEDS_TMA_ARGS);
     switch (g) {
         case 2: return launch_tma<2, 0, 0>(DEEDS_TMA_ARGS);
         case 3: return launch_tma<3, 0, 0>(DEEDS_TMA_ARGS);

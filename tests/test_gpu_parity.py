@@ -87,8 +87,10 @@ def test_data_cost_golden(api, golden):
         assert same_bits(cost, g[f"cost_{gs}_{hw}_{q}"]), (gs, hw, q)
 
 
-@pytest.mark.parametrize("gs,hw,q", [(8, 8, 5), (7, 7, 4), (6, 6, 3), (5, 5, 2), (4, 4, 1), (4, 3, 2)])
+@pytest.mark.parametrize("gs,hw,q", [(8, 8, 5), (7, 7, 4), (6, 6, 3), (5, 5, 2), (4, 4, 1), (4, 3, 2),
+                                     (7, 5, 4), (6, 4, 3), (5, 3, 2), (4, 2, 1)])
 def test_data_cost_phantom_vs_oracle(api, gs, hw, q):
+    # deedsBCV's and linearBCV's default level shapes (compile-time label widths) and one runtime-width shape
     from deedsbcv_gb300 import phantom
     shape = (64, 48, 72)
     pair = phantom.make_pair(shape, seed=12, max_disp=6.0)
