@@ -1210,27 +1210,72 @@ __device__ void add_offbar(const SoftTree& t, int c, float* dof3, float scale, f
 
 // ---- per-node bodies (one CTA per node; data of other nodes written in the same
 // sweep is read with __ldcg, after the producer's release has been observed)
+//
+// What a node reads that does not come from this sweep (its own rows from the
+// forward or earlier sweeps, its child list) is loaded before the dependency
+// wait into NodePre — one label per thread, the label threadIdx.x — so that after
+// the wait only the rows produced in this sweep remain on the critical path, and
+// the children's rows are then loaded together rather than one child after another.
+
+constexpr int kMaxChildren = 6;  // a 6-connected grid tree: at most 6 children (the root)
+
+struct NodePre {
+    float v0, v1, v2;  // own values at label threadIdx.x (meaning depends on the sweep)
+    int nch;
+    int ch[kMaxChildren];
+};
+
+// Own value at label l: prefetched for the thread's first label, else loaded.
+__device__ __forceinline__ float own(int l, float pre, const float* __restrict__ row) {
+    return l == (int)threadIdx.x ? pre : row[l];
+}
+
+__device__ __forceinline__ void load_children(const SoftTree& t, int c, NodePre& pre) {
+    const int k0 = t.child_ptr[c], k1 = t.child_ptr[c + 1];
+    pre.nch = k1 - k0;
+#pragma unroll
+    for (int i = 0; i < kMaxChildren; i++) pre.ch[i] = i < pre.nch ? t.children[k0 + i] : 0;
+}
+
+// v + sum over children in child order of (X[k][l] - xmin[k]) (xmin may be null):
+// all children's values are loaded before the in-order sum.
+__device__ __forceinline__ float add_children(const SoftTree& t, int c, const NodePre& pre, int l, float v,
+                                              const float* __restrict__ X, const float* __restrict__ xmin) {
+    const int L3 = t.len3;
+    if (pre.nch <= kMaxChildren) {
+        float xs[kMaxChildren], ms[kMaxChildren];
+#pragma unroll
+        for (int i = 0; i < kMaxChildren; i++) {
+            xs[i] = i < pre.nch ? __ldcg(X + (int64_t)pre.ch[i] * L3 + l) : 0.0f;
+            ms[i] = (xmin && i < pre.nch) ? __ldcg(xmin + pre.ch[i]) : 0.0f;
+        }
+#pragma unroll
+        for (int i = 0; i < kMaxChildren; i++)
+            if (i < pre.nch) v += xmin ? xs[i] - ms[i] : xs[i];
+        return v;
+    }
+    for (int ci = t.child_ptr[c]; ci < t.child_ptr[c + 1]; ci++) {
+        const int k = t.children[ci];
+        v += xmin ? __ldcg(X + (int64_t)k * L3 + l) - __ldcg(xmin + k) : __ldcg(X + (int64_t)k * L3 + l);
+    }
+    return v;
+}
 
 // Upward: B_c = C_c + sum_children (M_k - min M_k), stored minus its minimum (the
 // marginals and the parent's (message - min) are invariant to a constant shift of
 // B_c, and the centred values keep the exponents of the label-space transforms
 // small where the probability mass is); M_c = -tau S(-e_c B_c / tau).
-__device__ void node_up(const SoftTree& t, int c, const float* __restrict__ cost, float* __restrict__ B,
-                        float* __restrict__ M, float* __restrict__ Mmin, float* sh) {
+__device__ void node_up(const SoftTree& t, int c, const NodePre& pre, const float* __restrict__ cost,
+                        float* __restrict__ B, float* __restrict__ M, float* __restrict__ Mmin, float* sh) {
     const int L3 = t.len3;
     float* f = sh;
     float* t1 = sh + L3;
     float* t2 = sh + 2 * L3;
     float* red = sh + 3 * L3;
     const float e = c == t.root ? 0.0f : t.edgemst[c];
-    const int k0 = t.child_ptr[c], k1 = t.child_ptr[c + 1];
     float bmin = INFINITY;
     for (int l = threadIdx.x; l < L3; l += blockDim.x) {
-        float v = cost[(int64_t)c * L3 + l];
-        for (int ci = k0; ci < k1; ci++) {
-            const int k = t.children[ci];
-            v += __ldcg(M + (int64_t)k * L3 + l) - __ldcg(Mmin + k);
-        }
+        const float v = add_children(t, c, pre, l, own(l, pre.v0, cost + (int64_t)c * L3), M, Mmin);
         f[l] = v;
         bmin = fminf(bmin, v);
     }
@@ -1258,8 +1303,8 @@ __device__ void node_up(const SoftTree& t, int c, const float* __restrict__ cost
 // normalised in exact arithmetic; renormalising stops float rounding from drifting
 // along root-to-leaf paths (no effect on the exact gradient, whose parameter
 // derivatives are tangent to the normalised set).
-__device__ void node_down(const SoftTree& t, int c, const float* __restrict__ B, const float* __restrict__ M,
-                          float* __restrict__ logp, float* __restrict__ disp, float* sh) {
+__device__ void node_down(const SoftTree& t, int c, const NodePre& pre, const float* __restrict__ B,
+                          const float* __restrict__ M, float* __restrict__ logp, float* __restrict__ disp, float* sh) {
     const int L3 = t.len3, len = t.len;
     float* r = sh;
     float* t1 = sh + L3;
@@ -1268,16 +1313,16 @@ __device__ void node_down(const SoftTree& t, int c, const float* __restrict__ B,
     float* lc = logp + (int64_t)c * L3;
     const float* bc = B + (int64_t)c * L3;
     if (c == t.root) {
-        for (int l = threadIdx.x; l < L3; l += blockDim.x) r[l] = -bc[l] * t.itau;
+        for (int l = threadIdx.x; l < L3; l += blockDim.x) r[l] = -own(l, pre.v1, bc) * t.itau;
     } else {
         const int p = t.parents[c];
         const float e = t.edgemst[c];
         for (int lp = threadIdx.x; lp < L3; lp += blockDim.x)
-            r[lp] = __ldcg(logp + (int64_t)p * L3 + lp) + M[(int64_t)c * L3 + lp] * t.itau;
+            r[lp] = __ldcg(logp + (int64_t)p * L3 + lp) + own(lp, pre.v0, M + (int64_t)c * L3) * t.itau;
         __syncthreads();
         const float off3[3] = {edge_off(t, c, 0), edge_off(t, c, 1), edge_off(t, c, 2)};
         sep_lse(r, t1, t2, r, len, L3, t.itau, off3, -1.0f);  // output index = child label
-        for (int l = threadIdx.x; l < L3; l += blockDim.x) r[l] += -e * bc[l] * t.itau;
+        for (int l = threadIdx.x; l < L3; l += blockDim.x) r[l] += -e * own(l, pre.v1, bc) * t.itau;
     }
     float mx = -INFINITY;
     for (int l = threadIdx.x; l < L3; l += blockDim.x) mx = fmaxf(mx, r[l]);
@@ -1304,9 +1349,9 @@ __device__ void node_down(const SoftTree& t, int c, const float* __restrict__ B,
 // Adjoint of the marginals (leaves to root):
 //   h(l) = gE_c . d(l) p_c(l) + sum_children R_k(l)    (= dL/dlog p_c)
 //   Bbar_c = -e h/tau (root: -(h - p sum h)/tau, projected to zero mean);  R_c = S^T h w.r.t. r
-__device__ void node_down_adj(const SoftTree& t, int c, const float* __restrict__ M, const float* __restrict__ logp,
-                              const float* __restrict__ gdisp, float* __restrict__ R, float* __restrict__ Bbar,
-                              float* sh) {
+__device__ void node_down_adj(const SoftTree& t, int c, const NodePre& pre, const float* __restrict__ M,
+                              const float* __restrict__ logp, const float* __restrict__ gdisp, float* __restrict__ R,
+                              float* __restrict__ Bbar, float* sh) {
     const int L3 = t.len3, len = t.len;
     float* r = sh;
     float* t1 = sh + L3;
@@ -1316,14 +1361,13 @@ __device__ void node_down_adj(const SoftTree& t, int c, const float* __restrict_
     float* wa = sh + 5 * L3;
     float* red = sh + 6 * L3;
     const float* lc = logp + (int64_t)c * L3;
-    const int k0 = t.child_ptr[c], k1 = t.child_ptr[c + 1];
     const float gu = gdisp[c], gv = gdisp[t.sz + c], gw = gdisp[2 * t.sz + c];
     float tot = 0.0f;
     for (int l = threadIdx.x; l < L3; l += blockDim.x) {
         const float du = (float)(((l / len) % len - t.hw) * t.q), dv = (float)((l % len - t.hw) * t.q),
                     dw = (float)((l / (len * len) - t.hw) * t.q);
-        float v = (gu * du + gv * dv + gw * dw) * __expf(lc[l]);
-        for (int ci = k0; ci < k1; ci++) v += __ldcg(R + (int64_t)t.children[ci] * L3 + l);
+        const float v = add_children(t, c, pre, l, (gu * du + gv * dv + gw * dw) * __expf(own(l, pre.v0, lc)), R,
+                                     nullptr);
         h[l] = v;
         tot += v;
     }
@@ -1332,7 +1376,7 @@ __device__ void node_down_adj(const SoftTree& t, int c, const float* __restrict_
         tot = block_sum(tot, red);
         float mean = 0.0f;
         for (int l = threadIdx.x; l < L3; l += blockDim.x) {
-            wa[l] = -(h[l] - __expf(lc[l]) * tot) * t.itau;
+            wa[l] = -(h[l] - __expf(own(l, pre.v0, lc)) * tot) * t.itau;
             mean += wa[l];
         }
         mean = block_sum(mean, red) / (float)L3;
@@ -1343,7 +1387,7 @@ __device__ void node_down_adj(const SoftTree& t, int c, const float* __restrict_
     const float e = t.edgemst[c];
     for (int l = threadIdx.x; l < L3; l += blockDim.x) {
         bb[l] = -e * t.itau * h[l];
-        r[l] = logp[(int64_t)p * L3 + l] + M[(int64_t)c * L3 + l] * t.itau;
+        r[l] = own(l, pre.v2, logp + (int64_t)p * L3) + own(l, pre.v1, M + (int64_t)c * L3) * t.itau;
     }
     __syncthreads();
     const float off3[3] = {edge_off(t, c, 0), edge_off(t, c, 1), edge_off(t, c, 2)};
@@ -1360,8 +1404,8 @@ __device__ void node_down_adj(const SoftTree& t, int c, const float* __restrict_
 //   dL/dB_c += -e/tau S^T(-tau Mbar_c) = e S^T(Mbar_c).  Bbar_c is final afterwards
 // (= dL/dC_c); the exact value sums to zero over labels (shift invariance), and
 // projecting keeps rounding from accumulating as a common mode down the tree.
-__device__ void node_up_adj(const SoftTree& t, int c, const float* __restrict__ B, const float* __restrict__ R,
-                            float* __restrict__ Bbar, float* sh) {
+__device__ void node_up_adj(const SoftTree& t, int c, const NodePre& pre, const float* __restrict__ B,
+                            const float* __restrict__ R, float* __restrict__ Bbar, float* sh) {
     if (c == t.root) return;
     const int L3 = t.len3, len = t.len;
     float* f = sh;
@@ -1374,8 +1418,8 @@ __device__ void node_up_adj(const SoftTree& t, int c, const float* __restrict__ 
     const int p = t.parents[c];
     const float e = t.edgemst[c];
     for (int l = threadIdx.x; l < L3; l += blockDim.x) {
-        f[l] = -e * B[(int64_t)c * L3 + l] * t.itau;
-        mb[l] = R[(int64_t)c * L3 + l] * t.itau + __ldcg(Bbar + (int64_t)p * L3 + l);
+        f[l] = -e * own(l, pre.v0, B + (int64_t)c * L3) * t.itau;
+        mb[l] = own(l, pre.v1, R + (int64_t)c * L3) * t.itau + __ldcg(Bbar + (int64_t)p * L3 + l);
     }
     __syncthreads();
     const float off3[3] = {edge_off(t, c, 0), edge_off(t, c, 1), edge_off(t, c, 2)};
@@ -1387,7 +1431,7 @@ __device__ void node_up_adj(const SoftTree& t, int c, const float* __restrict__ 
     float* bb = Bbar + (int64_t)c * L3;
     float mean = 0.0f;
     for (int l = threadIdx.x; l < L3; l += blockDim.x) {
-        wa[l] = bb[l] + e * wa[l];
+        wa[l] = own(l, pre.v2, bb) + e * wa[l];
         mean += wa[l];
     }
     mean = block_sum(mean, red) / (float)L3;
@@ -1437,11 +1481,47 @@ struct SweepArgs {
 };
 
 template <int KIND>
-__device__ __forceinline__ void run_node(const SoftTree& t, int c, const SweepArgs& a, float* sh) {
-    if (KIND == kSweepUp) node_up(t, c, a.cost, a.B, a.M, a.Mmin, sh);
-    else if (KIND == kSweepDown) node_down(t, c, a.B, a.M, a.logp, a.disp, sh);
-    else if (KIND == kSweepDownAdj) node_down_adj(t, c, a.M, a.logp, a.gdisp, a.R, a.Bbar, sh);
-    else node_up_adj(t, c, a.B, a.R, a.Bbar, sh);
+__device__ __forceinline__ void run_node(const SoftTree& t, int c, const NodePre& pre, const SweepArgs& a,
+                                         float* sh) {
+    if (KIND == kSweepUp) node_up(t, c, pre, a.cost, a.B, a.M, a.Mmin, sh);
+    else if (KIND == kSweepDown) node_down(t, c, pre, a.B, a.M, a.logp, a.disp, sh);
+    else if (KIND == kSweepDownAdj) node_down_adj(t, c, pre, a.M, a.logp, a.gdisp, a.R, a.Bbar, sh);
+    else node_up_adj(t, c, pre, a.B, a.R, a.Bbar, sh);
+}
+
+// The node's inputs that precede this sweep (see NodePre), loaded before the wait.
+template <int KIND>
+__device__ __forceinline__ NodePre prefetch_node(const SoftTree& t, int c, const SweepArgs& a) {
+    NodePre pre;
+    pre.v0 = pre.v1 = pre.v2 = 0.0f;
+    pre.nch = 0;
+    const int l = threadIdx.x;
+    const bool in = l < t.len3;
+    const int64_t row = (int64_t)c * t.len3 + l;
+    const bool root = c == t.root;
+    if (KIND == kSweepUp) {
+        if (in) pre.v0 = a.cost[row];
+        load_children(t, c, pre);
+    } else if (KIND == kSweepDown) {
+        if (in) {
+            if (!root) pre.v0 = a.M[row];
+            pre.v1 = a.B[row];
+        }
+    } else if (KIND == kSweepDownAdj) {
+        if (in) {
+            pre.v0 = a.logp[row];
+            if (!root) {
+                pre.v1 = a.M[row];
+                pre.v2 = a.logp[(int64_t)t.parents[c] * t.len3 + l];
+            }
+        }
+        load_children(t, c, pre);
+    } else if (!root && in) {
+        pre.v0 = a.B[row];
+        pre.v1 = a.R[row];
+        pre.v2 = a.Bbar[row];
+    }
+    return pre;
 }
 
 template <int KIND>
@@ -1455,6 +1535,7 @@ __global__ void k_soft_sweep(SoftTree t, const int* __restrict__ ordered, SweepA
         const int tk = s_tk;
         if (tk >= t.sz) break;
         const int c = ordered[kTopDown ? tk : t.sz - 1 - tk];
+        const NodePre pre = prefetch_node<KIND>(t, c, a);
         if (threadIdx.x == 0 && ld_acquire(st.err) == 0) {
             // top-down: the parent is released (done = 1); bottom-up: every child has arrived
             const int* flag = kTopDown ? (c == t.root ? nullptr : st.done + t.parents[c]) : st.done + c;
@@ -1471,7 +1552,7 @@ __global__ void k_soft_sweep(SoftTree t, const int* __restrict__ ordered, SweepA
             }
         }
         __syncthreads();
-        run_node<KIND>(t, c, a, sh);
+        run_node<KIND>(t, c, pre, a, sh);
         __syncthreads();
         if (threadIdx.x == 0) {
             __threadfence();
