@@ -30,7 +30,7 @@ EXPORTS = [
     "deeds_soft_warp_backward_dev",
     "deeds_linear_default_params", "deeds_linear_register", "deeds_linear_register_dev", "deeds_lin_warp_dev",
     "deeds_lin_smooth_dev", "deeds_estimate_affine_dev", "deeds_affine_robust", "deeds_affine_warp_segmentation",
-    "deeds_gz_write", "deeds_gz_read", "deeds_gz_last_error",
+    "deeds_gz_write", "deeds_gz_read", "deeds_gz_last_error", "deeds_selftest_bounded_waits",
 ]
 NOALLOC_MAX_NODES = 131072
 STAGES = ["mind", "datacost", "mst_edges", "bp_up", "bp_down", "transform", "consistent", "tree_wait"]
@@ -159,6 +159,7 @@ def load():
     L.deeds_gz_read.argtypes = [C.c_char_p, P, S, C.POINTER(S), I]
     L.deeds_gz_last_error.argtypes = []
     L.deeds_gz_last_error.restype = C.c_char_p
+    L.deeds_selftest_bounded_waits.argtypes = [P, P, P, P]
     for name in EXPORTS:
         fn = getattr(L, name)
         if name not in ("deeds_default_params", "deeds_destroy", "deeds_last_error", "deeds_version",

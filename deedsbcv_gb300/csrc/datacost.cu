@@ -39,12 +39,16 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, int count) {
 __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
+// One try_wait round, suspended at most kTryWaitNs (the suspend-time hint caps the
+// otherwise system-dependent suspension, so a wait of kWaitLimit rounds is bounded
+// by about kWaitLimit microseconds); returns as soon as the phase completes.
+constexpr uint32_t kTryWaitNs = 1000;
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}"
         : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(kTryWaitNs)
         : "memory");
     return ok != 0;
 }
@@ -55,7 +59,7 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
         : "memory");
 }
 
-constexpr long long kWaitLimit = 1LL << 20;  // try_wait rounds (each suspends up to a hardware time slice)
+constexpr long long kWaitLimit = 1LL << 20;  // try_wait rounds of at most kTryWaitNs each: ~1 s
 
 // Bounded wait of one thread on an mbarrier phase; false if the limit expired.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
@@ -404,6 +408,25 @@ __global__ void k_popc_probe(int iters, unsigned long long* sink) {
 
 cudaError_t launch_popc_probe(int blocks, int threads, int iters, unsigned long long* d_sink, cudaStream_t s) {
     k_popc_probe<<<blocks, threads, 0, s>>>(iters, d_sink);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+namespace {
+// Self-test of the cost volume's bounded mbarrier wait: an mbarrier that expects
+// one arrival which never comes; status = 1 if the wait gave up, 2 otherwise.
+__global__ void k_selftest_mbar_wait(int* status) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        *status = mbar_wait_bounded(&bar, 0) ? 2 : 1;
+    }
+}
+}  // namespace
+
+cudaError_t launch_selftest_mbar_wait(int* status, cudaStream_t s) {
+    k_selftest_mbar_wait<<<1, 32, 0, s>>>(status);
     count_launches(1);
     return cudaGetLastError();
 }

@@ -116,6 +116,9 @@ cudaError_t launch_lin_smooth(float* d_c0, float* d_c1, int m1, int n1, int o1, 
 cudaError_t launch_lin_node_stats(const float* d_c0, const float* d_c1, const float* d_fixed, const float* d_moving,
                                   int m, int n, int o, int g, int len3, float* d_minval, int* d_minind,
                                   cudaStream_t s);
+// Self-tests of the bounded device-side waits (a flag / an mbarrier nothing releases).
+cudaError_t launch_selftest_flag_wait(const int* flag, int* err, int* status, cudaStream_t s);
+cudaError_t launch_selftest_mbar_wait(int* status, cudaStream_t s);
 cudaError_t launch_popc_probe(int blocks, int threads, int iters, unsigned long long* d_sink, cudaStream_t s);
 cudaError_t launch_jacobian(const float* u, const float* v, const float* w, int m, int n, int o, int g, double* d_acc,
                             cudaStream_t s);

@@ -1623,4 +1623,24 @@ deeds_status deeds_linear_register(deeds_ctx* ctx, const float* fixed, const flo
     return deeds_linear_register_dev(ctx, d_f, d_m, m, n, o, params, X_out, s);
 }
 
+deeds_status deeds_selftest_bounded_waits(deeds_ctx* ctx, int* sweep_gave_up, int* tma_gave_up, double* seconds) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    CK(cudaSetDevice(ctx->device));
+    deeds_status st = DEEDS_OK;
+    int* d = dbuf<int>(ctx, "selftest", 4, &st);
+    if (st) return st;
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemsetAsync(d, 0, 4 * sizeof(int), s));  // flag (never set), error word, two statuses
+    const auto t0 = std::chrono::steady_clock::now();
+    CK(launch_selftest_flag_wait(d, d + 1, d + 2, s));
+    CK(launch_selftest_mbar_wait(d + 3, s));
+    int h[4] = {0, 0, 0, 0};
+    CK(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (sweep_gave_up) *sweep_gave_up = h[2] == 1 && h[1] == 1;
+    if (tma_gave_up) *tma_gave_up = h[3] == 1;
+    return DEEDS_OK;
+}
+
 }  // extern "C"

@@ -1452,7 +1452,6 @@ __device__ void node_up_adj(const SoftTree& t, int c, const NodePre& pre, const 
 // node's children continues with the node, measured 6-9 % slower: claiming in
 // breadth order keeps each level's nodes in flight together.)
 
-constexpr long long kSweepSpinLimit = 1LL << 21;
 
 struct SweepState {
     int* ticket;  // next ticket
@@ -1467,6 +1466,22 @@ __device__ __forceinline__ int ld_acquire(const int* p) {
 }
 
 enum SweepKind { kSweepUp = 0, kSweepDown = 1, kSweepDownAdj = 2, kSweepUpAdj = 3 };
+
+constexpr long long kSweepSpinLimitV = 1LL << 21;  // ~0.13 s of 64 ns sleeps
+
+// Bounded wait of one thread until *flag >= need; on expiry sets *err and returns
+// false (the caller then skips every further wait).
+__device__ __forceinline__ bool bounded_wait_geq(const int* flag, int need, int* err) {
+    long long it = 0;
+    while (ld_acquire(flag) < need) {
+        if (++it > kSweepSpinLimitV) {
+            atomicExch(err, 1);
+            return false;
+        }
+        __nanosleep(64);
+    }
+    return true;
+}
 
 struct SweepArgs {
     const float* cost;
@@ -1540,16 +1555,7 @@ __global__ void k_soft_sweep(SoftTree t, const int* __restrict__ ordered, SweepA
             // top-down: the parent is released (done = 1); bottom-up: every child has arrived
             const int* flag = kTopDown ? (c == t.root ? nullptr : st.done + t.parents[c]) : st.done + c;
             const int need = kTopDown ? 1 : t.child_ptr[c + 1] - t.child_ptr[c];
-            if (flag && need > 0) {
-                long long it = 0;
-                while (ld_acquire(flag) < need) {
-                    if (++it > kSweepSpinLimit) {
-                        atomicExch(st.err, 1);
-                        break;
-                    }
-                    __nanosleep(64);
-                }
-            }
+            if (flag && need > 0) bounded_wait_geq(flag, need, st.err);
         }
         __syncthreads();
         run_node<KIND>(t, c, pre, a, sh);
@@ -1905,6 +1911,18 @@ cudaError_t launch_soft_tree_backward(const SoftTreeDev& d, int* sweep_mem, cons
     cudaError_t e = run_sweep<kSweepDownAdj>(t, d.ordered, a, st, sweep_mem, s);
     if (e == cudaSuccess) e = run_sweep<kSweepUpAdj>(t, d.ordered, a, st, sweep_mem, s);
     return e;
+}
+
+// Self-test of the sweeps' bounded wait: one thread waits on a flag that nothing
+// sets; status = 1 if the wait gave up and set the error word, 2 otherwise.
+__global__ void k_selftest_flag_wait(const int* flag, int* err, int* status) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *status = bounded_wait_geq(flag, 1, err) ? 2 : 1;
+}
+
+cudaError_t launch_selftest_flag_wait(const int* flag, int* err, int* status, cudaStream_t s) {
+    k_selftest_flag_wait<<<1, 32, 0, s>>>(flag, err, status);
+    count_launches(1);
+    return cudaGetLastError();
 }
 
 }  // namespace deeds

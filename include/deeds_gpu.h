@@ -362,6 +362,13 @@ deeds_status deeds_estimate_affine_dev(deeds_ctx* ctx, const float* d_fixed, con
  * (y | x | z | 1, len points each). */
 deeds_status deeds_affine_robust(const float* pts1, const float* pts2, int len, int rigid, float RT[16]);
 
+/* Self-test of the bounded device-side waits: the tree sweeps' wait on a flag and
+ * the cost volume's wait on a TMA mbarrier are each run on a flag / barrier that
+ * nothing releases; *sweep_gave_up / *tma_gave_up are set to 1 when the wait
+ * expired and reported it (the error word for the sweep), *seconds to the time
+ * both took.  The context stays usable afterwards. */
+deeds_status deeds_selftest_bounded_waits(deeds_ctx* ctx, int* sweep_gave_up, int* tma_gave_up, double* seconds);
+
 /* ---------------------------------------------------------------------------
  * Parallel gzip IO for NIfTI volumes (host only; the reference uses single-
  * threaded zlib, src/imageIOgzType.h:14-26, 212-218).  deeds_gz_write deflates
