@@ -82,6 +82,9 @@ __global__ void k_soft_sqdiff(const float* __restrict__ im, float* __restrict__ 
 // descriptor its float32 accuracy).  The operator is symmetric, so the same
 // kernel is its own adjoint.  Grid: x over i, y over j (32 x 8 blocks), z over
 // (k, channel): no index divisions by runtime sizes.
+// R > 0: compile-time radius (window loads unrolled and issued together); R = 0:
+// the radius r at run time.
+template <int R>
 __global__ void k_soft_box(const float* __restrict__ in, float* __restrict__ out, int m, int n, int o, int r, int axis) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -95,9 +98,20 @@ __global__ void k_soft_box(const float* __restrict__ in, float* __restrict__ out
     else if (axis == 1) { L = n; stride = m; c = j; }
     else { L = o; stride = mn; c = k; }
     const float* x = in + (p - (int64_t)c * stride);
-    const int a0 = max(0, c - r), a1 = min(L - 1, c + r);
     float acc = 0.0f;
-    for (int a = a0; a <= a1; a++) acc += x[a * stride];
+    if (R > 0) {
+        float v[2 * R + 1];
+#pragma unroll
+        for (int d = -R; d <= R; d++) {
+            const int a = c + d;
+            v[d + R] = (a >= 0 && a < L) ? __ldg(x + a * stride) : 0.0f;
+        }
+#pragma unroll
+        for (int d = 0; d <= 2 * R; d++) acc += v[d];
+    } else {
+        const int a0 = max(0, c - r), a1 = min(L - 1, c + r);
+        for (int a = a0; a <= a1; a++) acc += x[a * stride];
+    }
     out[p] = acc;
 }
 
@@ -1625,11 +1639,21 @@ __global__ void k_soft_offbar_to_prior(const float* __restrict__ offbar, const i
 // Host drivers
 
 // three box passes a -> b -> a -> b; the result is in b
-static void box3(float* a, float* b, int m, int n, int o, int r, cudaStream_t st) {
+template <int R>
+static void box3_r(float* a, float* b, int m, int n, int o, int r, cudaStream_t st) {
     const dim3 blk(32, 8), grid(blocks_for(m, 32), blocks_for(n, 8), 6 * o);
-    k_soft_box<<<grid, blk, 0, st>>>(a, b, m, n, o, r, 0);
-    k_soft_box<<<grid, blk, 0, st>>>(b, a, m, n, o, r, 1);
-    k_soft_box<<<grid, blk, 0, st>>>(a, b, m, n, o, r, 2);
+    k_soft_box<R><<<grid, blk, 0, st>>>(a, b, m, n, o, r, 0);
+    k_soft_box<R><<<grid, blk, 0, st>>>(b, a, m, n, o, r, 1);
+    k_soft_box<R><<<grid, blk, 0, st>>>(a, b, m, n, o, r, 2);
+}
+
+static void box3(float* a, float* b, int m, int n, int o, int r, cudaStream_t st) {
+    switch (r) {
+        case 1: box3_r<1>(a, b, m, n, o, r, st); break;
+        case 2: box3_r<2>(a, b, m, n, o, r, st); break;
+        case 3: box3_r<3>(a, b, m, n, o, r, st); break;
+        default: box3_r<0>(a, b, m, n, o, r, st); break;
+    }
 }
 
 cudaError_t launch_soft_offsets(const float* prior, const int* parents, int root, int sz, float q, float* off,
