@@ -67,6 +67,15 @@ int main(int argc, char** argv) {
         return -1;
     }
     const int m = vf.m, n = vf.n, o = vf.o;
+    std::string lv[3];
+    for (int l = 0; l < a.levels; l++) {
+        const char* sep = l ? "x" : "";
+        lv[0] += sep + std::to_string(a.grid[l]);
+        lv[1] += sep + std::to_string(a.search[l]);
+        lv[2] += sep + std::to_string(a.quant[l]);
+    }
+    std::printf("levels=%d G=%s L=%s Q=%s %s\n", a.levels, lv[0].c_str(), lv[1].c_str(), lv[2].c_str(),
+                a.rigid ? "rigid" : "affine");
     deeds_linear_params p;
     deeds_linear_default_params(&p);
     p.levels = a.levels;

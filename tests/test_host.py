@@ -141,3 +141,34 @@ def test_cli_mismatch_warning(pair_files):
     f, m, out = pair_files
     r = _cli("-F", f, "-M", m, "-O", out, "-G", "6x5x4", "-L", "5x4")
     assert "#grid=3, #search=2" in r.stdout
+
+
+def _linear_cli(*args):
+    exe = os.path.join(BUILD, "linearBCV")
+    if not os.path.exists(exe):
+        pytest.skip("CLI not built")
+    return subprocess.run([exe, *args], capture_output=True, text=True, timeout=60)
+
+
+@pytest.mark.parametrize("flags,expect", [
+    ([], "levels=4 G=7x6x5x4 L=5x4x3x2 Q=4x3x2x1 affine"),  # src/linearBCV.cpp:86-89
+    (["-G", "6x5", "-L", "4x3", "-Q", "3x2"], "levels=2 G=6x5 L=4x3 Q=3x2 affine"),
+    (["-R", "1"], "levels=4 G=7x6x5x4 L=5x4x3x2 Q=4x3x2x1 rigid"),
+])
+def test_linear_cli_parses_like_reference(pair_files, flags, expect):
+    f, m, out = pair_files
+    r = _linear_cli("-F", f, "-M", m, "-O", out, *flags)
+    assert "Starting linear reg. of f.nii.gz and m.nii.gz" in r.stdout
+    assert expect in r.stdout, r.stdout
+    if "-R" in flags:
+        assert "Searching only for rigid (6 parameter) transform" in r.stdout
+
+
+def test_linear_cli_usage_and_non_gz(tmp_path, pair_files):
+    r = _linear_cli("-h", "x", "y")
+    assert r.returncode == 1 and "./linearBCV -F fixed.nii.gz -M moving.nii.gz -O output" in r.stdout
+    f, m, out = pair_files
+    plain = tmp_path / "f.nii"
+    plain.write_bytes(b"\0" * 400)
+    r = _linear_cli("-F", str(plain), "-M", m, "-O", out)
+    assert "images must have nii.gz format" in r.stdout and r.returncode != 0
