@@ -116,6 +116,32 @@ struct StageScope {
     }
 };
 
+// Host timeline of one registration (DEEDS_TRACE=1 in the environment): the
+// moments the host-side inputs of the trees become ready, each tree is built and
+// the level loop stops waiting for it, printed to stderr at the end.
+struct Timeline {
+    bool on = false;
+    std::chrono::steady_clock::time_point t0;
+    std::mutex mu;
+    std::vector<std::pair<std::string, double>> ev;
+    void start() {
+        const char* e = std::getenv("DEEDS_TRACE");
+        on = e && e[0] == '1';
+        t0 = std::chrono::steady_clock::now();
+    }
+    void mark(const std::string& what) {
+        if (!on) return;
+        const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        std::lock_guard<std::mutex> lock(mu);
+        ev.emplace_back(what, ms);
+    }
+    void dump() {
+        if (!on) return;
+        std::lock_guard<std::mutex> lock(mu);
+        for (auto& e : ev) std::fprintf(stderr, "deeds trace %8.2f ms  %s\n", e.second, e.first.c_str());
+    }
+};
+
 void collect_marks(deeds_ctx* c) {
     for (auto& mk : c->marks) {
         float ms = 0.0f;
@@ -694,6 +720,8 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
     float thr[5];
     mind_thresholds(thr);
 
+    Timeline tl;
+    tl.start();
     PairBuffers B;
     st = acquire_buffers(ctx, m, n, o, P, B);
     if (st) return st;
@@ -771,11 +799,14 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
     std::thread builder([&, ev_images, ev_sads, dev]() {
         cudaSetDevice(dev);
         cudaEventSynchronize(ev_images);
+        tl.mark("images on host");
         float mean_f, sd_f, mean_w, sd_w;
         std::thread tw([&]() { image_stats(h_w0, sz, &mean_w, &sd_w); });
         image_stats(h_fix, sz, &mean_f, &sd_f);
         tw.join();
+        tl.mark("image statistics");
         cudaEventSynchronize(ev_sads);
+        tl.mark("block SADs on host");
         // finest trees are the slowest: start the workers in reverse level order
         std::vector<std::thread> workers;
         for (int t = 2 * L - 1; t >= 0; t--) {
@@ -783,6 +814,7 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
                 const int l = t / 2, d = t % 2;
                 try {
                     build_tree(h_sad[t], d == 0 ? sd_f : sd_w, m1s[l], n1s[l], o1s[l], P->grid[l], h_tree[t], pts[t]);
+                    tl.mark("tree level " + std::to_string(l) + (d ? " backward" : " forward") + " built");
                     ready[t].set_value();
                 } catch (...) {
                     ready[t].set_exception(std::current_exception());
@@ -844,6 +876,7 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
             const int t = 2 * l + d;
             {
                 const auto w0 = std::chrono::steady_clock::now();
+                tl.mark("level " + std::to_string(l) + (d ? " backward" : " forward") + " waits for its tree");
                 try {
                     ready_f[t].get();
                 } catch (const std::exception& ex) {
@@ -886,8 +919,11 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
     }
     int herr[2] = {0, 0};
     CK(cudaMemcpyAsync(herr, d_err, sizeof(herr), cudaMemcpyDeviceToHost, s));
+    tl.mark("all work queued");
     CK(cudaStreamSynchronize(s));
+    tl.mark("device done");
     if (builder.joinable()) builder.join();
+    tl.dump();
     if (ctx->prof) collect_marks(ctx);
     if (herr[0] == 3 || herr[1] == 3) return fail(ctx, DEEDS_ERR_TIMEOUT, "cost volume: a bounded wait for a TMA copy expired");
     if (herr[0] || herr[1])
