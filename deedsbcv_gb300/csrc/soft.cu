@@ -378,6 +378,87 @@ __global__ void k_soft_cost_adj_moving(const float* __restrict__ sF, const float
     for (int c = 0; c < 12; c++) sMbar[c * sz + qv] = -G.alpha1 * acc[c];
 }
 
+// The same gather with the grid spacing, label width and quantisation fixed at
+// compile time (the row-form level shapes): the label and sample loops unroll
+// and the node and lattice arithmetic uses constants.
+template <int G_, int LEN_, int Q_>
+__global__ void __launch_bounds__(128) k_soft_cost_adj_moving_t(const float* __restrict__ sF,
+                                                               const float* __restrict__ sM,
+                                                               const float* __restrict__ cbar,
+                                                               float* __restrict__ sMbar, SoftGeom G) {
+    constexpr int S = G_ > 4 ? 2 : 1, HW = (LEN_ - 1) / 2, LEN3 = LEN_ * LEN_ * LEN_;
+    const int64_t mn = (int64_t)G.m * G.n, sz = mn * G.o;
+    const int64_t qv = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (qv >= sz) return;
+    const int qi = (int)(qv % G.m), qj = (int)((qv / G.m) % G.n), qk = (int)(qv / mn);
+    float mq[12], acc[12];
+#pragma unroll
+    for (int c = 0; c < 12; c++) {
+        mq[c] = sM[c * sz + qv];
+        acc[c] = 0.0f;
+    }
+    const int ci = G.m1 * G_, cj = G.n1 * G_, ck = G.o1 * G_;
+    const float eps = G.eps;
+    constexpr int R = HW * Q_;
+    // away from the y faces every label has exactly one y preimage, qi - dy, inside
+    // the node-covered extent: a straight-line path whose loads can be issued together
+    const bool yint = qi >= (R > 1 ? R : 1) && qi <= min(ci - 1 - R, G.m - 2);
+    for (int lz = 0; lz < LEN_; lz++) {
+        int k0, k1;
+        preimage(qk, (lz - HW) * Q_, G.o, ck, k0, k1);
+        for (int pk = k0; pk <= k1; pk++) {
+            if (S > 1 && (pk % G_) % S) continue;
+            for (int lx = 0; lx < LEN_; lx++) {
+                int j0, j1;
+                preimage(qj, (lx - HW) * Q_, G.n, cj, j0, j1);
+                for (int pj = j0; pj <= j1; pj++) {
+                    if (S > 1 && (pj % G_) % S) continue;
+                    const int nbase = (pj / G_) * G.m1 + (pk / G_) * G.m1 * G.n1;
+                    const float* cbl = cbar + (int64_t)(lx * LEN_ + lz * LEN_ * LEN_);
+                    const float* fpk = sF + (int64_t)pj * G.m + (int64_t)pk * mn;
+                    if (yint) {
+                        float cbv[LEN_];
+#pragma unroll
+                        for (int ly = 0; ly < LEN_; ly++) {
+                            const int pi = qi - (ly - HW) * Q_;
+                            cbv[ly] = __ldg(cbl + (int64_t)(nbase + pi / G_) * LEN3 + ly);
+                        }
+#pragma unroll
+                        for (int ly = 0; ly < LEN_; ly++) {
+                            const float* fp = fpk + qi - (ly - HW) * Q_;
+#pragma unroll
+                            for (int c = 0; c < 12; c++)
+                                acc[c] += cbv[ly] * phi_grad(__ldg(fp + c * sz) - mq[c], eps);
+                        }
+                    } else {
+                        for (int ly = 0; ly < LEN_; ly++) {
+                            int i0, i1;
+                            preimage(qi, (ly - HW) * Q_, G.m, ci, i0, i1);
+                            for (int pi = i0; pi <= i1; pi++) {
+                                const float cb = __ldg(cbl + (int64_t)(nbase + pi / G_) * LEN3 + ly);
+                                const float* fp = fpk + pi;
+#pragma unroll
+                                for (int c = 0; c < 12; c++)
+                                    acc[c] += cb * phi_grad(__ldg(fp + c * sz) - mq[c], eps);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 12; c++) sMbar[c * sz + qv] = -G.alpha1 * acc[c];
+}
+
+template <int G_, int LEN_, int Q_>
+static cudaError_t run_adj_moving_t(const SoftGeom& G, const float* sF, const float* sM, const float* cbar,
+                                    float* sMbar, cudaStream_t st) {
+    const int64_t sz = (int64_t)G.m * G.n * G.o;
+    k_soft_cost_adj_moving_t<G_, LEN_, Q_><<<(unsigned)((sz + 127) / 128), 128, 0, st>>>(sF, sM, cbar, sMbar, G);
+    return cudaSuccess;
+}
+
 // ---------------------------------------------------------------------------
 // Halo form of the cost and its adjoint.  The moving descriptor values that one
 // node's samples reach under every label form one box (the node block grown by
@@ -1854,7 +1935,8 @@ cudaError_t launch_soft_cost_adj(const float* sF, const float* sM, const float* 
         cudaError_t e = cudaErrorNotSupported;
         switch (rs) { DEEDS_ROW_CASES(run_cost_adjF_rows, G, sF, sM, cbar, cost, sFbar, dot, st) default: break; }
         if (e != cudaSuccess) return e;
-        k_soft_cost_adj_moving<<<blocks_for(sz, 128), 128, 0, st>>>(sF, sM, cbar, sMbar, G);
+        switch (rs) { DEEDS_ROW_CASES(run_adj_moving_t, G, sF, sM, cbar, sMbar, st) default: break; }
+        if (e != cudaSuccess) return e;
         count_launches(2);
         return cudaGetLastError();
     }
