@@ -40,6 +40,16 @@ namespace {
 
 __device__ __forceinline__ float ld_cg(const float* p) { return __ldcg(p); }
 
+// Arrival counter increment with release and acquire semantics at GPU scope: the
+// CTA's earlier writes (made visible to this thread by the preceding barrier) are
+// released to whoever later observes the count, and this thread acquires every
+// sibling's released writes; a following barrier passes them on to the CTA.
+__device__ __forceinline__ int atom_add_acq_rel(int* p, int v) {
+    int old;
+    asm volatile("atom.add.acq_rel.gpu.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
 constexpr int bp_threads(int len) {
     return ((len * len + 31) / 32) * 32 < 64 ? 64 : ((len * len + 31) / 32) * 32;
 }
@@ -159,9 +169,7 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
                 // siblings exist: the last of them to arrive continues with the parent
                 if (tid == 0) {
                     mins[node] = mn;
-                    __threadfence();
-                    s_last = atomicAdd(arrived + p, 1) == c1 - c0 - 1;
-                    __threadfence();
+                    s_last = atom_add_acq_rel(arrived + p, 1) == c1 - c0 - 1;
                 }
                 __syncthreads();
                 if (!s_last) break;

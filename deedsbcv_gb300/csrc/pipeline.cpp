@@ -135,10 +135,26 @@ struct Timeline {
         std::lock_guard<std::mutex> lock(mu);
         ev.emplace_back(what, ms);
     }
+    // device-side marks: an event recorded on `s`, reported against the first one
+    std::vector<std::pair<std::string, cudaEvent_t>> dev;
+    void dmark(const std::string& what, cudaStream_t s) {
+        if (!on) return;
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return;
+        cudaEventRecord(e, s);
+        dev.emplace_back(what, e);
+    }
     void dump() {
         if (!on) return;
         std::lock_guard<std::mutex> lock(mu);
         for (auto& e : ev) std::fprintf(stderr, "deeds trace %8.2f ms  %s\n", e.second, e.first.c_str());
+        for (auto& d : dev) {
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, dev.front().second, d.second);
+            std::fprintf(stderr, "deeds trace device +%8.2f ms  %s\n", ms, d.first.c_str());
+        }
+        for (auto& d : dev) cudaEventDestroy(d.second);
+        dev.clear();
     }
 };
 
@@ -763,6 +779,7 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
     }
 
     // ---- inputs, affine-only warp of the moving image
+    tl.dmark("start", s);
     CK(cudaMemsetAsync(d_err, 0, 2 * sizeof(int), s));
     CK(launch_shift(d_fixed, fix, (int64_t)sz, P->intensity_shift, s));
     CK(launch_shift(d_moving, mov, (int64_t)sz, P->intensity_shift, s));
@@ -886,10 +903,12 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
                     ctx->stage_ms[DEEDS_STAGE_TREE_WAIT] +=
                         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
             }
+            tl.dmark("level " + std::to_string(l) + (d ? " backward" : " forward") + " BP starts", sd[d]);
             st = run_tree_bp(ctx, tags[d], pts[t], h_tree[t], cost[d], allinds[d], len, q, cur0[3 * d],
                              cur0[3 * d + 1], cur0[3 * d + 2], nxt[3 * d], nxt[3 * d + 1], nxt[3 * d + 2], d_err + d,
                              sd[d]);
             if (st) return st;
+            tl.dmark("level " + std::to_string(l) + (d ? " backward" : " forward") + " BP done", sd[d]);
         }
         CK(cudaEventRecord(ctx->ev_d, sd[1]));
         CK(cudaStreamWaitEvent(s, ctx->ev_d, 0));
@@ -917,6 +936,7 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
         CK(launch_warp_affine(mov, X, f, m, n, o, warped[0], ku, kv, kw, s));
         if (d_warped_out) CK(launch_shift(warped[0], d_warped_out, (int64_t)sz, -P->intensity_shift, s));
     }
+    tl.dmark("output done", s);
     int herr[2] = {0, 0};
     CK(cudaMemcpyAsync(herr, d_err, sizeof(herr), cudaMemcpyDeviceToHost, s));
     tl.mark("all work queued");
