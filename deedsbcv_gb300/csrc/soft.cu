@@ -1562,6 +1562,17 @@ __device__ __forceinline__ int ld_acquire(const int* p) {
 
 enum SweepKind { kSweepUp = 0, kSweepDown = 1, kSweepDownAdj = 2, kSweepUpAdj = 3 };
 
+// Publishing a finished node: a release store (top-down: the node is done) or a
+// release reduction (bottom-up: one more child of the parent has arrived) at GPU
+// scope; the preceding block barrier makes every thread's writes of the node part
+// of what is released, and waiters read the flag with ld.acquire.
+__device__ __forceinline__ void st_release(int* p, int v) {
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void red_release_add(int* p, int v) {
+    asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 constexpr long long kSweepSpinLimitV = 1LL << 21;  // ~0.13 s of 64 ns sleeps
 
 // Bounded wait of one thread until *flag >= need; on expiry sets *err and returns
@@ -1656,9 +1667,8 @@ __global__ void k_soft_sweep(SoftTree t, const int* __restrict__ ordered, SweepA
         run_node<KIND>(t, c, pre, a, sh);
         __syncthreads();
         if (threadIdx.x == 0) {
-            __threadfence();
-            if (kTopDown) atomicExch(st.done + c, 1);
-            else if (c != t.root) atomicAdd(st.done + t.parents[c], 1);
+            if (kTopDown) st_release(st.done + c, 1);
+            else if (c != t.root) red_release_add(st.done + t.parents[c], 1);
         }
     }
 }
