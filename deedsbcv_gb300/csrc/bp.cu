@@ -130,9 +130,14 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
             const float* row = cost + (int64_t)node * LEN3;
             for (int l = tid; l < LEN3; l += T) A[l] = __fmul_rn(ld_cg(row + l), e);
         }
+        // The chain's static tree data (parent, child range, displacements, edge
+        // weight) is loaded one step ahead, so a step begins without a dependent
+        // load and the next step's loads overlap this step's transform.
+        int p = t.parents[node];
+        int c0 = t.child_ptr[p], c1 = t.child_ptr[p + 1];
+        float un = t.u0[node], vn = t.v0[node], wn = t.w0[node];
+        float up = t.u0[p], vp = t.v0[p], wp = t.w0[p];
         for (;;) {
-            const int p = t.parents[node];
-            const int c0 = t.child_ptr[p], c1 = t.child_ptr[p + 1];
             // the parent's row still holds its data cost (it is only written after its
             // own message): load it now, its latency hides behind the transform
             float acc[NL];
@@ -142,9 +147,16 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
                 const int l = tid + k * T;
                 acc[k] = l < LEN3 ? ld_cg(prow + l) : 0.0f;
             }
-            const float ox = __fdiv_rn(t.u0[p] - t.u0[node], t.q);
-            const float oy = __fdiv_rn(t.v0[p] - t.v0[node], t.q);
-            const float oz = __fdiv_rn(t.w0[p] - t.w0[node], t.q);
+            const float ox = __fdiv_rn(up - un, t.q);
+            const float oy = __fdiv_rn(vp - vn, t.q);
+            const float oz = __fdiv_rn(wp - wn, t.q);
+            // next step: the grandparent's data and the parent's edge weight
+            const bool up_more = p != t.root;
+            const int gp = up_more ? t.parents[p] : p;
+            const float ep = up_more ? t.edgemst[p] : 0.0f;
+            const int gc0 = up_more ? t.child_ptr[gp] : 0, gc1 = up_more ? t.child_ptr[gp + 1] : 0;
+            const float ugp = up_more ? t.u0[gp] : 0.0f, vgp = up_more ? t.v0[gp] : 0.0f,
+                        wgp = up_more ? t.w0[gp] : 0.0f;
             __syncthreads();
             dt_lines<LEN, 0>(A, B, nullptr, ia, oy);
             __syncthreads();
@@ -203,14 +215,16 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
                 }
                 break;
             }
-            const float e = t.edgemst[p];
             __syncthreads();  // B (this message) has been consumed by every thread
 #pragma unroll
             for (int k = 0; k < NL; k++) {
                 const int l = tid + k * T;
-                if (l < LEN3) A[l] = __fmul_rn(acc[k], e);
+                if (l < LEN3) A[l] = __fmul_rn(acc[k], ep);
             }
             node = p;
+            un = up; vn = vp; wn = wp;
+            p = gp; c0 = gc0; c1 = gc1;
+            up = ugp; vp = vgp; wp = wgp;
         }
     }
 }
