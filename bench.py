@@ -280,11 +280,11 @@ def measure_soft(api, ctx, n_pairs=4, levels=SOFT_LEVELS, taus=SOFT_TAUS, shape=
         trees = [api.soft_tree(fx, m, n, o, lv[0], ctx) for lv in levels]
         data.append((fx, mv, torch.from_numpy(gt.astype(np.float32)).cuda(), trees))
 
-    def step(fx, mv, gt, trees, tau, backward=True):
+    def step(fx, mv, gt, trees, tau, backward=True, keep=True):
         F = fx.detach().requires_grad_(backward)
         M = mv.detach().requires_grad_(backward)
         a = torch.tensor(1.6, requires_grad=backward)
-        disp = api.soft_register_levels(F, M, a, shape, levels, tau=tau, trees=trees, ctx=ctx)
+        disp = api.soft_register_levels(F, M, a, shape, levels, tau=tau, trees=trees, ctx=ctx, keep_state=keep)
         loss = ((disp - gt) ** 2).mean()
         if backward:
             loss.backward()
@@ -297,14 +297,17 @@ def measure_soft(api, ctx, n_pairs=4, levels=SOFT_LEVELS, taus=SOFT_TAUS, shape=
         for fx, mv, gt, tree in data[:1]:
             step(fx, mv, gt, tree, tau)  # warm-up: buffers
         res = {}
-        for mode in ("forward", "forward_backward"):
+        # forward_backward keeps each level's forward state on the device for its
+        # backward; forward_backward_recompute is the memory-saving form whose
+        # backward recomputes it
+        for mode in ("forward", "forward_backward", "forward_backward_recompute"):
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
             losses = []
-            gnorm = 0.0
             for fx, mv, gt, tree in data:
-                loss, gf, gm, ga = step(fx, mv, gt, tree, tau, backward=(mode == "forward_backward"))
+                loss, gf, gm, ga = step(fx, mv, gt, tree, tau, backward=(mode != "forward"),
+                                        keep=(mode != "forward_backward_recompute"))
                 losses.append(loss)
             e1.record()
             torch.cuda.synchronize()

@@ -436,19 +436,39 @@ def _ptr(t):
     return C.c_void_p(t.data_ptr()) if t is not None else None
 
 
+class _KeptSoftState:
+    """A library slot that holds one soft level's forward state; released when
+    the backward has used it or when the autograd node goes away."""
+
+    def __init__(self, dctx, slot):
+        self.dctx, self.slot = dctx, slot
+
+    def release(self):
+        if self.slot is not None and self.dctx.handle:
+            self.dctx._L.deeds_soft_release(self.dctx.handle, self.slot)
+        self.slot = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
 class SoftDeedsLevel(torch.autograd.Function if torch is not None else object):
     """Expected displacement (3, sz1) [u, v, w] of one soft-min deeds level.
 
-    forward(fixed, moving, alpha, prior, dims, params, tree, ctx): fixed/moving are
-    flat float32 CUDA tensors (i fastest), alpha a 0-d tensor (its value replaces
-    params.alpha), prior None or the current grid field (3, sz1) that the pairwise
-    term is taken relative to (src/regularisation.h:205-208), tree = (ordered,
-    parents, edgemst) host arrays of the fixed image's MST at params.grid.  Backward
-    runs the library's adjoint kernels, which recompute the forward sweeps instead
-    of keeping message tensors."""
+    forward(fixed, moving, alpha, prior, dims, params, tree, ctx, keep): fixed/moving
+    are flat float32 CUDA tensors (i fastest), alpha a 0-d tensor (its value
+    replaces params.alpha), prior None or the current grid field (3, sz1) that the
+    pairwise term is taken relative to (src/regularisation.h:205-208), tree =
+    (ordered, parents, edgemst) host arrays of the fixed image's MST at params.grid.
+    With keep (and a gradient wanted) the library keeps the level's descriptors,
+    cost volume, messages and marginals on the device and the backward runs only
+    the adjoint kernels; without it the backward recomputes the forward state."""
 
     @staticmethod
-    def forward(fctx, fixed, moving, alpha, prior, dims, params, tree, dctx):
+    def forward(fctx, fixed, moving, alpha, prior, dims, params, tree, dctx, keep=True):
         params = soft_params(params.grid, params.radius, params.quant, float(alpha.detach()), params.tau, params.eps,
                              params.mind_radius)
         tree = _tree_arrays(tree)
@@ -461,8 +481,15 @@ class SoftDeedsLevel(torch.autograd.Function if torch is not None else object):
         if prior is not None:
             prior_c = prior.detach().contiguous()
             _dev(prior_c, torch.float32, 3 * sz1, "prior")
-        _soft_call(dctx, dctx._L.deeds_soft_forward_dev, fixed_c, moving_c, dims, params, tree, _ptr(prior_c),
-                   _ptr(out))
+        fctx.kept = None
+        if keep and any(fctx.needs_input_grad[:4]):
+            slot = C.c_int(-1)
+            _soft_call(dctx, dctx._L.deeds_soft_forward_keep_dev, fixed_c, moving_c, dims, params, tree,
+                       _ptr(prior_c), _ptr(out), C.byref(slot))
+            fctx.kept = _KeptSoftState(dctx, slot.value)
+        else:
+            _soft_call(dctx, dctx._L.deeds_soft_forward_dev, fixed_c, moving_c, dims, params, tree, _ptr(prior_c),
+                       _ptr(out))
         fctx.save_for_backward(fixed_c, moving_c, prior_c)
         fctx.soft = (dims, params, tree, dctx)
         fctx.alpha_like = (alpha.dtype, alpha.device) if isinstance(alpha, torch.Tensor) else (torch.float32, "cpu")
@@ -478,11 +505,20 @@ class SoftDeedsLevel(torch.autograd.Function if torch is not None else object):
         gm = torch.empty_like(moving) if need_m else None
         gp = torch.empty_like(prior) if (need_p and prior is not None) else None
         ga = C.c_float(0.0)
-        _soft_call(dctx, dctx._L.deeds_soft_backward_dev, fixed, moving, dims, params, tree, _ptr(prior),
-                   _ptr(gdisp), _ptr(gf), _ptr(gm), _ptr(gp), C.byref(ga) if need_a else None)
+        grads = (_ptr(gdisp), _ptr(gf), _ptr(gm), _ptr(gp), C.byref(ga) if need_a else None)
+        kept = fctx.kept
+        if kept is not None and kept.slot is not None:
+            m, n, o = dims
+            sz = m * n * o
+            dctx.check(dctx._L.deeds_soft_backward_kept_dev(
+                dctx.handle, kept.slot, _dev(fixed, torch.float32, sz, "fixed"),
+                _dev(moving, torch.float32, sz, "moving"), m, n, o, C.byref(params), _ptr(prior), *grads, _stream()))
+            kept.release()  # a second backward (retain_graph) recomputes
+        else:
+            _soft_call(dctx, dctx._L.deeds_soft_backward_dev, fixed, moving, dims, params, tree, _ptr(prior), *grads)
         adt, adev = fctx.alpha_like
         galpha = torch.tensor(ga.value, dtype=adt, device=adev) if need_a else None
-        return gf, gm, galpha, gp, None, None, None, None
+        return gf, gm, galpha, gp, None, None, None, None, None
 
 
 class SoftUpsample(torch.autograd.Function if torch is not None else object):
@@ -547,11 +583,12 @@ def soft_tree(fixed, m, n, o, g, ctx=None):
 
 
 def soft_level(fixed, moving, alpha, dims, grid=4, radius=3, quant=1, tau=0.5, eps=0.01, mind_radius=0, tree=None,
-               ctx=None):
+               ctx=None, keep_state=True):
     """Differentiable soft-min deeds level: expected displacement (3, sz1) [u, v, w].
 
     Gradients flow to ``fixed`` and ``moving`` (through the continuous MIND-SSC
-    descriptor) and to ``alpha`` (a float or 0-d tensor)."""
+    descriptor) and to ``alpha`` (a float or 0-d tensor).  keep_state=False trades
+    the resident forward state for a recomputation in the backward."""
     m, n, o = dims
     ctx = ctx or context(fixed.device.index or 0)
     if tree is None:
@@ -559,10 +596,11 @@ def soft_level(fixed, moving, alpha, dims, grid=4, radius=3, quant=1, tau=0.5, e
     if not isinstance(alpha, torch.Tensor):
         alpha = torch.tensor(float(alpha), dtype=torch.float32)
     params = soft_params(grid, radius, quant, float(alpha.detach()), tau, eps, mind_radius)
-    return SoftDeedsLevel.apply(fixed, moving, alpha, None, tuple(dims), params, tree, ctx)
+    return SoftDeedsLevel.apply(fixed, moving, alpha, None, tuple(dims), params, tree, ctx, keep_state)
 
 
-def soft_register_levels(fixed, moving, alpha, dims, levels, tau=0.5, eps=0.01, trees=None, ctx=None):
+def soft_register_levels(fixed, moving, alpha, dims, levels, tau=0.5, eps=0.01, trees=None, ctx=None,
+                         keep_state=True):
     """Differentiable multi-level soft-min registration (the level loop of
     src/deedsBCV0.cpp:222-306, forward direction).
 
@@ -571,7 +609,7 @@ def soft_register_levels(fixed, moving, alpha, dims, levels, tau=0.5, eps=0.01, 
     (zero at the first level), the moving image is warped by U at full resolution,
     and the soft level's expected displacement E is taken relative to U; the level
     returns U + E.  Returns the last grid field (3, sz1) [u, v, w].  trees: the
-    fixed image's MST per level (computed when None)."""
+    fixed image's MST per level (computed when None); keep_state as in soft_level."""
     m, n, o = dims
     ctx = ctx or context(fixed.device.index or 0)
     if not isinstance(alpha, torch.Tensor):
@@ -582,12 +620,12 @@ def soft_register_levels(fixed, moving, alpha, dims, levels, tau=0.5, eps=0.01, 
         tree = trees[li] if trees is not None else soft_tree(fixed, m, n, o, g, ctx)
         params = soft_params(g, hw, q, float(alpha.detach()), tau, eps, qs)
         if prev is None:
-            E = SoftDeedsLevel.apply(fixed, moving, alpha, None, tuple(dims), params, tree, ctx)
+            E = SoftDeedsLevel.apply(fixed, moving, alpha, None, tuple(dims), params, tree, ctx, keep_state)
             prev = E
         else:
             U = SoftUpsample.apply(prev, prev_dims, gdims, ctx)
             warped = SoftWarp.apply(moving, U, tuple(dims), gdims, ctx)
-            E = SoftDeedsLevel.apply(fixed, warped, alpha, U, tuple(dims), params, tree, ctx)
+            E = SoftDeedsLevel.apply(fixed, warped, alpha, U, tuple(dims), params, tree, ctx, keep_state)
             prev = U + E
         prev_dims = gdims
     return prev

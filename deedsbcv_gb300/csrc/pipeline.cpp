@@ -43,6 +43,8 @@ struct HostBuf {
     size_t cap = 0;
 };
 
+struct SoftKept;
+
 struct deeds_ctx {
     int device = 0;
     int sm_count = 0;
@@ -74,6 +76,9 @@ struct deeds_ctx {
     bool have_field = false;
     int fm = 0, fn = 0, fo = 0;
     float fX[16];
+    // soft-min levels whose forward state stays resident for their backward
+    // (deeds_soft_forward_keep_dev); index = slot
+    std::vector<std::shared_ptr<SoftKept>> kept;
 };
 
 namespace deeds {
@@ -1233,9 +1238,25 @@ struct SoftLevel {
     int* sweep = nullptr;  // persistent sweeps: ticket, per-node flags, error word
 };
 
+}  // namespace
+
+// One resident forward state: the level as set up, with the arguments it was set
+// up with, so that a backward can check it is given the same problem.
+struct SoftKept {
+    bool used = false, valid = false, prior = false;
+    int m = 0, n = 0, o = 0;
+    deeds_soft_params p{};
+    SoftLevel L;
+};
+
+namespace {
+
+// `tag` prefixes the names of the buffers that hold the level's state (tree,
+// descriptors, cost volume, messages, marginals, sweep flags); the MIND scratch
+// is shared by every level.
 deeds_status soft_setup(deeds_ctx* ctx, int m, int n, int o, const deeds_soft_params* p, const int* ordered,
                         const int* parents, const float* edgemst, const float* d_prior, cudaStream_t s,
-                        SoftLevel& L) {
+                        SoftLevel& L, const std::string& tag = "soft_") {
     if (deeds_status e = soft_check(ctx, m, n, o, p, &L.qs)) return e;
     if (!ordered || !parents || !edgemst) return fail(ctx, DEEDS_ERR_INVALID, "null tree array");
     L.m1 = m / p->grid; L.n1 = n / p->grid; L.o1 = o / p->grid;
@@ -1264,18 +1285,18 @@ deeds_status soft_setup(deeds_ctx* ctx, int m, int n, int o, const deeds_soft_pa
     // packed tree: ordered | parents | edgemst | child_ptr | children
     const size_t words = (size_t)L.sz1 * 5 + 2;
     uint32_t* h = hbuf<uint32_t>(ctx, "soft_tree_h", words, &st);
-    uint32_t* d = dbuf<uint32_t>(ctx, "soft_tree_d", words, &st);
+    uint32_t* d = dbuf<uint32_t>(ctx, tag + "tree_d", words, &st);
     L.w6 = dbuf<float>(ctx, "soft_w6", 6 * L.sz, &st);
     L.w6b = dbuf<float>(ctx, "soft_w6b", 6 * L.sz, &st);
-    L.sF = dbuf<float>(ctx, "soft_sF", 12 * L.sz, &st);
-    L.sM = dbuf<float>(ctx, "soft_sM", 12 * L.sz, &st);
-    L.cost = dbuf<float>(ctx, "soft_cost", L.sz1 * L.len3, &st);
-    L.B = dbuf<float>(ctx, "soft_B", L.sz1 * L.len3, &st);
-    L.M = dbuf<float>(ctx, "soft_M", L.sz1 * L.len3, &st);
-    L.Mmin = dbuf<float>(ctx, "soft_Mmin", L.sz1, &st);
-    L.logp = dbuf<float>(ctx, "soft_logp", L.sz1 * L.len3, &st);
-    L.disp = dbuf<float>(ctx, "soft_disp", 3 * (size_t)L.sz1, &st);
-    L.sweep = dbuf<int>(ctx, "soft_sweep", (size_t)L.sz1 + 2, &st);
+    L.sF = dbuf<float>(ctx, tag + "sF", 12 * L.sz, &st);
+    L.sM = dbuf<float>(ctx, tag + "sM", 12 * L.sz, &st);
+    L.cost = dbuf<float>(ctx, tag + "cost", L.sz1 * L.len3, &st);
+    L.B = dbuf<float>(ctx, tag + "B", L.sz1 * L.len3, &st);
+    L.M = dbuf<float>(ctx, tag + "M", L.sz1 * L.len3, &st);
+    L.Mmin = dbuf<float>(ctx, tag + "Mmin", L.sz1, &st);
+    L.logp = dbuf<float>(ctx, tag + "logp", L.sz1 * L.len3, &st);
+    L.disp = dbuf<float>(ctx, tag + "disp", 3 * (size_t)L.sz1, &st);
+    L.sweep = dbuf<int>(ctx, tag + "sweep", (size_t)L.sz1 + 2, &st);
     if (st) return st;
     CK(cudaMemsetAsync(L.sweep + L.sz1 + 1, 0, sizeof(int), s));
     CK(cudaStreamSynchronize(s));  // the pinned staging block is reused across calls
@@ -1300,7 +1321,7 @@ deeds_status soft_setup(deeds_ctx* ctx, int m, int n, int o, const deeds_soft_pa
     L.tree.off = nullptr;
     L.tree.offbar = nullptr;
     if (d_prior) {
-        float* off = dbuf<float>(ctx, "soft_off", 3 * (size_t)L.sz1, &st);
+        float* off = dbuf<float>(ctx, tag + "off", 3 * (size_t)L.sz1, &st);
         if (st) return st;
         CK(launch_soft_offsets(d_prior, L.tree.parents, L.tree.root, L.sz1, (float)p->quant, off, s));
         L.tree.off = off;
@@ -1323,6 +1344,54 @@ deeds_status soft_check_sweeps(deeds_ctx* ctx, const SoftLevel& L, cudaStream_t 
     CK(cudaMemcpyAsync(&herr, L.sweep + L.sz1 + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     if (herr) return fail(ctx, DEEDS_ERR_TIMEOUT, "a tree sweep gave up waiting for a node's dependencies");
+    return DEEDS_OK;
+}
+
+// The adjoint of one level whose forward state (descriptors, cost volume,
+// messages, marginals) is in L.
+deeds_status soft_run_backward(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, int m, int n, int o,
+                               const deeds_soft_params* p, SoftLevel& L, const float* d_gdisp, float* d_gfixed,
+                               float* d_gmoving, float* d_gprior, float* grad_alpha, cudaStream_t s) {
+    deeds_status st = DEEDS_OK;
+    // the MIND scratch is shared and may have been reallocated since L was set up
+    L.w6 = dbuf<float>(ctx, "soft_w6", 6 * L.sz, &st);
+    L.w6b = dbuf<float>(ctx, "soft_w6b", 6 * L.sz, &st);
+    if (st) return st;
+    L.tree.offbar = nullptr;
+    if (d_gprior) {
+        float* offbar = dbuf<float>(ctx, "soft_offbar", 3 * (size_t)L.sz1, &st);
+        if (st) return st;
+        CK(cudaMemsetAsync(offbar, 0, sizeof(float) * 3 * L.sz1, s));
+        L.tree.offbar = offbar;
+    }
+    float* R = dbuf<float>(ctx, "soft_R", L.sz1 * L.len3, &st);
+    float* Bbar = dbuf<float>(ctx, "soft_Bbar", L.sz1 * L.len3, &st);
+    float* sFbar = dbuf<float>(ctx, "soft_sFbar", 12 * L.sz, &st);
+    float* sMbar = dbuf<float>(ctx, "soft_sMbar", 12 * L.sz, &st);
+    float* dbar6 = dbuf<float>(ctx, "soft_dbar6", 6 * L.sz, &st);
+    double* dot = dbuf<double>(ctx, "soft_dot", 1, &st);
+    if (st) return st;
+    CK(launch_soft_tree_backward(L.tree, L.sweep, L.B, L.M, L.logp, d_gdisp, R, Bbar, s));
+    if (d_gprior) {
+        CK(cudaMemsetAsync(d_gprior, 0, sizeof(float) * 3 * L.sz1, s));
+        CK(launch_soft_offbar_to_prior(L.tree.offbar, L.tree.parents, L.tree.root, L.sz1, (float)p->quant, d_gprior,
+                                       s));
+    }
+    // Bbar is now dL/dcost
+    CK(launch_soft_cost_adj(L.sF, L.sM, Bbar, L.cost, sFbar, sMbar, dot, m, n, o, p->grid, p->radius, p->quant,
+                            soft_alpha1(p), p->eps, s));
+    if (d_gfixed) {
+        CK(cudaMemsetAsync(d_gfixed, 0, sizeof(float) * L.sz, s));
+        CK(launch_soft_descriptor_adj(d_fixed, L.w6, L.w6b, sFbar, dbar6, d_gfixed, m, n, o, L.qs, s));
+    }
+    if (d_gmoving) {
+        CK(cudaMemsetAsync(d_gmoving, 0, sizeof(float) * L.sz, s));
+        CK(launch_soft_descriptor_adj(d_moving, L.w6, L.w6b, sMbar, dbar6, d_gmoving, m, n, o, L.qs, s));
+    }
+    double hdot = 0.0;
+    if (grad_alpha) CK(cudaMemcpyAsync(&hdot, dot, sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (deeds_status e = soft_check_sweeps(ctx, L, s)) return e;
+    if (grad_alpha) *grad_alpha = (float)(-hdot / (double)p->alpha);
     return DEEDS_OK;
 }
 
@@ -1353,43 +1422,75 @@ deeds_status deeds_soft_backward_dev(deeds_ctx* ctx, const float* d_fixed, const
     cudaStream_t s = (cudaStream_t)stream;
     SoftLevel L;
     if (deeds_status e = soft_setup(ctx, m, n, o, p, ordered, parents, edgemst, d_prior, s, L)) return e;
-    deeds_status st = DEEDS_OK;
-    if (d_gprior) {
-        float* offbar = dbuf<float>(ctx, "soft_offbar", 3 * (size_t)L.sz1, &st);
-        if (st) return st;
-        CK(cudaMemsetAsync(offbar, 0, sizeof(float) * 3 * L.sz1, s));
-        L.tree.offbar = offbar;
-    }
-    float* R = dbuf<float>(ctx, "soft_R", L.sz1 * L.len3, &st);
-    float* Bbar = dbuf<float>(ctx, "soft_Bbar", L.sz1 * L.len3, &st);
-    float* sFbar = dbuf<float>(ctx, "soft_sFbar", 12 * L.sz, &st);
-    float* sMbar = dbuf<float>(ctx, "soft_sMbar", 12 * L.sz, &st);
-    float* dbar6 = dbuf<float>(ctx, "soft_dbar6", 6 * L.sz, &st);
-    double* dot = dbuf<double>(ctx, "soft_dot", 1, &st);
-    if (st) return st;
     // recompute the forward state (descriptors, cost, messages, marginals)
     if (deeds_status e = soft_run_forward(ctx, d_fixed, d_moving, m, n, o, p, L, L.disp, s)) return e;
-    CK(launch_soft_tree_backward(L.tree, L.sweep, L.B, L.M, L.logp, d_gdisp, R, Bbar, s));
-    if (d_gprior) {
-        CK(cudaMemsetAsync(d_gprior, 0, sizeof(float) * 3 * L.sz1, s));
-        CK(launch_soft_offbar_to_prior(L.tree.offbar, L.tree.parents, L.tree.root, L.sz1, (float)p->quant, d_gprior,
-                                       s));
+    return soft_run_backward(ctx, d_fixed, d_moving, m, n, o, p, L, d_gdisp, d_gfixed, d_gmoving, d_gprior,
+                             grad_alpha, s);
+}
+
+deeds_status deeds_soft_forward_keep_dev(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, int m, int n,
+                                         int o, const deeds_soft_params* p, const int* ordered, const int* parents,
+                                         const float* edgemst, const float* d_prior, float* d_disp, int* slot,
+                                         void* stream) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!d_fixed || !d_moving || !d_disp || !slot || !p) return fail(ctx, DEEDS_ERR_INVALID, "null pointer");
+    cudaStream_t s = (cudaStream_t)stream;
+    int k = 0;  // first free slot; its buffers (if any) are reused
+    while (k < (int)ctx->kept.size() && ctx->kept[k]->used) k++;
+    if (k == (int)ctx->kept.size()) ctx->kept.push_back(std::make_shared<SoftKept>());
+    SoftKept& K = *ctx->kept[k];
+    K.used = true;
+    K.valid = false;
+    *slot = k;
+    const std::string tag = "softk" + std::to_string(k) + "_";
+    if (deeds_status e = soft_setup(ctx, m, n, o, p, ordered, parents, edgemst, d_prior, s, K.L, tag)) return e;
+    if (deeds_status e = soft_run_forward(ctx, d_fixed, d_moving, m, n, o, p, K.L, d_disp, s)) return e;
+    if (deeds_status e = soft_check_sweeps(ctx, K.L, s)) return e;
+    K.m = m; K.n = n; K.o = o;
+    K.p = *p;
+    K.prior = d_prior != nullptr;
+    K.valid = true;
+    return DEEDS_OK;
+}
+
+deeds_status deeds_soft_backward_kept_dev(deeds_ctx* ctx, int slot, const float* d_fixed, const float* d_moving,
+                                          int m, int n, int o, const deeds_soft_params* p, const float* d_prior,
+                                          const float* d_gdisp, float* d_gfixed, float* d_gmoving, float* d_gprior,
+                                          float* grad_alpha, void* stream) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!d_fixed || !d_moving || !d_gdisp || !p) return fail(ctx, DEEDS_ERR_INVALID, "null pointer");
+    if (slot < 0 || slot >= (int)ctx->kept.size() || !ctx->kept[slot]->used || !ctx->kept[slot]->valid)
+        return fail(ctx, DEEDS_ERR_INVALID, "slot %d holds no forward state", slot);
+    SoftKept& K = *ctx->kept[slot];
+    const bool same = K.m == m && K.n == n && K.o == o && K.p.grid == p->grid && K.p.radius == p->radius &&
+                      K.p.quant == p->quant && K.p.mind_radius == p->mind_radius && K.p.alpha == p->alpha &&
+                      K.p.tau == p->tau && K.p.eps == p->eps && K.prior == (d_prior != nullptr);
+    if (!same) return fail(ctx, DEEDS_ERR_INVALID, "slot %d was filled for another level or parameters", slot);
+    if (d_gprior && !d_prior) return fail(ctx, DEEDS_ERR_INVALID, "grad_prior needs a prior field");
+    return soft_run_backward(ctx, d_fixed, d_moving, m, n, o, p, K.L, d_gdisp, d_gfixed, d_gmoving, d_gprior,
+                             grad_alpha, (cudaStream_t)stream);
+}
+
+deeds_status deeds_soft_release(deeds_ctx* ctx, int slot) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (slot < 0 || slot >= (int)ctx->kept.size() || !ctx->kept[slot]->used)
+        return fail(ctx, DEEDS_ERR_INVALID, "slot %d is not in use", slot);
+    ctx->kept[slot]->used = false;
+    ctx->kept[slot]->valid = false;
+    return DEEDS_OK;
+}
+
+deeds_status deeds_soft_trim(deeds_ctx* ctx) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    CK(cudaSetDevice(ctx->device));
+    for (size_t k = 0; k < ctx->kept.size(); k++) {
+        if (ctx->kept[k]->used) continue;
+        const std::string tag = "softk" + std::to_string(k) + "_";
+        for (auto it = ctx->dev.lower_bound(tag); it != ctx->dev.end() && it->first.compare(0, tag.size(), tag) == 0;) {
+            if (it->second.p) CK(cudaFree(it->second.p));
+            it = ctx->dev.erase(it);
+        }
     }
-    // Bbar is now dL/dcost
-    CK(launch_soft_cost_adj(L.sF, L.sM, Bbar, L.cost, sFbar, sMbar, dot, m, n, o, p->grid, p->radius, p->quant,
-                            soft_alpha1(p), p->eps, s));
-    if (d_gfixed) {
-        CK(cudaMemsetAsync(d_gfixed, 0, sizeof(float) * L.sz, s));
-        CK(launch_soft_descriptor_adj(d_fixed, L.w6, L.w6b, sFbar, dbar6, d_gfixed, m, n, o, L.qs, s));
-    }
-    if (d_gmoving) {
-        CK(cudaMemsetAsync(d_gmoving, 0, sizeof(float) * L.sz, s));
-        CK(launch_soft_descriptor_adj(d_moving, L.w6, L.w6b, sMbar, dbar6, d_gmoving, m, n, o, L.qs, s));
-    }
-    double hdot = 0.0;
-    if (grad_alpha) CK(cudaMemcpyAsync(&hdot, dot, sizeof(double), cudaMemcpyDeviceToHost, s));
-    if (deeds_status e = soft_check_sweeps(ctx, L, s)) return e;
-    if (grad_alpha) *grad_alpha = (float)(-hdot / (double)p->alpha);
     return DEEDS_OK;
 }
 

@@ -295,6 +295,34 @@ deeds_status deeds_soft_backward_dev(deeds_ctx* ctx, const float* d_fixed, const
                                      float* d_grad_fixed, float* d_grad_moving, float* d_grad_prior,
                                      float* grad_alpha, void* stream);
 
+/* Forward that keeps the level's state resident on the device (descriptors of
+ * both images, cost volume, tree, messages and marginals: about
+ * (96*m*n*o + 16*m1*n1*o1*(2hw+1)^3) bytes) under a slot of the context, written
+ * to *slot, so that deeds_soft_backward_kept_dev runs only the adjoint.  Same
+ * arguments and results as deeds_soft_forward_dev.  The slot stays in use until
+ * deeds_soft_release; a released slot's buffers serve the next keep forward
+ * (deeds_soft_trim frees those of unused slots). */
+deeds_status deeds_soft_forward_keep_dev(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, int m, int n,
+                                         int o, const deeds_soft_params* p, const int* ordered, const int* parents,
+                                         const float* edgemst, const float* d_prior, float* d_disp, int* slot,
+                                         void* stream);
+
+/* deeds_soft_backward_dev for the forward kept in `slot`: no recomputation.  The
+ * images, dimensions, parameters and prior must be those of that forward, with
+ * the images and prior unchanged since (dimensions, parameters and the presence
+ * of a prior are checked: DEEDS_ERR_INVALID otherwise).  May run any number of
+ * times while the slot is in use. */
+deeds_status deeds_soft_backward_kept_dev(deeds_ctx* ctx, int slot, const float* d_fixed, const float* d_moving,
+                                          int m, int n, int o, const deeds_soft_params* p, const float* d_prior,
+                                          const float* d_grad_disp, float* d_grad_fixed, float* d_grad_moving,
+                                          float* d_grad_prior, float* grad_alpha, void* stream);
+
+/* Ends the use of a kept slot (its buffers are kept for reuse). */
+deeds_status deeds_soft_release(deeds_ctx* ctx, int slot);
+
+/* Frees the device buffers of every kept slot not in use (synchronises the device). */
+deeds_status deeds_soft_trim(deeds_ctx* ctx);
+
 /* Differentiable trilinear upsampling of a field u|v|w from an mA x nA x oA grid to
  * m x n x o (the coordinates of upsampleDeformationsCL, src/transformations.h:245-279,
  * in float arithmetic), and its adjoint (gin overwritten). */

@@ -159,3 +159,94 @@ def test_soft_warp_invalid_arguments_raise(api):
         api.SoftWarp.apply(torch.zeros(8, device="cuda"), x, (2, 2, 2), (0, 2, 2), ctx)
     with pytest.raises(Exception):
         api.SoftUpsample.apply(x, (2, 2, 2), (4, 4, 0), ctx)
+
+
+def test_soft_kept_state_matches_recompute(api):
+    """The backward over the kept forward state gives the recomputing backward's
+    gradients, and a second backward through a retained graph (whose slot the
+    first backward released) recomputes to the same values."""
+    m, n, o = DIMS
+    f, mv = _pair(7)
+    fd, md = torch.from_numpy(f).cuda(), torch.from_numpy(mv).cuda()
+    trees = [api.soft_tree(fd, m, n, o, g) for g, *_ in LEVELS]
+    gl = LEVELS[-1][0]
+    gt = torch.from_numpy(np.random.default_rng(7).normal(0, 1, (3, (m // gl) * (n // gl) * (o // gl)))).float().cuda()
+
+    def run(keep):
+        F, M = fd.clone().requires_grad_(), md.clone().requires_grad_()
+        a = torch.tensor(1.6, requires_grad=True)
+        d = api.soft_register_levels(F, M, a, DIMS, LEVELS, tau=0.5, trees=trees, keep_state=keep)
+        loss = ((d - gt) ** 2).mean()
+        out = []
+        for retain in (True, False):
+            loss.backward(retain_graph=retain)
+            out.append((F.grad.clone(), M.grad.clone(), a.grad.clone()))
+            F.grad, M.grad, a.grad = None, None, None
+        return d.detach(), out
+
+    d0, r = run(False)
+    d1, k = run(True)
+    # Same kernels on the same inputs, but the cost kernels and the adjoints sum
+    # with float atomics, whose order varies between runs: across three levels
+    # the fields differ by ~1e-5 voxels.  A backward over the wrong or a stale
+    # state differs at order one.
+    assert (d0 - d1).abs().max().item() <= 1e-4
+    for got in (k[0], k[1], r[1]):
+        for x, y in zip(got, r[0]):
+            assert _rel(x.cpu().double(), y.cpu().double()) < 1e-3
+
+
+def test_soft_kept_slot_checks(api):
+    """deeds_soft_backward_kept_dev refuses a slot that holds no state or was
+    filled for other parameters; released slots are reused; trim frees them."""
+    import ctypes as C
+    m, n, o = DIMS
+    g, hw, q = 4, 2, 1
+    sz1 = (m // g) * (n // g) * (o // g)
+    f, mv = _pair(8)
+    fd, md = torch.from_numpy(f).cuda(), torch.from_numpy(mv).cuda()
+    ctx = api.Context(0)
+    tree = api._tree_arrays(api.soft_tree(fd, m, n, o, g, ctx))
+    params = api.soft_params(g, hw, q, 1.6, 0.5, 0.01, 1)
+    out = torch.empty(3 * sz1, device="cuda")
+    gd = torch.randn(3 * sz1, device="cuda")
+    gf = torch.empty_like(fd)
+    L = ctx._L
+
+    def keep():
+        slot = C.c_int(-1)
+        api._soft_call(ctx, L.deeds_soft_forward_keep_dev, fd, md, DIMS, params, tree, None, api._ptr(out),
+                       C.byref(slot))
+        return slot.value
+
+    def back(slot, p, prior=None):
+        return L.deeds_soft_backward_kept_dev(ctx.handle, slot, api._ptr(fd), api._ptr(md), m, n, o, C.byref(p),
+                                              api._ptr(prior), api._ptr(gd), api._ptr(gf), None, None, None,
+                                              api._stream())
+
+    s0 = keep()
+    s1 = keep()
+    assert (s0, s1) == (0, 1)
+    ctx.check(back(s0, params))
+    g_first = gf.clone()
+    ctx.check(back(s0, params))  # the state survives a backward
+    assert _rel(gf.cpu().double(), g_first.cpu().double()) < 1e-5
+    other = api.soft_params(g, hw, q, 1.7, 0.5, 0.01, 1)
+    with pytest.raises(api.DeedsError):
+        ctx.check(back(s0, other))
+    prior = torch.zeros(3 * sz1, device="cuda")
+    with pytest.raises(api.DeedsError):
+        ctx.check(back(s0, params, prior))
+    with pytest.raises(api.DeedsError):
+        ctx.check(back(5, params))
+    ctx.check(L.deeds_soft_release(ctx.handle, s0))
+    with pytest.raises(api.DeedsError):
+        ctx.check(L.deeds_soft_release(ctx.handle, s0))
+    with pytest.raises(api.DeedsError):
+        ctx.check(back(s0, params))
+    assert keep() == s0  # the first free slot is reused
+    for s in (s0, s1):
+        ctx.check(L.deeds_soft_release(ctx.handle, s))
+    ctx.check(L.deeds_soft_trim(ctx.handle))
+    assert keep() == 0
+    ctx.close()
