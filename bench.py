@@ -280,35 +280,52 @@ def measure_soft(api, ctx, n_pairs=4, levels=SOFT_LEVELS, taus=SOFT_TAUS, shape=
         trees = [api.soft_tree(fx, m, n, o, lv[0], ctx) for lv in levels]
         data.append((fx, mv, torch.from_numpy(gt.astype(np.float32)).cuda(), trees))
 
-    def step(fx, mv, gt, trees, tau, backward=True, keep=True):
-        F = fx.detach().requires_grad_(backward)
-        M = mv.detach().requires_grad_(backward)
-        a = torch.tensor(1.6, requires_grad=backward)
+    FX = torch.stack([d[0] for d in data])
+    MV = torch.stack([d[1] for d in data])
+    GT = torch.stack([d[2] for d in data])
+    TREES = [d[3] for d in data]
+
+    def step_one(fx, mv, gt, trees, tau, keep=True):
+        F, M = fx.detach().requires_grad_(), mv.detach().requires_grad_()
+        a = torch.tensor(1.6, requires_grad=True)
         disp = api.soft_register_levels(F, M, a, shape, levels, tau=tau, trees=trees, ctx=ctx, keep_state=keep)
         loss = ((disp - gt) ** 2).mean()
+        loss.backward()
+        return loss.detach()
+
+    def step_batch(tau, backward=True, keep=True):
+        # loss = sum over pairs of each pair's MSE: pair i's gradients are those
+        # of its own MSE
+        F, M = FX.detach().requires_grad_(backward), MV.detach().requires_grad_(backward)
+        a = torch.tensor(1.6, requires_grad=backward)
+        disp = api.soft_register_levels_batch(F, M, a, shape, levels, tau=tau, trees=TREES, ctx=ctx,
+                                              keep_state=keep)
+        per_pair = ((disp - GT) ** 2).mean(dim=(1, 2))
         if backward:
-            loss.backward()
-            return loss.detach(), F.grad, M.grad, a.grad
-        return loss.detach(), None, None, None
+            per_pair.sum().backward()
+            return per_pair.detach(), F.grad[-1], M.grad[-1], a.grad
+        return per_pair.detach(), None, None, None
 
     out = {}
     launches0 = api.kernel_launches()
     for tau in taus:
-        for fx, mv, gt, tree in data[:1]:
-            step(fx, mv, gt, tree, tau)  # warm-up: buffers
+        step_batch(tau)  # warm-up: buffers of every lane
+        step_batch(tau, keep=False)
+        step_one(*data[0], tau)
         res = {}
-        # forward_backward keeps each level's forward state on the device for its
-        # backward; forward_backward_recompute is the memory-saving form whose
-        # backward recomputes it
-        for mode in ("forward", "forward_backward", "forward_backward_recompute"):
+        # forward_backward: the pairs of each level run concurrently on lane
+        # streams and each level's forward state stays on the device for its
+        # backward; _recompute: the backward recomputes that state instead;
+        # _one_by_one: the pairs one after another through soft_register_levels
+        for mode in ("forward", "forward_backward", "forward_backward_recompute", "forward_backward_one_by_one"):
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
-            losses = []
-            for fx, mv, gt, tree in data:
-                loss, gf, gm, ga = step(fx, mv, gt, tree, tau, backward=(mode != "forward"),
-                                        keep=(mode != "forward_backward_recompute"))
-                losses.append(loss)
+            if mode == "forward_backward_one_by_one":
+                losses = torch.stack([step_one(fx, mv, gt, tr, tau) for fx, mv, gt, tr in data])
+            else:
+                losses, gf, gm, ga = step_batch(tau, backward=(mode != "forward"),
+                                                keep=(mode != "forward_backward_recompute"))
             e1.record()
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1)
@@ -316,8 +333,8 @@ def measure_soft(api, ctx, n_pairs=4, levels=SOFT_LEVELS, taus=SOFT_TAUS, shape=
             if mode == "forward_backward":
                 res["pairs_per_s"] = 1000.0 * len(data) / ms
                 res["grad_norms_last_pair"] = {"fixed": float(gf.norm()), "moving": float(gm.norm()),
-                                               "alpha": float(ga)}
-            res["mean_loss"] = float(torch.stack(losses).mean())
+                                               "alpha_all_pairs": float(ga)}
+                res["mean_loss"] = float(losses.mean())
         out[str(tau)] = res
     lv = " ".join(f"G{a}L{b}Q{c}" for a, b, c, _ in levels)
     return {"workload": f"{n_pairs} pairs {m}x{n}x{o} (seeds 200..{199 + n_pairs}), soft levels {lv}, label set "

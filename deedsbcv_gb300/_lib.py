@@ -28,7 +28,8 @@ EXPORTS = [
     "deeds_soft_default_params", "deeds_soft_descriptor_dev", "deeds_soft_cost_dev", "deeds_soft_forward_dev",
     "deeds_soft_backward_dev", "deeds_soft_upsample_dev", "deeds_soft_upsample_backward_dev", "deeds_soft_warp_dev",
     "deeds_soft_warp_backward_dev", "deeds_soft_forward_keep_dev", "deeds_soft_backward_kept_dev",
-    "deeds_soft_release", "deeds_soft_trim",
+    "deeds_soft_release", "deeds_soft_trim", "deeds_soft_forward_batch_dev", "deeds_soft_backward_batch_dev",
+    "deeds_soft_release_batch",
     "deeds_linear_default_params", "deeds_linear_register", "deeds_linear_register_dev", "deeds_lin_warp_dev",
     "deeds_lin_smooth_dev", "deeds_estimate_affine_dev", "deeds_affine_robust", "deeds_affine_warp_segmentation",
     "deeds_gz_write", "deeds_gz_read", "deeds_gz_last_error", "deeds_selftest_bounded_waits",
@@ -146,6 +147,10 @@ def load():
     L.deeds_soft_backward_kept_dev.argtypes = [P, I, P, P, I, I, I, SP, P, P, P, P, P, P, P]
     L.deeds_soft_release.argtypes = [P, I]
     L.deeds_soft_trim.argtypes = [P]
+    IP = C.POINTER(C.c_int)
+    L.deeds_soft_forward_batch_dev.argtypes = [P, I, P, P, I, I, I, SP, P, P, P, P, P, IP, P]
+    L.deeds_soft_backward_batch_dev.argtypes = [P, I, IP, P, P, I, I, I, SP, P, P, P, P, P, P, P, P, P, P]
+    L.deeds_soft_release_batch.argtypes = [P, I, IP]
     L.deeds_soft_upsample_dev.argtypes = [P, P, I, I, I, P, I, I, I, P]
     L.deeds_soft_upsample_backward_dev.argtypes = [P, P, I, I, I, P, I, I, I, P]
     L.deeds_soft_warp_dev.argtypes = [P, P, I, I, I, P, I, I, I, P, P]

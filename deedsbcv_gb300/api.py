@@ -631,6 +631,136 @@ def soft_register_levels(fixed, moving, alpha, dims, levels, tau=0.5, eps=0.01, 
     return prev
 
 
+def _ptrs(ts):
+    """ctypes array of the data pointers of a sequence of tensors / numpy arrays."""
+    vals = [t.data_ptr() if isinstance(t, torch.Tensor) else t.ctypes.data for t in ts]
+    return (C.c_void_p * len(vals))(*vals)
+
+
+class _KeptSoftBatch:
+    """The library slots holding a batch's forward states (one per pair, in the
+    pairs' lanes); released after the backward or with the autograd node."""
+
+    def __init__(self, dctx, slots):
+        self.dctx, self.slots = dctx, slots
+
+    def release(self):
+        if self.slots is not None and self.dctx.handle:
+            self.dctx._L.deeds_soft_release_batch(self.dctx.handle, len(self.slots), self.slots)
+        self.slots = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+class SoftDeedsLevelBatch(torch.autograd.Function if torch is not None else object):
+    """SoftDeedsLevel for P pairs of one size at once: fixed/moving (P, m*n*o),
+    prior None or (P, 3, sz1), trees a list of P MSTs; returns (P, 3, sz1).  The
+    library runs the pairs concurrently on lane streams (the tree sweeps of one
+    pair are latency-bound and leave SMs to the others).  keep as in
+    SoftDeedsLevel."""
+
+    @staticmethod
+    def forward(fctx, fixed, moving, alpha, prior, dims, params, trees, dctx, keep=True):
+        params = soft_params(params.grid, params.radius, params.quant, float(alpha.detach()), params.tau, params.eps,
+                             params.mind_radius)
+        m, n, o = dims
+        sz = m * n * o
+        g = params.grid
+        sz1 = (m // g) * (n // g) * (o // g)
+        npairs = fixed.shape[0]
+        trees = [_tree_arrays(t) for t in trees]
+        if len(trees) != npairs or moving.shape[0] != npairs:
+            raise ValueError("fixed, moving and trees need one entry per pair")
+        fixed_c, moving_c = fixed.detach().contiguous(), moving.detach().contiguous()
+        _dev(fixed_c, torch.float32, npairs * sz, "fixed")
+        _dev(moving_c, torch.float32, npairs * sz, "moving")
+        if fixed_c.numel() != npairs * sz or moving_c.numel() != npairs * sz:
+            raise ValueError(f"fixed/moving: expected ({npairs}, {sz})")
+        prior_c = None
+        if prior is not None:
+            prior_c = prior.detach().contiguous()
+            _dev(prior_c, torch.float32, npairs * 3 * sz1, "prior")
+        out = torch.empty(npairs, 3, sz1, dtype=torch.float32, device=fixed.device)
+        slots = None
+        if keep and any(fctx.needs_input_grad[:4]):
+            slots = (C.c_int * npairs)()
+        dctx.check(dctx._L.deeds_soft_forward_batch_dev(
+            dctx.handle, npairs, _ptrs(fixed_c.view(npairs, sz)), _ptrs(moving_c.view(npairs, sz)), m, n, o,
+            C.byref(params), _ptrs([t[0] for t in trees]), _ptrs([t[1] for t in trees]), _ptrs([t[2] for t in trees]),
+            _ptrs(prior_c.view(npairs, -1)) if prior_c is not None else None, _ptrs(out), slots, _stream()))
+        fctx.kept = _KeptSoftBatch(dctx, slots) if slots is not None else None
+        fctx.save_for_backward(fixed_c, moving_c, prior_c)
+        fctx.soft = (dims, params, trees, dctx)
+        fctx.alpha_like = (alpha.dtype, alpha.device)
+        return out
+
+    @staticmethod
+    def backward(fctx, gdisp):
+        fixed, moving, prior = fctx.saved_tensors
+        dims, params, trees, dctx = fctx.soft
+        m, n, o = dims
+        npairs = len(trees)
+        gdisp = gdisp.detach().contiguous().to(torch.float32)
+        need_f, need_m, need_a, need_p = fctx.needs_input_grad[:4]
+        fv, mv = fixed.view(npairs, -1), moving.view(npairs, -1)
+        gf = torch.empty_like(fixed) if need_f else None
+        gm = torch.empty_like(moving) if need_m else None
+        gp = torch.empty_like(prior) if (need_p and prior is not None) else None
+        ga = (C.c_float * npairs)() if need_a else None
+        kept = fctx.kept
+        slots = kept.slots if kept is not None else None
+        rows = lambda t: _ptrs(t.view(npairs, -1)) if t is not None else None  # noqa: E731
+        dctx.check(dctx._L.deeds_soft_backward_batch_dev(
+            dctx.handle, npairs, slots, _ptrs(fv), _ptrs(mv), m, n, o, C.byref(params), _ptrs([t[0] for t in trees]),
+            _ptrs([t[1] for t in trees]), _ptrs([t[2] for t in trees]), rows(prior), rows(gdisp), rows(gf), rows(gm),
+            rows(gp), ga, _stream()))
+        if slots is not None:
+            kept.release()  # a second backward (retain_graph) recomputes
+        adt, adev = fctx.alpha_like
+        galpha = torch.tensor(float(sum(ga)), dtype=adt, device=adev) if need_a else None
+        return gf, gm, galpha, gp, None, None, None, None, None
+
+
+def soft_register_levels_batch(fixed, moving, alpha, dims, levels, tau=0.5, eps=0.01, trees=None, ctx=None,
+                               keep_state=True):
+    """soft_register_levels for P pairs of one size at once, the pairs of each
+    level running concurrently (SoftDeedsLevelBatch).  fixed/moving: (P, m*n*o)
+    tensors or lists of P flat tensors; trees: per pair, the list of its
+    per-level MSTs (computed when None).  Returns the last grid fields
+    (P, 3, sz1); pair i's field and gradients are those of soft_register_levels
+    on pair i."""
+    m, n, o = dims
+    if isinstance(fixed, (list, tuple)):
+        fixed = torch.stack([f.reshape(-1) for f in fixed])
+    if isinstance(moving, (list, tuple)):
+        moving = torch.stack([mv.reshape(-1) for mv in moving])
+    npairs = fixed.shape[0]
+    ctx = ctx or context(fixed.device.index or 0)
+    if not isinstance(alpha, torch.Tensor):
+        alpha = torch.tensor(float(alpha), dtype=torch.float32)
+    if trees is None:
+        trees = [[soft_tree(fixed[i], m, n, o, lv[0], ctx) for lv in levels] for i in range(npairs)]
+    prev, prev_dims = None, None
+    for li, (g, hw, q, qs) in enumerate(levels):
+        gdims = (m // g, n // g, o // g)
+        params = soft_params(g, hw, q, float(alpha.detach()), tau, eps, qs)
+        level_trees = [trees[i][li] for i in range(npairs)]
+        if prev is None:
+            prev = SoftDeedsLevelBatch.apply(fixed, moving, alpha, None, tuple(dims), params, level_trees, ctx,
+                                             keep_state)
+        else:
+            U = torch.stack([SoftUpsample.apply(prev[i], prev_dims, gdims, ctx) for i in range(npairs)])
+            warped = torch.stack([SoftWarp.apply(moving[i], U[i], tuple(dims), gdims, ctx) for i in range(npairs)])
+            E = SoftDeedsLevelBatch.apply(fixed, warped, alpha, U, tuple(dims), params, level_trees, ctx, keep_state)
+            prev = U + E
+        prev_dims = gdims
+    return prev
+
+
 # ---------------------------------------------------------------------------
 # linearBCV (src/linearBCV.cpp): affine / rigid pre-registration.
 

@@ -1338,20 +1338,40 @@ deeds_status soft_run_forward(deeds_ctx* ctx, const float* d_fixed, const float*
     return DEEDS_OK;
 }
 
-// Reads the sweeps' error word (synchronises the stream).
-deeds_status soft_check_sweeps(deeds_ctx* ctx, const SoftLevel& L, cudaStream_t s) {
-    int herr = 0;
-    CK(cudaMemcpyAsync(&herr, L.sweep + L.sz1 + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    if (herr) return fail(ctx, DEEDS_ERR_TIMEOUT, "a tree sweep gave up waiting for a node's dependencies");
+// Pinned words a level reads back when its stream is done: the sweeps' error
+// word and the alpha dot product.  Pinned, so that the copies stay asynchronous
+// and several lanes can be in flight.
+struct SoftReadback {
+    int* err = nullptr;
+    double* dot = nullptr;
+};
+
+deeds_status soft_readback(deeds_ctx* ctx, SoftReadback& rb) {
+    deeds_status st = DEEDS_OK;
+    rb.err = hbuf<int>(ctx, "soft_rb_err", 1, &st);
+    rb.dot = hbuf<double>(ctx, "soft_rb_dot", 1, &st);
+    return st;
+}
+
+deeds_status soft_enqueue_status(deeds_ctx* ctx, const SoftLevel& L, const SoftReadback& rb, cudaStream_t s) {
+    CK(cudaMemcpyAsync(rb.err, L.sweep + L.sz1 + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
     return DEEDS_OK;
 }
 
-// The adjoint of one level whose forward state (descriptors, cost volume,
-// messages, marginals) is in L.
-deeds_status soft_run_backward(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, int m, int n, int o,
-                               const deeds_soft_params* p, SoftLevel& L, const float* d_gdisp, float* d_gfixed,
-                               float* d_gmoving, float* d_gprior, float* grad_alpha, cudaStream_t s) {
+// Waits for the stream and reads the sweeps' status.
+deeds_status soft_wait(deeds_ctx* ctx, const SoftReadback& rb, cudaStream_t s) {
+    CK(cudaStreamSynchronize(s));
+    if (*rb.err) return fail(ctx, DEEDS_ERR_TIMEOUT, "a tree sweep gave up waiting for a node's dependencies");
+    return DEEDS_OK;
+}
+
+// Enqueues the adjoint of one level whose forward state (descriptors, cost
+// volume, messages, marginals) is in L, and the read-back of its status and (with
+// want_alpha) of the alpha dot product.
+deeds_status soft_issue_backward(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, int m, int n, int o,
+                                 const deeds_soft_params* p, SoftLevel& L, const float* d_gdisp, float* d_gfixed,
+                                 float* d_gmoving, float* d_gprior, bool want_alpha, const SoftReadback& rb,
+                                 cudaStream_t s) {
     deeds_status st = DEEDS_OK;
     // the MIND scratch is shared and may have been reallocated since L was set up
     L.w6 = dbuf<float>(ctx, "soft_w6", 6 * L.sz, &st);
@@ -1388,11 +1408,70 @@ deeds_status soft_run_backward(deeds_ctx* ctx, const float* d_fixed, const float
         CK(cudaMemsetAsync(d_gmoving, 0, sizeof(float) * L.sz, s));
         CK(launch_soft_descriptor_adj(d_moving, L.w6, L.w6b, sMbar, dbar6, d_gmoving, m, n, o, L.qs, s));
     }
-    double hdot = 0.0;
-    if (grad_alpha) CK(cudaMemcpyAsync(&hdot, dot, sizeof(double), cudaMemcpyDeviceToHost, s));
-    if (deeds_status e = soft_check_sweeps(ctx, L, s)) return e;
-    if (grad_alpha) *grad_alpha = (float)(-hdot / (double)p->alpha);
+    if (want_alpha) CK(cudaMemcpyAsync(rb.dot, dot, sizeof(double), cudaMemcpyDeviceToHost, s));
+    return soft_enqueue_status(ctx, L, rb, s);
+}
+
+float soft_grad_alpha(const SoftReadback& rb, const deeds_soft_params* p) {
+    return (float)(-*rb.dot / (double)p->alpha);
+}
+
+// The first free kept slot of ctx (appended when none is free), marked in use.
+SoftKept& soft_acquire_slot(deeds_ctx* ctx, int* slot) {
+    int k = 0;
+    while (k < (int)ctx->kept.size() && ctx->kept[k]->used) k++;
+    if (k == (int)ctx->kept.size()) ctx->kept.push_back(std::make_shared<SoftKept>());
+    SoftKept& K = *ctx->kept[k];
+    K.used = true;
+    K.valid = false;
+    *slot = k;
+    return K;
+}
+
+std::string soft_slot_tag(int k) { return "softk" + std::to_string(k) + "_"; }
+
+void soft_fill_slot(SoftKept& K, int m, int n, int o, const deeds_soft_params* p, bool prior) {
+    K.m = m; K.n = n; K.o = o;
+    K.p = *p;
+    K.prior = prior;
+    K.valid = true;
+}
+
+// The kept state of `slot` if it was filled for exactly this problem, else NULL
+// with the context's error set.
+SoftKept* soft_kept_for(deeds_ctx* ctx, int slot, int m, int n, int o, const deeds_soft_params* p, bool prior) {
+    if (slot < 0 || slot >= (int)ctx->kept.size() || !ctx->kept[slot]->used || !ctx->kept[slot]->valid) {
+        fail(ctx, DEEDS_ERR_INVALID, "slot %d holds no forward state", slot);
+        return nullptr;
+    }
+    SoftKept& K = *ctx->kept[slot];
+    const bool same = K.m == m && K.n == n && K.o == o && K.p.grid == p->grid && K.p.radius == p->radius &&
+                      K.p.quant == p->quant && K.p.mind_radius == p->mind_radius && K.p.alpha == p->alpha &&
+                      K.p.tau == p->tau && K.p.eps == p->eps && K.prior == prior;
+    if (!same) {
+        fail(ctx, DEEDS_ERR_INVALID, "slot %d was filled for another level or parameters", slot);
+        return nullptr;
+    }
+    return &K;
+}
+
+// Pairs of a batch run in waves of at most this many lanes (child contexts with
+// their own streams and buffers); pair i of a wave runs on lane i.
+constexpr int kSoftMaxLanes = 8;
+
+deeds_status soft_lanes(deeds_ctx* ctx, int want) {
+    while ((int)ctx->lanes.size() < want) {
+        deeds_ctx* lane = nullptr;
+        deeds_status st = deeds_create(&lane, ctx->device);
+        if (st) return fail(ctx, st, "batch lane: %s", deeds_last_error(nullptr));
+        lane->tune = ctx->tune;
+        ctx->lanes.push_back(lane);
+    }
     return DEEDS_OK;
+}
+
+deeds_status lane_fail(deeds_ctx* ctx, deeds_ctx* lane, deeds_status st, int pair) {
+    return fail(ctx, st, "pair %d: %s", pair, lane->err.c_str());
 }
 
 }  // namespace
@@ -1406,9 +1485,12 @@ deeds_status deeds_soft_forward_dev(deeds_ctx* ctx, const float* d_fixed, const 
     if (!d_fixed || !d_moving || !d_disp) return fail(ctx, DEEDS_ERR_INVALID, "null pointer");
     cudaStream_t s = (cudaStream_t)stream;
     SoftLevel L;
+    SoftReadback rb;
+    if (deeds_status e = soft_readback(ctx, rb)) return e;
     if (deeds_status e = soft_setup(ctx, m, n, o, p, ordered, parents, edgemst, d_prior, s, L)) return e;
     if (deeds_status e = soft_run_forward(ctx, d_fixed, d_moving, m, n, o, p, L, d_disp, s)) return e;
-    return soft_check_sweeps(ctx, L, s);
+    if (deeds_status e = soft_enqueue_status(ctx, L, rb, s)) return e;
+    return soft_wait(ctx, rb, s);
 }
 
 deeds_status deeds_soft_backward_dev(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, int m, int n, int o,
@@ -1421,11 +1503,17 @@ deeds_status deeds_soft_backward_dev(deeds_ctx* ctx, const float* d_fixed, const
     if (d_gprior && !d_prior) return fail(ctx, DEEDS_ERR_INVALID, "grad_prior needs a prior field");
     cudaStream_t s = (cudaStream_t)stream;
     SoftLevel L;
+    SoftReadback rb;
+    if (deeds_status e = soft_readback(ctx, rb)) return e;
     if (deeds_status e = soft_setup(ctx, m, n, o, p, ordered, parents, edgemst, d_prior, s, L)) return e;
     // recompute the forward state (descriptors, cost, messages, marginals)
     if (deeds_status e = soft_run_forward(ctx, d_fixed, d_moving, m, n, o, p, L, L.disp, s)) return e;
-    return soft_run_backward(ctx, d_fixed, d_moving, m, n, o, p, L, d_gdisp, d_gfixed, d_gmoving, d_gprior,
-                             grad_alpha, s);
+    if (deeds_status e = soft_issue_backward(ctx, d_fixed, d_moving, m, n, o, p, L, d_gdisp, d_gfixed, d_gmoving,
+                                             d_gprior, grad_alpha != nullptr, rb, s))
+        return e;
+    if (deeds_status e = soft_wait(ctx, rb, s)) return e;
+    if (grad_alpha) *grad_alpha = soft_grad_alpha(rb, p);
+    return DEEDS_OK;
 }
 
 deeds_status deeds_soft_forward_keep_dev(deeds_ctx* ctx, const float* d_fixed, const float* d_moving, int m, int n,
@@ -1435,21 +1523,20 @@ deeds_status deeds_soft_forward_keep_dev(deeds_ctx* ctx, const float* d_fixed, c
     if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
     if (!d_fixed || !d_moving || !d_disp || !slot || !p) return fail(ctx, DEEDS_ERR_INVALID, "null pointer");
     cudaStream_t s = (cudaStream_t)stream;
-    int k = 0;  // first free slot; its buffers (if any) are reused
-    while (k < (int)ctx->kept.size() && ctx->kept[k]->used) k++;
-    if (k == (int)ctx->kept.size()) ctx->kept.push_back(std::make_shared<SoftKept>());
-    SoftKept& K = *ctx->kept[k];
-    K.used = true;
-    K.valid = false;
+    SoftReadback rb;
+    if (deeds_status e = soft_readback(ctx, rb)) return e;
+    int k = -1;
+    SoftKept& K = soft_acquire_slot(ctx, &k);
+    deeds_status e = soft_setup(ctx, m, n, o, p, ordered, parents, edgemst, d_prior, s, K.L, soft_slot_tag(k));
+    if (!e) e = soft_run_forward(ctx, d_fixed, d_moving, m, n, o, p, K.L, d_disp, s);
+    if (!e) e = soft_enqueue_status(ctx, K.L, rb, s);
+    if (!e) e = soft_wait(ctx, rb, s);
+    if (e) {
+        K.used = false;  // nothing is kept
+        return e;
+    }
+    soft_fill_slot(K, m, n, o, p, d_prior != nullptr);
     *slot = k;
-    const std::string tag = "softk" + std::to_string(k) + "_";
-    if (deeds_status e = soft_setup(ctx, m, n, o, p, ordered, parents, edgemst, d_prior, s, K.L, tag)) return e;
-    if (deeds_status e = soft_run_forward(ctx, d_fixed, d_moving, m, n, o, p, K.L, d_disp, s)) return e;
-    if (deeds_status e = soft_check_sweeps(ctx, K.L, s)) return e;
-    K.m = m; K.n = n; K.o = o;
-    K.p = *p;
-    K.prior = d_prior != nullptr;
-    K.valid = true;
     return DEEDS_OK;
 }
 
@@ -1459,16 +1546,18 @@ deeds_status deeds_soft_backward_kept_dev(deeds_ctx* ctx, int slot, const float*
                                           float* grad_alpha, void* stream) {
     if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
     if (!d_fixed || !d_moving || !d_gdisp || !p) return fail(ctx, DEEDS_ERR_INVALID, "null pointer");
-    if (slot < 0 || slot >= (int)ctx->kept.size() || !ctx->kept[slot]->used || !ctx->kept[slot]->valid)
-        return fail(ctx, DEEDS_ERR_INVALID, "slot %d holds no forward state", slot);
-    SoftKept& K = *ctx->kept[slot];
-    const bool same = K.m == m && K.n == n && K.o == o && K.p.grid == p->grid && K.p.radius == p->radius &&
-                      K.p.quant == p->quant && K.p.mind_radius == p->mind_radius && K.p.alpha == p->alpha &&
-                      K.p.tau == p->tau && K.p.eps == p->eps && K.prior == (d_prior != nullptr);
-    if (!same) return fail(ctx, DEEDS_ERR_INVALID, "slot %d was filled for another level or parameters", slot);
     if (d_gprior && !d_prior) return fail(ctx, DEEDS_ERR_INVALID, "grad_prior needs a prior field");
-    return soft_run_backward(ctx, d_fixed, d_moving, m, n, o, p, K.L, d_gdisp, d_gfixed, d_gmoving, d_gprior,
-                             grad_alpha, (cudaStream_t)stream);
+    SoftKept* K = soft_kept_for(ctx, slot, m, n, o, p, d_prior != nullptr);
+    if (!K) return DEEDS_ERR_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    SoftReadback rb;
+    if (deeds_status e = soft_readback(ctx, rb)) return e;
+    if (deeds_status e = soft_issue_backward(ctx, d_fixed, d_moving, m, n, o, p, K->L, d_gdisp, d_gfixed, d_gmoving,
+                                             d_gprior, grad_alpha != nullptr, rb, s))
+        return e;
+    if (deeds_status e = soft_wait(ctx, rb, s)) return e;
+    if (grad_alpha) *grad_alpha = soft_grad_alpha(rb, p);
+    return DEEDS_OK;
 }
 
 deeds_status deeds_soft_release(deeds_ctx* ctx, int slot) {
@@ -1480,16 +1569,175 @@ deeds_status deeds_soft_release(deeds_ctx* ctx, int slot) {
     return DEEDS_OK;
 }
 
-deeds_status deeds_soft_trim(deeds_ctx* ctx) {
-    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+static deeds_status soft_trim_one(deeds_ctx* ctx) {
     CK(cudaSetDevice(ctx->device));
     for (size_t k = 0; k < ctx->kept.size(); k++) {
         if (ctx->kept[k]->used) continue;
-        const std::string tag = "softk" + std::to_string(k) + "_";
+        const std::string tag = soft_slot_tag((int)k);
         for (auto it = ctx->dev.lower_bound(tag); it != ctx->dev.end() && it->first.compare(0, tag.size(), tag) == 0;) {
             if (it->second.p) CK(cudaFree(it->second.p));
             it = ctx->dev.erase(it);
         }
+    }
+    return DEEDS_OK;
+}
+
+deeds_status deeds_soft_trim(deeds_ctx* ctx) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (deeds_status e = soft_trim_one(ctx)) return e;
+    for (deeds_ctx* lane : ctx->lanes)
+        if (deeds_status e = soft_trim_one(lane)) return fail(ctx, e, "lane: %s", lane->err.c_str());
+    return DEEDS_OK;
+}
+
+deeds_status deeds_soft_forward_batch_dev(deeds_ctx* ctx, int npairs, const float* const* d_fixed,
+                                          const float* const* d_moving, int m, int n, int o,
+                                          const deeds_soft_params* p, const int* const* ordered,
+                                          const int* const* parents, const float* const* edgemst,
+                                          const float* const* d_prior, float* const* d_disp, int* slots,
+                                          void* stream) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (npairs < 0) return fail(ctx, DEEDS_ERR_INVALID, "npairs < 0");
+    if (npairs == 0) return DEEDS_OK;
+    if (!d_fixed || !d_moving || !p || !ordered || !parents || !edgemst || !d_disp)
+        return fail(ctx, DEEDS_ERR_INVALID, "null array");
+    for (int i = 0; i < npairs; i++) {
+        if (!d_fixed[i] || !d_moving[i] || !d_disp[i]) return fail(ctx, DEEDS_ERR_INVALID, "pair %d: null pointer", i);
+        if (d_prior && !d_prior[i]) return fail(ctx, DEEDS_ERR_INVALID, "pair %d: null prior", i);
+    }
+    int qs = 0;
+    if (deeds_status e = soft_check(ctx, m, n, o, p, &qs)) return e;
+    const int nl = std::min(npairs, kSoftMaxLanes);
+    if (deeds_status e = soft_lanes(ctx, nl)) return e;
+    cudaStream_t s = (cudaStream_t)stream;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaEventRecord(ctx->ev_a, s));  // inputs written on the caller's stream
+    if (slots)
+        for (int i = 0; i < npairs; i++) slots[i] = -1;
+    for (int w0 = 0; w0 < npairs; w0 += nl) {
+        const int w1 = std::min(npairs, w0 + nl);
+        std::vector<SoftLevel> local(w1 - w0);
+        std::vector<SoftLevel*> lv(w1 - w0);
+        std::vector<SoftReadback> rb(w1 - w0);
+        deeds_status err = DEEDS_OK;
+        int bad = -1;
+        for (int i = w0; i < w1 && !err; i++) {
+            deeds_ctx* lane = ctx->lanes[i - w0];
+            cudaStream_t ls = lane->stream;
+            std::string tag = "soft_";
+            if (slots) {
+                SoftKept& K = soft_acquire_slot(lane, &slots[i]);
+                lv[i - w0] = &K.L;
+                tag = soft_slot_tag(slots[i]);
+            } else {
+                lv[i - w0] = &local[i - w0];
+            }
+            SoftLevel& L = *lv[i - w0];
+            bad = i;
+            if (cudaStreamWaitEvent(ls, ctx->ev_a, 0) != cudaSuccess) err = fail(lane, DEEDS_ERR_CUDA, "event wait");
+            if (!err) err = soft_readback(lane, rb[i - w0]);
+            if (!err)
+                err = soft_setup(lane, m, n, o, p, ordered[i], parents[i], edgemst[i], d_prior ? d_prior[i] : nullptr,
+                                 ls, L, tag);
+            if (!err) err = soft_run_forward(lane, d_fixed[i], d_moving[i], m, n, o, p, L, d_disp[i], ls);
+            if (!err) err = soft_enqueue_status(lane, L, rb[i - w0], ls);
+        }
+        for (int i = w0; i < w1; i++) {  // every issued lane finishes before returning
+            deeds_ctx* lane = ctx->lanes[i - w0];
+            if (!rb[i - w0].err) continue;
+            deeds_status e = soft_wait(lane, rb[i - w0], lane->stream);
+            if (e && !err) { err = e; bad = i; }
+        }
+        if (err) {
+            if (slots)
+                for (int i = 0; i < w1; i++)
+                    if (slots[i] >= 0) {
+                        ctx->lanes[i % nl]->kept[slots[i]]->used = false;
+                        slots[i] = -1;
+                    }
+            return lane_fail(ctx, ctx->lanes[bad - w0], err, bad);
+        }
+        if (slots)
+            for (int i = w0; i < w1; i++)
+                soft_fill_slot(*ctx->lanes[i - w0]->kept[slots[i]], m, n, o, p, d_prior != nullptr);
+    }
+    return DEEDS_OK;
+}
+
+deeds_status deeds_soft_backward_batch_dev(deeds_ctx* ctx, int npairs, const int* slots,
+                                           const float* const* d_fixed, const float* const* d_moving, int m, int n,
+                                           int o, const deeds_soft_params* p, const int* const* ordered,
+                                           const int* const* parents, const float* const* edgemst,
+                                           const float* const* d_prior, const float* const* d_gdisp,
+                                           float* const* d_gfixed, float* const* d_gmoving, float* const* d_gprior,
+                                           float* grad_alpha, void* stream) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (npairs < 0) return fail(ctx, DEEDS_ERR_INVALID, "npairs < 0");
+    if (npairs == 0) return DEEDS_OK;
+    if (!d_fixed || !d_moving || !p || !d_gdisp) return fail(ctx, DEEDS_ERR_INVALID, "null array");
+    if (!slots && (!ordered || !parents || !edgemst))
+        return fail(ctx, DEEDS_ERR_INVALID, "the recomputing backward needs the trees");
+    if (d_gprior && !d_prior) return fail(ctx, DEEDS_ERR_INVALID, "grad_prior needs a prior field");
+    for (int i = 0; i < npairs; i++) {
+        if (!d_fixed[i] || !d_moving[i] || !d_gdisp[i]) return fail(ctx, DEEDS_ERR_INVALID, "pair %d: null pointer", i);
+        if (d_prior && !d_prior[i]) return fail(ctx, DEEDS_ERR_INVALID, "pair %d: null prior", i);
+    }
+    int qs = 0;
+    if (deeds_status e = soft_check(ctx, m, n, o, p, &qs)) return e;
+    const int nl = std::min(npairs, kSoftMaxLanes);
+    if (deeds_status e = soft_lanes(ctx, nl)) return e;
+    std::vector<SoftKept*> kept(npairs, nullptr);
+    if (slots)
+        for (int i = 0; i < npairs; i++) {
+            deeds_ctx* lane = ctx->lanes[i % nl];
+            kept[i] = soft_kept_for(lane, slots[i], m, n, o, p, d_prior != nullptr);
+            if (!kept[i]) return lane_fail(ctx, lane, DEEDS_ERR_INVALID, i);
+        }
+    cudaStream_t s = (cudaStream_t)stream;
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaEventRecord(ctx->ev_a, s));
+    for (int w0 = 0; w0 < npairs; w0 += nl) {
+        const int w1 = std::min(npairs, w0 + nl);
+        std::vector<SoftLevel> local(w1 - w0);
+        std::vector<SoftReadback> rb(w1 - w0);
+        deeds_status err = DEEDS_OK;
+        int bad = -1;
+        for (int i = w0; i < w1 && !err; i++) {
+            deeds_ctx* lane = ctx->lanes[i - w0];
+            cudaStream_t ls = lane->stream;
+            const float* prior = d_prior ? d_prior[i] : nullptr;
+            SoftLevel& L = slots ? kept[i]->L : local[i - w0];
+            bad = i;
+            if (cudaStreamWaitEvent(ls, ctx->ev_a, 0) != cudaSuccess) err = fail(lane, DEEDS_ERR_CUDA, "event wait");
+            if (!err) err = soft_readback(lane, rb[i - w0]);
+            if (!err && !slots) {
+                err = soft_setup(lane, m, n, o, p, ordered[i], parents[i], edgemst[i], prior, ls, L);
+                if (!err) err = soft_run_forward(lane, d_fixed[i], d_moving[i], m, n, o, p, L, L.disp, ls);
+            }
+            if (!err)
+                err = soft_issue_backward(lane, d_fixed[i], d_moving[i], m, n, o, p, L, d_gdisp[i],
+                                          d_gfixed ? d_gfixed[i] : nullptr, d_gmoving ? d_gmoving[i] : nullptr,
+                                          d_gprior ? d_gprior[i] : nullptr, grad_alpha != nullptr, rb[i - w0], ls);
+        }
+        for (int i = w0; i < w1; i++) {
+            deeds_ctx* lane = ctx->lanes[i - w0];
+            if (!rb[i - w0].err) continue;
+            deeds_status e = soft_wait(lane, rb[i - w0], lane->stream);
+            if (e && !err) { err = e; bad = i; }
+            if (!e && !err && grad_alpha) grad_alpha[i] = soft_grad_alpha(rb[i - w0], p);
+        }
+        if (err) return lane_fail(ctx, ctx->lanes[bad - w0], err, bad);
+    }
+    return DEEDS_OK;
+}
+
+deeds_status deeds_soft_release_batch(deeds_ctx* ctx, int npairs, const int* slots) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (npairs < 0 || (npairs > 0 && !slots)) return fail(ctx, DEEDS_ERR_INVALID, "bad slot list");
+    const int nl = std::min(npairs, kSoftMaxLanes);
+    for (int i = 0; i < npairs; i++) {
+        if (i % nl >= (int)ctx->lanes.size()) return fail(ctx, DEEDS_ERR_INVALID, "pair %d: no lane", i);
+        if (deeds_status e = deeds_soft_release(ctx->lanes[i % nl], slots[i])) return lane_fail(ctx, ctx->lanes[i % nl], e, i);
     }
     return DEEDS_OK;
 }

@@ -323,6 +323,38 @@ deeds_status deeds_soft_release(deeds_ctx* ctx, int slot);
 /* Frees the device buffers of every kept slot not in use (synchronises the device). */
 deeds_status deeds_soft_trim(deeds_ctx* ctx);
 
+/* Batched soft level: npairs pairs of one size and one parameter set, each with
+ * its own images, tree (ordered[i], parents[i], edgemst[i]) and, when d_prior is
+ * non-NULL, prior field, run concurrently on lane streams of the context (child
+ * contexts with their own buffers; at most 8 lanes, pair i of each group of 8 on
+ * lane i).  The tree sweeps are latency-bound, so pairs on different lanes fill
+ * each other's idle SMs.  The lanes start after the work already enqueued on
+ * `stream`; the call returns when every lane is done (synchronous, like the
+ * single-pair forms).  With slots non-NULL each pair's forward state is kept:
+ * slots[i] (written) names it in its lane, for deeds_soft_backward_batch_dev
+ * and deeds_soft_release_batch with the same npairs.  Errors name the pair. */
+deeds_status deeds_soft_forward_batch_dev(deeds_ctx* ctx, int npairs, const float* const* d_fixed,
+                                          const float* const* d_moving, int m, int n, int o,
+                                          const deeds_soft_params* p, const int* const* ordered,
+                                          const int* const* parents, const float* const* edgemst,
+                                          const float* const* d_prior, float* const* d_disp, int* slots,
+                                          void* stream);
+
+/* Backward of a batch: with slots (from deeds_soft_forward_batch_dev, same
+ * npairs) over the kept states, else recomputing each pair's forward from its
+ * tree.  d_grad_fixed / d_grad_moving / d_grad_prior: NULL or npairs pointers;
+ * grad_alpha: NULL or npairs floats (dL/dalpha per pair). */
+deeds_status deeds_soft_backward_batch_dev(deeds_ctx* ctx, int npairs, const int* slots,
+                                           const float* const* d_fixed, const float* const* d_moving, int m, int n,
+                                           int o, const deeds_soft_params* p, const int* const* ordered,
+                                           const int* const* parents, const float* const* edgemst,
+                                           const float* const* d_prior, const float* const* d_grad_disp,
+                                           float* const* d_grad_fixed, float* const* d_grad_moving,
+                                           float* const* d_grad_prior, float* grad_alpha, void* stream);
+
+/* Ends the use of a batch's kept slots. */
+deeds_status deeds_soft_release_batch(deeds_ctx* ctx, int npairs, const int* slots);
+
 /* Differentiable trilinear upsampling of a field u|v|w from an mA x nA x oA grid to
  * m x n x o (the coordinates of upsampleDeformationsCL, src/transformations.h:245-279,
  * in float arithmetic), and its adjoint (gin overwritten). */

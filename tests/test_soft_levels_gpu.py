@@ -250,3 +250,89 @@ def test_soft_kept_slot_checks(api):
     ctx.check(L.deeds_soft_trim(ctx.handle))
     assert keep() == 0
     ctx.close()
+
+
+def _batch_case(api, seeds, levels):
+    m, n, o = DIMS
+    pairs = [_pair(s) for s in seeds]
+    F = torch.stack([torch.from_numpy(f) for f, _ in pairs]).cuda()
+    M = torch.stack([torch.from_numpy(mv) for _, mv in pairs]).cuda()
+    trees = [[api.soft_tree(F[i], m, n, o, g) for g, *_ in levels] for i in range(len(seeds))]
+    gl = levels[-1][0]
+    gt = torch.from_numpy(np.random.default_rng(9).normal(0, 1, (len(seeds), 3, (m // gl) * (n // gl) * (o // gl))))
+    return F, M, trees, gt.float().cuda()
+
+
+@pytest.mark.parametrize("keep", [True, False])
+def test_soft_batch_matches_single_pairs(api, keep):
+    """Pairs run concurrently on lanes give each pair's own soft_register_levels
+    field and gradients; a second backward through the retained graph agrees."""
+    F, M, trees, gt = _batch_case(api, (11, 12, 13), LEVELS)
+    Fb, Mb = F.clone().requires_grad_(), M.clone().requires_grad_()
+    ab = torch.tensor(1.6, requires_grad=True)
+    d = api.soft_register_levels_batch(Fb, Mb, ab, DIMS, LEVELS, tau=0.5, trees=trees, keep_state=keep)
+    loss = ((d - gt) ** 2).mean(dim=(1, 2)).sum()
+    loss.backward(retain_graph=True)
+    first = (Fb.grad.clone(), Mb.grad.clone(), ab.grad.clone())
+    Fb.grad, Mb.grad, ab.grad = None, None, None
+    loss.backward()
+    for x, y in zip((Fb.grad, Mb.grad, ab.grad), first):
+        assert _rel(x.cpu().double(), y.cpu().double()) < 1e-3
+    ga_total = 0.0
+    for i in range(F.shape[0]):
+        Fi, Mi = F[i].clone().requires_grad_(), M[i].clone().requires_grad_()
+        ai = torch.tensor(1.6, requires_grad=True)
+        di = api.soft_register_levels(Fi, Mi, ai, DIMS, LEVELS, tau=0.5, trees=trees[i])
+        ((di - gt[i]) ** 2).mean().backward()
+        # float atomics in the cost kernels and adjoints: ~1e-5 voxels across levels
+        assert (d[i].detach() - di.detach()).abs().max().item() <= 1e-4
+        assert _rel(first[0][i].cpu().double(), Fi.grad.cpu().double()) < 1e-3
+        assert _rel(first[1][i].cpu().double(), Mi.grad.cpu().double()) < 1e-3
+        ga_total += ai.grad.item()
+    assert abs(first[2].item() - ga_total) <= 1e-3 * abs(ga_total) + 1e-5
+
+
+def test_soft_batch_more_pairs_than_lanes(api):
+    """Ten pairs run as a wave of eight lanes and a wave of two."""
+    lv = LEVELS[-1:]
+    F, M, trees, gt = _batch_case(api, tuple(range(20, 30)), lv)
+    Fb = F.clone().requires_grad_()
+    d = api.soft_register_levels_batch(Fb, M, 1.6, DIMS, lv, tau=0.5, trees=trees)
+    ((d - gt) ** 2).mean(dim=(1, 2)).sum().backward()
+    for i in (0, 7, 8, 9):
+        Fi = F[i].clone().requires_grad_()
+        di = api.soft_register_levels(Fi, M[i], 1.6, DIMS, lv, tau=0.5, trees=trees[i])
+        ((di - gt[i]) ** 2).mean().backward()
+        assert (d[i].detach() - di.detach()).abs().max().item() <= 1e-4
+        assert _rel(Fb.grad[i].cpu().double(), Fi.grad.cpu().double()) < 1e-3
+
+
+def test_soft_batch_error_names_pair_and_frees_slots(api):
+    """A bad tree in pair 2 fails the batch with the pair named; the slots that
+    the failed call took are free again, so the next batch reuses slot 0."""
+    import ctypes as C
+    lv = LEVELS[-1:]
+    F, M, trees, _ = _batch_case(api, (31, 32, 33), lv)
+    ctx = api.Context(0)
+    bad = [list(t) for t in trees]
+    o_, p_, e_ = api._tree_arrays(bad[2][0])
+    o_ = o_.copy()
+    o_[1] = o_[0]  # a node repeated in the order
+    bad[2][0] = (o_, p_, e_)
+    Fb = F.clone().requires_grad_()
+    with pytest.raises(api.DeedsError, match="pair 2"):
+        api.soft_register_levels_batch(Fb, M, 1.6, DIMS, lv, tau=0.5, trees=bad, ctx=ctx)
+    g, hw, q, qs = lv[0]
+    params = api.soft_params(g, hw, q, 1.6, 0.5, 0.01, qs)
+    sz1 = (DIMS[0] // g) * (DIMS[1] // g) * (DIMS[2] // g)
+    out = torch.empty(3, 3, sz1, device="cuda")
+    slots = (C.c_int * 3)()
+    ta = [api._tree_arrays(t[0]) for t in trees]
+    ctx.check(ctx._L.deeds_soft_forward_batch_dev(
+        ctx.handle, 3, api._ptrs(F), api._ptrs(M), *DIMS, C.byref(params), api._ptrs([t[0] for t in ta]),
+        api._ptrs([t[1] for t in ta]), api._ptrs([t[2] for t in ta]), None, api._ptrs(out), slots, api._stream()))
+    assert list(slots) == [0, 0, 0]  # each pair's lane had its slot 0 free again
+    ctx.check(ctx._L.deeds_soft_release_batch(ctx.handle, 3, slots))
+    with pytest.raises(api.DeedsError):
+        ctx.check(ctx._L.deeds_soft_release_batch(ctx.handle, 3, slots))
+    ctx.close()
