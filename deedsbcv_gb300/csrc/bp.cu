@@ -17,11 +17,11 @@
 // message per tree level.  Children's rows are left holding their messages and
 // the root row its total, as the reference leaves costall.
 //
-// The distance transform of a len^3 block is three axis passes; one thread owns
-// one line of len values, holds them and the 2*len parabola values in
-// registers and produces all len outputs of its line (len^2 candidates, fully
-// unrolled for the compile-time label width), keeping the reference's strict
-// '<' so the first minimiser wins.
+// The distance transform of a len^3 block is three axis passes; a thread owns
+// a run of consecutive outputs of one line, holds the line's len values and the
+// parabola values it needs in registers and scans all len candidates per output
+// (fully unrolled for the compile-time label width), keeping the reference's
+// strict '<' so the first minimiser wins.
 //
 // Downward pass (root to leaves, :258-293): one CTA per tree takes the root's
 // first minimum, then resolves one breadth level per step from the argmin
@@ -50,30 +50,43 @@ __device__ __forceinline__ int atom_add_acq_rel(int* p, int v) {
     return old;
 }
 
-constexpr int bp_threads(int len) {
-    return ((len * len + 31) / 32) * 32 < 64 ? 64 : ((len * len + 31) / 32) * 32;
+// A pass's LEN^2 lines are split into bp_parts(LEN) parts of consecutive
+// outputs, one thread per (line, part): one thread per line left a single warp
+// per scheduler at small label widths, and the passes ran latency-bound along
+// each line's compare chains.  Parts occupy separate whole-warp ranges of the
+// block, so the part index is warp-uniform and each part's output range is a
+// compile-time constant (its parabola values stay in registers).
+constexpr int bp_line_slots(int len) { return (len * len + 31) / 32 * 32; }
+
+constexpr int bp_parts(int len) {
+    // about three outputs per thread, at most 768 threads (registers); one part
+    // above 17 and below 7 labels per axis
+    return len >= 19 || len < 7
+               ? 1
+               : ((len + 2) / 3 < 768 / bp_line_slots(len) ? (len + 2) / 3 : 768 / bp_line_slots(len));
 }
 
-// One axis pass of the min-convolution: out[line, i] = min_s in[line, s] + (i - s + off)^2.
-template <int LEN, int AXIS>
-__device__ __forceinline__ void dt_lines(const float* in, float* out, const short* idx_in, short* idx_out,
-                                         float off) {
-    constexpr int LEN2 = LEN * LEN;
-    constexpr int STRIDE = AXIS == 0 ? 1 : (AXIS == 1 ? LEN : LEN2);
-    const int t = threadIdx.x;
-    if (t >= LEN2) return;
-    const int base = AXIS == 0 ? t * LEN : (AXIS == 1 ? (t % LEN) + (t / LEN) * LEN2 : t);
+constexpr int bp_threads(int len) {
+    return bp_parts(len) * bp_line_slots(len) < 64 ? 64 : bp_parts(len) * bp_line_slots(len);
+}
+
+// Outputs [I0, I1) of one line: out[i] = min_s in[s] + (i - s + off)^2, the
+// first minimiser on ties (strict '<', as the reference).
+template <int LEN, int AXIS, int I0, int I1>
+__device__ __forceinline__ void dt_part(const float* in, float* out, const short* idx_in, short* idx_out, float off,
+                                        int base) {
+    constexpr int STRIDE = AXIS == 0 ? 1 : (AXIS == 1 ? LEN : LEN * LEN);
     float v[LEN];
 #pragma unroll
     for (int s = 0; s < LEN; s++) v[s] = in[base + s * STRIDE];
-    float z[2 * LEN];
+    float z[2 * LEN];  // z[u] = (u - LEN + off)^2 for the u = i - s + LEN this part reads
 #pragma unroll
-    for (int u = 0; u < 2 * LEN; u++) {
+    for (int u = I0 + 1; u < I1 + LEN; u++) {
         const float d = (float)(u - LEN) + off;
         z[u] = d * d;
     }
 #pragma unroll
-    for (int i = 0; i < LEN; i++) {
+    for (int i = I0; i < I1; i++) {
         float best = v[0] + z[i + LEN];
         int bs = 0;
 #pragma unroll
@@ -84,6 +97,31 @@ __device__ __forceinline__ void dt_lines(const float* in, float* out, const shor
         out[base + i * STRIDE] = best;
         idx_out[base + i * STRIDE] = idx_in ? idx_in[base + bs * STRIDE] : (short)(base + bs * STRIDE);
     }
+}
+
+template <int LEN, int AXIS, int P>
+__device__ __forceinline__ void dt_dispatch(int part, const float* in, float* out, const short* idx_in,
+                                            short* idx_out, float off, int base) {
+    constexpr int K = bp_parts(LEN), OPP = (LEN + K - 1) / K;
+    if constexpr (P < K) {
+        if (part == P) {
+            constexpr int I0 = P * OPP, I1 = (P + 1) * OPP < LEN ? (P + 1) * OPP : LEN;
+            if constexpr (I0 < I1) dt_part<LEN, AXIS, I0, I1>(in, out, idx_in, idx_out, off, base);
+            return;
+        }
+        dt_dispatch<LEN, AXIS, P + 1>(part, in, out, idx_in, idx_out, off, base);
+    }
+}
+
+// One axis pass of the min-convolution: out[line, i] = min_s in[line, s] + (i - s + off)^2.
+template <int LEN, int AXIS>
+__device__ __forceinline__ void dt_lines(const float* in, float* out, const short* idx_in, short* idx_out,
+                                         float off) {
+    constexpr int LEN2 = LEN * LEN, LP = bp_line_slots(LEN);
+    const int part = threadIdx.x / LP, line = threadIdx.x - part * LP;
+    if (line >= LEN2) return;
+    const int base = AXIS == 0 ? line * LEN : (AXIS == 1 ? (line % LEN) + (line / LEN) * LEN2 : line);
+    dt_dispatch<LEN, AXIS, 0>(part, in, out, idx_in, idx_out, off, base);
 }
 
 __device__ float block_min(float v, float* red) {
