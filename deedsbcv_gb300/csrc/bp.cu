@@ -40,6 +40,26 @@ namespace {
 
 __device__ __forceinline__ float ld_cg(const float* p) { return __ldcg(p); }
 
+// Loads issued where they stand: volatile asm with a memory clobber is not moved
+// by the compiler, so a load meant to run ahead (its value used steps or passes
+// later) is not sunk next to its use.  .nc for the tree arrays (read-only for the
+// whole kernel), .cg for cost rows (written by other CTAs of the kernel).
+__device__ __forceinline__ int ld_ahead(const int* p) {
+    int v;
+    asm volatile("ld.global.nc.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ float ld_ahead(const float* p) {
+    float v;
+    asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ float ld_ahead_cg(const float* p) {
+    float v;
+    asm volatile("ld.global.cg.f32 %0, [%1];" : "=f"(v) : "l"(p) : "memory");
+    return v;
+}
+
 // Arrival counter increment with release and acquire semantics at GPU scope: the
 // CTA's earlier writes (made visible to this thread by the preceding barrier) are
 // released to whoever later observes the count, and this thread acquires every
@@ -56,6 +76,10 @@ __device__ __forceinline__ int atom_add_acq_rel(int* p, int v) {
 // each line's compare chains.  Parts occupy separate whole-warp ranges of the
 // block, so the part index is warp-uniform and each part's output range is a
 // compile-time constant (its parabola values stay in registers).
+// Children of a parent held in registers by the chain step (a node of the
+// 6-connected grid has at most 6 children; more would be read from memory).
+constexpr int kKidRegs = 6;
+
 constexpr int bp_line_slots(int len) { return (len * len + 31) / 32 * 32; }
 
 constexpr int bp_parts(int len) {
@@ -142,6 +166,7 @@ __device__ float block_min(float v, float* red) {
 template <int LEN>
 __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __restrict__ cost,
                                                            short* __restrict__ allinds, float* __restrict__ mins,
+                                                           const float* __restrict__ off,
                                                            int* __restrict__ arrived, int* __restrict__ work) {
     constexpr int LEN3 = LEN * LEN * LEN;
     constexpr int T = bp_threads(LEN);
@@ -168,13 +193,14 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
             const float* row = cost + (int64_t)node * LEN3;
             for (int l = tid; l < LEN3; l += T) A[l] = __fmul_rn(ld_cg(row + l), e);
         }
-        // The chain's static tree data (parent, child range, displacements, edge
-        // weight) is loaded one step ahead, so a step begins without a dependent
-        // load and the next step's loads overlap this step's transform.
+        // The chain's static tree data is pipelined: the grandparent's id is known
+        // one step ahead and everything else about it (child range, the parent's
+        // edge offsets) is loaded during the step before it is needed, so no load
+        // of a step waits for another load of the same step.
         int p = t.parents[node];
         int c0 = t.child_ptr[p], c1 = t.child_ptr[p + 1];
-        float un = t.u0[node], vn = t.v0[node], wn = t.w0[node];
-        float up = t.u0[p], vp = t.v0[p], wp = t.w0[p];
+        float on_x = off[node], on_y = off[t.sz + node], on_z = off[2 * t.sz + node];
+        int gp = p != t.root ? t.parents[p] : p;  // stays a valid node id at the root
         for (;;) {
             // the parent's row still holds its data cost (it is only written after its
             // own message): load it now, its latency hides behind the transform
@@ -183,18 +209,24 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
 #pragma unroll
             for (int k = 0; k < NL; k++) {
                 const int l = tid + k * T;
-                acc[k] = l < LEN3 ? ld_cg(prow + l) : 0.0f;
+                acc[k] = 0.0f;
+                if (l < LEN3) acc[k] = ld_ahead_cg(prow + l);
             }
-            const float ox = __fdiv_rn(up - un, t.q);
-            const float oy = __fdiv_rn(vp - vn, t.q);
-            const float oz = __fdiv_rn(wp - wn, t.q);
-            // next step: the grandparent's data and the parent's edge weight
-            const bool up_more = p != t.root;
-            const int gp = up_more ? t.parents[p] : p;
-            const float ep = up_more ? t.edgemst[p] : 0.0f;
-            const int gc0 = up_more ? t.child_ptr[gp] : 0, gc1 = up_more ? t.child_ptr[gp + 1] : 0;
-            const float ugp = up_more ? t.u0[gp] : 0.0f, vgp = up_more ? t.v0[gp] : 0.0f,
-                        wgp = up_more ? t.w0[gp] : 0.0f;
+            // the parent's children (the siblings this step may accumulate)
+            int kid[kKidRegs];
+#pragma unroll
+            for (int k = 0; k < kKidRegs; k++) {
+                kid[k] = -1;
+                if (c0 + k < c1) kid[k] = ld_ahead(t.children + c0 + k);
+            }
+            const float ox = on_x, oy = on_y, oz = on_z;
+            // next step: the parent's edge weight and the grandparent's data, all from
+            // ids already in registers; the step after next: the great-grandparent's id
+            const float ep = ld_ahead(t.edgemst + p);
+            const int gc0 = ld_ahead(t.child_ptr + gp), gc1 = ld_ahead(t.child_ptr + gp + 1);
+            const float opx = ld_ahead(off + p), opy = ld_ahead(off + t.sz + p), opz = ld_ahead(off + 2 * t.sz + p);
+            int ggp = gp;
+            if (gp != t.root) ggp = ld_ahead(t.parents + gp);
             __syncthreads();
             dt_lines<LEN, 0>(A, B, nullptr, ia, oy);
             __syncthreads();
@@ -226,8 +258,7 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
             }
             // the parent's row = data cost + sum over children in MST ordering
             // order of (message - min); this CTA's own message is still in B
-            for (int ci = c0; ci < c1; ci++) {
-                const int ch = t.children[ci];
+            auto add_child = [&](int ch) {
                 if (ch == node) {
 #pragma unroll
                     for (int k = 0; k < NL; k++) {
@@ -243,7 +274,11 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
                         if (l < LEN3) acc[k] = acc[k] + (ld_cg(chrow + l) - mch);
                     }
                 }
-            }
+            };
+#pragma unroll
+            for (int k = 0; k < kKidRegs; k++)
+                if (c0 + k < c1) add_child(kid[k]);
+            for (int ci = c0 + kKidRegs; ci < c1; ci++) add_child(t.children[ci]);
             if (p == t.root) {
                 float* rrow = cost + (int64_t)p * LEN3;
 #pragma unroll
@@ -260,9 +295,9 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
                 if (l < LEN3) A[l] = __fmul_rn(acc[k], ep);
             }
             node = p;
-            un = up; vn = vp; wn = wp;
+            on_x = opx; on_y = opy; on_z = opz;
             p = gp; c0 = gc0; c1 = gc1;
-            up = ugp; vp = vgp; wp = wgp;
+            gp = ggp;
         }
     }
 }
@@ -379,6 +414,22 @@ __global__ void __launch_bounds__(1024) k_bp_down(BpTree t, const float* __restr
     }
 }
 
+// Per node the offset of its edge in label units, (u0[parent] - u0[node]) / q
+// (src/regularisation.h:205-208), for x | y | z: constants of the upward pass,
+// computed for all nodes at once so that no chain step waits for a division.
+__global__ void k_bp_offsets(BpTree t, float* __restrict__ off) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= t.sz) return;
+    if (c == t.root) {  // never used: the root has no edge
+        off[c] = off[t.sz + c] = off[2 * t.sz + c] = 0.0f;
+        return;
+    }
+    const int p = t.parents[c];
+    off[c] = __fdiv_rn(t.u0[p] - t.u0[c], t.q);
+    off[t.sz + c] = __fdiv_rn(t.v0[p] - t.v0[c], t.q);
+    off[2 * t.sz + c] = __fdiv_rn(t.w0[p] - t.w0[c], t.q);
+}
+
 template <int LEN>
 cudaError_t launch_up(const BpTree& t, float* cost, short* allinds, float* mins, int* arrived, int* work,
                       int sm_count, cudaStream_t s) {
@@ -393,8 +444,10 @@ cudaError_t launch_up(const BpTree& t, float* cost, short* allinds, float* mins,
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
     int ctas = per_sm * sm_count;
     if (ctas > t.n_leaves) ctas = t.n_leaves;
-    k_bp_up<LEN><<<ctas, T, smem, s>>>(t, cost, allinds, mins, arrived, work);
-    count_launches(1);
+    float* off = mins + t.sz;
+    k_bp_offsets<<<(t.sz + 255) / 256, 256, 0, s>>>(t, off);
+    k_bp_up<LEN><<<ctas, T, smem, s>>>(t, cost, allinds, mins, off, arrived, work);
+    count_launches(2);
     return cudaGetLastError();
 }
 

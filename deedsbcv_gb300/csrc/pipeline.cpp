@@ -385,7 +385,7 @@ deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTre
                          const float* w0, float* u1, float* v1, float* w1, int* d_err, cudaStream_t s) {
     deeds_status st = DEEDS_OK;
     uint32_t* d_blk = dbuf<uint32_t>(ctx, "tree_" + tag, pt.total, &st);
-    float* d_mins = dbuf<float>(ctx, "mins_" + tag, pt.sz, &st);
+    float* d_mins = dbuf<float>(ctx, "mins_" + tag, 4 * (size_t)pt.sz, &st);  // mins | edge offsets x, y, z
     int* d_arrived = dbuf<int>(ctx, "arrived_" + tag, pt.sz, &st);
     int* d_work = dbuf<int>(ctx, "work_" + tag, 1, &st);
     if (st) return st;
@@ -453,7 +453,7 @@ deeds_status acquire_buffers(deeds_ctx* ctx, int m, int n, int o, const deeds_pa
         B.allinds[d] = dbuf<short>(ctx, "allinds_" + tg, B.max_cost, &st);
         B.mpad[d] = dbuf<uint64_t>(ctx, "mpad_" + tg, B.max_pad, &st);
         dbuf<uint32_t>(ctx, "tree_" + tg, pack_layout((int)B.max_sz1).total, &st);
-        dbuf<float>(ctx, "mins_" + tg, B.max_sz1, &st);
+        dbuf<float>(ctx, "mins_" + tg, 4 * B.max_sz1, &st);
         dbuf<int>(ctx, "arrived_" + tg, B.max_sz1, &st);
         dbuf<int>(ctx, "work_" + tg, 1, &st);
     }
