@@ -13,6 +13,7 @@
 // Compiled with -ffp-contract=off (host float arithmetic follows the reference).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <cmath>
@@ -51,6 +52,8 @@ struct deeds_ctx {
     cudaStream_t stream = nullptr;  // used by the host-pointer entry points
     cudaStream_t side = nullptr;    // MST edge costs and their copies
     cudaStream_t stream_b = nullptr;  // backward-direction chain of deeds_register*
+    cudaStream_t bg = nullptr;        // field-independent work deeds_register* overlaps with tree sweeps
+    cudaEvent_t ev_e = nullptr, ev_f = nullptr, ev_g = nullptr;
     cudaEvent_t ev_a = nullptr, ev_b = nullptr, ev_c = nullptr, ev_d = nullptr;
     std::string err;
     std::map<std::string, DevBuf> dev;
@@ -410,7 +413,11 @@ struct PairBuffers {
     size_t max_sz1 = 0, max_cost = 0, max_pad = 0;
     std::vector<int> m1s, n1s, o1s;
     float *fix, *mov, *warp0;
-    uint64_t *c_fix, *c_mov;
+    // MIND codes of the fixed and of the affine-warped moving image, one pair per
+    // distinct MIND step of the level schedule (field-independent)
+    std::vector<int> steps;
+    std::vector<uint64_t*> c_fix, c_mov;
+    float* mind_bg;  // MIND scratch of the stream that computes steps 1.. (deeds_ctx::bg)
     int* d_err;
     float* warped[2];
     uint64_t* c_warp[2];
@@ -440,8 +447,18 @@ deeds_status acquire_buffers(deeds_ctx* ctx, int m, int n, int o, const deeds_pa
     B.fix = dbuf<float>(ctx, "fix", sz, &st);
     B.mov = dbuf<float>(ctx, "mov", sz, &st);
     B.warp0 = dbuf<float>(ctx, "warp0", sz, &st);
-    B.c_fix = dbuf<uint64_t>(ctx, "c_fix", sz, &st);
-    B.c_mov = dbuf<uint64_t>(ctx, "c_mov", sz, &st);
+    B.steps.clear();
+    for (int l = 0; l < L; l++) {
+        const int qs = mind_step(P->quant[l]);
+        if (std::find(B.steps.begin(), B.steps.end(), qs) == B.steps.end()) B.steps.push_back(qs);
+    }
+    B.c_fix.assign(B.steps.size(), nullptr);
+    B.c_mov.assign(B.steps.size(), nullptr);
+    B.mind_bg = B.steps.size() > 1 ? dbuf<float>(ctx, "mind_bg", 6 * sz, &st) : nullptr;
+    for (size_t k = 0; k < B.steps.size(); k++) {
+        B.c_fix[k] = dbuf<uint64_t>(ctx, "c_fix_" + std::to_string(k), sz, &st);
+        B.c_mov[k] = dbuf<uint64_t>(ctx, "c_mov_" + std::to_string(k), sz, &st);
+    }
     B.d_err = dbuf<int>(ctx, "err", 2, &st);
     const char* tags[2] = {"f", "b"};
     for (int d = 0; d < 2; d++) {
@@ -530,6 +547,10 @@ deeds_status deeds_create(deeds_ctx** out, int device) {
     CK(cudaEventCreateWithFlags(&c->ev_c, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c->ev_d, cudaEventDisableTiming));
     CK(cudaStreamCreateWithFlags(&c->stream_b, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&c->bg, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&c->ev_e, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->ev_f, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&c->ev_g, cudaEventDisableTiming));
     *out = c.release();
     return DEEDS_OK;
 }
@@ -539,14 +560,14 @@ void deeds_destroy(deeds_ctx* ctx) {
     for (deeds_ctx* lane : ctx->lanes) deeds_destroy(lane);
     ctx->lanes.clear();
     cudaSetDevice(ctx->device);
-    for (cudaStream_t st : {ctx->stream, ctx->stream_b, ctx->side})
+    for (cudaStream_t st : {ctx->stream, ctx->stream_b, ctx->side, ctx->bg})
         if (st) cudaStreamSynchronize(st);
     for (auto& kv : ctx->dev) if (kv.second.p) cudaFree(kv.second.p);
     for (auto& kv : ctx->host) if (kv.second.p) cudaFreeHost(kv.second.p);
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
-    for (cudaEvent_t e : {ctx->ev_a, ctx->ev_b, ctx->ev_c, ctx->ev_d})
+    for (cudaEvent_t e : {ctx->ev_a, ctx->ev_b, ctx->ev_c, ctx->ev_d, ctx->ev_e, ctx->ev_f, ctx->ev_g})
         if (e) cudaEventDestroy(e);
-    for (cudaStream_t st : {ctx->stream, ctx->stream_b, ctx->side})
+    for (cudaStream_t st : {ctx->stream, ctx->stream_b, ctx->side, ctx->bg})
         if (st) cudaStreamDestroy(st);
     delete ctx;
 }
@@ -753,8 +774,6 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
     float* fix = B.fix;
     float* mov = B.mov;
     float* warp0 = B.warp0;
-    uint64_t* c_fix = B.c_fix;
-    uint64_t* c_mov = B.c_mov;
     int* d_err = B.d_err;
     float** warped = B.warped;
     uint64_t** c_warp = B.c_warp;
@@ -853,7 +872,7 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
     // ---- level loop (src/deedsBCV0.cpp:222-330)
     int m2 = m1s[0], n2 = n1s[0], o2 = o1s[0];
     CK(cudaMemsetAsync(grid, 0, 6 * max_sz1 * sizeof(float), s));
-    int prev_step = -1;
+    bool bg_joined = false;
     for (int l = 0; l < L; l++) {
         const int g = P->grid[l], hw = P->radius[l], q = P->quant[l];
         const int qs = mind_step(q);
@@ -861,12 +880,18 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
         const int len = 2 * hw + 1;
         if (P->verbose)
             printf("Level %d grid=%d with sizes: %dx%dx%d hw=%d quant=%d\n", l, g, m1, n1, o1, hw, q);
-        if (l == 0 || qs != prev_step) {
+        const size_t ks = std::find(B.steps.begin(), B.steps.end(), qs) - B.steps.begin();
+        uint64_t* c_fix = B.c_fix[ks];
+        uint64_t* c_mov = B.c_mov[ks];
+        if (ks > 0 && !bg_joined) {  // codes of the background stream (both directions follow s)
+            CK(cudaStreamWaitEvent(s, ctx->ev_g, 0));
+            bg_joined = true;
+        }
+        if (l == 0) {
             StageScope sc(ctx, DEEDS_STAGE_MIND, s);
             CK(launch_mind_ssc(warp0, m, n, o, qs, thr, mind_scr[0], c_mov, s));
             CK(launch_mind_ssc(fix, m, n, o, qs, thr, mind_scr[0], c_fix, s));
         }
-        prev_step = qs;
         int sy, sx, szs;
         float alpha1;
         data_cost_params(g, q, P->alpha, &sy, &sx, &szs, &alpha1);
@@ -893,6 +918,23 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
                 CK(data_cost_auto(ctx, d == 0 ? c_fix : c_mov, c_warp[d], mpad[d], m, n, o, g, hw, q, P->alpha,
                                   cost[d], d_err + d, sdd));
             }
+        }
+        if (l == 0 && B.steps.size() > 1) {
+            // the other levels' field-independent codes on their own stream, after both
+            // directions' level-0 cost volumes: they run while the coarsest tree sweeps
+            // leave most of the GPU idle; the first level that needs them waits (ev_g)
+            CK(cudaEventRecord(ctx->ev_e, sd[0]));
+            CK(cudaEventRecord(ctx->ev_f, sd[1]));
+            CK(cudaStreamWaitEvent(ctx->bg, ctx->ev_e, 0));
+            CK(cudaStreamWaitEvent(ctx->bg, ctx->ev_f, 0));
+            {
+                StageScope sc(ctx, DEEDS_STAGE_MIND, ctx->bg);
+                for (size_t k = 1; k < B.steps.size(); k++) {
+                    CK(launch_mind_ssc(warp0, m, n, o, B.steps[k], thr, B.mind_bg, B.c_mov[k], ctx->bg));
+                    CK(launch_mind_ssc(fix, m, n, o, B.steps[k], thr, B.mind_bg, B.c_fix[k], ctx->bg));
+                }
+            }
+            CK(cudaEventRecord(ctx->ev_g, ctx->bg));
         }
         for (int d = 0; d < 2; d++) {
             const int t = 2 * l + d;
