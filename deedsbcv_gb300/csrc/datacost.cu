@@ -79,6 +79,17 @@ __global__ void k_pad_codes(const uint64_t* __restrict__ M, uint64_t* __restrict
     Mp[y + (int64_t)x * mpp + (int64_t)z * mpp * np] = __ldg(M + src);
 }
 
+// Sum of the G sample-row partials of tile node t at label ly into its cost entry.
+template <int G>
+__device__ __forceinline__ void reduce_rows(const int* red, int nthr, int t, int ly, float* cost_lx, int len3,
+                                            float alpha1) {
+    const int* r = red + ly * nthr + t * G;
+    int sum = 0;
+#pragma unroll
+    for (int ii = 0; ii < G; ii++) sum += r[ii];
+    cost_lx[(int64_t)t * len3 + ly] = __fmul_rn((float)sum, alpha1);
+}
+
 // LEN_T/Q_T > 0: label width and quantisation fixed at compile time (the default
 // level schedule), so every label loop is exact and fully unrolled; 0: runtime
 // values, labels processed in chunks of 8 with guards.
@@ -93,7 +104,6 @@ __global__ void __launch_bounds__(256) k_data_cost_tma(const __grid_constant__ C
     constexpr int S = G > 4 ? 2 : 1;  // x and z sampling stride (RAND_SAMPLES=1, src/dataCostD.h:141-155)
     constexpr int NX = (G + S - 1) / S, NZ = (G + S - 1) / S;
     constexpr int NC = NX * NZ;       // sampled (x, z) columns per node
-    constexpr int WN = 32 / G;        // nodes per warp: lane = node * G + i
     constexpr int CHUNK = 8;          // labels accumulated per pass over the columns
     extern __shared__ __align__(128) uint64_t smem_raw[];
     // TMA destinations must start on 128-byte boundaries: align explicitly
@@ -104,7 +114,7 @@ __global__ void __launch_bounds__(256) k_data_cost_tma(const __grid_constant__ C
     const int bstride = (box + 15) & ~15;
     uint64_t* buf0 = smem;
     uint64_t* buf1 = smem + bstride;
-    int* red = reinterpret_cast<int*>(smem + 2 * bstride);  // [warps][len][32] partial sums
+    int* red = reinterpret_cast<int*>(smem + 2 * bstride);  // [len][threads] partial sums
     const int m1 = m / G, n1 = n / G;
     const int tiles_y = (m1 + ny_tile - 1) / ny_tile;
     int b = blockIdx.x;
@@ -117,7 +127,7 @@ __global__ void __launch_bounds__(256) k_data_cost_tma(const __grid_constant__ C
     const int y0 = y_first * G;  // padded y of the tile's first row (the pad offset cancels)
     const int y_al = y0 & ~1;    // TMA: the innermost coordinate must be 16-byte aligned
     const int yoff = y0 - y_al;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tid = threadIdx.x, nthr = blockDim.x;
     const int len2 = len * len, len3 = len2 * len;
     const int64_t mn = (int64_t)m * n;
     const uint32_t box_bytes = (uint32_t)box * 8u;
@@ -137,18 +147,23 @@ __global__ void __launch_bounds__(256) k_data_cost_tma(const __grid_constant__ C
             tma_load_3d(buf1, &map, &bars[1], y_al, xbase + q, zbase);
         }
     }
-    // this lane's node (within the tile) and sample row i; its fixed codes stay in registers
-    const int wn = lane / G, i = lane - (lane / G) * G;
-    const int tn = warp * WN + wn;  // node index within the tile
-    const bool active = lane < WN * G && tn < ny_here;
+    // this thread's node (within the tile) and sample row i: thread = node * G + i over
+    // the whole block, so a node's rows may straddle two warps and no lane idles
+    // but the last warp's tail; its fixed codes stay in registers
+    const int tn = tid / G, i = tid - (tid / G) * G;  // node index within the tile, sample row
+    const bool active = tn < ny_here;
     uint64_t fr[NC];
 #pragma unroll
     for (int c = 0; c < NC; c++) {
         const int j = c % NX, k = c / NX;
         fr[c] = active ? F[(y0 + tn * G + i) + (int64_t)(xbase + j * S) * m + (int64_t)(nzn * G + k * S) * mn] : 0ull;
     }
-    int* wred = red + warp * len * 32;
-    const int pos = yoff + tn * G + i;  // this lane's row in the box (for label ly add ly*q)
+    const int pos = yoff + tn * G + i;  // this thread's row in the box (for label ly add ly*q)
+    // partial sums: [warp][len][32] when g divides 32 (the warp reduces its own
+    // nodes), else [len][threads] (nodes straddle warps: the block reduces)
+    constexpr bool kWarpLocal = 32 % G == 0;
+    int* wred = kWarpLocal ? red + (tid >> 5) * len * 32 + (tid & 31) : red + tid;
+    const int wstride = kWarpLocal ? 32 : nthr;
     for (int lx = 0; lx < len; lx++) {
         const int slot = lx & 1;
         const uint64_t* sb = slot ? buf1 : buf0;
@@ -169,7 +184,7 @@ __global__ void __launch_bounds__(256) k_data_cost_tma(const __grid_constant__ C
                 for (int u = 0; u < LF; u++) acc[u] += __popcll(fr[c] ^ col[u * QF]);
             }
 #pragma unroll
-            for (int u = 0; u < LF; u++) wred[u * 32 + lane] = acc[u];
+            for (int u = 0; u < LF; u++) wred[u * wstride] = acc[u];
         } else if (active) {
             for (int ly0 = 0; ly0 < len; ly0 += CHUNK) {
                 int acc[CHUNK];
@@ -184,24 +199,29 @@ __global__ void __launch_bounds__(256) k_data_cost_tma(const __grid_constant__ C
                 }
 #pragma unroll
                 for (int u = 0; u < CHUNK; u++)
-                    if (ly0 + u < len) wred[(ly0 + u) * 32 + lane] = acc[u];
+                    if (ly0 + u < len) wred[(ly0 + u) * wstride] = acc[u];
             }
         }
-        __syncwarp();
-        // sum the G sample rows of each (node, ly) of this warp
-        for (int e = lane; e < WN * len; e += 32) {
-            const int en = e / len, ly = e - (e / len) * len;
-            const int node_t = warp * WN + en;
-            if (node_t < ny_here) {
-                const int* r = wred + ly * 32 + en * G;
-                int sum = 0;
-#pragma unroll
-                for (int ii = 0; ii < G; ii++) sum += r[ii];
-                const int node = (y_first + node_t) + nxn * m1 + nzn * m1 * n1;
-                cost[(int64_t)node * len3 + ly + lx * len + lz * len2] = __fmul_rn((float)sum, alpha1);
+        // sum the G sample rows of each (node, ly): within the warp when g divides 32
+        // (no node straddles two warps), else over the block
+        // (cost row of tile node t, label ly): node (y_first + t) + nxn m1 + nzn m1 n1
+        float* cost_lx = cost + (int64_t)(y_first + nxn * m1 + nzn * m1 * n1) * len3 + lx * len + lz * len2;
+        if constexpr (kWarpLocal) {
+            constexpr int WN = 32 / G;  // nodes per warp
+            __syncwarp();
+            const int warp = tid >> 5, lane = tid & 31;
+            const int* wr = red + warp * len * 32;
+            for (int e = lane; e < WN * len; e += 32) {
+                const int en = e / len, node_t = warp * WN + en;
+                if (node_t < ny_here) reduce_rows<G>(wr, 32, en, e - en * len, cost_lx + (int64_t)warp * WN * len3, len3,
+                                                     alpha1);
             }
+        } else {
+            __syncthreads();
+            for (int e = tid; e < ny_here * len; e += nthr)
+                reduce_rows<G>(red, nthr, e / len, e - (e / len) * len, cost_lx, len3, alpha1);
         }
-        __syncthreads();  // every thread is done with this buffer and with wred
+        __syncthreads();  // every thread is done with this buffer and with red
         if (tid == 0 && lx + 2 < len) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             mbar_expect_tx(&bars[slot], box_bytes);
@@ -271,12 +291,14 @@ EncodeTiledFn encode_fn() {
     return fn;
 }
 
+// threads of a cost-volume block: one per (node, sample row) of the tile, whole warps
+int data_cost_tma_threads(int g, int ny_tile) { return (ny_tile * g + 31) / 32 * 32; }
+
 size_t data_cost_tma_smem(int g, int hw, int q, int ny_tile) {
     const int S = g > 4 ? 2 : 1, NX = (g + S - 1) / S;
     const int len = 2 * hw + 1;
     const int yb = ((ny_tile * g + (len - 1) * q + 1) + 1) & ~1;
-    const int warps = (ny_tile + (32 / g) - 1) / (32 / g);
-    return (size_t)2 * ((NX * NX * yb + 15) & ~15) * 8 + (size_t)warps * len * 32 * 4 + 128;
+    return (size_t)2 * ((NX * NX * yb + 15) & ~15) * 8 + (size_t)data_cost_tma_threads(g, ny_tile) * len * 4 + 128;
 }
 
 template <int G, int LEN_T, int Q_T>
@@ -284,7 +306,6 @@ cudaError_t launch_tma(const uint64_t* d_F, const uint64_t* d_Mp, int mpp, int n
                        int hw, int q, int ny_tile, float alpha1, float* d_cost, int* d_err, cudaStream_t s) {
     constexpr int S = G > 4 ? 2 : 1;
     constexpr int NX = (G + S - 1) / S, NZ = (G + S - 1) / S;
-    constexpr int WN = 32 / G;
     const int len = 2 * hw + 1;
     const int yb = ((ny_tile * G + (len - 1) * q + 1) + 1) & ~1;  // +1 for the alignment shift, rounded to even
     CUtensorMap map;
@@ -298,7 +319,7 @@ cudaError_t launch_tma(const uint64_t* d_F, const uint64_t* d_Mp, int mpp, int n
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return cudaErrorInvalidValue;
-    const int warps = (ny_tile + WN - 1) / WN;
+    const int threads = data_cost_tma_threads(G, ny_tile);
     const size_t smem = data_cost_tma_smem(G, hw, q, ny_tile);
     cudaError_t e =
         cudaFuncSetAttribute(k_data_cost_tma<G, LEN_T, Q_T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -306,7 +327,7 @@ cudaError_t launch_tma(const uint64_t* d_F, const uint64_t* d_Mp, int mpp, int n
     const int m1 = m / G, n1 = n / G, o1 = o / G;
     const int tiles_y = (m1 + ny_tile - 1) / ny_tile;
     dim3 grid((unsigned)(tiles_y * n1 * o1), (unsigned)len);
-    k_data_cost_tma<G, LEN_T, Q_T><<<grid, warps * 32, smem, s>>>(map, d_F, d_cost, m, n, o, len, q, ny_tile, yb,
+    k_data_cost_tma<G, LEN_T, Q_T><<<grid, threads, smem, s>>>(map, d_F, d_cost, m, n, o, len, q, ny_tile, yb,
                                                                    alpha1, d_err);
     count_launches(1);
     return cudaGetLastError();
@@ -317,8 +338,7 @@ cudaError_t launch_tma(const uint64_t* d_F, const uint64_t* d_Mp, int mpp, int n
 bool data_cost_tma_supported(int g, int hw, int q, int ny_tile) {
     if (g < 2 || g > 8 || ny_tile < 1) return false;
     const int len = 2 * hw + 1;
-    const int warps = (ny_tile + (32 / g) - 1) / (32 / g);
-    if (warps * 32 > 256) return false;
+    if (data_cost_tma_threads(g, ny_tile) > 256) return false;
     const int yb = ((ny_tile * g + (len - 1) * q + 1) + 1) & ~1;
     if (yb > 256) return false;
     return data_cost_tma_smem(g, hw, q, ny_tile) <= 200 * 1024 && encode_fn() != nullptr;

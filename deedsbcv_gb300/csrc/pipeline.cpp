@@ -268,23 +268,32 @@ cudaError_t data_cost_auto(deeds_ctx* ctx, const uint64_t* F, const uint64_t* M,
     if (it != ctx->tune->tile.end()) {
         tile = it->second;
     } else {
-        const int wn = 32 / g;  // nodes per warp of the TMA kernel
-        const int cands[] = {wn, 2 * wn, 3 * wn, 4 * wn, 6 * wn, 8 * wn};
+        // tiles of whole warps' worth of (node, sample row) threads: 32k/g nodes
+        int cands[8];
+        for (int k = 1; k <= 8; k++) cands[k - 1] = 32 * k / g;
         tile = 0;
         float best = 1e30f;
         cudaEvent_t a, b;
         if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) return cudaErrorUnknown;
+        // once per shape and context: time the candidates with the device otherwise
+        // idle (other streams of the registration would skew the comparison), best
+        // of three launches each after a warm-up launch
+        cudaDeviceSynchronize();
         for (int c : cands) {
             if (!data_cost_tma_supported(g, hw, q, c) || c > m / g) continue;
             cudaError_t e = launch_data_cost_tma(F, M, Mpad, m, n, o, g, hw, q, c, alpha1, cost, d_err, s);
             if (e != cudaSuccess) { cudaGetLastError(); continue; }
-            cudaEventRecord(a, s);
-            for (int r = 0; r < 2; r++) launch_data_cost_tma(F, M, Mpad, m, n, o, g, hw, q, c, alpha1, cost, d_err, s);
-            cudaEventRecord(b, s);
-            if (cudaEventSynchronize(b) != cudaSuccess) { cudaGetLastError(); continue; }
-            float ms = 0.0f;
-            cudaEventElapsedTime(&ms, a, b);
-            if (ms < best) { best = ms; tile = c; }
+            float c_best = 1e30f;
+            for (int r = 0; r < 3; r++) {
+                cudaEventRecord(a, s);
+                launch_data_cost_tma(F, M, Mpad, m, n, o, g, hw, q, c, alpha1, cost, d_err, s);
+                cudaEventRecord(b, s);
+                if (cudaEventSynchronize(b) != cudaSuccess) { cudaGetLastError(); break; }
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, a, b);
+                c_best = std::min(c_best, ms);
+            }
+            if (c_best < best) { best = c_best; tile = c; }
         }
         cudaEventDestroy(a);
         cudaEventDestroy(b);
