@@ -94,6 +94,123 @@ __device__ __forceinline__ float sample(const float* __restrict__ v, const Corne
                         __ldg(v + c.o110), __ldg(v + c.o101), __ldg(v + c.o011), __ldg(v + c.o111));
 }
 
+// ---- The same blend in float-float, with a proof that it rounds the same way
+//
+// GB300 runs FP64 at a small fraction of its FP32 rate, and the blends above are
+// most of the warps' work.  blend8_apply evaluates a fixed expression: exact
+// weight factors 1-d (double), exact products of two of them, one rounded
+// product per weight, eight rounded products with the corner values, seven
+// rounded sums, one float term (dx*dy*dz*c111) and a final rounding to float.
+// With S = sum of |corner values| (weights are at most 1), its double result
+// differs from the exact value of the expression by at most ~2^-49.8 S (each of
+// the ~16 double roundings adds at most 2^-53 of an intermediate bounded by S).
+// The float-float evaluation below (Dekker/Knuth error-free sum and product
+// transformations, the product error through fmaf; every non-exact step has a
+// relative error of at most ~2^-45) differs from it by at most ~2^-42.6 S.  So
+// the two differ by less than eps = 2^-40 S.  If the float-float value lies
+// farther than eps from every midpoint between adjacent floats, both round to
+// the same float, and that float is returned; otherwise (a value near a
+// midpoint, non-finite or very small or large inputs) ff_blend8 reports failure
+// and the caller evaluates blend8_apply.
+struct FF {
+    float hi, lo;
+};
+
+__device__ __forceinline__ FF ff_two_sum(float a, float b) {  // exact: hi + lo = a + b
+    const float s = __fadd_rn(a, b);
+    const float bv = __fsub_rn(s, a);
+    const float av = __fsub_rn(s, bv);
+    return FF{s, __fadd_rn(__fsub_rn(a, av), __fsub_rn(b, bv))};
+}
+
+__device__ __forceinline__ FF ff_prod(float a, float b) {  // exact: hi + lo = a * b
+    const float p = __fmul_rn(a, b);
+    return FF{p, __fmaf_rn(a, b, -p)};
+}
+
+__device__ __forceinline__ FF ff_renorm(float a, float b) {  // |a| >= |b| or a == 0: exact
+    const float s = __fadd_rn(a, b);
+    return FF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ FF ff_mul(FF x, FF y) {
+    const FF p = ff_prod(x.hi, y.hi);
+    return ff_renorm(p.hi, __fadd_rn(p.lo, __fadd_rn(__fmul_rn(x.hi, y.lo), __fmul_rn(x.lo, y.hi))));
+}
+
+__device__ __forceinline__ FF ff_mul_f(FF x, float f) {
+    const FF p = ff_prod(x.hi, f);
+    return ff_renorm(p.hi, __fadd_rn(p.lo, __fmul_rn(x.lo, f)));
+}
+
+__device__ __forceinline__ FF ff_add(FF x, FF y) {
+    const FF s = ff_two_sum(x.hi, y.hi);
+    return ff_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo)));
+}
+
+struct FFWeights {
+    FF w000, w100, w010, w001, w110, w101, w011;
+    float dxdydz;
+};
+
+// The weights of blend8_weights in float-float (the same factors and products).
+__device__ __forceinline__ FFWeights ff_weights(float dx, float dy, float dz) {
+    FFWeights b;
+    const FF a = ff_two_sum(1.0f, -dx), bb = ff_two_sum(1.0f, -dy), c = ff_two_sum(1.0f, -dz);
+    const FF ab = ff_mul(a, bb);
+    const FF ady = ff_mul_f(a, dy);
+    const FF dxb = ff_mul_f(bb, dx);
+    const float dxdy = dx * dy;  // float, as the reference's dx*dy
+    b.w000 = ff_mul(ab, c);
+    b.w100 = ff_mul(ady, c);
+    b.w010 = ff_mul(dxb, c);
+    b.w001 = ff_mul_f(ab, dz);
+    b.w110 = ff_mul_f(c, dxdy);
+    b.w101 = ff_mul_f(ady, dz);
+    b.w011 = ff_mul_f(dxb, dz);
+    b.dxdydz = dxdy * dz;
+    return b;
+}
+
+// blend8_apply's result if it can be proven from the float-float evaluation.
+__device__ __forceinline__ bool ff_blend8(const FFWeights& b, float c000, float c100, float c010, float c001,
+                                          float c110, float c101, float c011, float c111, float& out) {
+    const float S = fabsf(c000) + fabsf(c100) + fabsf(c010) + fabsf(c001) + fabsf(c110) + fabsf(c101) +
+                    fabsf(c011) + fabsf(c111);
+    if (!(S >= 0x1p-60f && S <= 0x1p+100f)) return false;  // also NaN / infinite corners
+    FF acc = ff_mul_f(b.w000, c000);
+    acc = ff_add(acc, ff_mul_f(b.w100, c100));
+    acc = ff_add(acc, ff_mul_f(b.w010, c010));
+    acc = ff_add(acc, ff_mul_f(b.w001, c001));
+    acc = ff_add(acc, ff_mul_f(b.w110, c110));
+    acc = ff_add(acc, ff_mul_f(b.w101, c101));
+    acc = ff_add(acc, ff_mul_f(b.w011, c011));
+    acc = ff_add(acc, FF{b.dxdydz * c111, 0.0f});
+    const float f = __fadd_rn(acc.hi, acc.lo);  // the float nearest to hi + lo
+    const uint32_t bits = __float_as_uint(f) & 0x7fffffffu;
+    const uint32_t e = bits >> 23;
+    // half the gap to the next float on either side (below a power of two the gap halves)
+    const uint32_t he = (bits & 0x7fffffu) ? e - 24u : e - 25u;
+    if (e < 27u || e > 253u) return false;  // zero, tiny or huge: no fast answer
+    const float half_gap = __uint_as_float(he << 23);
+    const float d = __fadd_rn(__fsub_rn(acc.hi, f), acc.lo);  // (hi + lo) - f, to one rounding
+    const float eps = S * 0x1p-40f;
+    if (!(fabsf(d) * 1.0000005f + eps < half_gap)) return false;
+    out = f;
+    return true;
+}
+
+// sample() through the float-float evaluation, falling back to the double one.
+__device__ __forceinline__ float sample_ff(const float* __restrict__ v, const Corners& c, const FFWeights& w,
+                                           float dx, float dy, float dz) {
+    const float c000 = __ldg(v + c.o000), c100 = __ldg(v + c.o100), c010 = __ldg(v + c.o010),
+                c001 = __ldg(v + c.o001), c110 = __ldg(v + c.o110), c101 = __ldg(v + c.o101),
+                c011 = __ldg(v + c.o011), c111 = __ldg(v + c.o111);
+    float r;
+    if (ff_blend8(w, c000, c100, c010, c001, c110, c101, c011, c111, r)) return r;
+    return blend8_apply(blend8_weights(dx, dy, dz), c000, c100, c010, c001, c110, c101, c011, c111);
+}
+
 // Split a float coordinate into floor (as int) and fraction, as `int x=floor(x1);
 // float dx=x1-x;` does in the reference.
 __device__ __forceinline__ void split_coord(float c, int& i, float& f) {

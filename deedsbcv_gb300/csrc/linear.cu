@@ -36,7 +36,7 @@ __global__ void k_lin_warp(const float* __restrict__ in, Affine12 X, float* __re
         out[p] = 0.0f;
         return;
     }
-    out[p] = sample(in, corners(y, x, z, m, n, o), blend8_weights(dx, dy, dz));
+    out[p] = sample_ff(in, corners(y, x, z, m, n, o), ff_weights(dx, dy, dz), dx, dy, dz);
 }
 
 // One smoothing pass of estimateAffine2 (src/affineLTS1.h:124-158) along an axis

@@ -6,9 +6,11 @@
 // evaluates upsampleDeformationsCL's trilinear grid interpolation for its own
 // voxel (identical arithmetic) and immediately warps the image.  Interpolation
 // weights are evaluated in FP64 exactly where the reference's C++ promotes to
-// double (see common.cuh).  Roofline: per voxel 4 B image gather (L2) + 4 B
-// write; the grid field is L2-resident; on GB300 the FP64 blend (~80 DP ops per
-// voxel for field + image) bounds these kernels, not HBM.
+// double (see common.cuh).  The blends run in float-float first and take the
+// double evaluation only where the float-float value cannot prove the
+// reference's rounding (ff_blend8): GB300's FP64 rate would otherwise bound
+// these kernels (~80 DP operations per voxel for field + image).  Roofline: per
+// voxel 4 B image gather (L2) + 4 B write; the grid field is L2-resident.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -33,10 +35,10 @@ __device__ __forceinline__ void upsample_at(const Grid3& g, int i, int j, int k,
     split_coord(__fdiv_rn((float)i, g.sm), y, dy);
     split_coord(__fdiv_rn((float)k, g.so), z, dz);
     const Corners c = corners(y, x, z, g.m, g.n, g.o);
-    const Blend8Weights b = blend8_weights(dx, dy, dz);
-    u = sample(g.u, c, b);
-    v = sample(g.v, c, b);
-    w = sample(g.w, c, b);
+    const FFWeights b = ff_weights(dx, dy, dz);
+    u = sample_ff(g.u, c, b, dx, dy, dz);
+    v = sample_ff(g.v, c, b, dx, dy, dz);
+    w = sample_ff(g.w, c, b, dx, dy, dz);
 }
 
 struct Affine12 {
@@ -83,7 +85,7 @@ __global__ void k_warp_affine(const float* __restrict__ in, Affine12 X, int mode
     split_coord(x1, x, dx);
     split_coord(y1, y, dy);
     split_coord(z1, z, dz);
-    out[p] = sample(in, corners(y, x, z, m, n, o), blend8_weights(dx, dy, dz));
+    out[p] = sample_ff(in, corners(y, x, z, m, n, o), ff_weights(dx, dy, dz), dx, dy, dz);
 }
 
 // warpImageCL = interp3(flag=true) (src/dataCostD.h:213-223, src/transformations.h:9-22)
@@ -104,7 +106,7 @@ __global__ void k_warp_image(const float* __restrict__ in, int mode, Grid3 g, co
     split_coord(u, x, dx);
     split_coord(v, y, dy);
     split_coord(w, z, dz);
-    out[p] = sample(in, corners(y + i, x + j, z + k, m, n, o), blend8_weights(dx, dy, dz));
+    out[p] = sample_ff(in, corners(y + i, x + j, z + k, m, n, o), ff_weights(dx, dy, dz), dx, dy, dz);
 }
 
 // warpAffineS (src/dataCostD.h:241-266): nearest neighbour, round half away from zero.

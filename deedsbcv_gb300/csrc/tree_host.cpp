@@ -90,7 +90,7 @@ void image_stats(const float* im, size_t sz, float* mean_out, float* std_out) {
 }
 
 #ifndef DEEDS_HEAP_LOOKAHEAD
-#define DEEDS_HEAP_LOOKAHEAD 3
+#define DEEDS_HEAP_LOOKAHEAD 4  // levels ahead of the sift-down that are prefetched (two lines)
 #endif
 
 namespace {
@@ -180,11 +180,13 @@ class EdgeHeap {
 void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int g, int* ordered, int* parents,
                     float* edgemst) {
     const int sz = m1 * n1 * o1;
-    // -exp(-(sad/g^3) / (2 std)) in float, as edgecost2weight() (src/primsMST.h:48-50, :112-117)
+    // -exp(-(sad/g^3) / (2 std)) in float, as edgecost2weight() (src/primsMST.h:48-50, :112-117);
+    // stored vertex-major (w[v*6 + nb]): the six pushes of an added vertex read one line
     std::vector<float> w((size_t)sz * 6);
     const float g3 = (float)std::pow((double)g, 3.0);
     const float twostd = 2.0f * stddev;
-    for (size_t e = 0; e < (size_t)sz * 6; e++) w[e] = -std::exp(-(sad[e] / g3) / twostd);
+    for (int nb = 0; nb < 6; nb++)
+        for (size_t v = 0; v < (size_t)sz; v++) w[v * 6 + nb] = -std::exp(-(sad[(size_t)nb * sz + v] / g3) / twostd);
     const int mn1 = m1 * n1;
     // neighbour offsets in the reference's direction order -x,+x,-y,+y,-z,+z (src/primsMST.h:70-72)
     const int off[6] = {-m1, m1, -1, 1, -mn1, mn1};
@@ -200,7 +202,7 @@ void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int 
         const int k = last / mn1, rem = last - k * mn1, j = rem / m1, i = rem - j * m1;
         const bool ok[6] = {j > 0, j + 1 < n1, i > 0, i + 1 < m1, k > 0, k + 1 < o1};
         for (int nb = 0; nb < 6; nb++)
-            if (ok[nb]) heap.push(QueuedEdge{w[(size_t)nb * sz + last], (uint32_t)last * 8u + (uint32_t)nb});
+            if (ok[nb]) heap.push(QueuedEdge{w[(size_t)last * 6 + nb], (uint32_t)last * 8u + (uint32_t)nb});
         int from = -1, to = -1;
         while (to < 0) {
             if (heap.empty()) throw std::runtime_error("Prim: candidate heap exhausted (disconnected grid)");
@@ -231,7 +233,7 @@ void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int 
         const int k = c / mn1, rem = c - k * mn1, j = rem / m1, i = rem - j * m1;
         const int dxs[6] = {-1, 1, 0, 0, 0, 0}, dys[6] = {0, 0, -1, 1, 0, 0}, dzs[6] = {0, 0, 0, 0, -1, 1};
         for (int nb = 0; nb < 6; nb++)
-            if (i + dys[nb] + (j + dxs[nb]) * m1 + (k + dzs[nb]) * mn1 == p) edgemst[c] = -w[(size_t)nb * sz + c];
+            if (i + dys[nb] + (j + dxs[nb]) * m1 + (k + dzs[nb]) * mn1 == p) edgemst[c] = -w[(size_t)c * 6 + nb];
     }
 }
 
