@@ -23,68 +23,205 @@ namespace deeds {
 
 // The reference's statistics (src/primsMST.h:101-110) are sequential float sums:
 // mean += im[i], then var = float(double(var) + double(im[i]-mean)^2) -- a double
-// rounding per step.  The square of a float is exact in double, so each step
-// equals fmaf(d, d, var) (one rounding) except where the double rounding lands
-// on a float tie.  The variance chain is therefore run with fmaf (half the
-// dependency latency), keeping a checkpoint at the start of each of kChunks
-// chunks; the chunks are then replayed in parallel and every step is checked
-// against the reference's double-rounded formula.  From the first step where
-// the two differ (if any) the chain is recomputed with the reference formula,
-// so the result is always the reference's.
-void image_stats(const float* im, size_t sz, float* mean_out, float* std_out) {
-    float mean = 0.0f;
-    for (size_t i = 0; i < sz; i++) mean += im[i];
-    mean /= (float)sz;
-    constexpr int kChunks = 8;
-    float check[kChunks + 1];
-    size_t bound[kChunks + 1];
-    for (int c = 0; c <= kChunks; c++) bound[c] = sz * (size_t)c / kChunks;
-    float var = 0.0f;
-    for (int c = 0; c < kChunks; c++) {
-        check[c] = var;
-        for (size_t i = bound[c]; i < bound[c + 1]; i++) {
-            const float d = im[i] - mean;
-            var = std::fma(d, d, var);
+// rounding per step.  Both are evaluated exactly, in parallel chunks, using one
+// property of such chains.  Let every value of a chain lie in one binade
+// [2^(e-1), 2^e) (or its negative), where floats are the multiples of u =
+// 2^(e-24), at least one u inside its ends.  Then each step is "add the
+// increment exactly, round to the u-grid" (for the variance first to the double
+// grid u*2^-29, then to the u-grid), and shifting the running value by an even
+// multiple of u shifts every later value by the same amount: rounding to a grid
+// commutes with shifts by grid points, and ties to even see the same parity.
+// So a chunk is run (the reference arithmetic, step for step) from two guessed
+// start values in the binade of the estimated true start, one u apart; when the
+// true start is known, the trajectory whose start differs from it by an even
+// multiple of u gives the chunk's end by the same shift, provided both it and
+// its shifted copy stay inside the binade.  Chunks where the guess or the check
+// fails (the first ones, while the sum crosses binades quickly, or non-finite
+// data) are replayed from the true start sequentially.  The result is always the
+// reference's.
+namespace {
+
+struct Traj {
+    float end, lo, hi;  // last, smallest and largest value of the trajectory (start included)
+    bool exact;         // the variance's fast steps matched the reference formula
+};
+
+// binade exponent (|v| in [2^(e-1), 2^e)) and its grid step u; false for 0, tiny or non-finite v
+bool binade(float v, int& e, float& u) {
+    if (!std::isfinite(v) || std::fabs(v) < 0x1p-100f) return false;
+    std::frexp(v, &e);
+    u = std::ldexp(1.0f, e - 24);
+    return true;
+}
+
+// every value of [lo, hi] (shifted by d) strictly inside the binade e of sign neg
+bool inside(float lo, float hi, float d, int e, float u, bool neg) {
+    const double l = (double)lo + d, h = (double)hi + d;  // exact: small integers of u
+    const double inner = std::ldexp(1.0, e - 1) + u, outer = std::ldexp(1.0, e) - 2.0 * u;
+    return neg ? (l >= -outer && h <= -inner) : (l >= inner && h <= outer);
+}
+
+inline float mean_step(float v, float x) { return v + x; }
+inline float var_step(float v, float d) { return (float)((double)v + (double)d * (double)d); }
+
+Traj run_mean(const float* x, size_t lo, size_t hi, float v) {
+    Traj t{v, v, v, true};
+    for (size_t i = lo; i < hi; i++) {
+        v = mean_step(v, x[i]);
+        t.lo = std::min(t.lo, v);
+        t.hi = std::max(t.hi, v);
+    }
+    t.end = v;
+    return t;
+}
+
+// Two independent mean trajectories in one loop (their dependency chains overlap).
+void run_mean2(const float* x, size_t lo, size_t hi, float va, float vb, Traj& ta, Traj& tb) {
+    ta = Traj{va, va, va, true};
+    tb = Traj{vb, vb, vb, true};
+    for (size_t i = lo; i < hi; i++) {
+        va = mean_step(va, x[i]);
+        vb = mean_step(vb, x[i]);
+        ta.lo = std::min(ta.lo, va);
+        ta.hi = std::max(ta.hi, va);
+        tb.lo = std::min(tb.lo, vb);
+        tb.hi = std::max(tb.hi, vb);
+    }
+    ta.end = va;
+    tb.end = vb;
+}
+
+// The variance chain with fmaf (one rounding, shorter dependency) checked against
+// the reference's double-rounded step; the exact formula when they ever differ.
+Traj run_var(const float* x, float mean, size_t lo, size_t hi, float v0) {
+    Traj t{v0, v0, v0, true};
+    float v = v0;
+    for (size_t i = lo; i < hi; i++) {
+        const float d = x[i] - mean;
+        const float nv = std::fma(d, d, v);
+        if (nv != var_step(v, d)) {
+            t.exact = false;
+            break;
+        }
+        v = nv;
+        t.lo = std::min(t.lo, v);
+        t.hi = std::max(t.hi, v);
+    }
+    if (!t.exact) {
+        v = v0;
+        t = Traj{v0, v0, v0, true};
+        for (size_t i = lo; i < hi; i++) {
+            v = var_step(v, x[i] - mean);
+            t.lo = std::min(t.lo, v);
+            t.hi = std::max(t.hi, v);
         }
     }
-    check[kChunks] = var;
-    size_t first_bad[kChunks];
-    auto verify = [&](int c) {
-        first_bad[c] = sz;
-        float v = check[c];
-        for (size_t i = bound[c]; i < bound[c + 1]; i++) {
-            const float d = im[i] - mean;
-            const float fast = std::fma(d, d, v);
-            if ((float)((double)v + (double)d * (double)d) != fast) {
-                first_bad[c] = i;
-                return;
+    t.end = v;
+    return t;
+}
+
+// Two variance trajectories in one loop, each as run_var.
+void run_var2(const float* x, float mean, size_t lo, size_t hi, float va, float vb, Traj& ta, Traj& tb) {
+    ta = Traj{va, va, va, true};
+    tb = Traj{vb, vb, vb, true};
+    const float a0 = va, b0 = vb;
+    bool ok = true;
+    for (size_t i = lo; i < hi; i++) {
+        const float d = x[i] - mean;
+        const float na = std::fma(d, d, va), nb = std::fma(d, d, vb);
+        ok = ok && na == var_step(va, d) && nb == var_step(vb, d);
+        va = na;
+        vb = nb;
+        ta.lo = std::min(ta.lo, va);
+        ta.hi = std::max(ta.hi, va);
+        tb.lo = std::min(tb.lo, vb);
+        tb.hi = std::max(tb.hi, vb);
+    }
+    ta.end = va;
+    tb.end = vb;
+    if (!ok) {
+        ta = run_var(x, mean, lo, hi, a0);
+        tb = run_var(x, mean, lo, hi, b0);
+    }
+}
+
+// One chain over x: kind 0 = mean sum, 1 = variance sum around `mean`.
+float chain_sum(const float* x, size_t sz, int kind, float mean, int threads) {
+    const size_t nch = std::max<size_t>(1, std::min<size_t>(256, sz / 32768));
+    std::vector<size_t> bnd(nch + 1);
+    for (size_t c = 0; c <= nch; c++) bnd[c] = sz * c / nch;
+    std::vector<double> part(nch, 0.0);
+    std::vector<float> guess(nch, 0.0f), alt(nch, 0.0f);
+    std::vector<Traj> ta(nch), tb(nch);
+    std::vector<char> spec(nch, 0);
+    // chunk sums (estimates of where each chunk starts), then both trajectories
+    auto sums = [&](size_t c0, size_t c1) {
+        for (size_t c = c0; c < c1; c++) {
+            double a = 0.0;
+            for (size_t i = bnd[c]; i < bnd[c + 1]; i++) {
+                const double d = kind == 0 ? (double)x[i] : (double)(x[i] - mean);
+                a += kind == 0 ? d : d * d;
             }
-            v = fast;
+            part[c] = a;
         }
     };
-    if (sz >= ((size_t)1 << 20)) {
+    auto trajs = [&](size_t c0, size_t c1) {
+        for (size_t c = c0; c < c1; c++) {
+            int e;
+            float u;
+            if (!binade(guess[c], e, u)) continue;
+            // a second start one u away, in the same binade
+            const float g2 = std::fabs(guess[c] + u) < std::ldexp(1.0f, e) ? guess[c] + u : guess[c] - u;
+            alt[c] = g2;
+            if (kind == 0) run_mean2(x, bnd[c], bnd[c + 1], guess[c], g2, ta[c], tb[c]);
+            else run_var2(x, mean, bnd[c], bnd[c + 1], guess[c], g2, ta[c], tb[c]);
+            spec[c] = 1;
+        }
+    };
+    const int nt = std::max(1, std::min<int>(threads, (int)nch));
+    auto parallel = [&](auto fn) {
         std::vector<std::thread> th;
-        for (int c = 1; c < kChunks; c++) th.emplace_back(verify, c);
-        verify(0);
-        for (auto& t : th) t.join();
-    } else {
-        for (int c = 0; c < kChunks; c++) verify(c);
+        for (int t = 1; t < nt; t++) th.emplace_back(fn, nch * t / nt, nch * (t + 1) / nt);
+        fn((size_t)0, nch / nt);
+        for (auto& h : th) h.join();
+    };
+    parallel(sums);
+    double pre = 0.0;
+    for (size_t c = 0; c < nch; c++) {
+        guess[c] = (float)pre;
+        pre += part[c];
     }
-    for (int c = 0; c < kChunks; c++) {
-        if (first_bad[c] == sz) continue;
-        // replay the chunk's fast steps up to the first difference, then the reference formula
-        float v = check[c];
-        for (size_t i = bound[c]; i < first_bad[c]; i++) {
-            const float d = im[i] - mean;
-            v = std::fma(d, d, v);
+    parallel(trajs);
+    // the true chain, chunk by chunk
+    float v = 0.0f;
+    for (size_t c = 0; c < nch; c++) {
+        int e, eg;
+        float u, ug;
+        bool done = false;
+        if (spec[c] && binade(v, e, u) && binade(guess[c], eg, ug) && e == eg && std::signbit(v) == std::signbit(guess[c])) {
+            const double k = ((double)v - (double)guess[c]) / u;  // exact integer
+            const bool even = std::fmod(std::fabs(k), 2.0) == 0.0;
+            const Traj& t = even ? ta[c] : tb[c];
+            const float start = even ? guess[c] : alt[c];
+            const float d = v - start;  // exact: both multiples of u in one binade
+            const bool neg = std::signbit(v);
+            if (t.exact && inside(t.lo, t.hi, 0.0f, e, u, neg) && inside(t.lo, t.hi, d, e, u, neg)) {
+                v = t.end + d;  // exact: a multiple of u inside the binade
+                done = true;
+            }
         }
-        for (size_t i = first_bad[c]; i < sz; i++) {
-            const double d = (double)(im[i] - mean);
-            v = (float)((double)v + d * d);  // float += pow(float,2) in double
-        }
-        var = v;
-        break;
+        if (!done) v = kind == 0 ? run_mean(x, bnd[c], bnd[c + 1], v).end : run_var(x, mean, bnd[c], bnd[c + 1], v).end;
     }
+    return v;
+}
+
+}  // namespace
+
+void image_stats(const float* im, size_t sz, float* mean_out, float* std_out) {
+    const int threads = sz >= ((size_t)1 << 20) ? std::max(1, (int)std::thread::hardware_concurrency() / 2) : 1;
+    float mean = chain_sum(im, sz, 0, 0.0f, threads);
+    mean /= (float)sz;
+    const float var = chain_sum(im, sz, 1, mean, threads);
     *mean_out = mean;
     *std_out = std::sqrt(var / (float)sz);
 }

@@ -172,3 +172,49 @@ def test_linear_cli_usage_and_non_gz(tmp_path, pair_files):
     plain.write_bytes(b"\0" * 400)
     r = _linear_cli("-F", str(plain), "-M", m, "-O", out)
     assert "images must have nii.gz format" in r.stdout and r.returncode != 0
+
+
+def _stats_case(kind, n, seed):
+    rng = np.random.default_rng(seed)
+    if kind == "ct_integers":  # many exact ties when the running sum's grid step exceeds 1
+        return rng.choice(np.array([-1000.0, -1000.0, 0.0, 40.0, 1200.0], np.float32), n) + \
+            rng.integers(-50, 50, n).astype(np.float32)
+    if kind == "uniform":
+        return rng.uniform(-1024, 3000, n).astype(np.float32)
+    if kind == "crossing_zero":  # the sum wanders around zero through many binades
+        return rng.normal(0, 100, n).astype(np.float32)
+    if kind == "negative":
+        return -rng.uniform(0, 4000, n).astype(np.float32)
+    if kind == "offset":
+        return (1e6 + rng.uniform(0, 1, n)).astype(np.float32)
+    if kind == "huge":
+        return (rng.uniform(0.5, 1, n) * 1e30).astype(np.float32)
+    if kind == "tiny":
+        return (rng.uniform(-1, 1, n) * 1e-30).astype(np.float32)
+    if kind == "constant":
+        return np.full(n, 37.25, np.float32)
+    if kind == "steps":  # long runs of one value, then a jump
+        return np.repeat(rng.uniform(-500, 500, n // 4096 + 1), 4096)[:n].astype(np.float32)
+    x = rng.uniform(0, 100, n).astype(np.float32)  # nan / inf
+    x[n // 3] = np.nan if kind == "nan" else np.inf
+    return x
+
+
+@pytest.mark.parametrize("kind", ["ct_integers", "uniform", "crossing_zero", "negative", "offset", "huge", "tiny",
+                                  "constant", "steps", "nan", "inf"])
+@pytest.mark.parametrize("n", [(1 << 20) + 12345, 3 * 1000 * 1000])
+def test_image_stats_parallel_chunks_match_sequential_reference(lib, kind, n):
+    """The library evaluates the reference's sequential float sums in parallel
+    chunks (exact by a grid-translation argument); every case must give the
+    sequential oracle's mean and standard deviation to the bit."""
+    im = np.ascontiguousarray(_stats_case(kind, n, 5), np.float32)
+    mean = np.zeros(1, np.float32)
+    sd = np.zeros(1, np.float32)
+    ptr = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    assert lib.deeds_image_stats(ptr(im), im.size, ptr(mean), ptr(sd)) == 0
+    rm, rs = orc.image_stats(im)
+    got = np.array([mean[0], sd[0]], np.float32)
+    ref = np.array([rm, rs], np.float32)
+    assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)) or \
+        (np.isnan(got).tolist() == np.isnan(ref).tolist() and np.array_equal(got[~np.isnan(got)], ref[~np.isnan(ref)])), \
+        (kind, got, ref)
