@@ -75,134 +75,124 @@ Traj run_mean(const float* x, size_t lo, size_t hi, float v) {
     return t;
 }
 
-// Two independent mean trajectories in one loop (their dependency chains overlap).
+// Two independent mean trajectories in one loop (their dependency chains overlap;
+// the running extremes use four accumulators each so that they add no chain).
 void run_mean2(const float* x, size_t lo, size_t hi, float va, float vb, Traj& ta, Traj& tb) {
-    ta = Traj{va, va, va, true};
-    tb = Traj{vb, vb, vb, true};
-    for (size_t i = lo; i < hi; i++) {
+    float alo[4] = {va, va, va, va}, ahi[4] = {va, va, va, va};
+    float blo[4] = {vb, vb, vb, vb}, bhi[4] = {vb, vb, vb, vb};
+    size_t i = lo;
+    for (; i + 4 <= hi; i += 4)
+        for (int j = 0; j < 4; j++) {
+            va = mean_step(va, x[i + j]);
+            vb = mean_step(vb, x[i + j]);
+            alo[j] = std::min(alo[j], va);
+            ahi[j] = std::max(ahi[j], va);
+            blo[j] = std::min(blo[j], vb);
+            bhi[j] = std::max(bhi[j], vb);
+        }
+    for (; i < hi; i++) {
         va = mean_step(va, x[i]);
         vb = mean_step(vb, x[i]);
-        ta.lo = std::min(ta.lo, va);
-        ta.hi = std::max(ta.hi, va);
-        tb.lo = std::min(tb.lo, vb);
-        tb.hi = std::max(tb.hi, vb);
+        alo[0] = std::min(alo[0], va);
+        ahi[0] = std::max(ahi[0], va);
+        blo[0] = std::min(blo[0], vb);
+        bhi[0] = std::max(bhi[0], vb);
     }
-    ta.end = va;
-    tb.end = vb;
+    ta = Traj{va, std::min(std::min(alo[0], alo[1]), std::min(alo[2], alo[3])),
+              std::max(std::max(ahi[0], ahi[1]), std::max(ahi[2], ahi[3])), true};
+    tb = Traj{vb, std::min(std::min(blo[0], blo[1]), std::min(blo[2], blo[3])),
+              std::max(std::max(bhi[0], bhi[1]), std::max(bhi[2], bhi[3])), true};
 }
 
 // The variance chain with fmaf (one rounding, shorter dependency) checked against
 // the reference's double-rounded step; the exact formula when they ever differ.
+// The chain never decreases (it adds squares): its extremes are start and end.
 Traj run_var(const float* x, float mean, size_t lo, size_t hi, float v0) {
-    Traj t{v0, v0, v0, true};
     float v = v0;
+    unsigned bad = 0;
     for (size_t i = lo; i < hi; i++) {
         const float d = x[i] - mean;
         const float nv = std::fma(d, d, v);
-        if (nv != var_step(v, d)) {
-            t.exact = false;
-            break;
-        }
+        bad |= (unsigned)(nv != var_step(v, d));
         v = nv;
-        t.lo = std::min(t.lo, v);
-        t.hi = std::max(t.hi, v);
     }
-    if (!t.exact) {
+    if (bad) {
         v = v0;
-        t = Traj{v0, v0, v0, true};
-        for (size_t i = lo; i < hi; i++) {
-            v = var_step(v, x[i] - mean);
-            t.lo = std::min(t.lo, v);
-            t.hi = std::max(t.hi, v);
-        }
+        for (size_t i = lo; i < hi; i++) v = var_step(v, x[i] - mean);
     }
-    t.end = v;
-    return t;
+    return Traj{v, v0, v, true};
 }
 
-// Two variance trajectories in one loop, each as run_var.
+// Two variance trajectories in one loop, each as run_var.  The chain never
+// decreases (it adds squares), so its extremes are its start and end.
 void run_var2(const float* x, float mean, size_t lo, size_t hi, float va, float vb, Traj& ta, Traj& tb) {
-    ta = Traj{va, va, va, true};
-    tb = Traj{vb, vb, vb, true};
     const float a0 = va, b0 = vb;
-    bool ok = true;
+    unsigned bad = 0;
     for (size_t i = lo; i < hi; i++) {
         const float d = x[i] - mean;
         const float na = std::fma(d, d, va), nb = std::fma(d, d, vb);
-        ok = ok && na == var_step(va, d) && nb == var_step(vb, d);
+        bad |= (unsigned)(na != var_step(va, d)) | (unsigned)(nb != var_step(vb, d));
         va = na;
         vb = nb;
-        ta.lo = std::min(ta.lo, va);
-        ta.hi = std::max(ta.hi, va);
-        tb.lo = std::min(tb.lo, vb);
-        tb.hi = std::max(tb.hi, vb);
     }
-    ta.end = va;
-    tb.end = vb;
-    if (!ok) {
+    if (bad) {
         ta = run_var(x, mean, lo, hi, a0);
         tb = run_var(x, mean, lo, hi, b0);
+        return;
     }
+    ta = Traj{va, a0, va, true};
+    tb = Traj{vb, b0, vb, true};
 }
 
-// One chain over x: kind 0 = mean sum, 1 = variance sum around `mean`.
-float chain_sum(const float* x, size_t sz, int kind, float mean, int threads) {
-    const size_t nch = std::max<size_t>(1, std::min<size_t>(256, sz / 32768));
-    std::vector<size_t> bnd(nch + 1);
-    for (size_t c = 0; c <= nch; c++) bnd[c] = sz * c / nch;
-    std::vector<double> part(nch, 0.0);
-    std::vector<float> guess(nch, 0.0f), alt(nch, 0.0f);
+// The chunks of the two chains and their start estimates.
+struct ChainPlan {
+    size_t nch;
+    std::vector<size_t> bnd;
+    std::vector<double> sum_x, sum_x2;  // per chunk (estimates only: any order of addition)
+};
+
+template <class Fn>
+void parallel_chunks(size_t nch, int threads, Fn fn) {
+    const int nt = std::max(1, std::min<int>(threads, (int)nch));
+    std::vector<std::thread> th;
+    for (int t = 1; t < nt; t++) th.emplace_back(fn, nch * t / nt, nch * (t + 1) / nt);
+    fn((size_t)0, nch / nt);
+    for (auto& h : th) h.join();
+}
+
+// One chain over x: kind 0 = mean sum, 1 = variance sum around `mean`; `est[c]`
+// estimates the chain's value at the start of chunk c.
+float chain_sum(const float* x, const ChainPlan& P, int kind, float mean, const std::vector<float>& est,
+                int threads) {
+    const size_t nch = P.nch;
+    const std::vector<size_t>& bnd = P.bnd;
+    std::vector<float> alt(nch, 0.0f);
     std::vector<Traj> ta(nch), tb(nch);
     std::vector<char> spec(nch, 0);
-    // chunk sums (estimates of where each chunk starts), then both trajectories
-    auto sums = [&](size_t c0, size_t c1) {
-        for (size_t c = c0; c < c1; c++) {
-            double a = 0.0;
-            for (size_t i = bnd[c]; i < bnd[c + 1]; i++) {
-                const double d = kind == 0 ? (double)x[i] : (double)(x[i] - mean);
-                a += kind == 0 ? d : d * d;
-            }
-            part[c] = a;
-        }
-    };
-    auto trajs = [&](size_t c0, size_t c1) {
+    parallel_chunks(nch, threads, [&](size_t c0, size_t c1) {
         for (size_t c = c0; c < c1; c++) {
             int e;
             float u;
-            if (!binade(guess[c], e, u)) continue;
+            if (!binade(est[c], e, u)) continue;
             // a second start one u away, in the same binade
-            const float g2 = std::fabs(guess[c] + u) < std::ldexp(1.0f, e) ? guess[c] + u : guess[c] - u;
+            const float g2 = std::fabs(est[c] + u) < std::ldexp(1.0f, e) ? est[c] + u : est[c] - u;
             alt[c] = g2;
-            if (kind == 0) run_mean2(x, bnd[c], bnd[c + 1], guess[c], g2, ta[c], tb[c]);
-            else run_var2(x, mean, bnd[c], bnd[c + 1], guess[c], g2, ta[c], tb[c]);
+            if (kind == 0) run_mean2(x, bnd[c], bnd[c + 1], est[c], g2, ta[c], tb[c]);
+            else run_var2(x, mean, bnd[c], bnd[c + 1], est[c], g2, ta[c], tb[c]);
             spec[c] = 1;
         }
-    };
-    const int nt = std::max(1, std::min<int>(threads, (int)nch));
-    auto parallel = [&](auto fn) {
-        std::vector<std::thread> th;
-        for (int t = 1; t < nt; t++) th.emplace_back(fn, nch * t / nt, nch * (t + 1) / nt);
-        fn((size_t)0, nch / nt);
-        for (auto& h : th) h.join();
-    };
-    parallel(sums);
-    double pre = 0.0;
-    for (size_t c = 0; c < nch; c++) {
-        guess[c] = (float)pre;
-        pre += part[c];
-    }
-    parallel(trajs);
+    });
     // the true chain, chunk by chunk
     float v = 0.0f;
     for (size_t c = 0; c < nch; c++) {
         int e, eg;
         float u, ug;
         bool done = false;
-        if (spec[c] && binade(v, e, u) && binade(guess[c], eg, ug) && e == eg && std::signbit(v) == std::signbit(guess[c])) {
-            const double k = ((double)v - (double)guess[c]) / u;  // exact integer
+        if (spec[c] && binade(v, e, u) && binade(est[c], eg, ug) && e == eg && std::signbit(v) == std::signbit(est[c])) {
+            const double k = ((double)v - (double)est[c]) / u;  // exact integer
             const bool even = std::fmod(std::fabs(k), 2.0) == 0.0;
             const Traj& t = even ? ta[c] : tb[c];
-            const float start = even ? guess[c] : alt[c];
+            const float start = even ? est[c] : alt[c];
             const float d = v - start;  // exact: both multiples of u in one binade
             const bool neg = std::signbit(v);
             if (t.exact && inside(t.lo, t.hi, 0.0f, e, u, neg) && inside(t.lo, t.hi, d, e, u, neg)) {
@@ -219,9 +209,50 @@ float chain_sum(const float* x, size_t sz, int kind, float mean, int threads) {
 
 void image_stats(const float* im, size_t sz, float* mean_out, float* std_out) {
     const int threads = sz >= ((size_t)1 << 20) ? std::max(1, (int)std::thread::hardware_concurrency() / 2) : 1;
-    float mean = chain_sum(im, sz, 0, 0.0f, threads);
+    ChainPlan P;
+    P.nch = std::max<size_t>(1, std::min<size_t>(256, sz / 32768));
+    P.bnd.resize(P.nch + 1);
+    for (size_t c = 0; c <= P.nch; c++) P.bnd[c] = sz * c / P.nch;
+    P.sum_x.assign(P.nch, 0.0);
+    P.sum_x2.assign(P.nch, 0.0);
+    // one pass for both chains' estimates: per chunk sum of x and of x^2 (four
+    // independent accumulators each)
+    parallel_chunks(P.nch, threads, [&](size_t c0, size_t c1) {
+        for (size_t c = c0; c < c1; c++) {
+            double s[4] = {0, 0, 0, 0}, q[4] = {0, 0, 0, 0};
+            size_t i = P.bnd[c];
+            for (; i + 4 <= P.bnd[c + 1]; i += 4)
+                for (int j = 0; j < 4; j++) {
+                    const double v = im[i + j];
+                    s[j] += v;
+                    q[j] += v * v;
+                }
+            for (; i < P.bnd[c + 1]; i++) {
+                s[0] += im[i];
+                q[0] += (double)im[i] * im[i];
+            }
+            P.sum_x[c] = (s[0] + s[1]) + (s[2] + s[3]);
+            P.sum_x2[c] = (q[0] + q[1]) + (q[2] + q[3]);
+        }
+    });
+    std::vector<float> est(P.nch);
+    double pre = 0.0, total = 0.0;
+    for (size_t c = 0; c < P.nch; c++) total += P.sum_x[c];
+    for (size_t c = 0; c < P.nch; c++) {
+        est[c] = (float)pre;
+        pre += P.sum_x[c];
+    }
+    float mean = chain_sum(im, P, 0, 0.0f, est, threads);
     mean /= (float)sz;
-    const float var = chain_sum(im, sz, 1, mean, threads);
+    // sum over a chunk of (x - m)^2 = sum x^2 - 2 m sum x + n m^2, m the estimated mean
+    const double m = total / (double)sz;
+    pre = 0.0;
+    for (size_t c = 0; c < P.nch; c++) {
+        est[c] = (float)pre;
+        const double n = (double)(P.bnd[c + 1] - P.bnd[c]);
+        pre += std::max(0.0, P.sum_x2[c] - 2.0 * m * P.sum_x[c] + n * m * m);
+    }
+    const float var = chain_sum(im, P, 1, mean, est, threads);
     *mean_out = mean;
     *std_out = std::sqrt(var / (float)sz);
 }
