@@ -882,13 +882,13 @@ __global__ void __launch_bounds__(ColGeom<G_, LEN_, Q_>::ADJ_BLOCK, 4)
                 }
 #pragma unroll
                 for (int ly = 0; ly < LEN_; ly++) {
-                    const float w = cbl[ly];
+                    const float w = cbl[ly], nw = -w;
 #pragma unroll
                     for (int i = 0; i < G_; i++) {
                         const float d = f[i] - v[i + ly * Q_];
-                        const float gr = w * d * rsqrtf(d * d + eps2);
-                        gf[i] += gr;
-                        gm[i + ly * Q_] -= gr;
+                        const float t = d * rsqrtf(d * d + eps2);  // phi'(d)
+                        gf[i] = fmaf(w, t, gf[i]);
+                        gm[i + ly * Q_] = fmaf(nw, t, gm[i + ly * Q_]);
                     }
                 }
 #pragma unroll
