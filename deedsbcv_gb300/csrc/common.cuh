@@ -148,6 +148,23 @@ __device__ __forceinline__ FF ff_add(FF x, FF y) {
     return ff_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo)));
 }
 
+// The float nearest to acc (a normalised float-float value) if every value
+// within eps of acc rounds to the same float; false if acc is that close to a
+// midpoint between adjacent floats, or zero, tiny or huge.
+__device__ __forceinline__ bool ff_round_safe(FF acc, float eps, float& out) {
+    const float f = __fadd_rn(acc.hi, acc.lo);  // the float nearest to hi + lo
+    const uint32_t bits = __float_as_uint(f) & 0x7fffffffu;
+    const uint32_t e = bits >> 23;
+    if (e < 27u || e > 253u) return false;
+    // half the gap to the next float on either side (below a power of two the gap halves)
+    const uint32_t he = (bits & 0x7fffffu) ? e - 24u : e - 25u;
+    const float half_gap = __uint_as_float(he << 23);
+    const float d = __fadd_rn(__fsub_rn(acc.hi, f), acc.lo);  // (hi + lo) - f, to one rounding
+    if (!(fabsf(d) * 1.0000005f + eps < half_gap)) return false;
+    out = f;
+    return true;
+}
+
 struct FFWeights {
     FF w000, w100, w010, w001, w110, w101, w011;
     float dxdydz;
@@ -186,18 +203,7 @@ __device__ __forceinline__ bool ff_blend8(const FFWeights& b, float c000, float 
     acc = ff_add(acc, ff_mul_f(b.w101, c101));
     acc = ff_add(acc, ff_mul_f(b.w011, c011));
     acc = ff_add(acc, FF{b.dxdydz * c111, 0.0f});
-    const float f = __fadd_rn(acc.hi, acc.lo);  // the float nearest to hi + lo
-    const uint32_t bits = __float_as_uint(f) & 0x7fffffffu;
-    const uint32_t e = bits >> 23;
-    // half the gap to the next float on either side (below a power of two the gap halves)
-    const uint32_t he = (bits & 0x7fffffu) ? e - 24u : e - 25u;
-    if (e < 27u || e > 253u) return false;  // zero, tiny or huge: no fast answer
-    const float half_gap = __uint_as_float(he << 23);
-    const float d = __fadd_rn(__fsub_rn(acc.hi, f), acc.lo);  // (hi + lo) - f, to one rounding
-    const float eps = S * 0x1p-40f;
-    if (!(fabsf(d) * 1.0000005f + eps < half_gap)) return false;
-    out = f;
-    return true;
+    return ff_round_safe(acc, S * 0x1p-40f, out);
 }
 
 // sample() through the float-float evaluation, falling back to the double one.

@@ -47,6 +47,22 @@ __global__ void k_lin_warp(const float* __restrict__ in, Affine12 X, float* __re
 // node itself, read before its update).  A thread owns one (line, label) and
 // walks the line; consecutive threads hold consecutive labels of the same node
 // (coalesced).  blockIdx.y selects one of two volumes.
+// The step in float-float (see ff_blend8 in common.cuh for the method): the
+// reference evaluates E = cur + (0.5 next + 0.5 prev) with two double roundings,
+// so its result is within 2^-52 S of E (S = |cur| + |next|/2 + |prev|/2); the
+// float-float sum below (exact halves, exact two-sums, one float rounding of the
+// low parts) is within 2^-47 S of E.  When no float midpoint lies within 2^-43 S
+// of it, both round to the same float; otherwise the caller takes the double
+// expression.
+__device__ __forceinline__ bool smooth_step_ff(float cur, float next, float prev, float& out) {
+    const float h1 = 0.5f * next, h2 = 0.5f * prev;
+    const float S = fabsf(cur) + fabsf(h1) + fabsf(h2);
+    if (!(S >= 0x1p-60f && S <= 0x1p+100f)) return false;  // also NaN / infinite values
+    const FF s1 = ff_two_sum(h1, h2);
+    const FF s2 = ff_two_sum(cur, s1.hi);
+    return ff_round_safe(ff_two_sum(s2.hi, __fadd_rn(s2.lo, s1.lo)), S * 0x1p-43f, out);
+}
+
 struct SmoothLines {
     int len, stride;           // along the smoothed axis
     int a_len, a_stride;       // first other axis
@@ -68,8 +84,11 @@ __global__ void k_lin_smooth(float* __restrict__ c0, float* __restrict__ c1, Smo
     float prev = cur;  // node 0: the lower neighbour is itself, not yet updated
     for (int s = 0; s < L.len; s++) {
         const float next = s + 1 < L.len ? p[(s + 1) * step] : cur;  // upper neighbour: not yet updated
-        const double add = __dadd_rn(__dmul_rn(0.5, f2d(next)), __dmul_rn(0.5, f2d(prev)));
-        const float v = __double2float_rn(__dadd_rn(f2d(cur), add));
+        float v;
+        if (!smooth_step_ff(cur, next, prev, v)) {
+            const double add = __dadd_rn(__dmul_rn(0.5, f2d(next)), __dmul_rn(0.5, f2d(prev)));
+            v = __double2float_rn(__dadd_rn(f2d(cur), add));
+        }
         p[s * step] = v;
         prev = v;
         cur = next;

@@ -59,6 +59,32 @@ def test_lin_smooth_bit_exact(api, shape):
     assert np.array_equal(t.cpu().numpy().view(np.uint32), ref.view(np.uint32))
 
 
+@pytest.mark.parametrize("kind", ["midpoints", "tiny", "nan", "mixed_sign"])
+def test_lin_smooth_both_evaluations_bit_exact(api, kind):
+    """The smoothing step runs in float-float when that provably rounds like the
+    reference's double expression, else in double: even integers near 2^24 give
+    sums on float midpoints (the double path decides), tiny values fall below the
+    float-float range, NaN propagates, mixed signs cancel."""
+    m1, n1, o1, len3 = 9, 7, 8, 125
+    rng = np.random.default_rng(7)
+    size = m1 * n1 * o1 * len3
+    if kind == "midpoints":
+        cost = (16777216.0 + 2.0 * rng.integers(0, 8, size)).astype(np.float32)
+    elif kind == "tiny":
+        cost = (rng.uniform(0, 1, size) * 1e-30).astype(np.float32)
+    elif kind == "nan":
+        cost = rng.uniform(0, 100, size).astype(np.float32)
+        cost[rng.integers(0, size, 20)] = np.nan
+    else:
+        cost = rng.normal(0, 1000, size).astype(np.float32)
+    t = _cuda(cost)
+    api.smoothCosts(t, m1, n1, o1, len3)
+    ref = orc.lin_smooth(cost, m1, n1, o1, len3)
+    got = t.cpu().numpy()
+    both_nan = np.isnan(got) & np.isnan(ref)
+    assert np.all(both_nan | (got.view(np.uint32) == ref.view(np.uint32)))
+
+
 @pytest.mark.parametrize("key", ["5_3_2", "4_2_1"])
 @pytest.mark.parametrize("rigid", [0, 1])
 def test_estimate_affine_bit_exact(api, golden, key, rigid):
