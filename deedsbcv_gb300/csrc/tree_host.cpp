@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <memory>
 #include <stdexcept>
 #include <thread>
 #include <vector>
@@ -286,19 +287,19 @@ struct QueuedEdge {
 // grandchildren, which changes timing, not order.
 class EdgeHeap {
   public:
-    explicit EdgeHeap(size_t reserve) { a_.reserve(reserve); }
-    bool empty() const { return a_.empty(); }
+    explicit EdgeHeap(size_t reserve) { grow(std::max<size_t>(reserve, 64)); }
+    bool empty() const { return n_ == 0; }
     void push(QueuedEdge e) {
-        a_.push_back(e);
-        sift_up(a_.size() - 1, 0, e);
+        if (n_ == cap_) grow(2 * cap_);
+        a_[n_++] = e;
+        sift_up(n_ - 1, 0, e);
     }
     QueuedEdge pop() {
         const QueuedEdge top = a_[0];
-        const QueuedEdge last = a_.back();
-        a_.pop_back();
-        const size_t len = a_.size();
+        const QueuedEdge last = a_[--n_];
+        const size_t len = n_;
         if (len == 0) return top;
-        QueuedEdge* d = a_.data();
+        QueuedEdge* d = a_;
         size_t hole = 0, child = 0;
         while (child < (len - 1) / 2) {
             // The descendants of the hole k levels down are the 2^k contiguous
@@ -331,8 +332,19 @@ class EdgeHeap {
     }
 
   private:
+    // Storage with entry 1 on a 64-byte boundary: the siblings 2i+1, 2i+2 that
+    // every sift-down level compares then share one cache line.
+    void grow(size_t cap) {
+        std::unique_ptr<QueuedEdge[]> mem(new QueuedEdge[cap + 16]);
+        const uintptr_t b = reinterpret_cast<uintptr_t>(mem.get() + 1);
+        QueuedEdge* a = mem.get() + ((64 - (b & 63)) & 63) / sizeof(QueuedEdge);
+        if (n_) std::memcpy(a, a_, n_ * sizeof(QueuedEdge));
+        mem_ = std::move(mem);
+        a_ = a;
+        cap_ = cap;
+    }
     void sift_up(size_t hole, size_t top, QueuedEdge v) {
-        QueuedEdge* d = a_.data();
+        QueuedEdge* d = a_;
         size_t parent = (hole - 1) / 2;
         while (hole > top && d[parent].weight > v.weight) {
             d[hole] = d[parent];
@@ -341,7 +353,9 @@ class EdgeHeap {
         }
         d[hole] = v;
     }
-    std::vector<QueuedEdge> a_;
+    std::unique_ptr<QueuedEdge[]> mem_;
+    QueuedEdge* a_ = nullptr;
+    size_t n_ = 0, cap_ = 0;
 };
 }  // namespace
 
