@@ -218,3 +218,22 @@ def test_image_stats_parallel_chunks_match_sequential_reference(lib, kind, n):
     assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)) or \
         (np.isnan(got).tolist() == np.isnan(ref).tolist() and np.array_equal(got[~np.isnan(got)], ref[~np.isnan(ref)])), \
         (kind, got, ref)
+
+
+@pytest.mark.parametrize("dims,levels", [((48, 40, 64), 4), ((13, 11, 17), 6), ((24, 20, 32), 2)])
+def test_host_prims_tie_heavy_matches_oracle(lib, dims, levels):
+    """Block SADs drawn from a few values make most edge weights bit-equal, so
+    the tree is decided by the heap's element moves alone: the library's heap
+    (vertex-major weights, aligned storage, prefetching) must pop in exactly the
+    order of the oracle's std::push_heap / std::pop_heap restatement."""
+    m1, n1, o1 = dims
+    sz = m1 * n1 * o1
+    rng = np.random.default_rng(sz + levels)
+    sad = (rng.integers(0, levels, 6 * sz) * np.float32(64.0)).astype(np.float32)
+    ptr = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    got = [np.zeros(sz, np.int32), np.zeros(sz, np.int32), np.zeros(sz, np.float32)]
+    ref = [np.zeros(sz, np.int32), np.zeros(sz, np.int32), np.zeros(sz, np.float32)]
+    assert lib.deeds_prims_from_sad(ptr(sad), C.c_float(37.5), m1, n1, o1, 4, *(ptr(a) for a in got)) == 0
+    orc.lib().orc_prims_from_sad(ptr(sad), C.c_float(37.5), m1, n1, o1, 4, *(ptr(a) for a in ref))
+    for a, b in zip(got, ref):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
