@@ -726,6 +726,8 @@ deeds_status deeds_consistent_dev(deeds_ctx* ctx, float* d_u, float* d_v, float*
     if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
     if (!d_u || !d_v || !d_w || !d_u2 || !d_v2 || !d_w2 || m < 1 || n < 1 || o < 1 || g < 1)
         return fail(ctx, DEEDS_ERR_INVALID, "bad arguments");
+    if (n > 65535 || o > 65535)  // grid y / z of the iteration kernel; checked before any launch
+        return fail(ctx, DEEDS_ERR_INVALID, "deeds_consistent_dev: n and o must be at most 65535");
     CK(cudaSetDevice(ctx->device));
     deeds_status st = DEEDS_OK;
     float* scratch = dbuf<float>(ctx, "consistent", (size_t)12 * m * n * o, &st);

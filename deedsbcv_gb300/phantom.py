@@ -168,6 +168,18 @@ def make_pair(shape, seed=0, n_organs=None, max_disp=6.0, spacing=16, contrast="
     return out
 
 
+def batch_workload(n=16, seed=100):
+    """The uneven-size batch: n (shape, seed) pairs with dims drawn uniformly from
+    128x112x144 up to 224x192x288; pair i is make_pair(shape, seed + 1 + i,
+    max_disp=10.0)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        shape = (int(rng.integers(128, 225)), int(rng.integers(112, 193)), int(rng.integers(144, 289)))
+        out.append((shape, seed + 1 + i))
+    return out
+
+
 def dice(a, b):
     """Mean Dice over the labels present in ``a`` except 0 (diceMulti's formula)."""
     a = np.asarray(a).ravel(order="F")

@@ -190,13 +190,19 @@ deeds_status deeds_consistent_dev(deeds_ctx* ctx, float* d_u, float* d_v, float*
  * that must not block on the device synchronisation cudaMalloc/cudaFree can
  * imply.  Same kernels and results as deeds_consistent_dev, but the 12 grid
  * fields of scratch live in a fixed device array of DEEDS_NOALLOC_MAX_NODES
- * nodes that every GPU loading the library holds (6 MiB) until exit; no context
- * is needed and nothing is allocated.  Grids with more than
- * DEEDS_NOALLOC_MAX_NODES nodes are rejected with DEEDS_ERR_INVALID.  The first
- * call on a device resolves the array's device address (with that device
- * current), so make it before any stream capture.  All calls share the array:
- * calls that overlap on the GPU race.  Errors are reported by status only (no
- * message is recorded, as that would allocate). */
+ * nodes (6 MiB); no context is needed and no call allocates.  With lazy module
+ * loading (the CUDA default) that array is reserved when the first call on a
+ * device loads the library's module into its context, and the device holds it
+ * until the context ends (process exit or cudaDeviceReset): make the first
+ * call per device at start-up, before a memory pool reserves the device and
+ * before any stream capture; it resolves the array's device address with that
+ * device current.  The address is kept per device and context, so a call in a
+ * new context of the device (e.g. after cudaDeviceReset) resolves it again,
+ * which again loads the module and reserves the array.  Grids with more than
+ * DEEDS_NOALLOC_MAX_NODES nodes, or with n or o above 65535, are rejected with
+ * DEEDS_ERR_INVALID before anything runs.  All calls share the array: calls
+ * that overlap on the GPU race.  Errors are reported by status only (no message
+ * is recorded, as that would allocate). */
 #define DEEDS_NOALLOC_MAX_NODES 131072
 deeds_status deeds_consistent_noalloc_dev(float* d_u, float* d_v, float* d_w, float* d_u2, float* d_v2, float* d_w2,
                                           int m, int n, int o, int g, void* stream);

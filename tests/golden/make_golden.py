@@ -9,6 +9,7 @@ writes are committed and travel with the tests.
 
     python tests/golden/make_golden.py                 # every fixture
     python tests/golden/make_golden.py --linear-only   # linear.npz alone
+    python tests/golden/make_golden.py --apply-only    # apply.npz alone
 """
 from __future__ import annotations
 
@@ -160,12 +161,68 @@ def make_linear(d, rng):
         fh.write("\n".join(logs))
 
 
+def write_matrix(path, X):
+    """The affine matrix text file read by -A: line i holds X[i] X[i+4] X[i+8] X[i+12]
+    (src/applyBCV.cpp:118-135)."""
+    with open(path, "w") as f:
+        for i in range(4):
+            f.write("  ".join(f"{float(X[i + 4 * k]):.6f}" for k in range(4)) + "\n")
+
+
+def make_apply(d):
+    """applyBCV / applyBCVfloat (src/applyBCV.cpp:54-204, src/applyBCVfloat.cpp): the
+    reference deedsBCV binary registers the end-to-end pair of e2e.npz (same inputs
+    and flags; its flow must equal the stored one), then the reference
+    applyBCVfloat warps a float image with non-integer values (0.37 x the moving
+    image + 11.125) through the written displacement file, without and with an
+    affine matrix file, and applyBCV warps the moving labels with the matrix."""
+    e = np.load(os.path.join(HERE, "e2e.npz"))
+    em, en, eo = (int(v) for v in e["dims"])
+    fpath, mpath = os.path.join(d, "f.nii.gz"), os.path.join(d, "m.nii.gz")
+    nifti.write(fpath, e["fixed"])
+    nifti.write(mpath, e["moving"])
+    stem = os.path.join(d, "out")
+    run(os.path.join(REF, "deedsBCV"), "-F", fpath, "-M", mpath, "-O", stem, "-G", "6x5x4", "-L", "5x4x3",
+        "-Q", "3x2x1")
+    flow = nifti.read_dat(stem + "_displacements.dat")
+    assert np.array_equal(flow, e["flow"]), "the reference's flow on the e2e inputs changed"
+    fimg = (e["moving"].astype(np.float32) * np.float32(0.37) + np.float32(11.125)).astype(np.float32)
+    ipath = os.path.join(d, "img.nii.gz")
+    nifti.write(ipath, fimg)
+    X = np.array([0.98, 0.03, -0.02, 1.25, -0.01, 1.02, 0.04, -0.8, 0.02, -0.03, 0.99, 0.6,
+                  0.0, 0.0, 0.0, 1.0], np.float32)
+    mat = os.path.join(d, "matrix.txt")
+    write_matrix(mat, X)
+    Xf = np.zeros(16, np.float32)  # the matrix as the reference reads it back (%f text)
+    with open(mat) as f:
+        for i, line in enumerate(f):
+            for k, tok in enumerate(line.split()):
+                Xf[i + 4 * k] = np.float32(tok)
+    outs = {}
+    for key, extra in (("warped_float", []), ("warped_float_affine", ["-A", mat])):
+        dst = os.path.join(d, key + ".nii.gz")
+        run(os.path.join(REF, "applyBCVfloat"), "-M", ipath, "-O", stem, "-D", dst, *extra)
+        outs[key] = nifti.read(dst)[0].ravel(order="F").astype(np.float32)
+    spath = os.path.join(d, "seg.nii.gz")
+    seg = e["moving_labels"].astype(np.int16)
+    nifti.write(spath, seg)
+    dst = os.path.join(d, "seg_affine.nii.gz")
+    run(os.path.join(REF, "applyBCV"), "-M", spath, "-O", stem, "-D", dst, "-A", mat)
+    outs["warped_seg_affine"] = nifti.read(dst)[0].ravel(order="F").astype(np.int16)
+    # inputs are those of e2e.npz (flow, moving labels); the float image is derived from its moving image
+    np.savez_compressed(os.path.join(HERE, "apply.npz"), X=Xf, **outs)
+
+
 def main():
     if not os.path.exists(os.path.join(REF, "ref_linear")):
         run("make", "-C", os.path.join(ROOT, "oracle"), "ref")
     if "--linear-only" in sys.argv:  # regenerate linear.npz alone
         with tempfile.TemporaryDirectory() as d:
             make_linear(d, np.random.default_rng(20241204))
+        return
+    if "--apply-only" in sys.argv:  # regenerate apply.npz alone
+        with tempfile.TemporaryDirectory() as d:
+            make_apply(d)
         return
     rng = np.random.default_rng(20241203)
     out = {}
@@ -290,6 +347,8 @@ def main():
             f.write(log)
     with tempfile.TemporaryDirectory() as d:
         make_linear(d, np.random.default_rng(20241204))
+    with tempfile.TemporaryDirectory() as d:
+        make_apply(d)
     for fn in sorted(os.listdir(HERE)):
         if fn.endswith(".npz"):
             print(fn, os.path.getsize(os.path.join(HERE, fn)))

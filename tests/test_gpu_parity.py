@@ -240,6 +240,53 @@ def test_apply_flow_matches_register(api, golden):
     assert img.dtype == np.float32 and img.shape == (m * n * o,)
 
 
+def _apply_inputs(e):
+    m, n, o = (int(x) for x in e["dims"])
+    img = (e["moving"].astype(np.float32) * np.float32(0.37) + np.float32(11.125)).astype(np.float32)
+    return (m, n, o), img, e["moving_labels"].astype(np.int16)
+
+
+def test_apply_float_matches_reference_applybcvfloat(api, golden):
+    """applyBCVfloat (src/applyBCVfloat.cpp: upsampling + trilinear warpAffine of a
+    float image through the .dat) and applyBCV with an affine matrix, against the
+    reference binaries' outputs on the e2e flow: bit-exact."""
+    e, a = golden("e2e"), golden("apply")
+    dims, img, lab = _apply_inputs(e)
+    got = api.apply_flow(e["flow"], img, dims=dims)
+    assert same_bits(got, a["warped_float"])
+    got = api.apply_flow(e["flow"], img, dims=dims, X=a["X"])
+    assert same_bits(got, a["warped_float_affine"])
+    seg = api.apply_flow(e["flow"], lab, dims=dims, X=a["X"])
+    assert np.array_equal(seg, a["warped_seg_affine"])
+
+
+def test_cli_applybcvfloat_matches_reference(api, golden, tmp_path):
+    """The applyBCVfloat / applyBCV executables on NIfTI files, with -A matrix text in
+    the reference's layout (line i: X[i] X[i+4] X[i+8] X[i+12])."""
+    import subprocess
+    from deedsbcv_gb300 import build, nifti
+    e, a = golden("e2e"), golden("apply")
+    dims, img, lab = _apply_inputs(e)
+    stem = str(tmp_path / "out")
+    nifti.write_dat(stem + "_displacements.dat", e["flow"])
+    ipath, spath = str(tmp_path / "img.nii.gz"), str(tmp_path / "seg.nii.gz")
+    nifti.write(ipath, img.ravel(order="F").reshape(dims, order="F"))
+    nifti.write(spath, lab)
+    mat = str(tmp_path / "matrix.txt")
+    with open(mat, "w") as f:
+        for i in range(4):
+            f.write("  ".join(f"{float(a['X'][i + 4 * k]):.6f}" for k in range(4)) + "\n")
+    for exe, src, extra, key in (("applyBCVfloat", ipath, [], "warped_float"),
+                                 ("applyBCVfloat", ipath, ["-A", mat], "warped_float_affine"),
+                                 ("applyBCV", spath, ["-A", mat], "warped_seg_affine")):
+        out = str(tmp_path / (key + ".nii.gz"))
+        r = subprocess.run([os.path.join(build.OUT, exe), "-M", src, "-O", stem, "-D", out] + extra,
+                           capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stdout + r.stderr
+        vol, _ = nifti.read(out)
+        assert same_bits(vol.ravel(order="F").astype(a[key].dtype), a[key]), key
+
+
 def test_register_device_equals_host(api):
     from deedsbcv_gb300 import phantom
     shape = (48, 40, 56)

@@ -97,3 +97,29 @@ def test_register_end_to_end_matches_reference_binary(golden):
     assert np.array_equal((warped - np.float32(1024)).view(np.uint32), e["warped"].view(np.uint32))
     seg = orc.warp_affine_s(e["moving_labels"].astype(np.int16), np.eye(4, dtype=np.float32).ravel(), ux, vx, wx, m, n, o)
     assert np.array_equal(seg, e["warped_seg"])
+
+
+def _apply_inputs(e):
+    """The applyBCV / applyBCVfloat inputs of apply.npz: the e2e flow, the float
+    image 0.37 x moving + 11.125 and the moving labels."""
+    m, n, o = (int(x) for x in e["dims"])
+    img = (e["moving"].astype(np.float32) * np.float32(0.37) + np.float32(11.125)).astype(np.float32)
+    return (m, n, o), e["flow"], img.ravel(order="F"), e["moving_labels"].astype(np.int16).ravel(order="F")
+
+
+def test_apply_float_and_affine_match_reference_binaries(golden):
+    """applyBCVfloat (trilinear, with and without an affine matrix) and applyBCV with
+    a matrix (src/applyBCV.cpp:161-198): the grid step inferred from the .dat size,
+    upsampling, then the warp; the reference binaries wrote apply.npz."""
+    e, a = golden("e2e"), golden("apply")
+    (m, n, o), flow, img, lab = _apply_inputs(e)
+    sz1 = flow.size // 3
+    g = int(round((m * n * o / sz1) ** (1.0 / 3.0)))
+    ux, vx, wx = orc.upsample(flow[:sz1], flow[sz1:2 * sz1], flow[2 * sz1:], m, n, o, m // g, n // g, o // g)
+    eye = np.eye(4, dtype=np.float32).ravel()
+    w = orc.warp_affine(img, eye, ux, vx, wx, m, n, o)
+    assert np.array_equal(w.view(np.uint32), a["warped_float"].view(np.uint32))
+    w = orc.warp_affine(img, a["X"], ux, vx, wx, m, n, o)
+    assert np.array_equal(w.view(np.uint32), a["warped_float_affine"].view(np.uint32))
+    s = orc.warp_affine_s(lab, a["X"], ux, vx, wx, m, n, o)
+    assert np.array_equal(s, a["warped_seg_affine"])

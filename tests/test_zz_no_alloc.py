@@ -53,6 +53,23 @@ def test_noalloc_matches_context_path_twice(lib, shape, g):
     ctx.close()
 
 
+def test_noalloc_warm_call_allocates_nothing(lib):
+    """The whole point of the entry point: once the first call on the device has
+    loaded the module (which reserves the fixed array), later calls leave the
+    device's free memory unchanged."""
+    shape, g = (48, 40, 64), 4
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    warm = _fields(21, shape)
+    assert lib.deeds_consistent_noalloc_dev(*_ptrs(warm), *shape, g, stream) == 0
+    fresh = _fields(22, shape)  # inputs allocated before the measurement
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    assert lib.deeds_consistent_noalloc_dev(*_ptrs(fresh), *shape, g, stream) == 0
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before
+
+
 def test_noalloc_rejects_oversized_grid(lib):
     from deedsbcv_gb300._lib import NOALLOC_MAX_NODES
     shape = (64, 64, NOALLOC_MAX_NODES // (64 * 64) + 1)
@@ -60,3 +77,16 @@ def test_noalloc_rejects_oversized_grid(lib):
     p = C.c_void_p(t.data_ptr())
     st = lib.deeds_consistent_noalloc_dev(p, p, p, p, p, p, *shape, 4, C.c_void_p(0))
     assert st == 1  # DEEDS_ERR_INVALID, nothing launched
+
+
+def test_noalloc_rejects_grid_beyond_launch_limits(lib):
+    """Few nodes in total but n above the kernels' 65535 grid limit: rejected
+    before any launch, so the caller's fields are left as they were."""
+    shape = (1, 70000, 1)
+    fields = _fields(5, shape)
+    before = [f.clone() for f in fields]
+    st = lib.deeds_consistent_noalloc_dev(*_ptrs(fields), *shape, 4, C.c_void_p(0))
+    assert st == 1  # DEEDS_ERR_INVALID
+    torch.cuda.synchronize()
+    for a, b in zip(before, fields):
+        assert torch.equal(a, b)
