@@ -279,12 +279,14 @@ struct QueuedEdge {
 //   push: append, then move the new element up while its parent compares
 //         "less" (parent weight > new weight);
 //   pop:  take the root; move a hole from the root down to a leaf, always into
-//         the child that compares greater (the lighter edge; the left child
-//         when the right one is not strictly lighter), including the
+//         the child that compares greater (the lighter edge; the right child
+//         unless it is strictly heavier than the left one), including the
 //         single-child case at the end of an even-length heap; then place the
 //         former last element at the hole and move it up as in push.
-// It differs only in being branch-free in the descent and prefetching the
-// grandchildren, which changes timing, not order.
+// It differs only in how the descent is evaluated: branch-free, two levels per
+// step while both are full levels (the four grandchildren are compared in the
+// same step as the two children, which halves the dependent load-compare chain),
+// and with the path prefetched ahead; that changes timing, not order.
 class EdgeHeap {
   public:
     explicit EdgeHeap(size_t reserve) { grow(std::max<size_t>(reserve, 64)); }
@@ -300,8 +302,32 @@ class EdgeHeap {
         const size_t len = n_;
         if (len == 0) return top;
         QueuedEdge* d = a_;
-        size_t hole = 0, child = 0;
-        while (child < (len - 1) / 2) {
+        size_t hole = 0;
+        const size_t lim = (len - 1) / 2;
+        // Two levels per step while the deeper of the two possible children still
+        // has children below it (both levels are then full descents).  Choices as
+        // the single-level step below: right (c + 1) unless it is strictly heavier.
+        while (2 * hole + 2 < lim) {
+            {
+                const size_t first = ((hole + 1) << DEEDS_HEAP_LOOKAHEAD) - 1;
+                if (first < len) {
+                    __builtin_prefetch(d + first);
+                    if (first + 8 < len) __builtin_prefetch(d + first + 8);
+                }
+            }
+            const size_t c = 2 * hole + 1, gc = 4 * hole + 3;
+            const float lw = d[c].weight, rw = d[c + 1].weight;
+            const float g0 = d[gc].weight, g1 = d[gc + 1].weight, g2 = d[gc + 2].weight, g3 = d[gc + 3].weight;
+            const size_t p1 = (size_t)!(rw > lw);
+            const size_t p2a = (size_t)!(g1 > g0), p2b = (size_t)!(g3 > g2);
+            const size_t p2 = p2a ^ ((p2a ^ p2b) & (0 - p1));  // p1 ? p2b : p2a, without a branch
+            const size_t c1 = c + p1, c2 = gc + 2 * p1 + p2;
+            d[hole] = d[c1];
+            d[c1] = d[c2];
+            hole = c2;
+        }
+        size_t child = hole;
+        while (child < lim) {
             // The descendants of the hole k levels down are the 2^k contiguous
             // entries from 2^k (hole + 1) - 1: prefetch those DEEDS_HEAP_LOOKAHEAD
             // levels ahead so the misses of a root-to-leaf walk overlap.
@@ -317,7 +343,7 @@ class EdgeHeap {
             const size_t gc = 2 * child + 1;
             if (gc < len) __builtin_prefetch(d + gc);
             if (gc - 2 < len) __builtin_prefetch(d + gc - 2);
-            // the left child wins unless the right one is strictly lighter
+            // the right child wins unless it is strictly heavier than the left one
             child -= (size_t)(d[child].weight > d[child - 1].weight);
             d[hole] = d[child];
             hole = child;
