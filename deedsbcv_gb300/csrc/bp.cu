@@ -24,9 +24,9 @@
 // strict '<' so the first minimiser wins.
 //
 // Downward pass (root to leaves, :258-293): one CTA per tree takes the root's
-// first minimum, then resolves one breadth level per step from the argmin
-// tables, keeping the previous level's labels in shared memory and prefetching
-// the argmin rows of the next levels into L2.
+// first minimum, then its threads walk heavy-path chains (each follows the child
+// with the deepest subtree) from the argmin tables, a chain starting once its
+// first node's parent has a label; no barrier per breadth level.
 //
 // Roofline: dependency bound (tree depth 265-987 per tree at 192x160x256).
 // Algorithmic traffic: one read + one write of the cost volume and one write of
@@ -302,22 +302,40 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
     }
 }
 
-// Root argmin (first minimum) and breadth-level backtrack for one tree.  Per
-// level the only dependent access is the argmin-table gather; the next level's
-// node ids, parent positions and current displacements are loaded before it.
+// Labels of the downward pass live in global memory and are exchanged between
+// threads of the one CTA that runs the pass: relaxed CTA-scope accesses (the label
+// is the only datum passed, so no ordering beyond the access itself is needed).
+__device__ __forceinline__ int ld_label(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.cta.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_label(int* p, int v) {
+    asm volatile("st.relaxed.cta.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+constexpr long long kDownSpinLimit = 1LL << 21;  // polls of a 64 ns sleep: ~0.13 s, far beyond a pass
+
+// Root argmin (first minimum), then the backtrack (src/regularisation.h:258-293)
+// over heavy-path chains.  The reference resolves one breadth level after another;
+// here a thread claims a chain (chains in breadth order of their first node),
+// waits until the first node's parent has its label, and then walks the chain
+// down to its leaf, one argmin-table gather per node with no barrier in between.
+// The chains follow the deepest subtree at every node, so the longest root-leaf
+// path is walked by few threads without waiting: the pass costs about one gather
+// latency per node of that path.  Each thread prefetches the argmin row of the
+// next node of its chain into L2.  Waits are bounded (error 4 on expiry); a label
+// or a table entry out of range records error 2 and reads label 0 instead.
 __global__ void __launch_bounds__(1024) k_bp_down(BpTree t, const float* __restrict__ cost,
                                                  short* __restrict__ allinds, float* __restrict__ u1,
-                                                 float* __restrict__ v1, float* __restrict__ w1,
+                                                 float* __restrict__ v1, float* __restrict__ w1, int* labels,
                                                  int* __restrict__ err) {
-    extern __shared__ int sm_down[];  // two buffers of max_width labels, then the level ranges
     __shared__ float s_val[32];
     __shared__ int s_idx[32];
+    __shared__ int s_next;
+    __shared__ int s_abort;
     const int len = t.len, len3 = len * len * len, hw = (len - 1) / 2;
-    const int W = t.max_width;
-    int* s_sel = sm_down;
-    int* s_ls = sm_down + 2 * W;
-    for (int i = threadIdx.x; i <= t.n_levels; i += blockDim.x) s_ls[i] = t.level_start[i];
-    const int root = t.ordered[0];
+    const int root = t.root;
     const float* rr = cost + (int64_t)root * len3;
     float bv = INFINITY;
     int bi = 0x7fffffff;
@@ -346,71 +364,64 @@ __global__ void __launch_bounds__(1024) k_bp_down(BpTree t, const float* __restr
             // the reference scans with value=cost[0], index=0 and '<' (src/regularisation.h:258-279):
             // a NaN at 0 keeps index 0, NaNs elsewhere never win
             if (isnan(__ldcg(rr)) || bi < 0 || bi >= len3) bi = 0;
-            s_sel[0] = bi;
+            st_label(labels + root, bi);
             const int i = bi % len, j = (bi / len) % len, k = bi / (len * len);
             u1[root] = (float)(j - hw) * t.q + t.u0[root];
             v1[root] = (float)(i - hw) * t.q + t.v0[root];
             w1[root] = (float)(k - hw) * t.q + t.w0[root];
+            s_next = 0;
+            s_abort = 0;
         }
     }
     __syncthreads();
     const int row_lines = (len3 * 2 + 127) / 128;
-    // first node of the next level owned by this thread, loaded one level ahead
-    int nc = -1, npp = 0;
-    float nu = 0.0f, nv = 0.0f, nw = 0.0f;
-    auto preload = [&](int lev) {
-        nc = -1;
-        if (lev < t.n_levels) {
-            const int ti = s_ls[lev] + (int)threadIdx.x;
-            if (ti < s_ls[lev + 1]) {
-                nc = t.ordered[ti];
-                npp = t.parent_pos[ti];
-                nu = t.u0[nc]; nv = t.v0[nc]; nw = t.w0[nc];
+    for (;;) {
+        const int c = atomicAdd(&s_next, 1);
+        if (c >= t.n_chains) return;
+        int i = t.chain_ptr[c];
+        const int e = t.chain_ptr[c + 1];
+        int lp;
+        if (t.chain_nodes[i] == root) {
+            lp = ld_label(labels + root);  // written before the barrier
+            i++;
+        } else {
+            const int* flag = labels + t.parents[t.chain_nodes[i]];
+            long long it = 0;
+            while ((lp = ld_label(flag)) < 0) {
+                if (++it > kDownSpinLimit || *(volatile int*)&s_abort) {
+                    atomicCAS(err, 0, 4);
+                    *(volatile int*)&s_abort = 1;
+                    return;
+                }
+                __nanosleep(64);
             }
         }
-    };
-    preload(1);
-    for (int lev = 1; lev < t.n_levels; lev++) {
-        const int b = s_ls[lev], e = s_ls[lev + 1], pb = s_ls[lev - 1];
-        const int* prev = s_sel + ((lev - 1) & 1) * W;
-        int* cur = s_sel + (lev & 1) * W;
-        const int c = nc, pp = npp;
-        const float cu = nu, cv = nv, cw = nw;
-        preload(lev + 1);
-        // warm L2 with the argmin rows two levels ahead
-        if (lev + 2 < t.n_levels) {
-            const int b2 = s_ls[lev + 2], e2 = s_ls[lev + 3];
-            for (int qq = threadIdx.x; qq < (e2 - b2) * row_lines; qq += blockDim.x) {
-                const int cc = t.ordered[b2 + qq / row_lines];
-                const char* a = reinterpret_cast<const char*>(allinds + (int64_t)cc * len3) + (qq % row_lines) * 128;
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+        int nxt = i < e ? t.chain_nodes[i] : -1;
+        while (nxt >= 0) {
+            const int node = nxt;
+            nxt = i + 1 < e ? t.chain_nodes[i + 1] : -1;
+            if (nxt >= 0) {
+                const char* a = reinterpret_cast<const char*>(allinds + (int64_t)nxt * len3);
+                for (int k = 0; k < row_lines; k++) asm volatile("prefetch.global.L2 [%0];" ::"l"(a + 128 * k));
             }
-        }
-        for (int ti = b + threadIdx.x; ti < e; ti += blockDim.x) {
-            int cc, ppos;
-            float a0, a1, a2;
-            if (ti == b + (int)threadIdx.x) { cc = c; ppos = pp; a0 = cu; a1 = cv; a2 = cw; }
-            else {
-                cc = t.ordered[ti]; ppos = t.parent_pos[ti];
-                a0 = t.u0[cc]; a1 = t.v0[cc]; a2 = t.w0[cc];
-            }
-            int sp = prev[ppos - pb];
-            if (sp < 0 || sp >= len3) {  // never for a completed upward pass; keeps reads in bounds
+            const float a0 = t.u0[node], a1 = t.v0[node], a2 = t.w0[node];
+            if (lp < 0 || lp >= len3) {  // never for a completed upward pass; keeps reads in bounds
                 atomicCAS(err, 0, 2);
-                sp = 0;
+                lp = 0;
             }
-            int l = allinds[(int64_t)cc * len3 + sp];
+            int l = allinds[(int64_t)node * len3 + lp];
             if (l < 0 || l >= len3) {  // never for a completed upward pass; keeps reads in bounds
                 atomicCAS(err, 0, 2);
                 l = 0;
             }
-            cur[ti - b] = l;
-            const int i = l % len, j = (l / len) % len, k = l / (len * len);
-            u1[cc] = (float)(j - hw) * t.q + a0;
-            v1[cc] = (float)(i - hw) * t.q + a1;
-            w1[cc] = (float)(k - hw) * t.q + a2;
+            st_label(labels + node, l);
+            const int ii = l % len, jj = (l / len) % len, kk = l / (len * len);
+            u1[node] = (float)(jj - hw) * t.q + a0;
+            v1[node] = (float)(ii - hw) * t.q + a1;
+            w1[node] = (float)(kk - hw) * t.q + a2;
+            lp = l;
+            i++;
         }
-        __syncthreads();
     }
 }
 
@@ -475,19 +486,12 @@ cudaError_t launch_bp_up(const BpTree& t, float* d_cost, short* d_allinds, float
     }
 }
 
-size_t bp_down_smem_bytes(int max_width, int n_levels) {
-    return (size_t)(2 * max_width + n_levels + 1) * sizeof(int);
-}
-
 cudaError_t launch_bp_down(const BpTree& t, const float* d_cost, short* d_allinds, float* d_u1, float* d_v1,
-                           float* d_w1, int* d_err, cudaStream_t s) {
-    const size_t smem = bp_down_smem_bytes(t.max_width, t.n_levels);
-    if (smem > 200 * 1024) return cudaErrorInvalidValue;
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_bp_down, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-    }
-    k_bp_down<<<1, 1024, smem, s>>>(t, d_cost, d_allinds, d_u1, d_v1, d_w1, d_err);
+                           float* d_w1, int* d_labels, int* d_err, cudaStream_t s) {
+    if (t.n_chains < 1 || !t.chain_ptr || !t.chain_nodes) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(d_labels, 0xff, sizeof(int) * (size_t)t.sz, s);  // -1: no label yet
+    if (e != cudaSuccess) return e;
+    k_bp_down<<<1, 1024, 0, s>>>(t, d_cost, d_allinds, d_u1, d_v1, d_w1, d_labels, d_err);
     count_launches(1);
     return cudaGetLastError();
 }

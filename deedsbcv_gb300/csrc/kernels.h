@@ -31,6 +31,9 @@ struct BpTree {
     const int* level_start;  // [n_levels+1] ranges into ordered
     const int* ordered;      // [sz] breadth-level order
     const int* parent_pos;   // [sz] position in `ordered` of the parent of ordered[t]
+    int n_chains;            // heavy-path chains (downward pass)
+    const int* chain_ptr;    // [n_chains+1] ranges into chain_nodes
+    const int* chain_nodes;  // [sz] each chain's nodes from its start down to a leaf
 };
 
 // A displacement field given at full resolution (mode 1), on a control grid
@@ -56,9 +59,9 @@ cudaError_t launch_edge_sad(const float* d_im, int m, int n, int o, int g, float
 // d_mins: 4 * t.sz floats (per-node message minima, then the x | y | z edge offsets)
 cudaError_t launch_bp_up(const BpTree& t, float* d_cost, short* d_allinds, float* d_mins, int* d_arrived, int* d_work,
                          int sm_count, cudaStream_t s);
-size_t bp_down_smem_bytes(int max_width, int n_levels);
+// d_labels: t.sz ints of scratch (each node's selected label)
 cudaError_t launch_bp_down(const BpTree& t, const float* d_cost, short* d_allinds, float* d_u1, float* d_v1,
-                           float* d_w1, int* d_err, cudaStream_t s);
+                           float* d_w1, int* d_labels, int* d_err, cudaStream_t s);
 cudaError_t launch_shift(const float* d_in, float* d_out, int64_t n, float shift, cudaStream_t s);
 cudaError_t launch_upsample(const float* u0, const float* v0, const float* w0, int m2, int n2, int o2, float* u,
                             float* v, float* w, int m, int n, int o, cudaStream_t s);

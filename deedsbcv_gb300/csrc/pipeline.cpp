@@ -326,8 +326,8 @@ deeds_status check_params(deeds_ctx* ctx, const deeds_params* p, int m, int n, i
 
 // One tree's host arrays packed for a single H2D copy (4-byte words).
 struct PackedTree {
-    int sz = 0, n_leaves = 0, n_levels = 0, max_width = 0;
-    size_t o_ordered, o_parents, o_edgemst, o_cptr, o_children, o_leaves, o_lstart, o_ppos, total;
+    int sz = 0, n_leaves = 0, n_levels = 0, max_width = 0, n_chains = 0;
+    size_t o_ordered, o_parents, o_edgemst, o_cptr, o_children, o_leaves, o_lstart, o_ppos, o_chptr, o_chnodes, total;
 };
 
 PackedTree pack_layout(int sz) {
@@ -342,6 +342,8 @@ PackedTree pack_layout(int sz) {
     t.o_leaves = o; o += sz;
     t.o_lstart = o; o += sz + 1;
     t.o_ppos = o; o += sz;
+    t.o_chptr = o; o += sz + 1;
+    t.o_chnodes = o; o += sz;
     t.total = o;
     return t;
 }
@@ -355,6 +357,9 @@ void pack_schedule(const TreeSchedule& s, uint32_t* blk, PackedTree& t) {
     std::memcpy(blk + t.o_leaves, s.leaves.data(), sizeof(int) * s.leaves.size());
     std::memcpy(blk + t.o_lstart, s.level_start.data(), sizeof(int) * s.level_start.size());
     std::memcpy(blk + t.o_ppos, s.parent_pos.data(), sizeof(int) * s.parent_pos.size());
+    t.n_chains = (int)s.chain_ptr.size() - 1;
+    std::memcpy(blk + t.o_chptr, s.chain_ptr.data(), sizeof(int) * s.chain_ptr.size());
+    std::memcpy(blk + t.o_chnodes, s.chain_nodes.data(), sizeof(int) * s.chain_nodes.size());
 }
 
 // Build one tree on the host into the packed pinned block `blk`.
@@ -388,6 +393,9 @@ BpTree device_tree(const PackedTree& t, const uint32_t* dblk, const uint32_t* hb
     b.level_start = reinterpret_cast<const int*>(dblk + t.o_lstart);
     b.ordered = reinterpret_cast<const int*>(dblk + t.o_ordered);
     b.parent_pos = reinterpret_cast<const int*>(dblk + t.o_ppos);
+    b.n_chains = t.n_chains;
+    b.chain_ptr = reinterpret_cast<const int*>(dblk + t.o_chptr);
+    b.chain_nodes = reinterpret_cast<const int*>(dblk + t.o_chnodes);
     return b;
 }
 
@@ -401,8 +409,6 @@ deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTre
     int* d_arrived = dbuf<int>(ctx, "arrived_" + tag, pt.sz, &st);
     int* d_work = dbuf<int>(ctx, "work_" + tag, 1, &st);
     if (st) return st;
-    if (bp_down_smem_bytes(pt.max_width, pt.n_levels) > 200 * 1024)
-        return fail(ctx, DEEDS_ERR_INVALID, "MST breadth level of %d nodes is too wide", pt.max_width);
     CK(cudaMemcpyAsync(d_blk, h_blk, pt.total * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
     const BpTree bt = device_tree(pt, d_blk, h_blk, len, (float)q, u0, v0, w0);
     {
@@ -411,7 +417,8 @@ deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTre
     }
     {
         StageScope sc(ctx, DEEDS_STAGE_BP_DOWN, s);
-        CK(launch_bp_down(bt, d_cost, d_allinds, u1, v1, w1, d_err, s));
+        // the upward pass is done with its arrival counters: they hold the labels now
+        CK(launch_bp_down(bt, d_cost, d_allinds, u1, v1, w1, d_arrived, d_err, s));
     }
     return DEEDS_OK;
 }

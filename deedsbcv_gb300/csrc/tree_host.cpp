@@ -477,6 +477,27 @@ void build_schedule(const int* ordered, const int* parents, int sz, TreeSchedule
     }
     s.parent_pos.assign(sz, 0);
     for (int t = 1; t < sz; t++) s.parent_pos[t] = pos[parents[ordered[t]]];
+    // heavy children: subtree heights bottom-up (ordering is breadth-level, so every
+    // child is visited before its parent); in reverse order '>=' keeps the first
+    // child of equal height
+    std::vector<int> height(sz, 0), heavy(sz, -1);
+    for (int t = sz - 1; t >= 1; t--) {
+        const int c = ordered[t], p = parents[c];
+        if (height[c] + 1 >= height[p]) {
+            height[p] = height[c] + 1;
+            heavy[p] = c;
+        }
+    }
+    s.chain_ptr.clear();
+    s.chain_nodes.clear();
+    s.chain_nodes.reserve(sz);
+    for (int t = 0; t < sz; t++) {
+        const int v = ordered[t];
+        if (t > 0 && heavy[parents[v]] == v) continue;  // continues its parent's chain
+        s.chain_ptr.push_back((int)s.chain_nodes.size());
+        for (int c = v; c >= 0; c = heavy[c]) s.chain_nodes.push_back(c);
+    }
+    s.chain_ptr.push_back((int)s.chain_nodes.size());
 }
 
 }  // namespace deeds

@@ -13,6 +13,12 @@ struct TreeSchedule {
     std::vector<int> children;     // in MST ordering order
     std::vector<int> leaves;       // nodes without children (root excluded), deepest first
     std::vector<int> parent_pos;   // [sz] position in ordered of the parent of ordered[t]
+    // Heavy-path chains for the downward pass: from each chain start (the root,
+    // and every child that is not its parent's heavy child) down through heavy
+    // children (the child with the deepest subtree, the first such on ties) to a
+    // leaf; chains in breadth order of their starts, every node in exactly one.
+    std::vector<int> chain_ptr;    // [n_chains+1] ranges into chain_nodes
+    std::vector<int> chain_nodes;  // [sz]
 };
 
 void image_stats(const float* im, size_t sz, float* mean_out, float* std_out);
