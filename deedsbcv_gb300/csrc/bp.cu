@@ -148,6 +148,97 @@ __device__ __forceinline__ void dt_lines(const float* in, float* out, const shor
     dt_dispatch<LEN, AXIS, 0>(part, in, out, idx_in, idx_out, off, base);
 }
 
+// Three-input minimum (PTX min.f32 with three sources, sm_100 and later): like
+// fminf, a NaN source is ignored unless all are NaN.
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+}
+
+// Minimum of N values as a tree of three-input minima (depth log3 N instead of
+// the N-long compare chain of a sequential scan).
+template <int N>
+__device__ __forceinline__ float min_all(const float* c) {
+    if constexpr (N == 1) {
+        return c[0];
+    } else if constexpr (N == 2) {
+        return fminf(c[0], c[1]);
+    } else {
+        constexpr int M = (N + 2) / 3;
+        float t[M];
+#pragma unroll
+        for (int g = 0; g < M; g++) {
+            if (3 * g + 2 < N) t[g] = fmin3(c[3 * g], c[3 * g + 1], c[3 * g + 2]);
+            else if (3 * g + 1 < N) t[g] = fminf(c[3 * g], c[3 * g + 1]);
+            else t[g] = c[3 * g];
+        }
+        return min_all<M>(t);
+    }
+}
+
+// Outputs [I0, I1) of one line, values only: out[i] = min_s in[s] + (i - s + off)^2.
+// The minimum of the candidates is the value the reference's strict-'<' scan ends
+// with (which candidate attains it does not change the value; costs are never
+// -0).  NaN: the scan starts from candidate 0 and never replaces a NaN start, so a
+// NaN candidate 0 is the result; later NaN candidates never win (as in fminf).
+template <int LEN, int AXIS, int I0, int I1>
+__device__ __forceinline__ void dt_part_val(const float* in, float* out, float off, int base) {
+    constexpr int STRIDE = AXIS == 0 ? 1 : (AXIS == 1 ? LEN : LEN * LEN);
+    float v[LEN];
+#pragma unroll
+    for (int s = 0; s < LEN; s++) v[s] = in[base + s * STRIDE];
+    float z[2 * LEN];
+#pragma unroll
+    for (int u = I0 + 1; u < I1 + LEN; u++) {
+        const float d = (float)(u - LEN) + off;
+        z[u] = d * d;
+    }
+#pragma unroll
+    for (int i = I0; i < I1; i++) {
+        float c[LEN];
+#pragma unroll
+        for (int s = 0; s < LEN; s++) c[s] = v[s] + z[i - s + LEN];
+        const float m = min_all<LEN>(c);
+        out[base + i * STRIDE] = c[0] != c[0] ? c[0] : m;
+    }
+}
+
+template <int LEN, int AXIS, int P>
+__device__ __forceinline__ void dt_dispatch_val(int part, const float* in, float* out, float off, int base) {
+    constexpr int K = bp_parts(LEN), OPP = (LEN + K - 1) / K;
+    if constexpr (P < K) {
+        if (part == P) {
+            constexpr int I0 = P * OPP, I1 = (P + 1) * OPP < LEN ? (P + 1) * OPP : LEN;
+            if constexpr (I0 < I1) dt_part_val<LEN, AXIS, I0, I1>(in, out, off, base);
+            return;
+        }
+        dt_dispatch_val<LEN, AXIS, P + 1>(part, in, out, off, base);
+    }
+}
+
+template <int LEN, int AXIS>
+__device__ __forceinline__ void dt_lines_val(const float* in, float* out, float off) {
+    constexpr int LEN2 = LEN * LEN, LP = bp_line_slots(LEN);
+    const int part = threadIdx.x / LP, line = threadIdx.x - part * LP;
+    if (line >= LEN2) return;
+    const int base = AXIS == 0 ? line * LEN : (AXIS == 1 ? (line % LEN) + (line / LEN) * LEN2 : line);
+    dt_dispatch_val<LEN, AXIS, 0>(part, in, out, off, base);
+}
+
+// Block-wide minimum with one barrier: warps reduce by shuffles, then every thread
+// reduces the per-warp values.  `red` must not be rewritten before every thread has
+// read it (the caller's next barrier).
+__device__ __forceinline__ float block_min1(float v, float* red) {
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    const int nw = (int)(blockDim.x >> 5);
+    v = red[0];
+    for (int w = 1; w < nw; w++) v = fminf(v, red[w]);
+    return v;
+}
+
 __device__ float block_min(float v, float* red) {
     for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -165,7 +256,7 @@ __device__ float block_min(float v, float* red) {
 
 template <int LEN>
 __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __restrict__ cost,
-                                                           short* __restrict__ allinds, float* __restrict__ mins,
+                                                           float* __restrict__ pre, float* __restrict__ mins,
                                                            const float* __restrict__ off,
                                                            int* __restrict__ arrived, int* __restrict__ work) {
     constexpr int LEN3 = LEN * LEN * LEN;
@@ -174,8 +265,6 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
     extern __shared__ float smem[];
     float* A = smem;
     float* B = A + LEN3;
-    short* ia = reinterpret_cast<short*>(B + LEN3);
-    short* ib = ia + LEN3;
     __shared__ float red[32];
     __shared__ int s_node, s_last;
     const int tid = threadIdx.x;
@@ -191,7 +280,12 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
         {
             const float e = t.edgemst[node];
             const float* row = cost + (int64_t)node * LEN3;
-            for (int l = tid; l < LEN3; l += T) A[l] = __fmul_rn(ld_cg(row + l), e);
+            float* prow = pre + (int64_t)node * LEN3;
+            for (int l = tid; l < LEN3; l += T) {
+                const float a = __fmul_rn(ld_cg(row + l), e);
+                A[l] = a;
+                prow[l] = a;
+            }
         }
         // The chain's static tree data is pipelined: the grandparent's id is known
         // one step ahead and everything else about it (child range, the parent's
@@ -228,22 +322,20 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
             int ggp = gp;
             if (gp != t.root) ggp = ld_ahead(t.parents + gp);
             __syncthreads();
-            dt_lines<LEN, 0>(A, B, nullptr, ia, oy);
+            dt_lines_val<LEN, 0>(A, B, oy);
             __syncthreads();
-            dt_lines<LEN, 1>(B, A, ia, ib, ox);
+            dt_lines_val<LEN, 1>(B, A, ox);
             __syncthreads();
-            dt_lines<LEN, 2>(A, B, ib, ia, oz);  // message in B, argmin chain in ia
+            dt_lines_val<LEN, 2>(A, B, oz);  // message in B (its argmins: k_bp_argmin, from `pre`)
             __syncthreads();
             float mn = INFINITY;
             float* crow = cost + (int64_t)node * LEN3;
-            short* arow = allinds + (int64_t)node * LEN3;
             for (int l = tid; l < LEN3; l += T) {
                 const float v = B[l];
                 mn = fminf(mn, v);
                 crow[l] = v;
-                arow[l] = ia[l];
             }
-            mn = block_min(mn, red);  // ends with a barrier: all stores of this CTA precede
+            mn = block_min1(mn, red);  // its barrier orders all stores of this CTA before the arrival
             // *std::min_element (src/regularisation.h:222) starts from element 0 and only
             // replaces it on '<': a NaN first element is the result, later NaNs are skipped
             if (isnan(B[0])) mn = B[0];
@@ -289,10 +381,15 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
                 break;
             }
             __syncthreads();  // B (this message) has been consumed by every thread
+            float* pprow = pre + (int64_t)p * LEN3;
 #pragma unroll
             for (int k = 0; k < NL; k++) {
                 const int l = tid + k * T;
-                if (l < LEN3) A[l] = __fmul_rn(acc[k], ep);
+                if (l < LEN3) {
+                    const float a = __fmul_rn(acc[k], ep);
+                    A[l] = a;
+                    pprow[l] = a;
+                }
             }
             node = p;
             on_x = opx; on_y = opy; on_z = opz;
@@ -396,14 +493,22 @@ __global__ void __launch_bounds__(1024) k_bp_down(BpTree t, const float* __restr
                 __nanosleep(64);
             }
         }
-        int nxt = i < e ? t.chain_nodes[i] : -1;
-        while (nxt >= 0) {
-            const int node = nxt;
-            nxt = i + 1 < e ? t.chain_nodes[i + 1] : -1;
-            if (nxt >= 0) {
-                const char* a = reinterpret_cast<const char*>(allinds + (int64_t)nxt * len3);
-                for (int k = 0; k < row_lines; k++) asm volatile("prefetch.global.L2 [%0];" ::"l"(a + 128 * k));
-            }
+        // The chain's node ids run three ahead of the walk: the id a step prefetches
+        // for was loaded a step earlier, so neither the prefetch nor the gather waits
+        // for an id load; the argmin rows are prefetched into L2 two nodes ahead.
+        auto node_at = [&](int k) { return k < e ? ld_ahead(t.chain_nodes + k) : -1; };
+        auto prefetch_row = [&](int v) {
+            if (v < 0) return;
+            const char* a = reinterpret_cast<const char*>(allinds + (int64_t)v * len3);
+            for (int k = 0; k < row_lines; k++) asm volatile("prefetch.global.L2 [%0];" ::"l"(a + 128 * k));
+        };
+        int cur = node_at(i), n1 = node_at(i + 1), n2 = node_at(i + 2);
+        prefetch_row(n1);
+        while (cur >= 0) {
+            const int node = cur;
+            const int n3 = node_at(i + 3);
+            prefetch_row(n2);
+            cur = n1; n1 = n2; n2 = n3;
             const float a0 = t.u0[node], a1 = t.v0[node], a2 = t.w0[node];
             if (lp < 0 || lp >= len3) {  // never for a completed upward pass; keeps reads in bounds
                 atomicCAS(err, 0, 2);
@@ -441,12 +546,49 @@ __global__ void k_bp_offsets(BpTree t, float* __restrict__ off) {
     off[2 * t.sz + c] = __fdiv_rn(t.w0[p] - t.w0[c], t.q);
 }
 
+// Argmin tables of the upward sweep (allinds, src/regularisation.h:37-107): the
+// sweep itself computes message values only; here every node's three passes are
+// run again from its stored scaled row (`pre`, the transform's input) with the
+// reference's strict-'<' first-minimiser scans, which reproduce the sweep's
+// values bit for bit and record, per parent label, the child label.  The nodes
+// are independent, so this runs across the whole GPU (persistent CTAs striding
+// over nodes) instead of on the sweep's dependency chain.  The root has no edge
+// (its row is written by the downward pass).
 template <int LEN>
-cudaError_t launch_up(const BpTree& t, float* cost, short* allinds, float* mins, int* arrived, int* work,
-                      int sm_count, cudaStream_t s) {
+__global__ void __launch_bounds__(bp_threads(LEN)) k_bp_argmin(BpTree t, const float* __restrict__ pre,
+                                                               const float* __restrict__ off,
+                                                               short* __restrict__ allinds) {
     constexpr int LEN3 = LEN * LEN * LEN;
     constexpr int T = bp_threads(LEN);
-    const size_t smem = (size_t)LEN3 * (2 * sizeof(float) + 2 * sizeof(short));
+    extern __shared__ float smem[];
+    float* A = smem;
+    float* B = A + LEN3;
+    short* ia = reinterpret_cast<short*>(B + LEN3);
+    short* ib = ia + LEN3;
+    for (int node = blockIdx.x; node < t.sz; node += gridDim.x) {
+        if (node == t.root) continue;
+        const float* prow = pre + (int64_t)node * LEN3;
+        for (int l = threadIdx.x; l < LEN3; l += T) A[l] = ld_cg(prow + l);
+        const float ox = off[node], oy = off[t.sz + node], oz = off[2 * t.sz + node];
+        __syncthreads();
+        dt_lines<LEN, 0>(A, B, nullptr, ia, oy);
+        __syncthreads();
+        dt_lines<LEN, 1>(B, A, ia, ib, ox);
+        __syncthreads();
+        dt_lines<LEN, 2>(A, B, ib, ia, oz);
+        __syncthreads();
+        short* arow = allinds + (int64_t)node * LEN3;
+        for (int l = threadIdx.x; l < LEN3; l += T) arow[l] = ia[l];
+        __syncthreads();  // A / ia are rewritten by the next node
+    }
+}
+
+template <int LEN>
+cudaError_t launch_up(const BpTree& t, float* cost, short* allinds, float* pre, float* mins, int* arrived,
+                      int* work, int sm_count, cudaStream_t s) {
+    constexpr int LEN3 = LEN * LEN * LEN;
+    constexpr int T = bp_threads(LEN);
+    const size_t smem = (size_t)LEN3 * 2 * sizeof(float);
     cudaError_t e = cudaFuncSetAttribute(k_bp_up<LEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
@@ -457,31 +599,41 @@ cudaError_t launch_up(const BpTree& t, float* cost, short* allinds, float* mins,
     if (ctas > t.n_leaves) ctas = t.n_leaves;
     float* off = mins + t.sz;
     k_bp_offsets<<<(t.sz + 255) / 256, 256, 0, s>>>(t, off);
-    k_bp_up<LEN><<<ctas, T, smem, s>>>(t, cost, allinds, mins, off, arrived, work);
-    count_launches(2);
+    k_bp_up<LEN><<<ctas, T, smem, s>>>(t, cost, pre, mins, off, arrived, work);
+    const size_t smem_a = (size_t)LEN3 * (2 * sizeof(float) + 2 * sizeof(short));
+    e = cudaFuncSetAttribute(k_bp_argmin<LEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_a);
+    if (e != cudaSuccess) return e;
+    int per_sm_a = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_a, k_bp_argmin<LEN>, T, smem_a);
+    if (e != cudaSuccess) return e;
+    if (per_sm_a < 1) return cudaErrorInvalidConfiguration;
+    int ctas_a = per_sm_a * sm_count;
+    if (ctas_a > t.sz) ctas_a = t.sz;
+    k_bp_argmin<LEN><<<ctas_a, T, smem_a, s>>>(t, pre, off, allinds);
+    count_launches(3);
     return cudaGetLastError();
 }
 
 }  // namespace
 
-cudaError_t launch_bp_up(const BpTree& t, float* d_cost, short* d_allinds, float* d_mins, int* d_arrived, int* d_work,
-                         int sm_count, cudaStream_t s) {
+cudaError_t launch_bp_up(const BpTree& t, float* d_cost, short* d_allinds, float* d_pre, float* d_mins, int* d_arrived,
+                         int* d_work, int sm_count, cudaStream_t s) {
     if (t.n_leaves <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(d_arrived, 0, sizeof(int) * (size_t)t.sz, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d_work, 0, sizeof(int), s);
     if (e != cudaSuccess) return e;
     switch (t.len) {
-        case 1: return launch_up<1>(t, d_cost, d_allinds, d_mins, d_arrived, d_work, sm_count, s);
-        case 3: return launch_up<3>(t, d_cost, d_allinds, d_mins, d_arrived, d_work, sm_count, s);
-        case 5: return launch_up<5>(t, d_cost, d_allinds, d_mins, d_arrived, d_work, sm_count, s);
-        case 7: return launch_up<7>(t, d_cost, d_allinds, d_mins, d_arrived, d_work, sm_count, s);
-        case 9: return launch_up<9>(t, d_cost, d_allinds, d_mins, d_arrived, d_work, sm_count, s);
-        case 11: return launch_up<11>(t, d_cost, d_allinds, d_mins, d_arrived, d_work, sm_count, s);
-        case 13: return launch_up<13>(t, d_cost, d_allinds, d_mins, d_arrived, d_work, sm_count, s);
-        case 15: return launch_up<15>(t, d_cost, d_allinds, d_mins, d_arrived, d_work, sm_count, s);
-        case 17: return launch_up<17>(t, d_cost, d_allinds, d_mins, d_arrived, d_work, sm_count, s);
-        case 19: return launch_up<19>(t, d_cost, d_allinds, d_mins, d_arrived, d_work, sm_count, s);
-        case 21: return launch_up<21>(t, d_cost, d_allinds, d_mins, d_arrived, d_work, sm_count, s);
+        case 1: return launch_up<1>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
+        case 3: return launch_up<3>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
+        case 5: return launch_up<5>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
+        case 7: return launch_up<7>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
+        case 9: return launch_up<9>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
+        case 11: return launch_up<11>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
+        case 13: return launch_up<13>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
+        case 15: return launch_up<15>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
+        case 17: return launch_up<17>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
+        case 19: return launch_up<19>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
+        case 21: return launch_up<21>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
         default: return cudaErrorInvalidValue;
     }
 }

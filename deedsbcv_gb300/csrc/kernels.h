@@ -56,9 +56,10 @@ cudaError_t launch_data_cost_tma(const uint64_t* d_F, const uint64_t* d_M, uint6
                                  int g, int hw, int q, int ny_tile, float alpha1, float* d_cost, int* d_err,
                                  cudaStream_t s);
 cudaError_t launch_edge_sad(const float* d_im, int m, int n, int o, int g, float* d_sad, cudaStream_t s);
-// d_mins: 4 * t.sz floats (per-node message minima, then the x | y | z edge offsets)
-cudaError_t launch_bp_up(const BpTree& t, float* d_cost, short* d_allinds, float* d_mins, int* d_arrived, int* d_work,
-                         int sm_count, cudaStream_t s);
+// d_mins: 4 * t.sz floats (per-node message minima, then the x | y | z edge offsets);
+// d_pre: t.sz * len^3 floats (each node's scaled row, the transform's input)
+cudaError_t launch_bp_up(const BpTree& t, float* d_cost, short* d_allinds, float* d_pre, float* d_mins, int* d_arrived,
+                         int* d_work, int sm_count, cudaStream_t s);
 // d_labels: t.sz ints of scratch (each node's selected label)
 cudaError_t launch_bp_down(const BpTree& t, const float* d_cost, short* d_allinds, float* d_u1, float* d_v1,
                            float* d_w1, int* d_labels, int* d_err, cudaStream_t s);

@@ -408,12 +408,13 @@ deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTre
     float* d_mins = dbuf<float>(ctx, "mins_" + tag, 4 * (size_t)pt.sz, &st);  // mins | edge offsets x, y, z
     int* d_arrived = dbuf<int>(ctx, "arrived_" + tag, pt.sz, &st);
     int* d_work = dbuf<int>(ctx, "work_" + tag, 1, &st);
+    float* d_pre = dbuf<float>(ctx, "pre_" + tag, (size_t)pt.sz * len * len * len, &st);
     if (st) return st;
     CK(cudaMemcpyAsync(d_blk, h_blk, pt.total * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
     const BpTree bt = device_tree(pt, d_blk, h_blk, len, (float)q, u0, v0, w0);
     {
         StageScope sc(ctx, DEEDS_STAGE_BP_UP, s);
-        CK(launch_bp_up(bt, d_cost, d_allinds, d_mins, d_arrived, d_work, ctx->sm_count, s));
+        CK(launch_bp_up(bt, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, ctx->sm_count, s));
     }
     {
         StageScope sc(ctx, DEEDS_STAGE_BP_DOWN, s);
@@ -489,6 +490,7 @@ deeds_status acquire_buffers(deeds_ctx* ctx, int m, int n, int o, const deeds_pa
         dbuf<float>(ctx, "mins_" + tg, 4 * B.max_sz1, &st);
         dbuf<int>(ctx, "arrived_" + tg, B.max_sz1, &st);
         dbuf<int>(ctx, "work_" + tg, 1, &st);
+        dbuf<float>(ctx, "pre_" + tg, B.max_cost, &st);  // scaled rows of the upward sweep (argmin input)
     }
     B.grid = dbuf<float>(ctx, "grid", 18 * B.max_sz1, &st);
     B.ku = dbuf<float>(ctx, "keep_u", sz, &st);
@@ -684,6 +686,7 @@ deeds_status deeds_tree_bp_dev(deeds_ctx* ctx, float* d_cost, const float* d_u0,
     int herr = 0;
     CK(cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    if (herr == 4) return fail(ctx, DEEDS_ERR_TIMEOUT, "belief propagation: a bounded wait for a parent's label expired");
     if (herr) return fail(ctx, DEEDS_ERR_INTERNAL, "belief propagation produced an out-of-range argmin index");
     return DEEDS_OK;
 }
@@ -1011,6 +1014,8 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
     tl.dump();
     if (ctx->prof) collect_marks(ctx);
     if (herr[0] == 3 || herr[1] == 3) return fail(ctx, DEEDS_ERR_TIMEOUT, "cost volume: a bounded wait for a TMA copy expired");
+    if (herr[0] == 4 || herr[1] == 4)
+        return fail(ctx, DEEDS_ERR_TIMEOUT, "belief propagation: a bounded wait for a parent's label expired");
     if (herr[0] || herr[1])
         return fail(ctx, DEEDS_ERR_INTERNAL, "belief propagation produced an out-of-range argmin index");
     ctx->have_field = true;
