@@ -20,7 +20,7 @@ ERR_NAMES = {1: "DEEDS_ERR_INVALID", 2: "DEEDS_ERR_CUDA", 3: "DEEDS_ERR_NOMEM", 
 EXPORTS = [
     "deeds_default_params", "deeds_create", "deeds_destroy", "deeds_last_error", "deeds_version",
     "deeds_register", "deeds_register_dev", "deeds_warp_segmentation", "deeds_apply_flow",
-    "deeds_mind_ssc_dev", "deeds_data_cost_dev", "deeds_mst_edges_dev", "deeds_image_stats",
+    "deeds_mind_ssc_dev", "deeds_data_cost_dev", "deeds_mst_edges_dev", "deeds_image_stats", "deeds_image_stats_dev", "deeds_mst_path_counts",
     "deeds_prims_from_sad", "deeds_tree_bp_dev", "deeds_upsample_dev", "deeds_warp_affine_dev",
     "deeds_warp_image_dev", "deeds_warp_seg_dev", "deeds_consistent_dev", "deeds_jacobian_dev",
     "deeds_set_profiling", "deeds_stage_times", "deeds_reset_stage_times", "deeds_kernel_launches",
@@ -32,10 +32,11 @@ EXPORTS = [
     "deeds_soft_release_batch",
     "deeds_linear_default_params", "deeds_linear_register", "deeds_linear_register_dev", "deeds_lin_warp_dev",
     "deeds_lin_smooth_dev", "deeds_estimate_affine_dev", "deeds_affine_robust", "deeds_affine_warp_segmentation",
+    "deeds_fuse_labels_dev", "deeds_multi_atlas",
     "deeds_gz_write", "deeds_gz_read", "deeds_gz_last_error", "deeds_selftest_bounded_waits",
 ]
 NOALLOC_MAX_NODES = 131072
-STAGES = ["mind", "datacost", "mst_edges", "bp_up", "bp_down", "transform", "consistent", "tree_wait"]
+STAGES = ["mind", "datacost", "mst_edges", "bp_up", "bp_down", "transform", "consistent", "tree_wait", "bp_argmin"]
 
 
 class DeedsParams(C.Structure):
@@ -121,6 +122,11 @@ def load():
     L.deeds_data_cost_dev.argtypes = [P, P, P, I, I, I, I, I, I, F, P, P]
     L.deeds_mst_edges_dev.argtypes = [P, P, I, I, I, I, P, P]
     L.deeds_image_stats.argtypes = [P, S, P, P]
+    L.deeds_image_stats_dev.argtypes = [P, P, S, P, P]
+    L.deeds_mst_path_counts.argtypes = [P]
+    L.deeds_fuse_labels_dev.argtypes = [P, P, P, P, I, I, I, I, I, F, I, P, P]
+    L.deeds_multi_atlas.argtypes = [P, P, P, P, I, I, I, I, C.POINTER(DeedsParams), I, I, F, I, P, P, P]
+    L.deeds_mst_path_counts.restype = None
     L.deeds_prims_from_sad.argtypes = [P, F, I, I, I, I, P, P, P]
     L.deeds_tree_bp_dev.argtypes = [P, P, P, P, P, I, I, I, I, I, P, P, P, P, P, P, P, P]
     L.deeds_upsample_dev.argtypes = [P, P, P, I, I, I, P, P, P, I, I, I, P]

@@ -169,6 +169,66 @@ def image_stats(im_host):
     return float(mean[0]), float(sd[0])
 
 
+def fuse_labels_device(target, images, labels, m, n, o, radius=2, eps=1.0, power=2, ctx=None):
+    """Multi-atlas label fusion of atlases already warped onto ``target``
+    (flat m*n*o float32 CUDA tensors, i fastest; ``labels`` int16 CUDA tensors): per voxel the label with
+    the largest sum of weights (1 / (patch SSD + eps))^power, the patch being the
+    (2 radius + 1)^3 window (clamp-to-edge); power 0 is majority voting.
+    Returns the fused labels (int16 CUDA tensor)."""
+    ctx = ctx or context(target.device.index or 0)
+    n_atlas = len(images)
+    if n_atlas != len(labels):
+        raise ValueError("images and labels differ in count")
+    sz = m * n * o
+    ims = (C.c_void_p * n_atlas)(*[_dev(a, torch.float32, sz, "image").value for a in images])
+    labs = (C.c_void_p * n_atlas)(*[_dev(a, torch.int16, sz, "labels").value for a in labels])
+    out = torch.empty(sz, dtype=torch.int16, device=target.device)
+    ctx.check(ctx._L.deeds_fuse_labels_dev(ctx.handle, _dev(target, torch.float32, sz, "target"), ims, labs, n_atlas,
+                                            m, n, o, int(radius), C.c_float(eps), int(power),
+                                            C.c_void_p(out.data_ptr()), _stream()))
+    return out
+
+
+def multi_atlas(target, atlas_images, atlas_labels, params=None, lanes=3, radius=2, eps=1.0, power=2, ctx=None):
+    """Multi-atlas segmentation of ``target`` (numpy (m, n, o) volumes): every
+    atlas image is registered to the target with deeds (batched), its labels are
+    warped with the resulting field, and the warped labels are fused on the GPU
+    (see fuse_labels_device).  Returns (fused labels, warped atlas labels, warped
+    atlas images) as Fortran-ordered numpy arrays (int16, int16 (n, m, n, o),
+    float32 (n, m, n, o))."""
+    ctx = ctx or context(0)
+    params = params or default_params()
+    tgt = np.asfortranarray(np.asarray(target, np.float32))
+    m, n, o = tgt.shape
+    sz = m * n * o
+    n_atlas = len(atlas_images)
+    ims = [np.ascontiguousarray(np.asarray(a, np.float32).ravel(order="F")) for a in atlas_images]
+    labs = [np.ascontiguousarray(np.asarray(a).astype(np.int16).ravel(order="F")) for a in atlas_labels]
+    t_flat = np.ascontiguousarray(tgt.ravel(order="F"))
+    fused = np.zeros(sz, np.int16)
+    wl = np.zeros(n_atlas * sz, np.int16)
+    wi = np.zeros(n_atlas * sz, np.float32)
+    p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    ims_p = (C.c_void_p * n_atlas)(*[a.ctypes.data for a in ims])
+    labs_p = (C.c_void_p * n_atlas)(*[a.ctypes.data for a in labs])
+    ctx.check(ctx._L.deeds_multi_atlas(ctx.handle, p(t_flat), ims_p, labs_p, n_atlas, m, n, o, C.byref(params),
+                                        int(lanes), int(radius), C.c_float(eps), int(power), p(fused), p(wl), p(wi)))
+    shp = lambda a: a.reshape((m, n, o), order="F")  # noqa: E731
+    return (shp(fused), [shp(wl[k * sz:(k + 1) * sz]) for k in range(n_atlas)],
+            [shp(wi[k * sz:(k + 1) * sz]) for k in range(n_atlas)])
+
+
+def image_stats_device(im, ctx=None):
+    """The reference's mean and standard deviation of a float32 CUDA tensor,
+    computed on the device (bit-identical to ``image_stats``)."""
+    ctx = ctx or context(im.device.index or 0)
+    out = torch.empty(2, dtype=torch.float32, device=im.device)
+    ctx.check(ctx._L.deeds_image_stats_dev(ctx.handle, _dev(im, torch.float32, im.numel(), "im"), im.numel(),
+                                            C.c_void_p(out.data_ptr()), _stream()))
+    mean, sd = out.cpu().tolist()
+    return mean, sd
+
+
 def primsGraph(im, m, n, o, g, ctx=None):
     """MST of the control grid: (ordered, parents, edgemst) as numpy arrays.
 

@@ -30,7 +30,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompil
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread", "-Wall", "-Wno-unused-function",
              f"-I{CUDA_HOME}/include"]
 
-CU_SOURCES = ["mind.cu", "datacost.cu", "mst.cu", "bp.cu", "transform.cu", "noalloc.cu", "soft.cu", "soft_warp.cu",
+CU_SOURCES = ["mind.cu", "datacost.cu", "mst.cu", "stats.cu", "fusion.cu", "bp.cu", "transform.cu", "noalloc.cu", "soft.cu", "soft_warp.cu",
               "linear.cu"]
 # soft.cu has no bit-exactness contract (its reference is a float64 definition),
 # so it may contract multiply-adds and flush denormals (its operands never are:

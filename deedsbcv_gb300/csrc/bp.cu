@@ -565,11 +565,32 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_argmin(BpTree t, const f
     float* B = A + LEN3;
     short* ia = reinterpret_cast<short*>(B + LEN3);
     short* ib = ia + LEN3;
-    for (int node = blockIdx.x; node < t.sz; node += gridDim.x) {
-        if (node == t.root) continue;
-        const float* prow = pre + (int64_t)node * LEN3;
-        for (int l = threadIdx.x; l < LEN3; l += T) A[l] = ld_cg(prow + l);
+    constexpr int NL = (LEN3 + T - 1) / T;
+    // The next node's row is loaded into registers while this node's passes run,
+    // so the loop waits for global memory only once.
+    float nxt[NL];
+    auto fetch = [&](int v) {
+        const float* prow = pre + (int64_t)v * LEN3;
+#pragma unroll
+        for (int k = 0; k < NL; k++) {
+            const int l = threadIdx.x + k * T;
+            nxt[k] = 0.0f;
+            if (v < t.sz && l < LEN3) nxt[k] = ld_ahead_cg(prow + l);
+        }
+    };
+    int node = blockIdx.x;
+    if (node == t.root) node += gridDim.x;
+    fetch(node);
+    for (; node < t.sz;) {
+#pragma unroll
+        for (int k = 0; k < NL; k++) {
+            const int l = threadIdx.x + k * T;
+            if (l < LEN3) A[l] = nxt[k];
+        }
         const float ox = off[node], oy = off[t.sz + node], oz = off[2 * t.sz + node];
+        int next = node + gridDim.x;
+        if (next == t.root) next += gridDim.x;
+        fetch(next);
         __syncthreads();
         dt_lines<LEN, 0>(A, B, nullptr, ia, oy);
         __syncthreads();
@@ -580,6 +601,7 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_argmin(BpTree t, const f
         short* arow = allinds + (int64_t)node * LEN3;
         for (int l = threadIdx.x; l < LEN3; l += T) arow[l] = ia[l];
         __syncthreads();  // A / ia are rewritten by the next node
+        node = next;
     }
 }
 
@@ -600,6 +622,17 @@ cudaError_t launch_up(const BpTree& t, float* cost, short* allinds, float* pre, 
     float* off = mins + t.sz;
     k_bp_offsets<<<(t.sz + 255) / 256, 256, 0, s>>>(t, off);
     k_bp_up<LEN><<<ctas, T, smem, s>>>(t, cost, pre, mins, off, arrived, work);
+    count_launches(2);
+    return cudaGetLastError();
+}
+
+template <int LEN>
+cudaError_t launch_argmin(const BpTree& t, short* allinds, const float* pre, const float* mins, int sm_count,
+                          cudaStream_t s) {
+    constexpr int LEN3 = LEN * LEN * LEN;
+    constexpr int T = bp_threads(LEN);
+    const float* off = mins + t.sz;
+    cudaError_t e;
     const size_t smem_a = (size_t)LEN3 * (2 * sizeof(float) + 2 * sizeof(short));
     e = cudaFuncSetAttribute(k_bp_argmin<LEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_a);
     if (e != cudaSuccess) return e;
@@ -610,7 +643,7 @@ cudaError_t launch_up(const BpTree& t, float* cost, short* allinds, float* pre, 
     int ctas_a = per_sm_a * sm_count;
     if (ctas_a > t.sz) ctas_a = t.sz;
     k_bp_argmin<LEN><<<ctas_a, T, smem_a, s>>>(t, pre, off, allinds);
-    count_launches(3);
+    count_launches(1);
     return cudaGetLastError();
 }
 
@@ -634,6 +667,25 @@ cudaError_t launch_bp_up(const BpTree& t, float* d_cost, short* d_allinds, float
         case 17: return launch_up<17>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
         case 19: return launch_up<19>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
         case 21: return launch_up<21>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_bp_argmin(const BpTree& t, short* d_allinds, const float* d_pre, const float* d_mins, int sm_count,
+                             cudaStream_t s) {
+    if (t.n_leaves <= 0) return cudaSuccess;
+    switch (t.len) {
+        case 1: return launch_argmin<1>(t, d_allinds, d_pre, d_mins, sm_count, s);
+        case 3: return launch_argmin<3>(t, d_allinds, d_pre, d_mins, sm_count, s);
+        case 5: return launch_argmin<5>(t, d_allinds, d_pre, d_mins, sm_count, s);
+        case 7: return launch_argmin<7>(t, d_allinds, d_pre, d_mins, sm_count, s);
+        case 9: return launch_argmin<9>(t, d_allinds, d_pre, d_mins, sm_count, s);
+        case 11: return launch_argmin<11>(t, d_allinds, d_pre, d_mins, sm_count, s);
+        case 13: return launch_argmin<13>(t, d_allinds, d_pre, d_mins, sm_count, s);
+        case 15: return launch_argmin<15>(t, d_allinds, d_pre, d_mins, sm_count, s);
+        case 17: return launch_argmin<17>(t, d_allinds, d_pre, d_mins, sm_count, s);
+        case 19: return launch_argmin<19>(t, d_allinds, d_pre, d_mins, sm_count, s);
+        case 21: return launch_argmin<21>(t, d_allinds, d_pre, d_mins, sm_count, s);
         default: return cudaErrorInvalidValue;
     }
 }

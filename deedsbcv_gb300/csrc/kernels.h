@@ -56,10 +56,18 @@ cudaError_t launch_data_cost_tma(const uint64_t* d_F, const uint64_t* d_M, uint6
                                  int g, int hw, int q, int ny_tile, float alpha1, float* d_cost, int* d_err,
                                  cudaStream_t s);
 cudaError_t launch_edge_sad(const float* d_im, int m, int n, int o, int g, float* d_sad, cudaStream_t s);
+// Mean and standard deviation of one or two images in the reference's sequential
+// float semantics (stats.cu): out[2*img + 0 / 1]; im1 unused when nimg is 1.
+size_t image_stats_scratch_bytes(size_t sz, int nimg);
+cudaError_t launch_image_stats(const float* im0, const float* im1, int nimg, size_t sz, void* scratch, float* out,
+                               cudaStream_t s);
 // d_mins: 4 * t.sz floats (per-node message minima, then the x | y | z edge offsets);
 // d_pre: t.sz * len^3 floats (each node's scaled row, the transform's input)
 cudaError_t launch_bp_up(const BpTree& t, float* d_cost, short* d_allinds, float* d_pre, float* d_mins, int* d_arrived,
                          int* d_work, int sm_count, cudaStream_t s);
+// the argmin tables (allinds) of every node from the sweep's stored rows (after launch_bp_up)
+cudaError_t launch_bp_argmin(const BpTree& t, short* d_allinds, const float* d_pre, const float* d_mins, int sm_count,
+                             cudaStream_t s);
 // d_labels: t.sz ints of scratch (each node's selected label)
 cudaError_t launch_bp_down(const BpTree& t, const float* d_cost, short* d_allinds, float* d_u1, float* d_v1,
                            float* d_w1, int* d_labels, int* d_err, cudaStream_t s);
@@ -121,6 +129,15 @@ cudaError_t launch_lin_smooth(float* d_c0, float* d_c1, int m1, int n1, int o1, 
 cudaError_t launch_lin_node_stats(const float* d_c0, const float* d_c1, const float* d_fixed, const float* d_moving,
                                   int m, int n, int o, int g, int len3, float* d_minval, int* d_minind,
                                   cudaStream_t s);
+// Multi-atlas label fusion (fusion.cu): atlases warped onto the target vote per voxel.
+constexpr int kFuseMaxAtlases = 64;
+struct FusionAtlases {
+    const float* image[kFuseMaxAtlases];     // warped atlas images (m*n*o)
+    const int16_t* labels[kFuseMaxAtlases];  // warped atlas labels (m*n*o)
+};
+size_t fuse_scratch_floats(int n_atlas, int m, int n, int o);
+cudaError_t launch_fuse_labels(const float* d_target, const FusionAtlases& at, int n_atlas, int m, int n, int o,
+                               int radius, float eps, int power, float* d_scratch, int16_t* d_out, cudaStream_t s);
 // Self-tests of the bounded device-side waits (a flag / an mbarrier nothing releases).
 cudaError_t launch_selftest_flag_wait(const int* flag, int* err, int* status, cudaStream_t s);
 cudaError_t launch_selftest_mbar_wait(int* status, cudaStream_t s);

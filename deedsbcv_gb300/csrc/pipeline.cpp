@@ -417,6 +417,10 @@ deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTre
         CK(launch_bp_up(bt, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, ctx->sm_count, s));
     }
     {
+        StageScope sc(ctx, DEEDS_STAGE_BP_ARGMIN, s);
+        CK(launch_bp_argmin(bt, d_allinds, d_pre, d_mins, ctx->sm_count, s));
+    }
+    {
         StageScope sc(ctx, DEEDS_STAGE_BP_DOWN, s);
         // the upward pass is done with its arrival counters: they hold the labels now
         CK(launch_bp_down(bt, d_cost, d_allinds, u1, v1, w1, d_arrived, d_err, s));
@@ -442,7 +446,9 @@ struct PairBuffers {
     float* cost[2];
     short* allinds[2];
     uint64_t* mpad[2];
-    float *grid, *ku, *kv, *kw, *cons_scr, *h_fix, *h_w0;
+    float *grid, *ku, *kv, *kw, *cons_scr;
+    void* stats_scr;  // image statistics (deeds::launch_image_stats)
+    float *d_stats, *h_stats;  // mean, std of the fixed and of the affine-warped moving image
     std::vector<float*> h_sad, d_sad;
     std::vector<PackedTree> pts;
     std::vector<uint32_t*> h_tree;
@@ -497,8 +503,9 @@ deeds_status acquire_buffers(deeds_ctx* ctx, int m, int n, int o, const deeds_pa
     B.kv = dbuf<float>(ctx, "keep_v", sz, &st);
     B.kw = dbuf<float>(ctx, "keep_w", sz, &st);
     B.cons_scr = dbuf<float>(ctx, "consistent", 12 * B.max_sz1, &st);
-    B.h_fix = hbuf<float>(ctx, "h_fix", sz, &st);
-    B.h_w0 = hbuf<float>(ctx, "h_w0", sz, &st);
+    B.stats_scr = dbuf<char>(ctx, "stats_scr", image_stats_scratch_bytes(sz, 2), &st);
+    B.d_stats = dbuf<float>(ctx, "stats", 4, &st);
+    B.h_stats = hbuf<float>(ctx, "h_stats", 4, &st);
     B.h_sad.assign(2 * L, nullptr); B.d_sad.assign(2 * L, nullptr);
     B.pts.assign(2 * L, PackedTree()); B.h_tree.assign(2 * L, nullptr);
     for (int l = 0; l < L; l++) {
@@ -559,7 +566,14 @@ deeds_status deeds_create(deeds_ctx** out, int device) {
     CK(cudaSetDevice(device));
     CK(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device));
     CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-    CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    {
+        // the MST inputs (image statistics, block SADs) start the host trees, which
+        // the level loop waits for: their small kernels go ahead of the throughput
+        // kernels of the other streams
+        int least = 0, greatest = 0;
+        CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        CK(cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, greatest));
+    }
     CK(cudaEventCreateWithFlags(&c->ev_a, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c->ev_b, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c->ev_c, cudaEventDisableTiming));
@@ -654,6 +668,21 @@ deeds_status deeds_mst_edges_dev(deeds_ctx* ctx, const float* d_im, int m, int n
     return DEEDS_OK;
 }
 
+void deeds_mst_path_counts(long long out[4]) {
+    if (out) mst_path_counts(out);
+}
+
+deeds_status deeds_image_stats_dev(deeds_ctx* ctx, const float* d_im, size_t count, float* d_out, void* stream) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!d_im || !d_out || count == 0) return fail(ctx, DEEDS_ERR_INVALID, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    deeds_status st = DEEDS_OK;
+    void* scr = dbuf<char>(ctx, "stats_scr_api", image_stats_scratch_bytes(count, 1), &st);
+    if (st) return st;
+    CK(launch_image_stats(d_im, nullptr, 1, count, scr, d_out, (cudaStream_t)stream));
+    return DEEDS_OK;
+}
+
 deeds_status deeds_tree_bp_dev(deeds_ctx* ctx, float* d_cost, const float* d_u0, const float* d_v0, const float* d_w0,
                                int m1, int n1, int o1, int hw, int q, const int* ordered, const int* parents,
                                const float* edgemst, float* d_u1, float* d_v1, float* d_w1, int16_t* d_allinds,
@@ -686,6 +715,7 @@ deeds_status deeds_tree_bp_dev(deeds_ctx* ctx, float* d_cost, const float* d_u0,
     int herr = 0;
     CK(cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    if (ctx->prof) collect_marks(ctx);
     if (herr == 4) return fail(ctx, DEEDS_ERR_TIMEOUT, "belief propagation: a bounded wait for a parent's label expired");
     if (herr) return fail(ctx, DEEDS_ERR_INTERNAL, "belief propagation produced an out-of-range argmin index");
     return DEEDS_OK;
@@ -808,8 +838,7 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
     float* kv = B.kv;
     float* kw = B.kw;
     float* cons_scr = B.cons_scr;
-    float* h_fix = B.h_fix;
-    float* h_w0 = B.h_w0;
+    float* h_stats = B.h_stats;
     std::vector<float*>& h_sad = B.h_sad;
     std::vector<float*>& d_sad = B.d_sad;
     std::vector<PackedTree>& pts = B.pts;
@@ -834,12 +863,16 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
         CK(launch_warp_affine(mov, X, zero, m, n, o, warp0, nullptr, nullptr, nullptr, s));
     }
 
-    // ---- MST inputs on the side stream: both images to the host first (for the
-    // statistics), then every level's block SADs; host trees on worker threads
+    // ---- MST inputs on the side stream: the image statistics of both images
+    // (exact, on the device) to the host first, then every level's block SADs;
+    // host trees on worker threads
     CK(cudaEventRecord(ctx->ev_a, s));
     CK(cudaStreamWaitEvent(ctx->side, ctx->ev_a, 0));
-    CK(cudaMemcpyAsync(h_fix, fix, sz * sizeof(float), cudaMemcpyDeviceToHost, ctx->side));
-    CK(cudaMemcpyAsync(h_w0, warp0, sz * sizeof(float), cudaMemcpyDeviceToHost, ctx->side));
+    {
+        StageScope sc(ctx, DEEDS_STAGE_MST, ctx->side);
+        CK(launch_image_stats(fix, warp0, 2, sz, B.stats_scr, B.d_stats, ctx->side));
+    }
+    CK(cudaMemcpyAsync(h_stats, B.d_stats, 4 * sizeof(float), cudaMemcpyDeviceToHost, ctx->side));
     CK(cudaEventRecord(ctx->ev_b, ctx->side));
     for (int l = L - 1; l >= 0; l--) {  // finest first: those trees take longest on the host
         const size_t sz1 = (size_t)m1s[l] * n1s[l] * o1s[l];
@@ -856,17 +889,13 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
     std::vector<std::promise<void>> ready(2 * L);
     std::vector<std::shared_future<void>> ready_f(2 * L);
     for (int t = 0; t < 2 * L; t++) ready_f[t] = ready[t].get_future().share();
-    cudaEvent_t ev_images = ctx->ev_b, ev_sads = ctx->ev_c;
+    cudaEvent_t ev_stats = ctx->ev_b, ev_sads = ctx->ev_c;
     const int dev = ctx->device;
-    std::thread builder([&, ev_images, ev_sads, dev]() {
+    std::thread builder([&, ev_stats, ev_sads, dev]() {
         cudaSetDevice(dev);
-        cudaEventSynchronize(ev_images);
-        tl.mark("images on host");
-        float mean_f, sd_f, mean_w, sd_w;
-        std::thread tw([&]() { image_stats(h_w0, sz, &mean_w, &sd_w); });
-        image_stats(h_fix, sz, &mean_f, &sd_f);
-        tw.join();
-        tl.mark("image statistics");
+        cudaEventSynchronize(ev_stats);
+        const float sd_f = h_stats[1], sd_w = h_stats[3];
+        tl.mark("image statistics on host");
         cudaEventSynchronize(ev_sads);
         tl.mark("block SADs on host");
         // finest trees are the slowest: start the workers in reverse level order
@@ -1166,6 +1195,98 @@ deeds_status deeds_apply_flow(deeds_ctx* ctx, const float* flow, size_t flow_len
         CK(launch_warp_affine(static_cast<float*>(d_in), X, f, m, n, o, static_cast<float*>(d_out), nullptr, nullptr,
                               nullptr, s));
     CK(cudaMemcpyAsync(out, d_out, sz * esz, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return DEEDS_OK;
+}
+
+deeds_status deeds_fuse_labels_dev(deeds_ctx* ctx, const float* d_target, const float* const* d_images,
+                                   const int16_t* const* d_labels, int n_atlas, int m, int n, int o, int radius,
+                                   float eps, int power, int16_t* d_out, void* stream) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!d_target || !d_images || !d_labels || !d_out || m < 1 || n < 1 || o < 1)
+        return fail(ctx, DEEDS_ERR_INVALID, "bad arguments");
+    if (n_atlas < 1 || n_atlas > DEEDS_FUSE_MAX_ATLASES)
+        return fail(ctx, DEEDS_ERR_INVALID, "%d atlases (1..%d)", n_atlas, DEEDS_FUSE_MAX_ATLASES);
+    if (radius < 0 || power < 0 || !(eps > 0.0f)) return fail(ctx, DEEDS_ERR_INVALID, "radius/power/eps");
+    FusionAtlases at{};
+    for (int a = 0; a < n_atlas; a++) {
+        if (!d_images[a] || !d_labels[a]) return fail(ctx, DEEDS_ERR_INVALID, "atlas %d: null pointer", a);
+        at.image[a] = d_images[a];
+        at.labels[a] = d_labels[a];
+    }
+    CK(cudaSetDevice(ctx->device));
+    deeds_status st = DEEDS_OK;
+    float* scr = dbuf<float>(ctx, "fuse_scratch", fuse_scratch_floats(n_atlas, m, n, o), &st);
+    if (st) return st;
+    CK(launch_fuse_labels(d_target, at, n_atlas, m, n, o, radius, eps, power, scr, d_out, (cudaStream_t)stream));
+    return DEEDS_OK;
+}
+
+deeds_status deeds_multi_atlas(deeds_ctx* ctx, const float* target, const float* const* atlas_images,
+                               const int16_t* const* atlas_labels, int n_atlas, int m, int n, int o,
+                               const deeds_params* params, int lanes, int radius, float eps, int power,
+                               int16_t* labels_out, int16_t* warped_labels_out, float* warped_images_out) {
+    if (!ctx) return fail(nullptr, DEEDS_ERR_INVALID, "ctx is NULL");
+    if (!target || !atlas_images || !atlas_labels || !labels_out || m < 1 || n < 1 || o < 1)
+        return fail(ctx, DEEDS_ERR_INVALID, "bad arguments");
+    if (n_atlas < 1 || n_atlas > DEEDS_FUSE_MAX_ATLASES)
+        return fail(ctx, DEEDS_ERR_INVALID, "%d atlases (1..%d)", n_atlas, DEEDS_FUSE_MAX_ATLASES);
+    deeds_params P;
+    if (params) P = *params;
+    else deeds_default_params(&P);
+    if (P.levels < 1 || P.levels > 10) return fail(ctx, DEEDS_ERR_INVALID, "levels %d", P.levels);
+    const size_t sz = (size_t)m * n * o;
+    const int g = P.grid[P.levels - 1];
+    if (g < 1 || m / g < 1 || n / g < 1 || o / g < 1) return fail(ctx, DEEDS_ERR_INVALID, "grid step %d", g);
+    const size_t sz1 = (size_t)(m / g) * (n / g) * (o / g);
+    // 1. every atlas registered to the target
+    std::vector<float> flows(n_atlas * 3 * sz1), own_images;
+    float* warped = warped_images_out;
+    if (!warped) {
+        own_images.resize((size_t)n_atlas * sz);
+        warped = own_images.data();
+    }
+    std::vector<deeds_pair> pairs(n_atlas);
+    for (int a = 0; a < n_atlas; a++) {
+        if (!atlas_images[a] || !atlas_labels[a]) return fail(ctx, DEEDS_ERR_INVALID, "atlas %d: null pointer", a);
+        pairs[a] = deeds_pair{target, atlas_images[a], m, n, o, nullptr, flows.data() + a * 3 * sz1, warped + a * sz};
+    }
+    deeds_status st = deeds_register_batch(ctx, pairs.data(), n_atlas, &P, lanes);
+    if (st) return st;
+    // 2. each atlas' labels warped with its flow
+    std::vector<int16_t> own;
+    int16_t* wl = warped_labels_out;
+    if (!wl) {
+        own.resize((size_t)n_atlas * sz);
+        wl = own.data();
+    }
+    float ident[16] = {0};
+    ident[0] = ident[5] = ident[10] = ident[15] = 1.0f;
+    for (int a = 0; a < n_atlas; a++) {
+        st = deeds_apply_flow(ctx, flows.data() + a * 3 * sz1, 3 * sz1, g, ident, atlas_labels[a], 0, m, n, o,
+                              wl + a * sz);
+        if (st) return st;
+    }
+    // 3. the vote on the device
+    CK(cudaSetDevice(ctx->device));
+    float* d_t = dbuf<float>(ctx, "fuse_target", sz, &st);
+    float* d_im = dbuf<float>(ctx, "fuse_images", (size_t)n_atlas * sz, &st);
+    int16_t* d_lab = dbuf<int16_t>(ctx, "fuse_labels", (size_t)n_atlas * sz, &st);
+    int16_t* d_out = dbuf<int16_t>(ctx, "fuse_out", sz, &st);
+    if (st) return st;
+    cudaStream_t s = ctx->stream;
+    CK(cudaMemcpyAsync(d_t, target, sz * sizeof(float), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_im, warped, (size_t)n_atlas * sz * sizeof(float), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(d_lab, wl, (size_t)n_atlas * sz * sizeof(int16_t), cudaMemcpyHostToDevice, s));
+    std::vector<const float*> ims(n_atlas);
+    std::vector<const int16_t*> labs(n_atlas);
+    for (int a = 0; a < n_atlas; a++) {
+        ims[a] = d_im + a * sz;
+        labs[a] = d_lab + a * sz;
+    }
+    st = deeds_fuse_labels_dev(ctx, d_t, ims.data(), labs.data(), n_atlas, m, n, o, radius, eps, power, d_out, s);
+    if (st) return st;
+    CK(cudaMemcpyAsync(labels_out, d_out, sz * sizeof(int16_t), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     return DEEDS_OK;
 }

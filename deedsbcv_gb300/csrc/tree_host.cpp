@@ -10,6 +10,7 @@
 // statistics are sequential float sums as in the reference.  Compiled with
 // -ffp-contract=off.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -385,44 +386,284 @@ class EdgeHeap {
 };
 }  // namespace
 
+namespace {
+
+// Undirected grid edges are numbered 3 v + axis: axis 0 joins v and v + m1 (+x),
+// 1 joins v and v + 1 (+y), 2 joins v and v + m1 n1 (+z).  `w` holds the
+// reference's weight of each directed edge, vertex-major (w[v*6 + nb]); both
+// directions of an edge carry the same weight (one block SAD).
+inline float edge_weight(const float* w, int id) {
+    static const int plus_dir[3] = {1, 3, 5};
+    return w[(size_t)(id / 3) * 6 + plus_dir[id % 3]];
+}
+
+// Monotone map of a float to an unsigned key (ascending floats, ascending keys).
+inline uint32_t float_key(float f) {
+    uint32_t b;
+    std::memcpy(&b, &f, 4);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+inline float key_float(uint32_t k) {
+    const uint32_t b = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    float f;
+    std::memcpy(&f, &b, 4);
+    return f;
+}
+
+// Kruskal's view of the minimum spanning trees of the grid.  Edges are taken in
+// weight order, all edges of one weight w as a group.  The components of the
+// edges lighter than w are the same for every spanning tree of minimum weight,
+// and each such tree contains a spanning forest of the group's "useful" edges
+// (those joining two different components), with the same number r of edges.
+// When the useful edges form a forest themselves (k useful edges = r), every
+// minimum tree contains all of them; otherwise the group is ambiguous and the
+// trees differ only in the forest they pick from it, independently per group.
+// So Prim's tree (the reference's) = the forced edges + Prim's picks in the
+// ambiguous groups, and with no ambiguous group it is this tree outright.
+struct MstGroups {
+    std::vector<int> forced;       // tree edges of unambiguous groups
+    std::vector<int> amb_of_edge;  // [3 sz] ambiguous group of a useful edge, -1 otherwise
+    std::vector<int> amb_rank;     // per ambiguous group: edges every minimum tree takes from it
+};
+
+// False when a weight is NaN (the order is then the heap's own business).
+bool mst_groups(const float* w, int m1, int n1, int o1, MstGroups& G) {
+    const int sz = m1 * n1 * o1, mn1 = m1 * n1;
+    std::vector<uint64_t> a, b;
+    a.reserve((size_t)3 * sz);
+    for (int v = 0; v < sz; v++) {
+        const int k = v / mn1, rem = v - k * mn1, j = rem / m1, i = rem - j * m1;
+        const bool has[3] = {j + 1 < n1, i + 1 < m1, k + 1 < o1};
+        for (int ax = 0; ax < 3; ax++) {
+            if (!has[ax]) continue;
+            const float f = edge_weight(w, 3 * v + ax);
+            if (std::isnan(f)) return false;
+            a.push_back((uint64_t)float_key(f) << 32 | (uint32_t)(3 * v + ax));
+        }
+    }
+    // LSD radix sort on the 32-bit key (three passes of 11 bits)
+    b.resize(a.size());
+    for (int pass = 0; pass < 3; pass++) {
+        const int shift = 32 + 11 * pass;
+        std::vector<size_t> cnt(2049, 0);
+        for (uint64_t x : a) cnt[((x >> shift) & 2047u) + 1]++;
+        for (int d = 0; d < 2048; d++) cnt[d + 1] += cnt[d];
+        for (uint64_t x : a) b[cnt[(x >> shift) & 2047u]++] = x;
+        a.swap(b);
+    }
+    // union-find: union by size, path halving
+    std::vector<int> par(sz), size(sz, 1);
+    for (int v = 0; v < sz; v++) par[v] = v;
+    auto find = [&](int x) {
+        while (par[x] != x) {
+            par[x] = par[par[x]];
+            x = par[x];
+        }
+        return x;
+    };
+    auto unite = [&](int rp, int rq) {
+        if (size[rp] < size[rq]) std::swap(rp, rq);
+        par[rq] = rp;
+        size[rp] += size[rq];
+    };
+    auto ends = [&](int id, int& p, int& q) {
+        const int v = id / 3, ax = id % 3;
+        p = v;
+        q = v + (ax == 0 ? m1 : ax == 1 ? 1 : mn1);
+    };
+    G.forced.clear();
+    G.forced.reserve(sz);
+    G.amb_rank.clear();
+    G.amb_of_edge.assign((size_t)3 * sz, -1);
+    std::vector<int> useful;
+    size_t s = 0;
+    while (s < a.size()) {
+        const uint32_t key = (uint32_t)(a[s] >> 32);
+        const float f = key_float(key);
+        size_t e = s + 1;
+        while (e < a.size() && ((uint32_t)(a[e] >> 32) == key || key_float((uint32_t)(a[e] >> 32)) == f)) e++;
+        if (e == s + 1) {  // a weight of its own: never ambiguous
+            const int id = (int)(uint32_t)a[s];
+            int p, q;
+            ends(id, p, q);
+            const int rp = find(p), rq = find(q);
+            if (rp != rq) {
+                unite(rp, rq);
+                G.forced.push_back(id);
+            }
+            s = e;
+            continue;
+        }
+        useful.clear();
+        for (size_t t = s; t < e; t++) {
+            int p, q;
+            ends((int)(uint32_t)a[t], p, q);
+            if (find(p) != find(q)) useful.push_back((int)(uint32_t)a[t]);
+        }
+        const size_t first = G.forced.size();
+        for (int id : useful) {
+            int p, q;
+            ends(id, p, q);
+            const int rp = find(p), rq = find(q);
+            if (rp != rq) {
+                unite(rp, rq);
+                G.forced.push_back(id);
+            }
+        }
+        const int r = (int)(G.forced.size() - first);
+        if ((size_t)r != useful.size()) {  // a cycle among the useful edges: Prim decides
+            G.forced.resize(first);
+            const int gi = (int)G.amb_rank.size();
+            for (int id : useful) G.amb_of_edge[id] = gi;
+            G.amb_rank.push_back(r);
+        }
+        s = e;
+    }
+    return true;
+}
+
+std::atomic<long long> g_mst_counts[4];  // trees without ambiguity, trees with, Prim steps run, Prim steps of a full run
+
+}  // namespace
+
+void mst_path_counts(long long out[4]) {
+    for (int i = 0; i < 4; i++) out[i] = g_mst_counts[i].load();
+}
+
 void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int g, int* ordered, int* parents,
                     float* edgemst) {
     const int sz = m1 * n1 * o1;
     // -exp(-(sad/g^3) / (2 std)) in float, as edgecost2weight() (src/primsMST.h:48-50, :112-117);
     // stored vertex-major (w[v*6 + nb]): the six pushes of an added vertex read one line
-    std::vector<float> w((size_t)sz * 6);
+    // (the two directions of an edge normally have one SAD, computed once from the
+    // image, so one weight: it is evaluated once and mirrored; SADs given per
+    // direction that differ keep their own weights)
+    std::vector<float> w((size_t)sz * 6, -1.0f);
     const float g3 = (float)std::pow((double)g, 3.0);
     const float twostd = 2.0f * stddev;
-    for (int nb = 0; nb < 6; nb++)
-        for (size_t v = 0; v < (size_t)sz; v++) w[v * 6 + nb] = -std::exp(-(sad[(size_t)nb * sz + v] / g3) / twostd);
     const int mn1 = m1 * n1;
     // neighbour offsets in the reference's direction order -x,+x,-y,+y,-z,+z (src/primsMST.h:70-72)
     const int off[6] = {-m1, m1, -1, 1, -mn1, mn1};
-    EdgeHeap heap((size_t)sz * 3);
-    std::vector<uint8_t> in_tree(sz, 0);
+    bool symmetric = true;
+    for (int v = 0; v < sz; v++) {
+        const int k = v / mn1, rem = v - k * mn1, j = rem / m1, i = rem - j * m1;
+        const bool has[3] = {j + 1 < n1, i + 1 < m1, k + 1 < o1};
+        for (int ax = 0; ax < 3; ax++) {
+            if (!has[ax]) continue;
+            const int nb = 2 * ax + 1, u = v + off[nb];
+            const float s1 = sad[(size_t)nb * sz + v], s2 = sad[(size_t)(nb - 1) * sz + u];
+            const float wt = -std::exp(-(s1 / g3) / twostd);
+            w[(size_t)v * 6 + nb] = wt;
+            if (std::memcmp(&s1, &s2, 4) == 0) {
+                w[(size_t)u * 6 + nb - 1] = wt;
+            } else {
+                w[(size_t)u * 6 + nb - 1] = -std::exp(-(s2 / g3) / twostd);
+                symmetric = false;
+            }
+        }
+    }
     std::vector<int> depth(sz, 0);
     for (int v = 0; v < sz; v++) parents[v] = -1;
     const int root = m1 / 2 + (n1 / 2) * m1 + (o1 / 2) * m1 * n1;
-    in_tree[root] = 1;
-    int last = root;
-    for (int added = 1; added < sz; added++) {
-        // push the new vertex's edges to its in-grid neighbours, in direction order
-        const int k = last / mn1, rem = last - k * mn1, j = rem / m1, i = rem - j * m1;
-        const bool ok[6] = {j > 0, j + 1 < n1, i > 0, i + 1 < m1, k > 0, k + 1 < o1};
-        for (int nb = 0; nb < 6; nb++)
-            if (ok[nb]) heap.push(QueuedEdge{w[(size_t)last * 6 + nb], (uint32_t)last * 8u + (uint32_t)nb});
-        int from = -1, to = -1;
-        while (to < 0) {
-            if (heap.empty()) throw std::runtime_error("Prim: candidate heap exhausted (disconnected grid)");
-            const QueuedEdge e = heap.pop();
-            const int ef = (int)(e.from_dir >> 3), et = ef + off[e.from_dir & 7u];
-            const bool a = in_tree[ef], b = in_tree[et];
-            if (a != b) { from = a ? ef : et; to = a ? et : ef; }
+
+    // The tree Prim's walk would give (src/primsMST.h:120-165): Kruskal's forced
+    // edges, plus the walk itself only until it has made its picks in every
+    // ambiguous tie group (its heap decides those ties); no walk when no group is
+    // ambiguous.  A NaN weight, or an edge whose two directions differ: the whole
+    // walk.
+    MstGroups G;
+    const bool grouped = sz > 1 && symmetric && mst_groups(w.data(), m1, n1, o1, G);
+    std::vector<int> tree_edges;
+    if (grouped) tree_edges = G.forced;
+    int pending = grouped ? (int)G.amb_rank.size() : -1;  // ambiguous groups still open (-1: full walk)
+    std::vector<int> taken(grouped ? G.amb_rank.size() : 0, 0);
+    long long steps = 0;
+    if (pending != 0) {
+        EdgeHeap heap((size_t)sz * 3);
+        std::vector<uint8_t> in_tree(sz, 0);
+        in_tree[root] = 1;
+        int last = root;
+        for (int added = 1; added < sz && pending != 0; added++) {
+            // push the new vertex's edges to its in-grid neighbours, in direction order
+            const int k = last / mn1, rem = last - k * mn1, j = rem / m1, i = rem - j * m1;
+            const bool ok[6] = {j > 0, j + 1 < n1, i > 0, i + 1 < m1, k > 0, k + 1 < o1};
+            for (int nb = 0; nb < 6; nb++)
+                if (ok[nb]) heap.push(QueuedEdge{w[(size_t)last * 6 + nb], (uint32_t)last * 8u + (uint32_t)nb});
+            int from = -1, to = -1;
+            uint32_t dir = 0;
+            while (to < 0) {
+                if (heap.empty()) throw std::runtime_error("Prim: candidate heap exhausted (disconnected grid)");
+                const QueuedEdge e = heap.pop();
+                const int ef = (int)(e.from_dir >> 3), et = ef + off[e.from_dir & 7u];
+                const bool a = in_tree[ef], b = in_tree[et];
+                if (a != b) {
+                    from = a ? ef : et;
+                    to = a ? et : ef;
+                    dir = e.from_dir;
+                }
+            }
+            in_tree[to] = 1;
+            depth[to] = depth[from] + 1;
+            parents[to] = from;
+            last = to;
+            steps++;
+            if (pending > 0) {
+                // the undirected id of the edge just added: from its pushing end and direction
+                const int ef = (int)(dir >> 3), nb = (int)(dir & 7u);
+                const int id = (nb & 1) ? 3 * ef + nb / 2 : 3 * (ef + off[nb]) + nb / 2;
+                const int gi = G.amb_of_edge[id];
+                if (gi >= 0) {
+                    tree_edges.push_back(id);
+                    if (++taken[gi] == G.amb_rank[gi]) pending--;
+                }
+            }
         }
-        in_tree[to] = 1;
-        depth[to] = depth[from] + 1;
-        parents[to] = from;
-        last = to;
+    }
+    g_mst_counts[grouped && G.amb_rank.empty() ? 0 : 1]++;
+    g_mst_counts[2] += steps;
+    g_mst_counts[3] += sz - 1;
+    if (grouped) {
+        // parents and depths of the assembled tree: breadth-first from the root
+        if ((int)tree_edges.size() != sz - 1) throw std::runtime_error("MST assembly: wrong edge count");
+        std::vector<int> deg_ptr(sz + 1, 0), adj(2 * (size_t)(sz - 1));
+        auto ends = [&](int id, int& p, int& q) {
+            const int v = id / 3, ax = id % 3;
+            p = v;
+            q = v + (ax == 0 ? m1 : ax == 1 ? 1 : mn1);
+        };
+        for (int id : tree_edges) {
+            int p, q;
+            ends(id, p, q);
+            deg_ptr[p + 1]++;
+            deg_ptr[q + 1]++;
+        }
+        for (int v = 0; v < sz; v++) deg_ptr[v + 1] += deg_ptr[v];
+        std::vector<int> fill(deg_ptr.begin(), deg_ptr.end() - 1);
+        for (int id : tree_edges) {
+            int p, q;
+            ends(id, p, q);
+            adj[fill[p]++] = q;
+            adj[fill[q]++] = p;
+        }
+        for (int v = 0; v < sz; v++) parents[v] = -1;
+        std::vector<int> queue(sz);
+        std::vector<uint8_t> seen(sz, 0);
+        size_t qh = 0, qt = 0;
+        queue[qt++] = root;
+        seen[root] = 1;
+        depth[root] = 0;
+        while (qh < qt) {
+            const int v = queue[qh++];
+            for (int e = deg_ptr[v]; e < deg_ptr[v + 1]; e++) {
+                const int u = adj[e];
+                if (seen[u]) continue;
+                seen[u] = 1;
+                parents[u] = v;
+                depth[u] = depth[v] + 1;
+                queue[qt++] = u;
+            }
+        }
+        if ((int)qt != sz) throw std::runtime_error("MST assembly: tree does not span the grid");
     }
     // breadth-level order, stable in node id (src/primsMST.h:166-190)
     int maxd = 0;

@@ -25,5 +25,10 @@ void image_stats(const float* im, size_t sz, float* mean_out, float* std_out);
 void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int g, int* ordered, int* parents,
                     float* edgemst);
 void build_schedule(const int* ordered, const int* parents, int sz, TreeSchedule& s);
+// Process-wide counts of the MST constructions: trees whose minimum spanning tree
+// is unique (no Prim walk), trees with ambiguous ties (a Prim walk until its tie
+// picks are made, or all of it when a weight is NaN), Prim steps walked, and the
+// steps full walks of the same trees would take.
+void mst_path_counts(long long out[4]);
 
 }  // namespace deeds

@@ -168,6 +168,35 @@ def make_pair(shape, seed=0, n_organs=None, max_disp=6.0, spacing=16, contrast="
     return out
 
 
+def make_atlases(shape, n_atlases=4, seed=0, n_organs=None, max_disp=6.0, spacing=16):
+    """A multi-atlas segmentation case: one anatomy seen n_atlases + 1 times.
+
+    The target is the anatomy rendered with noise; atlas k is the same anatomy
+    deformed by its own seeded B-spline field (moving(p) = anatomy(p + disp_k(p)))
+    with its own noise, and its labels deformed alike.  Returns dict(target,
+    target_labels, atlas_images, atlas_labels) of Fortran-ordered volumes."""
+    shape = tuple(int(s) for s in shape)
+    rng = np.random.default_rng(seed)
+    if n_organs is None:
+        n_organs = int(rng.integers(6, 13))
+    body, labels = _organ_labels(shape, n_organs, rng)
+    organ_hu = rng.uniform(-100.0, 300.0, n_organs).astype(np.float32)
+    clean = _render(body, labels, organ_hu, -1000.0, 0.0)
+    grid = np.meshgrid(*[np.arange(s, dtype=np.float32) for s in shape], indexing="ij")
+    images, labs = [], []
+    for k in range(n_atlases):
+        r = np.random.default_rng((seed, k + 1))
+        disp = _bspline_field(shape, spacing, max_disp, r)
+        coords = [grid[d] + disp[d] for d in range(3)]
+        im = ndimage.map_coordinates(clean, coords, order=1, mode="nearest").astype(np.float32)
+        im += r.normal(0.0, 20.0, shape).astype(np.float32)
+        images.append(np.asfortranarray(im))
+        labs.append(np.asfortranarray(ndimage.map_coordinates(labels, coords, order=0, mode="nearest").astype(np.uint8)))
+    target = clean + rng.normal(0.0, 20.0, shape).astype(np.float32)
+    return {"target": np.asfortranarray(target.astype(np.float32)), "target_labels": np.asfortranarray(labels),
+            "atlas_images": images, "atlas_labels": labs}
+
+
 def batch_workload(n=16, seed=100):
     """The uneven-size batch: n (shape, seed) pairs with dims drawn uniformly from
     128x112x144 up to 224x192x288; pair i is make_pair(shape, seed + 1 + i,

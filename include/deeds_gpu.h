@@ -150,6 +150,19 @@ deeds_status deeds_image_stats(const float* im, size_t count, float* mean, float
 deeds_status deeds_prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int g, int* ordered,
                                   int* parents, float* edgemst);
 
+/* The image statistics of primsGraph() (src/primsMST.h:101-110) on the device:
+ * the reference's sequential float mean and standard deviation of d_im
+ * (count floats), to the bit, written to d_out[0] (mean) and d_out[1] (std).
+ * The registration computes these on the device for its host trees. */
+deeds_status deeds_image_stats_dev(deeds_ctx* ctx, const float* d_im, size_t count, float* d_out, void* stream);
+
+/* Diagnostic counters of the host MST construction (process-wide, since load):
+ * out[0] trees whose minimum spanning tree is unique (built without a Prim
+ * walk), out[1] trees with ambiguous equal-weight edges (Prim's heap walk decides
+ * them, stopped once it has), out[2] Prim steps walked, out[3] steps that full
+ * walks of the same trees would take.  Every tree equals primsGraph()'s. */
+void deeds_mst_path_counts(long long out[4]);
+
 /* regularisationCL(): exact min-sum belief propagation on the MST with 3-D
  * quadratic distance-transform messages (src/regularisation.h:6-303).
  * d_cost (sz1*len3) is overwritten with the upward-pass state (each non-root
@@ -225,7 +238,8 @@ deeds_status deeds_jacobian_dev(deeds_ctx* ctx, const float* d_u, const float* d
 #define DEEDS_STAGE_TRANSFORM 5  /* upsampling and warps */
 #define DEEDS_STAGE_CONSISTENT 6 /* inverse-consistent mapping */
 #define DEEDS_STAGE_TREE_WAIT 7  /* host time spent waiting for Prim trees */
-#define DEEDS_NUM_STAGES 8
+#define DEEDS_STAGE_BP_ARGMIN 8  /* argmin tables of the upward pass (from its stored rows) */
+#define DEEDS_NUM_STAGES 9
 
 /* Enable/disable per-stage CUDA-event timing in deeds_register*(). */
 deeds_status deeds_set_profiling(deeds_ctx* ctx, int on);
@@ -434,6 +448,37 @@ deeds_status deeds_affine_robust(const float* pts1, const float* pts2, int len, 
  * expired and reported it (the error word for the sweep), *seconds to the time
  * both took.  The context stays usable afterwards. */
 deeds_status deeds_selftest_bounded_waits(deeds_ctx* ctx, int* sweep_gave_up, int* tma_gave_up, double* seconds);
+
+/* ---------------------------------------------------------------------------
+ * Multi-atlas segmentation.  The reference names joint label fusion of several
+ * registered atlases as future work (README.md:8, README.md:201) and has no
+ * implementation; these entry points register atlases to a target with the
+ * deeds path above and fuse their warped labels by locally weighted voting:
+ *   D_i(x) = window sum over the (2*radius+1)^3 patch around x (clamp-to-edge;
+ *            separable: i, then j, then k) of (target - image_i)^2;
+ *   w_i(x) = (1 / (D_i(x) + eps))^power   (power 0: majority vote);
+ *   label(x) = argmax over labels L of sum_i w_i [labels_i(x) == L] (sums in
+ *              atlas order; ties to the smaller label).
+ */
+#define DEEDS_FUSE_MAX_ATLASES 64
+
+/* Fusion of atlases already warped onto the target (device pointers: d_images
+ * and d_labels are host arrays of n_atlas device pointers, each m*n*o).
+ * Asynchronous on `stream`; scratch (2 * n_atlas * m*n*o floats) belongs to ctx. */
+deeds_status deeds_fuse_labels_dev(deeds_ctx* ctx, const float* d_target, const float* const* d_images,
+                                   const int16_t* const* d_labels, int n_atlas, int m, int n, int o, int radius,
+                                   float eps, int power, int16_t* d_out, void* stream);
+
+/* End to end (host buffers): registers every atlas image to the target
+ * (deeds_register_batch with `lanes`; identity affine), warps each atlas' labels
+ * with its flow (as deeds_apply_flow, nearest neighbour), fuses them with the
+ * warped atlas images, and writes the fused labels (m*n*o).  warped_labels_out
+ * and warped_images_out (nullable) receive the n_atlas warped label volumes and
+ * warped images back to back.  Synchronous. */
+deeds_status deeds_multi_atlas(deeds_ctx* ctx, const float* target, const float* const* atlas_images,
+                               const int16_t* const* atlas_labels, int n_atlas, int m, int n, int o,
+                               const deeds_params* params, int lanes, int radius, float eps, int power,
+                               int16_t* labels_out, int16_t* warped_labels_out, float* warped_images_out);
 
 /* ---------------------------------------------------------------------------
  * Parallel gzip IO for NIfTI volumes (host only; the reference uses single-

@@ -237,3 +237,93 @@ def test_host_prims_tie_heavy_matches_oracle(lib, dims, levels):
     orc.lib().orc_prims_from_sad(ptr(sad), C.c_float(37.5), m1, n1, o1, 4, *(ptr(a) for a in ref))
     for a, b in zip(got, ref):
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def _symmetric_sad(m1, n1, o1, draw):
+    """Per-node SADs to the 6 neighbours (nb order -x,+x,-y,+y,-z,+z) with one value
+    per undirected edge, as block SADs of an image have; 0 off the grid."""
+    sz = m1 * n1 * o1
+    sad = np.zeros(6 * sz, np.float32)
+    v = np.arange(sz)
+    i, j, k = v % m1, (v // m1) % n1, v // (m1 * n1)
+    for ax, (ok, step) in enumerate(((j + 1 < n1, m1), (i + 1 < m1, 1), (k + 1 < o1, m1 * n1))):
+        src = v[ok]
+        vals = draw(src.size).astype(np.float32)
+        sad[(2 * ax + 1) * sz + src] = vals
+        sad[(2 * ax) * sz + src + step] = vals
+    return sad
+
+
+def _prims_both(lib, sad, sd, dims, g):
+    m1, n1, o1 = dims
+    sz = m1 * n1 * o1
+    ptr = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    got = [np.zeros(sz, np.int32), np.zeros(sz, np.int32), np.zeros(sz, np.float32)]
+    ref = [np.zeros(sz, np.int32), np.zeros(sz, np.int32), np.zeros(sz, np.float32)]
+    assert lib.deeds_prims_from_sad(ptr(sad), C.c_float(sd), m1, n1, o1, g, *(ptr(a) for a in got)) == 0
+    orc.lib().orc_prims_from_sad(ptr(sad), C.c_float(sd), m1, n1, o1, g, *(ptr(a) for a in ref))
+    return got, ref
+
+
+def _counts(lib):
+    a = (C.c_longlong * 4)()
+    lib.deeds_mst_path_counts(a)
+    return list(a)
+
+
+@pytest.mark.parametrize("dims", [(24, 20, 32), (13, 11, 17), (1, 9, 7), (5, 1, 6)])
+def test_unique_mst_without_prim_walk(lib, dims):
+    """Continuous edge weights: the minimum spanning tree is unique, so the
+    library builds it by Kruskal's grouping alone (no heap walk); it must be
+    Prim's tree node for node."""
+    rng = np.random.default_rng(sum(dims))
+    sad = _symmetric_sad(*dims, lambda k: rng.uniform(0, 5000, k))
+    before = _counts(lib)
+    got, ref = _prims_both(lib, sad, 137.0, dims, 4)
+    after = _counts(lib)
+    for a, b in zip(got, ref):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert after[0] - before[0] == 1 and after[2] == before[2], (before, after)
+
+
+@pytest.mark.parametrize("dims,levels", [((24, 20, 32), 40), ((48, 40, 64), 400), ((13, 11, 17), 3)])
+def test_ambiguous_ties_decided_by_partial_prim_walk(lib, dims, levels):
+    """Symmetric SADs from a few values: many equal weights on cycles, so Prim's
+    heap decides ties.  The library walks Prim's heap only until every ambiguous
+    group has its picks and takes the rest from Kruskal's forced edges; the tree
+    must still equal the full walk's."""
+    rng = np.random.default_rng(levels)
+    sad = _symmetric_sad(*dims, lambda k: rng.integers(0, levels, k) * 64.0)
+    before = _counts(lib)
+    got, ref = _prims_both(lib, sad, 37.5, dims, 4)
+    after = _counts(lib)
+    for a, b in zip(got, ref):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert after[1] - before[1] == 1
+
+
+def test_mst_paths_on_phantom_levels(lib):
+    """Block SADs of a CT-like phantom at every default grid: trees identical to
+    the oracle's full Prim walk, whichever construction each level takes."""
+    shape = (96, 80, 128)
+    pair = phantom.make_pair(shape, seed=11)
+    for name in ("fixed", "moving"):
+        im = np.ascontiguousarray(pair[name].ravel(order="F") + np.float32(1024), np.float32)
+        _, sd = orc.image_stats(im)
+        for g in (8, 7, 6, 5, 4):
+            sad = orc.edge_sad(im, *shape, g)
+            dims = tuple(s // g for s in shape)
+            got, ref = _prims_both(lib, sad, sd, dims, g)
+            for a, b in zip(got, ref):
+                assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (name, g)
+
+
+def test_nan_weights_take_the_full_walk(lib):
+    """A zero standard deviation makes zero SADs NaN weights: the order is then the
+    heap's alone, so the library walks it fully, as the reference."""
+    dims = (9, 7, 5)
+    rng = np.random.default_rng(3)
+    sad = _symmetric_sad(*dims, lambda k: rng.integers(0, 3, k) * 8.0)
+    got, ref = _prims_both(lib, sad, 0.0, dims, 2)
+    for a, b in zip(got, ref):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
