@@ -25,8 +25,9 @@
 //
 // Downward pass (root to leaves, :258-293): one CTA per tree takes the root's
 // first minimum, then its threads walk heavy-path chains (each follows the child
-// with the deepest subtree) from the argmin tables, a chain starting once its
-// first node's parent has a label; no barrier per breadth level.
+// with the deepest subtree) from the argmin tables; a walker queues the chains
+// that branch off a node once it has that node's label; no barrier per breadth
+// level.
 //
 // Roofline: dependency bound (tree depth 265-987 per tree at 192x160x256).
 // Algorithmic traffic: one read + one write of the cost volume and one write of
@@ -239,21 +240,6 @@ __device__ __forceinline__ float block_min1(float v, float* red) {
     return v;
 }
 
-__device__ float block_min(float v, float* red) {
-    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    __syncthreads();
-    if (lane == 0) red[w] = v;
-    __syncthreads();
-    if (w == 0) {
-        v = lane < (int)(blockDim.x >> 5) ? red[lane] : INFINITY;
-        for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
-        if (lane == 0) red[0] = v;
-    }
-    __syncthreads();
-    return red[0];
-}
-
 template <int LEN>
 __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __restrict__ cost,
                                                            float* __restrict__ pre, float* __restrict__ mins,
@@ -399,38 +385,43 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
     }
 }
 
-// Labels of the downward pass live in global memory and are exchanged between
-// threads of the one CTA that runs the pass: relaxed CTA-scope accesses (the label
-// is the only datum passed, so no ordering beyond the access itself is needed).
-__device__ __forceinline__ int ld_label(const int* p) {
-    int v;
-    asm volatile("ld.relaxed.cta.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+// The downward pass's queue of chains ready to walk: 64-bit entries (the label
+// of the chain's first node's parent in the high word, the chain id in the low
+// word; all ones = not yet written), exchanged between the threads of the one
+// CTA that runs the pass.  An entry carries all a walker needs, so relaxed
+// CTA-scope accesses suffice.
+__device__ __forceinline__ unsigned long long ld_queue(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.cta.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ void st_label(int* p, int v) {
-    asm volatile("st.relaxed.cta.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+__device__ __forceinline__ void st_queue(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.relaxed.cta.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
 constexpr long long kDownSpinLimit = 1LL << 21;  // polls of a 64 ns sleep: ~0.13 s, far beyond a pass
+constexpr unsigned long long kQueueEmpty = ~0ull;
 
 // Root argmin (first minimum), then the backtrack (src/regularisation.h:258-293)
-// over heavy-path chains.  The reference resolves one breadth level after another;
-// here a thread claims a chain (chains in breadth order of their first node),
-// waits until the first node's parent has its label, and then walks the chain
-// down to its leaf, one argmin-table gather per node with no barrier in between.
-// The chains follow the deepest subtree at every node, so the longest root-leaf
-// path is walked by few threads without waiting: the pass costs about one gather
-// latency per node of that path.  Each thread prefetches the argmin row of the
-// next node of its chain into L2.  Waits are bounded (error 4 on expiry); a label
-// or a table entry out of range records error 2 and reads label 0 instead.
+// over heavy-path chains (from a chain's first node down through the child with
+// the deepest subtree to a leaf).  The reference resolves one breadth level
+// after another; here a thread walks a whole chain, one argmin-table gather per
+// node with no barrier in between, and at every node it queues the chains that
+// start at the node's other children together with the node's label.  Threads
+// take queue slots by ticket (slot k holds the k-th chain queued; every chain is
+// queued exactly once), so a thread only ever waits for a chain that some walker
+// is about to queue, and the longest root-leaf path (chain 0) is walked without
+// waiting: the pass costs about one gather latency per node of that path.  Each
+// walker prefetches its argmin rows two nodes ahead into L2.  Waits are bounded
+// (error 4 on expiry); a label or a table entry out of range records error 2 and
+// reads label 0 instead.
 __global__ void __launch_bounds__(1024) k_bp_down(BpTree t, const float* __restrict__ cost,
                                                  short* __restrict__ allinds, float* __restrict__ u1,
-                                                 float* __restrict__ v1, float* __restrict__ w1, int* labels,
-                                                 int* __restrict__ err) {
+                                                 float* __restrict__ v1, float* __restrict__ w1,
+                                                 unsigned long long* queue, int* __restrict__ err) {
     __shared__ float s_val[32];
     __shared__ int s_idx[32];
-    __shared__ int s_next;
-    __shared__ int s_abort;
+    __shared__ int s_head, s_tail, s_abort;
     const int len = t.len, len3 = len * len * len, hw = (len - 1) / 2;
     const int root = t.root;
     const float* rr = cost + (int64_t)root * len3;
@@ -461,41 +452,51 @@ __global__ void __launch_bounds__(1024) k_bp_down(BpTree t, const float* __restr
             // the reference scans with value=cost[0], index=0 and '<' (src/regularisation.h:258-279):
             // a NaN at 0 keeps index 0, NaNs elsewhere never win
             if (isnan(__ldcg(rr)) || bi < 0 || bi >= len3) bi = 0;
-            st_label(labels + root, bi);
             const int i = bi % len, j = (bi / len) % len, k = bi / (len * len);
             u1[root] = (float)(j - hw) * t.q + t.u0[root];
             v1[root] = (float)(i - hw) * t.q + t.v0[root];
             w1[root] = (float)(k - hw) * t.q + t.w0[root];
-            s_next = 0;
+            st_queue(queue, (unsigned long long)(unsigned)bi << 32);  // chain 0 starts at the root
+            s_head = 0;
+            s_tail = 1;
             s_abort = 0;
         }
     }
     __syncthreads();
     const int row_lines = (len3 * 2 + 127) / 128;
+    auto enqueue = [&](int node, int label) {
+        for (int b = t.branch_ptr[node]; b < t.branch_ptr[node + 1]; b++) {
+            const int slot = atomicAdd(&s_tail, 1);
+            st_queue(queue + slot, (unsigned long long)(unsigned)label << 32 | (unsigned)t.branch_chain[b]);
+        }
+    };
     for (;;) {
-        const int c = atomicAdd(&s_next, 1);
-        if (c >= t.n_chains) return;
+        const int ticket = atomicAdd(&s_head, 1);
+        if (ticket >= t.n_chains) return;
+        unsigned long long q;
+        long long it = 0;
+        while ((q = ld_queue(queue + ticket)) == kQueueEmpty) {  // queued, or about to be
+            if (++it > kDownSpinLimit || *(volatile int*)&s_abort) {
+                atomicCAS(err, 0, 4);
+                *(volatile int*)&s_abort = 1;
+                return;
+            }
+            __nanosleep(64);
+        }
+        const int c = (int)(q & 0xffffffffull);
+        int lp = (int)(q >> 32);
         int i = t.chain_ptr[c];
         const int e = t.chain_ptr[c + 1];
-        int lp;
-        if (t.chain_nodes[i] == root) {
-            lp = ld_label(labels + root);  // written before the barrier
+        if (t.chain_nodes[i] == root) {  // chain 0: the root's label is lp; queue its other children's chains
+            enqueue(root, lp);
             i++;
-        } else {
-            const int* flag = labels + t.parents[t.chain_nodes[i]];
-            long long it = 0;
-            while ((lp = ld_label(flag)) < 0) {
-                if (++it > kDownSpinLimit || *(volatile int*)&s_abort) {
-                    atomicCAS(err, 0, 4);
-                    *(volatile int*)&s_abort = 1;
-                    return;
-                }
-                __nanosleep(64);
-            }
         }
-        // The chain's node ids run three ahead of the walk: the id a step prefetches
-        // for was loaded a step earlier, so neither the prefetch nor the gather waits
-        // for an id load; the argmin rows are prefetched into L2 two nodes ahead.
+        // The chain's node ids run three ahead of the walk and each node's range of
+        // branch chains one ahead: the id a step prefetches for, and the range a step
+        // queues from, were loaded a step earlier, so neither the prefetch, the
+        // gather nor the queueing waits for an id load; the argmin rows are
+        // prefetched into L2 two nodes ahead.  A node's first branch chain ids are
+        // loaded before its gather.
         auto node_at = [&](int k) { return k < e ? ld_ahead(t.chain_nodes + k) : -1; };
         auto prefetch_row = [&](int v) {
             if (v < 0) return;
@@ -503,12 +504,22 @@ __global__ void __launch_bounds__(1024) k_bp_down(BpTree t, const float* __restr
             for (int k = 0; k < row_lines; k++) asm volatile("prefetch.global.L2 [%0];" ::"l"(a + 128 * k));
         };
         int cur = node_at(i), n1 = node_at(i + 1), n2 = node_at(i + 2);
+        int cb0 = 0, cb1 = 0, nb0 = 0, nb1 = 0;
+        if (cur >= 0) { cb0 = ld_ahead(t.branch_ptr + cur); cb1 = ld_ahead(t.branch_ptr + cur + 1); }
+        if (n1 >= 0) { nb0 = ld_ahead(t.branch_ptr + n1); nb1 = ld_ahead(t.branch_ptr + n1 + 1); }
         prefetch_row(n1);
         while (cur >= 0) {
             const int node = cur;
+            const int b0 = cb0, b1 = cb1;
             const int n3 = node_at(i + 3);
             prefetch_row(n2);
+            cb0 = nb0; cb1 = nb1;
+            if (n2 >= 0) { nb0 = ld_ahead(t.branch_ptr + n2); nb1 = ld_ahead(t.branch_ptr + n2 + 1); }
             cur = n1; n1 = n2; n2 = n3;
+            constexpr int kBr = 4;  // branch chain ids held in registers (more are read in the loop)
+            int br[kBr];
+#pragma unroll
+            for (int k = 0; k < kBr; k++) br[k] = b0 + k < b1 ? ld_ahead(t.branch_chain + b0 + k) : -1;
             const float a0 = t.u0[node], a1 = t.v0[node], a2 = t.w0[node];
             if (lp < 0 || lp >= len3) {  // never for a completed upward pass; keeps reads in bounds
                 atomicCAS(err, 0, 2);
@@ -519,7 +530,11 @@ __global__ void __launch_bounds__(1024) k_bp_down(BpTree t, const float* __restr
                 atomicCAS(err, 0, 2);
                 l = 0;
             }
-            st_label(labels + node, l);
+            const unsigned long long hi = (unsigned long long)(unsigned)l << 32;
+#pragma unroll
+            for (int k = 0; k < kBr; k++)
+                if (br[k] >= 0) st_queue(queue + atomicAdd(&s_tail, 1), hi | (unsigned)br[k]);
+            for (int b = b0 + kBr; b < b1; b++) st_queue(queue + atomicAdd(&s_tail, 1), hi | (unsigned)t.branch_chain[b]);
             const int ii = l % len, jj = (l / len) % len, kk = l / (len * len);
             u1[node] = (float)(jj - hw) * t.q + a0;
             v1[node] = (float)(ii - hw) * t.q + a1;
@@ -691,11 +706,12 @@ cudaError_t launch_bp_argmin(const BpTree& t, short* d_allinds, const float* d_p
 }
 
 cudaError_t launch_bp_down(const BpTree& t, const float* d_cost, short* d_allinds, float* d_u1, float* d_v1,
-                           float* d_w1, int* d_labels, int* d_err, cudaStream_t s) {
-    if (t.n_chains < 1 || !t.chain_ptr || !t.chain_nodes) return cudaErrorInvalidValue;
-    cudaError_t e = cudaMemsetAsync(d_labels, 0xff, sizeof(int) * (size_t)t.sz, s);  // -1: no label yet
+                           float* d_w1, unsigned long long* d_queue, int* d_err, cudaStream_t s) {
+    if (t.n_chains < 1 || !t.chain_ptr || !t.chain_nodes || !t.branch_ptr || !t.branch_chain)
+        return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(d_queue, 0xff, sizeof(unsigned long long) * (size_t)t.n_chains, s);  // empty
     if (e != cudaSuccess) return e;
-    k_bp_down<<<1, 1024, 0, s>>>(t, d_cost, d_allinds, d_u1, d_v1, d_w1, d_labels, d_err);
+    k_bp_down<<<1, 1024, 0, s>>>(t, d_cost, d_allinds, d_u1, d_v1, d_w1, d_queue, d_err);
     count_launches(1);
     return cudaGetLastError();
 }

@@ -34,6 +34,8 @@ struct BpTree {
     int n_chains;            // heavy-path chains (downward pass)
     const int* chain_ptr;    // [n_chains+1] ranges into chain_nodes
     const int* chain_nodes;  // [sz] each chain's nodes from its start down to a leaf
+    const int* branch_ptr;   // [sz+1] per node: range of the chains starting at its children
+    const int* branch_chain; // [n_chains-1]
 };
 
 // A displacement field given at full resolution (mode 1), on a control grid
@@ -68,9 +70,9 @@ cudaError_t launch_bp_up(const BpTree& t, float* d_cost, short* d_allinds, float
 // the argmin tables (allinds) of every node from the sweep's stored rows (after launch_bp_up)
 cudaError_t launch_bp_argmin(const BpTree& t, short* d_allinds, const float* d_pre, const float* d_mins, int sm_count,
                              cudaStream_t s);
-// d_labels: t.sz ints of scratch (each node's selected label)
+// d_queue: t.n_chains 64-bit words of scratch (chains ready to walk)
 cudaError_t launch_bp_down(const BpTree& t, const float* d_cost, short* d_allinds, float* d_u1, float* d_v1,
-                           float* d_w1, int* d_labels, int* d_err, cudaStream_t s);
+                           float* d_w1, unsigned long long* d_queue, int* d_err, cudaStream_t s);
 cudaError_t launch_shift(const float* d_in, float* d_out, int64_t n, float shift, cudaStream_t s);
 cudaError_t launch_upsample(const float* u0, const float* v0, const float* w0, int m2, int n2, int o2, float* u,
                             float* v, float* w, int m, int n, int o, cudaStream_t s);

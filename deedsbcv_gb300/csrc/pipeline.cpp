@@ -327,7 +327,8 @@ deeds_status check_params(deeds_ctx* ctx, const deeds_params* p, int m, int n, i
 // One tree's host arrays packed for a single H2D copy (4-byte words).
 struct PackedTree {
     int sz = 0, n_leaves = 0, n_levels = 0, max_width = 0, n_chains = 0;
-    size_t o_ordered, o_parents, o_edgemst, o_cptr, o_children, o_leaves, o_lstart, o_ppos, o_chptr, o_chnodes, total;
+    size_t o_ordered, o_parents, o_edgemst, o_cptr, o_children, o_leaves, o_lstart, o_ppos, o_chptr, o_chnodes,
+        o_brptr, o_brchain, total;
 };
 
 PackedTree pack_layout(int sz) {
@@ -344,6 +345,8 @@ PackedTree pack_layout(int sz) {
     t.o_ppos = o; o += sz;
     t.o_chptr = o; o += sz + 1;
     t.o_chnodes = o; o += sz;
+    t.o_brptr = o; o += sz + 1;
+    t.o_brchain = o; o += sz;
     t.total = o;
     return t;
 }
@@ -360,6 +363,8 @@ void pack_schedule(const TreeSchedule& s, uint32_t* blk, PackedTree& t) {
     t.n_chains = (int)s.chain_ptr.size() - 1;
     std::memcpy(blk + t.o_chptr, s.chain_ptr.data(), sizeof(int) * s.chain_ptr.size());
     std::memcpy(blk + t.o_chnodes, s.chain_nodes.data(), sizeof(int) * s.chain_nodes.size());
+    std::memcpy(blk + t.o_brptr, s.branch_ptr.data(), sizeof(int) * s.branch_ptr.size());
+    std::memcpy(blk + t.o_brchain, s.branch_chain.data(), sizeof(int) * s.branch_chain.size());
 }
 
 // Build one tree on the host into the packed pinned block `blk`.
@@ -396,6 +401,8 @@ BpTree device_tree(const PackedTree& t, const uint32_t* dblk, const uint32_t* hb
     b.n_chains = t.n_chains;
     b.chain_ptr = reinterpret_cast<const int*>(dblk + t.o_chptr);
     b.chain_nodes = reinterpret_cast<const int*>(dblk + t.o_chnodes);
+    b.branch_ptr = reinterpret_cast<const int*>(dblk + t.o_brptr);
+    b.branch_chain = reinterpret_cast<const int*>(dblk + t.o_brchain);
     return b;
 }
 
@@ -408,6 +415,7 @@ deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTre
     float* d_mins = dbuf<float>(ctx, "mins_" + tag, 4 * (size_t)pt.sz, &st);  // mins | edge offsets x, y, z
     int* d_arrived = dbuf<int>(ctx, "arrived_" + tag, pt.sz, &st);
     int* d_work = dbuf<int>(ctx, "work_" + tag, 1, &st);
+    unsigned long long* d_queue = dbuf<unsigned long long>(ctx, "queue_" + tag, pt.sz, &st);
     float* d_pre = dbuf<float>(ctx, "pre_" + tag, (size_t)pt.sz * len * len * len, &st);
     if (st) return st;
     CK(cudaMemcpyAsync(d_blk, h_blk, pt.total * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
@@ -422,8 +430,7 @@ deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTre
     }
     {
         StageScope sc(ctx, DEEDS_STAGE_BP_DOWN, s);
-        // the upward pass is done with its arrival counters: they hold the labels now
-        CK(launch_bp_down(bt, d_cost, d_allinds, u1, v1, w1, d_arrived, d_err, s));
+        CK(launch_bp_down(bt, d_cost, d_allinds, u1, v1, w1, d_queue, d_err, s));
     }
     return DEEDS_OK;
 }
@@ -496,6 +503,7 @@ deeds_status acquire_buffers(deeds_ctx* ctx, int m, int n, int o, const deeds_pa
         dbuf<float>(ctx, "mins_" + tg, 4 * B.max_sz1, &st);
         dbuf<int>(ctx, "arrived_" + tg, B.max_sz1, &st);
         dbuf<int>(ctx, "work_" + tg, 1, &st);
+        dbuf<unsigned long long>(ctx, "queue_" + tg, B.max_sz1, &st);
         dbuf<float>(ctx, "pre_" + tg, B.max_cost, &st);  // scaled rows of the upward sweep (argmin input)
     }
     B.grid = dbuf<float>(ctx, "grid", 18 * B.max_sz1, &st);
@@ -565,21 +573,24 @@ deeds_status deeds_create(deeds_ctx** out, int device) {
     deeds_ctx* ctx = c.get();
     CK(cudaSetDevice(device));
     CK(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device));
-    CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     {
-        // the MST inputs (image statistics, block SADs) start the host trees, which
-        // the level loop waits for: their small kernels go ahead of the throughput
-        // kernels of the other streams
+        // Priorities (numerically lower = sooner): the MST inputs (image statistics,
+        // block SADs) start the host trees that the level loop waits for, so their
+        // small kernels go first; the two direction streams, which carry the
+        // latency-bound tree sweeps, come before the background stream's MIND codes
+        // of later levels, which only fill SMs the sweeps leave idle.
         int least = 0, greatest = 0;
         CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        const int mid = greatest + 1 <= least ? greatest + 1 : least;
         CK(cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, greatest));
+        CK(cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, mid));
+        CK(cudaStreamCreateWithPriority(&c->stream_b, cudaStreamNonBlocking, mid));
+        CK(cudaStreamCreateWithPriority(&c->bg, cudaStreamNonBlocking, least));
     }
     CK(cudaEventCreateWithFlags(&c->ev_a, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c->ev_b, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c->ev_c, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c->ev_d, cudaEventDisableTiming));
-    CK(cudaStreamCreateWithFlags(&c->stream_b, cudaStreamNonBlocking));
-    CK(cudaStreamCreateWithFlags(&c->bg, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&c->ev_e, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c->ev_f, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c->ev_g, cudaEventDisableTiming));
@@ -805,8 +816,14 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
     deeds_status st = check_params(ctx, P, m, n, o);
     if (st) return st;
     CK(cudaSetDevice(ctx->device));
-    // forward chain on the caller's stream, backward chain on the context's second stream
-    cudaStream_t s = (cudaStream_t)stream;
+    // forward chain on the context's stream (after the caller's stream has reached
+    // this call: the inputs), backward chain on the context's second stream; the
+    // call returns when all of it is done
+    cudaStream_t s = ctx->stream;
+    if ((cudaStream_t)stream != s) {
+        CK(cudaEventRecord(ctx->ev_d, (cudaStream_t)stream));
+        CK(cudaStreamWaitEvent(s, ctx->ev_d, 0));
+    }
     cudaStream_t sd[2] = {s, ctx->stream_b};
     const int L = P->levels;
     const size_t sz = (size_t)m * n * o;
@@ -986,13 +1003,23 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
             }
             CK(cudaEventRecord(ctx->ev_g, ctx->bg));
         }
-        for (int d = 0; d < 2; d++) {
-            const int t = 2 * l + d;
+        // each direction's sweeps are queued as soon as its own tree is built (the two
+        // directions' trees finish at different times; their streams are independent)
+        bool queued[2] = {false, false};
+        for (int k = 0; k < 2; k++) {
+            int d = -1;
             {
                 const auto w0 = std::chrono::steady_clock::now();
-                tl.mark("level " + std::to_string(l) + (d ? " backward" : " forward") + " waits for its tree");
+                tl.mark("level " + std::to_string(l) + " waits for a tree");
+                while (d < 0) {
+                    for (int c = 0; c < 2 && d < 0; c++)
+                        if (!queued[c] && ready_f[2 * l + c].wait_for(std::chrono::seconds(0)) == std::future_status::ready)
+                            d = c;
+                    if (d < 0) ready_f[2 * l + (queued[0] ? 1 : 0)].wait_for(std::chrono::microseconds(50));
+                }
+                queued[d] = true;
                 try {
-                    ready_f[t].get();
+                    ready_f[2 * l + d].get();
                 } catch (const std::exception& ex) {
                     return fail(ctx, DEEDS_ERR_INTERNAL, "MST construction failed: %s", ex.what());
                 }
@@ -1000,6 +1027,7 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
                     ctx->stage_ms[DEEDS_STAGE_TREE_WAIT] +=
                         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
             }
+            const int t = 2 * l + d;
             tl.dmark("level " + std::to_string(l) + (d ? " backward" : " forward") + " BP starts", sd[d]);
             st = run_tree_bp(ctx, tags[d], pts[t], h_tree[t], cost[d], allinds[d], len, q, cur0[3 * d],
                              cur0[3 * d + 1], cur0[3 * d + 2], nxt[3 * d], nxt[3 * d + 1], nxt[3 * d + 2], d_err + d,

@@ -20,16 +20,16 @@
 // and its shifted copy stay inside the binade, and evaluates every other segment
 // from the true start.  The result is the reference's to the bit for any data.
 //
-// Two levels: chunks of 8192 elements; a chunk whose own trajectory leaves its
-// binade (the sum crosses a power of two: about log2(sum / first element) chunks
-// per chain) or that has no usable estimate is also run as 32 sub-segments,
-// in parallel before the walk, so the walk replays at most a sub-segment of 257
-// elements (staged in shared memory) where a chunk fails.  No thread walks a
-// long stretch of global memory alone.
+// Two levels: chunks of 2048 elements; a chunk whose own trajectory leaves its
+// binade or comes near one of its ends (the sum crosses a power of two: about
+// log2(sum / first element) chunks per chain) or that has no usable estimate is
+// also run as 32 sub-segments, in parallel before the walk, so the walk replays
+// at most a few sub-segments of 65 elements (staged in shared memory) where a
+// chunk fails.  No thread walks a long stretch of global memory alone.
 //
-// Work: 4 B per voxel read by the chunk sums and once per chain (coalesced,
-// through shared memory), plus the crossing chunks twice more.  Dependency
-// bound: 8192 float adds per chunk chain and ~1000 sequential chunk checks.
+// Work: 4 B per voxel read by the chunk sums and once per chain, plus the
+// crossing chunks twice more.  Dependency bound: 2048 steps per chunk chain and
+// ~4000 sequential chunk checks (bit operations and float compares).
 #include <algorithm>
 #include <cmath>
 
@@ -40,7 +40,7 @@ namespace deeds {
 
 namespace {
 
-constexpr int kStatsChunk = 8192;  // elements per chunk (bounds sz * c / nch: 8192 to 16383)
+constexpr int kStatsChunk = 2048;  // elements per chunk (bounds sz * c / nch: 2048 to 4095)
 constexpr int kSub = 32;           // sub-segments of a chunk run in parallel
 
 struct ChunkRun {
@@ -51,13 +51,28 @@ struct ChunkRun {
     int cross;               // chunk level: 1 when its sub-segment runs exist
 };
 
+// A chunk's trajectories in units of u of their binade, for the walk's integer
+// check: values are multiples of u with magnitudes in [2^23, 2^24) units.  A
+// trajectory that leaves the binade carries lo > hi (never accepted).
+struct WalkRec {
+    int e, neg;                  // binade and sign of start_a (e = 0: no usable trajectories)
+    int cross;                   // the chunk's sub-segment runs exist
+    int sa, sb, ea, eb;          // starts and ends
+    int loa, hia, lob, hib;      // extremes of each trajectory
+};
+
 __device__ __forceinline__ size_t chunk_lo(size_t sz, int nch, int c) { return sz * (size_t)c / (size_t)nch; }
 
-// binade exponent (|v| in [2^(e-1), 2^e)) and its grid step u; false for 0, tiny or non-finite v
+// 2^k as a float, for k in the normal range (bit construction: exact)
+__device__ __forceinline__ float pow2f(int k) { return __uint_as_float((unsigned)(k + 127) << 23); }
+
+// binade exponent (|v| in [2^(e-1), 2^e)) and its grid step u; false for 0, tiny
+// (below 2^-100) or non-finite v.  From the exponent bits: v = f 2^e, f in [0.5, 1).
 __device__ __forceinline__ bool binade(float v, int& e, float& u) {
-    if (!isfinite(v) || fabsf(v) < 0x1p-100f) return false;
-    frexpf(v, &e);
-    u = ldexpf(1.0f, e - 24);
+    const int be = (int)((__float_as_uint(v) >> 23) & 0xffu);
+    if (be == 0xff || be < 27) return false;
+    e = be - 126;
+    u = pow2f(e - 24);
     return true;
 }
 
@@ -68,12 +83,14 @@ __device__ __forceinline__ bool binade(float v, int& e, float& u) {
 // sum below 2^e is exact, while a sum at or above 2^e rounds to a value at or
 // above 2^e (rounding is monotone and 2^e is a float) and fails as it must.
 __device__ __forceinline__ bool inside(float lo, float hi, float d, int e, float u, bool neg) {
-    const float inner = ldexpf(1.0f, e - 1) + u, outer = ldexpf(1.0f, e) - 2.0f * u;
+    const float inner = pow2f(e - 1) + u, outer = pow2f(e) - 2.0f * u;
     const float l = lo + d, h = hi + d;
     return neg ? (l >= -outer && h <= -inner) : (l >= inner && h <= outer);
 }
 
-__device__ __forceinline__ float var_step_double(float v, float d) {
+// Kept out of line so that the compiler cannot if-convert the rare double path
+// of var_step into every step (FP64 is slow on this part).
+__device__ __noinline__ float var_step_double(float v, float d) {
     return (float)((double)v + (double)d * (double)d);
 }
 
@@ -126,7 +143,7 @@ __device__ __forceinline__ bool shift_ok(const ChunkRun& cr, float v, float& nv)
         return false;
     // both are multiples of u below 2^e in magnitude: their distance in units of u
     // is the difference of two exact integers below 2^24
-    const float inv_u = ldexpf(1.0f, 24 - e);  // exact scalings by a power of two
+    const float inv_u = pow2f(24 - e);  // exact scalings by a power of two
     const int k = (int)(fabsf(v) * inv_u) - (int)(fabsf(cr.start_a) * inv_u);
     const bool even = (k & 1) == 0;
     const float start = even ? cr.start_a : cr.start_b;
@@ -145,7 +162,7 @@ __device__ __forceinline__ void spec_starts(float est, ChunkRun& cr) {
     float u;
     cr.start_a = est;
     if (binade(est, e, u)) {
-        cr.start_b = fabsf(est + u) < ldexpf(1.0f, e) ? est + u : est - u;  // one u away, same binade
+        cr.start_b = fabsf(est + u) < pow2f(e) ? est + u : est - u;  // one u away, same binade
         cr.spec = 1;
     } else {
         cr.start_b = est;
@@ -295,37 +312,137 @@ __global__ void __launch_bounds__(1024) k_stats_starts(size_t sz, int nch, const
     }
 }
 
-// Both trajectories of every speculated chunk, one thread per chunk.  The
-// thread reads its chunk 32 elements at a time into registers (32 independent
-// loads in flight; the sectors a load brings serve the next seven of the same
-// thread from L1).  A chunk whose trajectory leaves its binade, or that has no
-// usable estimate, is marked for sub-segment runs.  Grid (ceil(nch / 64), nimg).
+// Both trajectories of every speculated chunk, one lane per chunk: a warp owns
+// 32 consecutive chunks and loads them 32 elements per chunk at a time, one
+// coalesced 128-byte row per load (the row's base broadcast from its lane), into
+// a padded shared tile that each lane then reads along its own row.  A chunk
+// whose trajectory leaves its binade or comes near one of its ends, or that has
+// no usable estimate, is marked for sub-segment runs; every chunk's integer
+// walk record is written.  Grid (ceil(nch / 32), nimg), 32 threads.
 template <int KIND>
-__global__ void __launch_bounds__(64) k_stats_traj(const float* __restrict__ im0, const float* __restrict__ im1,
+__global__ void __launch_bounds__(32) k_stats_traj(const float* __restrict__ im0, const float* __restrict__ im1,
                                                    size_t sz, int nch, const float* __restrict__ means,
-                                                   ChunkRun* __restrict__ run) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= nch) return;
+                                                   ChunkRun* __restrict__ run, WalkRec* __restrict__ walk) {
+    __shared__ float tile[32][33];
     const float* x = blockIdx.y == 0 ? im0 : im1;
-    ChunkRun cr = run[(size_t)blockIdx.y * nch + c];
-    const size_t lo = chunk_lo(sz, nch, c), hi = chunk_lo(sz, nch, c + 1);
-    const int len = (int)(hi - lo);
-    const float* xc = x + lo;
-    const float mean = KIND == 1 ? means[blockIdx.y] : 0.0f;
-    if (cr.spec) {
-        float t[32];
-        int k0 = 0;
-        for (; k0 + 32 <= len; k0 += 32) {
-#pragma unroll
-            for (int k = 0; k < 32; k++) t[k] = __ldg(xc + k0 + k);
-            run_pair<KIND>(t, 32, mean, cr);
-        }
-        for (; k0 < len; k0++) run_pair<KIND>(xc + k0, 1, mean, cr);
+    const int lane = threadIdx.x;
+    const int c = blockIdx.x * 32 + lane;
+    size_t lo = 0;
+    int len = 0;
+    ChunkRun cr;
+    cr.spec = 0;
+    if (c < nch) {
+        lo = chunk_lo(sz, nch, c);
+        len = (int)(chunk_lo(sz, nch, c + 1) - lo);
+        cr = run[(size_t)blockIdx.y * nch + c];
     }
-    int e;
-    float u;
-    cr.cross = !cr.spec || !binade(cr.start_a, e, u) || !inside(cr.lo_a, cr.hi_a, 0.0f, e, u, signbit(cr.start_a));
+    const float mean = KIND == 1 ? means[blockIdx.y] : 0.0f;
+    const int maxlen = (int)(sz / (size_t)nch) + 1;  // chunk lengths are floor or ceil of sz / nch
+    for (int k0 = 0; k0 < maxlen; k0 += 32) {
+#pragma unroll
+        for (int r = 0; r < 32; r++) {
+            const size_t base = __shfl_sync(0xffffffffu, lo, r);
+            const int n = __shfl_sync(0xffffffffu, len, r);
+            tile[r][lane] = k0 + lane < n ? __ldg(x + base + k0 + lane) : 0.0f;
+        }
+        __syncwarp();
+        if (cr.spec) {
+            const int n = min(32, len - k0);
+            if (n > 0) run_pair<KIND>(&tile[lane][0], n, mean, cr);
+        }
+        __syncwarp();
+    }
+    if (c >= nch) return;
+    // also marked: chunks whose trajectory comes within 2^-12 of the binade's
+    // width of an end, which a shift onto the true start could push out
+    int e = 0;
+    float u = 0.0f;
+    bool in = cr.spec && binade(cr.start_a, e, u);
+    const bool neg = signbit(cr.start_a);
+    WalkRec w;
+    w.e = 0;
+    if (in) {
+        const float margin = pow2f(e - 13);
+        // (fminf / fmaxf skip NaN, so a trajectory that met a NaN is recognised by its end)
+        const bool ina = isfinite(cr.end_a) && inside(cr.lo_a, cr.hi_a, 0.0f, e, u, neg);
+        const bool inb = isfinite(cr.end_b) && inside(cr.lo_b, cr.hi_b, 0.0f, e, u, neg);
+        const float inv_u = pow2f(24 - e);
+        w.e = e;
+        w.neg = neg;
+        w.sa = (int)(cr.start_a * inv_u);
+        w.sb = (int)(cr.start_b * inv_u);
+        w.ea = (int)(cr.end_a * inv_u);
+        w.eb = (int)(cr.end_b * inv_u);
+        w.loa = ina ? (int)(cr.lo_a * inv_u) : 1;
+        w.hia = ina ? (int)(cr.hi_a * inv_u) : 0;
+        w.lob = inb ? (int)(cr.lo_b * inv_u) : 1;
+        w.hib = inb ? (int)(cr.hi_b * inv_u) : 0;
+        in = ina && inside(cr.lo_a, cr.hi_a, margin, e, u, neg) && inside(cr.lo_a, cr.hi_a, -margin, e, u, neg);
+    }
+    cr.cross = !in;
+    w.cross = cr.cross;
     run[(size_t)blockIdx.y * nch + c] = cr;
+    walk[(size_t)blockIdx.y * nch + c] = w;
+}
+
+// Second estimates of every chunk's start: the exclusive prefix of the first
+// pass's float increments (end - start of each speculated chunk's trajectory;
+// the double chunk sum where there was none).  The float chain drops the parts
+// of small terms that round away against a large sum, so these follow the true
+// chain far more closely than the exact sums do.  One block of 1024 threads per
+// image.
+template <int KIND>
+__global__ void __launch_bounds__(1024) k_stats_restarts(size_t sz, int nch, const double* __restrict__ sx,
+                                                         const double* __restrict__ sx2, ChunkRun* __restrict__ run) {
+    const int img = blockIdx.x;
+    const double* s = sx + (size_t)img * nch;
+    const double* q = sx2 + (size_t)img * nch;
+    ChunkRun* r = run + (size_t)img * nch;
+    __shared__ double part[1024];
+    __shared__ double total_s;
+    const int T = blockDim.x, t = threadIdx.x;
+    const int per = (nch + T - 1) / T;
+    const int c0 = min(nch, t * per), c1 = min(nch, c0 + per);
+    double m = 0.0;
+    if (KIND == 1) {
+        double a = 0.0;
+        for (int c = c0; c < c1; c++) a += s[c];
+        part[t] = a;
+        __syncthreads();
+        if (t == 0) {
+            double tot = 0.0;
+            for (int k = 0; k < T; k++) tot += part[k];
+            total_s = tot;
+        }
+        __syncthreads();
+        m = total_s / (double)sz;
+        __syncthreads();
+    }
+    auto inc = [&](int c) {
+        const ChunkRun& cr = r[c];
+        if (cr.spec) return (double)cr.end_a - (double)cr.start_a;
+        if (KIND == 0) return s[c];
+        const double n = (double)(chunk_lo(sz, nch, c + 1) - chunk_lo(sz, nch, c));
+        return fmax(0.0, q[c] - 2.0 * m * s[c] + n * m * m);
+    };
+    double a = 0.0;
+    for (int c = c0; c < c1; c++) a += inc(c);
+    part[t] = a;
+    __syncthreads();
+    for (int off = 1; off < T; off <<= 1) {
+        const double v = t >= off ? part[t - off] : 0.0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    double pre = t > 0 ? part[t - 1] : 0.0;
+    for (int c = c0; c < c1; c++) {  // each thread rewrites only its own chunks
+        const float est = (float)pre;
+        pre += inc(c);
+        ChunkRun cr;
+        spec_starts(est, cr);
+        r[c] = cr;
+    }
 }
 
 // Sub-segment runs of the chunks marked by k_stats_traj: the chunk is staged in
@@ -419,39 +536,64 @@ __device__ float warp_segment(const float* __restrict__ xg, int n, float v, floa
 }
 
 // The true chain, chunk by chunk (one warp per image; every lane holds the same
-// value): a chunk whose trajectories can be shifted onto the true start gives
-// its end directly, any other chunk is evaluated by warp_segment.  The chunk
-// records are read 32 at a time.  KIND 0 writes the mean, KIND 1 the standard
-// deviation (out[2 img + 0 / 1]).  Dynamic shared memory: the largest chunk.
+// value).  While the value lies in a binade it is kept as an integer V in units
+// of u, and a chunk whose trajectory (chosen by the parity of V - its start) and
+// that trajectory shifted by V - start stay inside the binade gives V' = its end
+// + the shift, with integer operations only; any other chunk is evaluated by
+// warp_segment from the float value.  The walk records are read 32 at a time.
+// KIND 0 writes the mean, KIND 1 the standard deviation (out[2 img + 0 / 1]).
+// Dynamic shared memory: the largest chunk.
 template <int KIND>
 __global__ void __launch_bounds__(32) k_stats_stitch(const float* __restrict__ im0, const float* __restrict__ im1,
                                                      size_t sz, int nch, const ChunkRun* __restrict__ run,
-                                                     const ChunkRun* __restrict__ sub, float* __restrict__ means,
-                                                     float* __restrict__ out) {
+                                                     const WalkRec* __restrict__ walk, const ChunkRun* __restrict__ sub,
+                                                     float* __restrict__ means, float* __restrict__ out) {
     extern __shared__ float buf[];
-    __shared__ ChunkRun batch[32];
+    __shared__ WalkRec batch[32];
     const int img = blockIdx.x, lane = threadIdx.x;
     const float* x = img == 0 ? im0 : im1;
-    const ChunkRun* r = run + (size_t)img * nch;
     const float mean = KIND == 1 ? means[img] : 0.0f;
+    constexpr int IN = (1 << 23) + 1, OUT = (1 << 24) - 2;
     float v = 0.0f;
+    int ve = 0, vneg = 0, V = 0;  // ve = 0: v is not held as an integer (0, tiny or not finite)
+    // the next batch of records is loaded into registers while this one is walked
+    WalkRec nextrec;
+    if (lane < nch) nextrec = walk[(size_t)img * nch + lane];
     for (int c0 = 0; c0 < nch && !isnan(v); c0 += 32) {
         __syncwarp();
-        if (c0 + lane < nch) batch[lane] = r[c0 + lane];
+        batch[lane] = nextrec;
+        if (c0 + 32 + lane < nch) nextrec = walk[(size_t)img * nch + c0 + 32 + lane];
         __syncwarp();
         const int nb = min(32, nch - c0);
         for (int k = 0; k < nb; k++) {
-            if (isnan(v)) break;  // absorbing for both chains: the result is NaN
-            float nv;
-            if (!shift_ok(batch[k], v, nv)) {
-                const int c = c0 + k;
-                const size_t lo = chunk_lo(sz, nch, c), hi = chunk_lo(sz, nch, c + 1);
-                const ChunkRun* sr = batch[k].cross ? sub + ((size_t)img * nch + c) * kSub : nullptr;
-                nv = warp_segment<KIND>(x + lo, (int)(hi - lo), v, mean, sr, buf);
+            const WalkRec& w = batch[k];
+            bool ok = false;
+            if (ve != 0 && w.e == ve && w.neg == vneg) {
+                const bool odd = ((V - w.sa) & 1) != 0;
+                const int S = odd ? w.sb : w.sa, E = odd ? w.eb : w.ea;
+                const int LO = odd ? w.lob : w.loa, HI = odd ? w.hib : w.hia;
+                const int D = V - S, l = LO + D, h = HI + D;
+                ok = LO <= HI && (vneg ? (l >= -OUT && h <= -IN) : (l >= IN && h <= OUT));
+                if (ok) V = E + D;
             }
-            v = nv;
+            if (ok) continue;
+            // the float value, then the chunk exactly
+            if (ve != 0) v = (float)V * pow2f(ve - 24);
+            if (isnan(v)) break;  // absorbing for both chains: the result is NaN
+            const int c = c0 + k;
+            const size_t lo = chunk_lo(sz, nch, c), hi = chunk_lo(sz, nch, c + 1);
+            const ChunkRun* sr = w.cross ? sub + ((size_t)img * nch + c) * kSub : nullptr;
+            v = warp_segment<KIND>(x + lo, (int)(hi - lo), v, mean, sr, buf);
+            float u;
+            if (binade(v, ve, u)) {
+                vneg = signbit(v) ? 1 : 0;
+                V = (int)(v * pow2f(24 - ve));
+            } else {
+                ve = 0;
+            }
         }
     }
+    if (ve != 0) v = (float)V * pow2f(ve - 24);
     if (lane == 0) {
         if (KIND == 0) {
             const float m = v / (float)sz;
@@ -472,7 +614,7 @@ constexpr int kSegSmemMax = (int)((2 * (size_t)kStatsChunk + 2) * sizeof(float))
 
 size_t image_stats_scratch_bytes(size_t sz, int nimg) {
     const size_t nch = (size_t)stats_chunks(sz);
-    return 256 + (size_t)nimg * nch * (2 * sizeof(double) + sizeof(ChunkRun) * (1 + kSub)) + 64;
+    return 256 + (size_t)nimg * nch * (2 * sizeof(double) + sizeof(ChunkRun) * (1 + kSub) + sizeof(WalkRec)) + 64;
 }
 
 // Mean and standard deviation of one or two images (im1 may be null when nimg
@@ -492,6 +634,8 @@ cudaError_t launch_image_stats(const float* im0, const float* im1, int nimg, siz
     ChunkRun* run = reinterpret_cast<ChunkRun*>(p);
     p += (size_t)nimg * nch * sizeof(ChunkRun);
     ChunkRun* sub = reinterpret_cast<ChunkRun*>(p);
+    p += (size_t)nimg * nch * kSub * sizeof(ChunkRun);
+    WalkRec* walk = reinterpret_cast<WalkRec*>(p);
     if (!im1) im1 = im0;
     // the shared-memory limits are set to the bound on every call, never lowered,
     // so concurrent callers cannot race on them
@@ -501,17 +645,21 @@ cudaError_t launch_image_stats(const float* im0, const float* im1, int nimg, siz
                           (const void*)k_stats_sub<1>})
         if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, kSegSmemMax);
     if (e != cudaSuccess) return e;
-    const dim3 tgrid((nch + 63) / 64, nimg), cgrid(nch, nimg);
+    const dim3 tgrid((nch + 31) / 32, nimg), cgrid(nch, nimg);
     k_stats_sums<<<cgrid, 256, 0, s>>>(im0, im1, sz, nch, sx, sx2);
     k_stats_starts<0><<<nimg, 1024, 0, s>>>(sz, nch, sx, sx2, run);
-    k_stats_traj<0><<<tgrid, 64, 0, s>>>(im0, im1, sz, nch, means, run);
+    k_stats_traj<0><<<tgrid, 32, 0, s>>>(im0, im1, sz, nch, means, run, walk);
+    k_stats_restarts<0><<<nimg, 1024, 0, s>>>(sz, nch, sx, sx2, run);
+    k_stats_traj<0><<<tgrid, 32, 0, s>>>(im0, im1, sz, nch, means, run, walk);
     k_stats_sub<0><<<cgrid, 32, seg_smem, s>>>(im0, im1, sz, nch, means, run, sub);
-    k_stats_stitch<0><<<nimg, 32, seg_smem, s>>>(im0, im1, sz, nch, run, sub, means, out);
+    k_stats_stitch<0><<<nimg, 32, seg_smem, s>>>(im0, im1, sz, nch, run, walk, sub, means, out);
     k_stats_starts<1><<<nimg, 1024, 0, s>>>(sz, nch, sx, sx2, run);
-    k_stats_traj<1><<<tgrid, 64, 0, s>>>(im0, im1, sz, nch, means, run);
+    k_stats_traj<1><<<tgrid, 32, 0, s>>>(im0, im1, sz, nch, means, run, walk);
+    k_stats_restarts<1><<<nimg, 1024, 0, s>>>(sz, nch, sx, sx2, run);
+    k_stats_traj<1><<<tgrid, 32, 0, s>>>(im0, im1, sz, nch, means, run, walk);
     k_stats_sub<1><<<cgrid, 32, seg_smem, s>>>(im0, im1, sz, nch, means, run, sub);
-    k_stats_stitch<1><<<nimg, 32, seg_smem, s>>>(im0, im1, sz, nch, run, sub, means, out);
-    count_launches(9);
+    k_stats_stitch<1><<<nimg, 32, seg_smem, s>>>(im0, im1, sz, nch, run, walk, sub, means, out);
+    count_launches(13);
     return cudaGetLastError();
 }
 

@@ -739,6 +739,14 @@ void build_schedule(const int* ordered, const int* parents, int sz, TreeSchedule
         for (int c = v; c >= 0; c = heavy[c]) s.chain_nodes.push_back(c);
     }
     s.chain_ptr.push_back((int)s.chain_nodes.size());
+    // per node, the chains that start at its children (every chain but the first)
+    const int n_chains = (int)s.chain_ptr.size() - 1;
+    s.branch_ptr.assign(sz + 1, 0);
+    for (int c = 1; c < n_chains; c++) s.branch_ptr[parents[s.chain_nodes[s.chain_ptr[c]]] + 1]++;
+    for (int v = 0; v < sz; v++) s.branch_ptr[v + 1] += s.branch_ptr[v];
+    s.branch_chain.assign(n_chains > 0 ? n_chains - 1 : 0, 0);
+    std::vector<int> bfill(s.branch_ptr.begin(), s.branch_ptr.end() - 1);
+    for (int c = 1; c < n_chains; c++) s.branch_chain[bfill[parents[s.chain_nodes[s.chain_ptr[c]]]]++] = c;
 }
 
 }  // namespace deeds

@@ -19,6 +19,8 @@ struct TreeSchedule {
     // leaf; chains in breadth order of their starts, every node in exactly one.
     std::vector<int> chain_ptr;    // [n_chains+1] ranges into chain_nodes
     std::vector<int> chain_nodes;  // [sz]
+    std::vector<int> branch_ptr;   // [sz+1] per node: range of the chains that start at its children
+    std::vector<int> branch_chain; // [n_chains-1] those chain ids, ascending
 };
 
 void image_stats(const float* im, size_t sz, float* mean_out, float* std_out);
