@@ -392,6 +392,10 @@ def measure_soft(api, ctx, n_pairs=4, levels=SOFT_LEVELS, taus=SOFT_TAUS, shape=
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1)
             res[mode + "_ms_per_pair"] = ms / len(data)
+            if mode == "forward_backward_recompute":
+                # the form that recomputes each level's forward state in the backward
+                # instead of keeping it on the device
+                res["pairs_per_s_recompute"] = 1000.0 * len(data) / ms
             if mode == "forward_backward":
                 res["pairs_per_s"] = 1000.0 * len(data) / ms
                 res["grad_norms_last_pair"] = {"fixed": float(gf.norm()), "moving": float(gm.norm()),

@@ -632,7 +632,11 @@ cudaError_t launch_up(const BpTree& t, float* cost, short* allinds, float* pre, 
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bp_up<LEN>, T, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    int ctas = per_sm * sm_count;
+    // at most two CTAs per SM: the sweep is bound by its deepest chain, whose steps
+    // slow down when more CTAs share its SM (the two directions' sweeps and the
+    // argmin tables run concurrently), while two per SM still finish the rest of
+    // the nodes well within the chain's time (measured: 12.36 -> 12.43 pairs/s)
+    int ctas = (per_sm < 2 ? per_sm : 2) * sm_count;
     if (ctas > t.n_leaves) ctas = t.n_leaves;
     float* off = mins + t.sz;
     k_bp_offsets<<<(t.sz + 255) / 256, 256, 0, s>>>(t, off);
@@ -655,7 +659,10 @@ cudaError_t launch_argmin(const BpTree& t, short* allinds, const float* pre, con
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_a, k_bp_argmin<LEN>, T, smem_a);
     if (e != cudaSuccess) return e;
     if (per_sm_a < 1) return cudaErrorInvalidConfiguration;
-    int ctas_a = per_sm_a * sm_count;
+    // short-lived CTAs of a few nodes each (rather than one persistent wave), so
+    // that a higher-priority sweep's CTAs get SMs as these retire
+    int ctas_a = (t.sz + 3) / 4;
+    if (ctas_a < per_sm_a * sm_count) ctas_a = per_sm_a * sm_count;
     if (ctas_a > t.sz) ctas_a = t.sz;
     k_bp_argmin<LEN><<<ctas_a, T, smem_a, s>>>(t, pre, off, allinds);
     count_launches(1);

@@ -173,10 +173,22 @@ __global__ void k_quantise(const float* __restrict__ D, uint64_t* __restrict__ c
 #pragma unroll
     for (int l = 0; l < 12; l++) { v[l] = v[l] - mn_v; noise = noise + v[l]; }
     noise = fmaxf(__fdiv_rn(noise, 12.0f), 1e-6f);
+    // The level only counts the thresholds above the correctly rounded quotient
+    // RN(v / noise).  v * RN(1 / noise) is within 1.5 ulp of it (two roundings of
+    // at most half an ulp each, relative 2^-24, on a quotient whose own rounding is
+    // half an ulp), so unless a threshold lies within 2^-20 (relative, ~8 ulp) of
+    // that product both give the same count; near a threshold the IEEE division
+    // decides.  noise >= 1e-6 (fmaxf drops a NaN sum); NaN, infinite, zero and
+    // tiny quotients fall on the same side of every threshold both ways.
+    const float rcp = __frcp_rn(noise);
     uint64_t code = 0;
 #pragma unroll
     for (int l = 0; l < 12; l++) {
-        const float x = __fdiv_rn(v[l], noise);
+        float x = __fmul_rn(v[l], rcp);
+        const float lo = __fmul_rn(x, 1.0f - 0x1p-20f), hi = __fmul_rn(x, 1.0f + 0x1p-20f);
+        const bool near = (t0 >= lo && t0 <= hi) | (t1 >= lo && t1 <= hi) | (t2 >= lo && t2 <= hi) |
+                          (t3 >= lo && t3 <= hi) | (t4 >= lo && t4 <= hi);
+        if (near) x = __fdiv_rn(v[l], noise);
         const int lvl = (t0 > x) + (t1 > x) + (t2 > x) + (t3 > x) + (t4 > x);
         code |= (uint64_t)((1u << lvl) - 1u) << (5 * l);  // thermometer {0,1,3,7,15,31}
     }

@@ -53,6 +53,10 @@ struct deeds_ctx {
     cudaStream_t side = nullptr;    // MST edge costs and their copies
     cudaStream_t stream_b = nullptr;  // backward-direction chain of deeds_register*
     cudaStream_t bg = nullptr;        // field-independent work deeds_register* overlaps with tree sweeps
+    // per direction: the argmin tables of a sweep at the lowest priority, so that
+    // they yield SMs to the other direction's latency-bound sweep
+    cudaStream_t low[2] = {nullptr, nullptr};
+    cudaEvent_t ev_up[2] = {nullptr, nullptr}, ev_arg[2] = {nullptr, nullptr};
     cudaEvent_t ev_e = nullptr, ev_f = nullptr, ev_g = nullptr;
     cudaEvent_t ev_a = nullptr, ev_b = nullptr, ev_c = nullptr, ev_d = nullptr;
     std::string err;
@@ -425,8 +429,17 @@ deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTre
         CK(launch_bp_up(bt, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, ctx->sm_count, s));
     }
     {
-        StageScope sc(ctx, DEEDS_STAGE_BP_ARGMIN, s);
-        CK(launch_bp_argmin(bt, d_allinds, d_pre, d_mins, ctx->sm_count, s));
+        // the argmin tables on the direction's low-priority stream, joined back before
+        // the downward pass
+        const int dl = tag == "b" ? 1 : 0;
+        CK(cudaEventRecord(ctx->ev_up[dl], s));
+        CK(cudaStreamWaitEvent(ctx->low[dl], ctx->ev_up[dl], 0));
+        {
+            StageScope sc(ctx, DEEDS_STAGE_BP_ARGMIN, ctx->low[dl]);
+            CK(launch_bp_argmin(bt, d_allinds, d_pre, d_mins, ctx->sm_count, ctx->low[dl]));
+        }
+        CK(cudaEventRecord(ctx->ev_arg[dl], ctx->low[dl]));
+        CK(cudaStreamWaitEvent(s, ctx->ev_arg[dl], 0));
     }
     {
         StageScope sc(ctx, DEEDS_STAGE_BP_DOWN, s);
@@ -586,6 +599,11 @@ deeds_status deeds_create(deeds_ctx** out, int device) {
         CK(cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, mid));
         CK(cudaStreamCreateWithPriority(&c->stream_b, cudaStreamNonBlocking, mid));
         CK(cudaStreamCreateWithPriority(&c->bg, cudaStreamNonBlocking, least));
+        for (int d = 0; d < 2; d++) {
+            CK(cudaStreamCreateWithPriority(&c->low[d], cudaStreamNonBlocking, least));
+            CK(cudaEventCreateWithFlags(&c->ev_up[d], cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&c->ev_arg[d], cudaEventDisableTiming));
+        }
     }
     CK(cudaEventCreateWithFlags(&c->ev_a, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&c->ev_b, cudaEventDisableTiming));
@@ -603,14 +621,15 @@ void deeds_destroy(deeds_ctx* ctx) {
     for (deeds_ctx* lane : ctx->lanes) deeds_destroy(lane);
     ctx->lanes.clear();
     cudaSetDevice(ctx->device);
-    for (cudaStream_t st : {ctx->stream, ctx->stream_b, ctx->side, ctx->bg})
+    for (cudaStream_t st : {ctx->stream, ctx->stream_b, ctx->side, ctx->bg, ctx->low[0], ctx->low[1]})
         if (st) cudaStreamSynchronize(st);
     for (auto& kv : ctx->dev) if (kv.second.p) cudaFree(kv.second.p);
     for (auto& kv : ctx->host) if (kv.second.p) cudaFreeHost(kv.second.p);
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
-    for (cudaEvent_t e : {ctx->ev_a, ctx->ev_b, ctx->ev_c, ctx->ev_d, ctx->ev_e, ctx->ev_f, ctx->ev_g})
+    for (cudaEvent_t e : {ctx->ev_a, ctx->ev_b, ctx->ev_c, ctx->ev_d, ctx->ev_e, ctx->ev_f, ctx->ev_g, ctx->ev_up[0],
+                          ctx->ev_up[1], ctx->ev_arg[0], ctx->ev_arg[1]})
         if (e) cudaEventDestroy(e);
-    for (cudaStream_t st : {ctx->stream, ctx->stream_b, ctx->side, ctx->bg})
+    for (cudaStream_t st : {ctx->stream, ctx->stream_b, ctx->side, ctx->bg, ctx->low[0], ctx->low[1]})
         if (st) cudaStreamDestroy(st);
     delete ctx;
 }
