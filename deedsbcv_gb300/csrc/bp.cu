@@ -240,20 +240,101 @@ __device__ __forceinline__ float block_min1(float v, float* red) {
     return v;
 }
 
+// Argmin table of one node (allinds, src/regularisation.h:37-107).  The sweep
+// computes message values only; a node's three passes are run again here from
+// its stored scaled row (`pre`, the transforms' input) with the reference's
+// strict-'<' first-minimiser scans, which reproduce the sweep's values bit for
+// bit and record, per parent label, the child label.  Uses A, B, ia, ib; the
+// caller's barrier precedes (shared memory free) and follows.
+template <int LEN>
+__device__ __forceinline__ void node_argmin(const BpTree& t, int node, const float* __restrict__ pre,
+                                            const float* __restrict__ off, short* __restrict__ allinds, float* A,
+                                            float* B, short* ia, short* ib) {
+    constexpr int LEN3 = LEN * LEN * LEN;
+    constexpr int T = bp_threads(LEN);
+    const float* prow = pre + (int64_t)node * LEN3;
+    for (int l = threadIdx.x; l < LEN3; l += T) A[l] = ld_cg(prow + l);
+    const float ox = off[node], oy = off[t.sz + node], oz = off[2 * t.sz + node];
+    __syncthreads();
+    dt_lines<LEN, 0>(A, B, nullptr, ia, oy);
+    __syncthreads();
+    dt_lines<LEN, 1>(B, A, ia, ib, ox);
+    __syncthreads();
+    dt_lines<LEN, 2>(A, B, ib, ia, oz);
+    __syncthreads();
+    short* arow = allinds + (int64_t)node * LEN3;
+    for (int l = threadIdx.x; l < LEN3; l += T) arow[l] = ia[l];
+}
+
+// Slots of the sweep's shared-memory list of a chain's finished nodes (flushed
+// to the global list when full).
+constexpr int kChainSlots = 1024;
+
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed_gpu(int* p, int v) {
+    asm volatile("st.relaxed.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+constexpr long long kArgminSpinLimit = 1LL << 21;  // polls of a 256 ns sleep: ~0.5 s, far beyond a sweep
+
+// Takes the next entry of the list of finished nodes by ticket (work[1]: tickets
+// handed out, work[2]: entries reserved; `done`: the entries, -1 until written).
+// Used after the sweep, when every reserved entry is written; the wait for it
+// is bounded all the same (error 4).  Returns -1 when the entries are exhausted.
+// One thread.
+__device__ __forceinline__ int take_finished(const BpTree& t, int* work, int* done, int* err) {
+    const int k = atomicAdd(work + 1, 1);
+    if (k >= ld_acquire_gpu(work + 2)) return -1;
+    int v;
+    long long it = 0;
+    while ((v = ld_acquire_gpu(done + k)) < 0) {
+        if (++it > kArgminSpinLimit || ld_acquire_gpu(err) != 0) {
+            atomicCAS(err, 0, 4);
+            return -1;
+        }
+        __nanosleep(256);
+    }
+    return v;
+}
+
 template <int LEN>
 __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __restrict__ cost,
                                                            float* __restrict__ pre, float* __restrict__ mins,
                                                            const float* __restrict__ off,
-                                                           int* __restrict__ arrived, int* __restrict__ work) {
+                                                           int* __restrict__ arrived, int* __restrict__ work,
+                                                           int* __restrict__ done, short* __restrict__ allinds,
+                                                           int* __restrict__ err) {
     constexpr int LEN3 = LEN * LEN * LEN;
     constexpr int T = bp_threads(LEN);
     constexpr int NL = (LEN3 + T - 1) / T;
     extern __shared__ float smem[];
     float* A = smem;
     float* B = A + LEN3;
+    short* ia = reinterpret_cast<short*>(B + LEN3);
+    short* ib = ia + LEN3;
+    int* s_chain = reinterpret_cast<int*>(ib + LEN3);  // this chain's finished nodes (2 LEN3 shorts: 4-aligned)
     __shared__ float red[32];
     __shared__ int s_node, s_last;
     const int tid = threadIdx.x;
+    __shared__ int s_nchain;  // entries of s_chain (written by thread 0)
+    if (tid == 0) s_nchain = 0;
+    // The argmin tables of a chain's nodes: when the chain ends at a sibling (this
+    // CTA did not arrive last at the parent, so nobody waits for it) the CTA computes
+    // them itself; the chain that reaches the root (the sweep's last) appends its
+    // nodes to the list of finished nodes (`done`, work[2] counts entries), which
+    // k_bp_argmin_rest works off across the GPU after the sweep.  The barrier before
+    // an append makes every thread's rows visible to thread 0, whose GPU-scope fence
+    // orders them before its relaxed list stores.
+    auto publish_list = [&]() {  // thread 0
+        __threadfence();
+        const int slot = atomicAdd(work + 2, s_nchain);
+        for (int k = 0; k < s_nchain; k++) st_relaxed_gpu(done + slot + k, s_chain[k]);
+        s_nchain = 0;
+    };
     for (;;) {
         __syncthreads();  // previous chain finished with s_node / smem
         if (tid == 0) {
@@ -325,6 +406,10 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
             // *std::min_element (src/regularisation.h:222) starts from element 0 and only
             // replaces it on '<': a NaN first element is the result, later NaNs are skipped
             if (isnan(B[0])) mn = B[0];
+            if (tid == 0) {
+                if (s_nchain == kChainSlots) publish_list();
+                s_chain[s_nchain++] = node;
+            }
             if (c1 - c0 > 1) {
                 // siblings exist: the last of them to arrive continues with the parent
                 if (tid == 0) {
@@ -332,7 +417,16 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
                     s_last = atom_add_acq_rel(arrived + p, 1) == c1 - c0 - 1;
                 }
                 __syncthreads();
-                if (!s_last) break;
+                if (!s_last) {
+                    // every thread's scaled rows were stored before the barriers since
+                    for (int k = 0; k < s_nchain; k++) {
+                        __syncthreads();
+                        node_argmin<LEN>(t, s_chain[k], pre, off, allinds, A, B, ia, ib);
+                    }
+                    __syncthreads();
+                    if (tid == 0) s_nchain = 0;
+                    break;
+                }
             }
             // the parent's row = data cost + sum over children in MST ordering
             // order of (message - min); this CTA's own message is still in B
@@ -364,6 +458,8 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
                     const int l = tid + k * T;
                     if (l < LEN3) rrow[l] = acc[k];
                 }
+                __syncthreads();
+                if (tid == 0) publish_list();
                 break;
             }
             __syncthreads();  // B (this message) has been consumed by every thread
@@ -561,71 +657,44 @@ __global__ void k_bp_offsets(BpTree t, float* __restrict__ off) {
     off[2 * t.sz + c] = __fdiv_rn(t.w0[p] - t.w0[c], t.q);
 }
 
-// Argmin tables of the upward sweep (allinds, src/regularisation.h:37-107): the
-// sweep itself computes message values only; here every node's three passes are
-// run again from its stored scaled row (`pre`, the transform's input) with the
-// reference's strict-'<' first-minimiser scans, which reproduce the sweep's
-// values bit for bit and record, per parent label, the child label.  The nodes
-// are independent, so this runs across the whole GPU (persistent CTAs striding
-// over nodes) instead of on the sweep's dependency chain.  The root has no edge
-// (its row is written by the downward pass).
+// The argmin tables of the nodes in the list of finished nodes (the chain that
+// reached the root, and chains longer than the sweep's shared list), after the
+// sweep: every entry is written by then.  Persistent CTAs take entries by ticket.
 template <int LEN>
-__global__ void __launch_bounds__(bp_threads(LEN)) k_bp_argmin(BpTree t, const float* __restrict__ pre,
-                                                               const float* __restrict__ off,
-                                                               short* __restrict__ allinds) {
+__global__ void __launch_bounds__(bp_threads(LEN)) k_bp_argmin_rest(BpTree t, const float* __restrict__ pre,
+                                                                    const float* __restrict__ off,
+                                                                    int* __restrict__ work, int* __restrict__ done,
+                                                                    short* __restrict__ allinds,
+                                                                    int* __restrict__ err) {
     constexpr int LEN3 = LEN * LEN * LEN;
-    constexpr int T = bp_threads(LEN);
     extern __shared__ float smem[];
     float* A = smem;
     float* B = A + LEN3;
     short* ia = reinterpret_cast<short*>(B + LEN3);
     short* ib = ia + LEN3;
-    constexpr int NL = (LEN3 + T - 1) / T;
-    // The next node's row is loaded into registers while this node's passes run,
-    // so the loop waits for global memory only once.
-    float nxt[NL];
-    auto fetch = [&](int v) {
-        const float* prow = pre + (int64_t)v * LEN3;
-#pragma unroll
-        for (int k = 0; k < NL; k++) {
-            const int l = threadIdx.x + k * T;
-            nxt[k] = 0.0f;
-            if (v < t.sz && l < LEN3) nxt[k] = ld_ahead_cg(prow + l);
-        }
-    };
-    int node = blockIdx.x;
-    if (node == t.root) node += gridDim.x;
-    fetch(node);
-    for (; node < t.sz;) {
-#pragma unroll
-        for (int k = 0; k < NL; k++) {
-            const int l = threadIdx.x + k * T;
-            if (l < LEN3) A[l] = nxt[k];
-        }
-        const float ox = off[node], oy = off[t.sz + node], oz = off[2 * t.sz + node];
-        int next = node + gridDim.x;
-        if (next == t.root) next += gridDim.x;
-        fetch(next);
+    __shared__ int s_node;
+    for (;;) {
         __syncthreads();
-        dt_lines<LEN, 0>(A, B, nullptr, ia, oy);
+        if (threadIdx.x == 0) s_node = take_finished(t, work, done, err);
         __syncthreads();
-        dt_lines<LEN, 1>(B, A, ia, ib, ox);
-        __syncthreads();
-        dt_lines<LEN, 2>(A, B, ib, ia, oz);
-        __syncthreads();
-        short* arow = allinds + (int64_t)node * LEN3;
-        for (int l = threadIdx.x; l < LEN3; l += T) arow[l] = ia[l];
-        __syncthreads();  // A / ia are rewritten by the next node
-        node = next;
+        if (s_node < 0) return;
+        node_argmin<LEN>(t, s_node, pre, off, allinds, A, B, ia, ib);
     }
+}
+
+// dynamic shared memory of the sweep and of the argmin kernel: A, B (floats),
+// ia, ib (shorts, padded to a word), and for the sweep the chain list
+template <int LEN>
+constexpr size_t bp_smem(bool sweep) {
+    constexpr size_t LEN3 = (size_t)LEN * LEN * LEN;
+    return LEN3 * 2 * sizeof(float) + 2 * LEN3 * sizeof(short) + (sweep ? kChainSlots * sizeof(int) : 0);
 }
 
 template <int LEN>
 cudaError_t launch_up(const BpTree& t, float* cost, short* allinds, float* pre, float* mins, int* arrived,
-                      int* work, int sm_count, cudaStream_t s) {
-    constexpr int LEN3 = LEN * LEN * LEN;
+                      int* work, int* done, int* err, int sm_count, cudaStream_t s) {
     constexpr int T = bp_threads(LEN);
-    const size_t smem = (size_t)LEN3 * 2 * sizeof(float);
+    const size_t smem = bp_smem<LEN>(true);
     cudaError_t e = cudaFuncSetAttribute(k_bp_up<LEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
@@ -633,38 +702,33 @@ cudaError_t launch_up(const BpTree& t, float* cost, short* allinds, float* pre, 
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
     // at most two CTAs per SM: the sweep is bound by its deepest chain, whose steps
-    // slow down when more CTAs share its SM (the two directions' sweeps and the
-    // argmin tables run concurrently), while two per SM still finish the rest of
-    // the nodes well within the chain's time (measured: 12.36 -> 12.43 pairs/s)
+    // slow down when more CTAs share its SM (the two directions' sweeps run
+    // concurrently), while two per SM still finish the rest of the nodes well
+    // within the chain's time
     int ctas = (per_sm < 2 ? per_sm : 2) * sm_count;
     if (ctas > t.n_leaves) ctas = t.n_leaves;
     float* off = mins + t.sz;
     k_bp_offsets<<<(t.sz + 255) / 256, 256, 0, s>>>(t, off);
-    k_bp_up<LEN><<<ctas, T, smem, s>>>(t, cost, pre, mins, off, arrived, work);
+    k_bp_up<LEN><<<ctas, T, smem, s>>>(t, cost, pre, mins, off, arrived, work, done, allinds, err);
     count_launches(2);
     return cudaGetLastError();
 }
 
 template <int LEN>
-cudaError_t launch_argmin(const BpTree& t, short* allinds, const float* pre, const float* mins, int sm_count,
-                          cudaStream_t s) {
-    constexpr int LEN3 = LEN * LEN * LEN;
+cudaError_t launch_argmin(const BpTree& t, short* allinds, const float* pre, const float* mins, int* work, int* done,
+                          int* err, int sm_count, cudaStream_t s) {
     constexpr int T = bp_threads(LEN);
     const float* off = mins + t.sz;
-    cudaError_t e;
-    const size_t smem_a = (size_t)LEN3 * (2 * sizeof(float) + 2 * sizeof(short));
-    e = cudaFuncSetAttribute(k_bp_argmin<LEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_a);
+    const size_t smem = bp_smem<LEN>(false);
+    cudaError_t e = cudaFuncSetAttribute(k_bp_argmin_rest<LEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    int per_sm_a = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_a, k_bp_argmin<LEN>, T, smem_a);
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bp_argmin_rest<LEN>, T, smem);
     if (e != cudaSuccess) return e;
-    if (per_sm_a < 1) return cudaErrorInvalidConfiguration;
-    // short-lived CTAs of a few nodes each (rather than one persistent wave), so
-    // that a higher-priority sweep's CTAs get SMs as these retire
-    int ctas_a = (t.sz + 3) / 4;
-    if (ctas_a < per_sm_a * sm_count) ctas_a = per_sm_a * sm_count;
-    if (ctas_a > t.sz) ctas_a = t.sz;
-    k_bp_argmin<LEN><<<ctas_a, T, smem_a, s>>>(t, pre, off, allinds);
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    int ctas = per_sm * sm_count;
+    if (ctas > t.sz) ctas = t.sz;
+    k_bp_argmin_rest<LEN><<<ctas, T, smem, s>>>(t, pre, off, work, done, allinds, err);
     count_launches(1);
     return cudaGetLastError();
 }
@@ -672,42 +736,43 @@ cudaError_t launch_argmin(const BpTree& t, short* allinds, const float* pre, con
 }  // namespace
 
 cudaError_t launch_bp_up(const BpTree& t, float* d_cost, short* d_allinds, float* d_pre, float* d_mins, int* d_arrived,
-                         int* d_work, int sm_count, cudaStream_t s) {
+                         int* d_work, int* d_done, int* d_err, int sm_count, cudaStream_t s) {
     if (t.n_leaves <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(d_arrived, 0, sizeof(int) * (size_t)t.sz, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(d_work, 0, sizeof(int), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_work, 0, 3 * sizeof(int), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_done, 0xff, sizeof(int) * (size_t)t.sz, s);  // -1: not written
     if (e != cudaSuccess) return e;
     switch (t.len) {
-        case 1: return launch_up<1>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
-        case 3: return launch_up<3>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
-        case 5: return launch_up<5>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
-        case 7: return launch_up<7>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
-        case 9: return launch_up<9>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
-        case 11: return launch_up<11>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
-        case 13: return launch_up<13>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
-        case 15: return launch_up<15>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
-        case 17: return launch_up<17>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
-        case 19: return launch_up<19>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
-        case 21: return launch_up<21>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, sm_count, s);
+        case 1: return launch_up<1>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, s);
+        case 3: return launch_up<3>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, s);
+        case 5: return launch_up<5>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, s);
+        case 7: return launch_up<7>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, s);
+        case 9: return launch_up<9>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, s);
+        case 11: return launch_up<11>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, s);
+        case 13: return launch_up<13>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, s);
+        case 15: return launch_up<15>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, s);
+        case 17: return launch_up<17>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, s);
+        case 19: return launch_up<19>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, s);
+        case 21: return launch_up<21>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, s);
         default: return cudaErrorInvalidValue;
     }
 }
 
-cudaError_t launch_bp_argmin(const BpTree& t, short* d_allinds, const float* d_pre, const float* d_mins, int sm_count,
-                             cudaStream_t s) {
+cudaError_t launch_bp_argmin(const BpTree& t, short* d_allinds, const float* d_pre, const float* d_mins, int* d_work,
+                             int* d_done, int* d_err, int sm_count, cudaStream_t s) {
     if (t.n_leaves <= 0) return cudaSuccess;
     switch (t.len) {
-        case 1: return launch_argmin<1>(t, d_allinds, d_pre, d_mins, sm_count, s);
-        case 3: return launch_argmin<3>(t, d_allinds, d_pre, d_mins, sm_count, s);
-        case 5: return launch_argmin<5>(t, d_allinds, d_pre, d_mins, sm_count, s);
-        case 7: return launch_argmin<7>(t, d_allinds, d_pre, d_mins, sm_count, s);
-        case 9: return launch_argmin<9>(t, d_allinds, d_pre, d_mins, sm_count, s);
-        case 11: return launch_argmin<11>(t, d_allinds, d_pre, d_mins, sm_count, s);
-        case 13: return launch_argmin<13>(t, d_allinds, d_pre, d_mins, sm_count, s);
-        case 15: return launch_argmin<15>(t, d_allinds, d_pre, d_mins, sm_count, s);
-        case 17: return launch_argmin<17>(t, d_allinds, d_pre, d_mins, sm_count, s);
-        case 19: return launch_argmin<19>(t, d_allinds, d_pre, d_mins, sm_count, s);
-        case 21: return launch_argmin<21>(t, d_allinds, d_pre, d_mins, sm_count, s);
+        case 1: return launch_argmin<1>(t, d_allinds, d_pre, d_mins, d_work, d_done, d_err, sm_count, s);
+        case 3: return launch_argmin<3>(t, d_allinds, d_pre, d_mins, d_work, d_done, d_err, sm_count, s);
+        case 5: return launch_argmin<5>(t, d_allinds, d_pre, d_mins, d_work, d_done, d_err, sm_count, s);
+        case 7: return launch_argmin<7>(t, d_allinds, d_pre, d_mins, d_work, d_done, d_err, sm_count, s);
+        case 9: return launch_argmin<9>(t, d_allinds, d_pre, d_mins, d_work, d_done, d_err, sm_count, s);
+        case 11: return launch_argmin<11>(t, d_allinds, d_pre, d_mins, d_work, d_done, d_err, sm_count, s);
+        case 13: return launch_argmin<13>(t, d_allinds, d_pre, d_mins, d_work, d_done, d_err, sm_count, s);
+        case 15: return launch_argmin<15>(t, d_allinds, d_pre, d_mins, d_work, d_done, d_err, sm_count, s);
+        case 17: return launch_argmin<17>(t, d_allinds, d_pre, d_mins, d_work, d_done, d_err, sm_count, s);
+        case 19: return launch_argmin<19>(t, d_allinds, d_pre, d_mins, d_work, d_done, d_err, sm_count, s);
+        case 21: return launch_argmin<21>(t, d_allinds, d_pre, d_mins, d_work, d_done, d_err, sm_count, s);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -65,11 +65,13 @@ cudaError_t launch_image_stats(const float* im0, const float* im1, int nimg, siz
                                cudaStream_t s);
 // d_mins: 4 * t.sz floats (per-node message minima, then the x | y | z edge offsets);
 // d_pre: t.sz * len^3 floats (each node's scaled row, the transform's input)
+// d_work: 3 ints; d_done: t.sz ints (list of finished nodes); d_err: error word (4: a bounded wait expired).
+// The sweep's idle CTAs compute the argmin tables of finished nodes.
 cudaError_t launch_bp_up(const BpTree& t, float* d_cost, short* d_allinds, float* d_pre, float* d_mins, int* d_arrived,
-                         int* d_work, int sm_count, cudaStream_t s);
-// the argmin tables (allinds) of every node from the sweep's stored rows (after launch_bp_up)
-cudaError_t launch_bp_argmin(const BpTree& t, short* d_allinds, const float* d_pre, const float* d_mins, int sm_count,
-                             cudaStream_t s);
+                         int* d_work, int* d_done, int* d_err, int sm_count, cudaStream_t s);
+// the argmin tables (allinds) of the nodes the sweep left, from its stored rows (after launch_bp_up)
+cudaError_t launch_bp_argmin(const BpTree& t, short* d_allinds, const float* d_pre, const float* d_mins, int* d_work,
+                             int* d_done, int* d_err, int sm_count, cudaStream_t s);
 // d_queue: t.n_chains 64-bit words of scratch (chains ready to walk)
 cudaError_t launch_bp_down(const BpTree& t, const float* d_cost, short* d_allinds, float* d_u1, float* d_v1,
                            float* d_w1, unsigned long long* d_queue, int* d_err, cudaStream_t s);

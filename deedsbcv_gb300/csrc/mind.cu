@@ -202,8 +202,9 @@ static void mind_passes(const float* d_im, int m, int n, int o, float* d_scratch
     const size_t smem = (size_t)(2 * (TJ + 2 * QS) * (CH + 2 * QS + 1) + 6 * TJ * (CH + 1)) * sizeof(float);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_pass_i<QS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_pass_i<QS><<<dim3((n + TJ - 1) / TJ, o), 6 * TJ, smem, s>>>(d_im, d_scratch, m, n, o);
-    k_pass_jk<QS><<<dim3((m + 127) / 128, o, 6), 128, 0, s>>>(d_scratch, m, n, o, 1);
-    k_pass_jk<QS><<<dim3((m + 127) / 128, n, 6), 128, 0, s>>>(d_scratch, m, n, o, 2);
+    // 64 i per block: the usual volume extents are multiples of 64, so no lane idles
+    k_pass_jk<QS><<<dim3((m + 63) / 64, o, 6), 64, 0, s>>>(d_scratch, m, n, o, 1);
+    k_pass_jk<QS><<<dim3((m + 63) / 64, n, 6), 64, 0, s>>>(d_scratch, m, n, o, 2);
 }
 
 cudaError_t launch_mind_ssc(const float* d_im, int m, int n, int o, int qs, const float thr[5], float* d_scratch,
@@ -219,7 +220,7 @@ cudaError_t launch_mind_ssc(const float* d_im, int m, int n, int o, int qs, cons
         default: return cudaErrorInvalidValue;
     }
     {
-        dim3 blk(128), grd((m + 127) / 128, n, o);
+        dim3 blk(64), grd((m + 63) / 64, n, o);
         k_quantise<<<grd, blk, 0, s>>>(d_scratch, d_codes, m, n, o, qs, thr[0], thr[1], thr[2], thr[3], thr[4]);
     }
     count_launches(4);

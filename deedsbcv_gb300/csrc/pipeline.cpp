@@ -418,7 +418,8 @@ deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTre
     uint32_t* d_blk = dbuf<uint32_t>(ctx, "tree_" + tag, pt.total, &st);
     float* d_mins = dbuf<float>(ctx, "mins_" + tag, 4 * (size_t)pt.sz, &st);  // mins | edge offsets x, y, z
     int* d_arrived = dbuf<int>(ctx, "arrived_" + tag, pt.sz, &st);
-    int* d_work = dbuf<int>(ctx, "work_" + tag, 1, &st);
+    int* d_work = dbuf<int>(ctx, "work_" + tag, 3, &st);
+    int* d_done = dbuf<int>(ctx, "done_" + tag, pt.sz, &st);
     unsigned long long* d_queue = dbuf<unsigned long long>(ctx, "queue_" + tag, pt.sz, &st);
     float* d_pre = dbuf<float>(ctx, "pre_" + tag, (size_t)pt.sz * len * len * len, &st);
     if (st) return st;
@@ -426,7 +427,7 @@ deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTre
     const BpTree bt = device_tree(pt, d_blk, h_blk, len, (float)q, u0, v0, w0);
     {
         StageScope sc(ctx, DEEDS_STAGE_BP_UP, s);
-        CK(launch_bp_up(bt, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, ctx->sm_count, s));
+        CK(launch_bp_up(bt, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, ctx->sm_count, s));
     }
     {
         // the argmin tables on the direction's low-priority stream, joined back before
@@ -436,7 +437,7 @@ deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTre
         CK(cudaStreamWaitEvent(ctx->low[dl], ctx->ev_up[dl], 0));
         {
             StageScope sc(ctx, DEEDS_STAGE_BP_ARGMIN, ctx->low[dl]);
-            CK(launch_bp_argmin(bt, d_allinds, d_pre, d_mins, ctx->sm_count, ctx->low[dl]));
+            CK(launch_bp_argmin(bt, d_allinds, d_pre, d_mins, d_work, d_done, d_err, ctx->sm_count, ctx->low[dl]));
         }
         CK(cudaEventRecord(ctx->ev_arg[dl], ctx->low[dl]));
         CK(cudaStreamWaitEvent(s, ctx->ev_arg[dl], 0));
@@ -515,7 +516,8 @@ deeds_status acquire_buffers(deeds_ctx* ctx, int m, int n, int o, const deeds_pa
         dbuf<uint32_t>(ctx, "tree_" + tg, pack_layout((int)B.max_sz1).total, &st);
         dbuf<float>(ctx, "mins_" + tg, 4 * B.max_sz1, &st);
         dbuf<int>(ctx, "arrived_" + tg, B.max_sz1, &st);
-        dbuf<int>(ctx, "work_" + tg, 1, &st);
+        dbuf<int>(ctx, "work_" + tg, 3, &st);
+        dbuf<int>(ctx, "done_" + tg, B.max_sz1, &st);
         dbuf<unsigned long long>(ctx, "queue_" + tg, B.max_sz1, &st);
         dbuf<float>(ctx, "pre_" + tg, B.max_cost, &st);  // scaled rows of the upward sweep (argmin input)
     }
