@@ -591,14 +591,16 @@ __global__ void __launch_bounds__(1024) k_bp_down(BpTree t, const float* __restr
         // branch chains one ahead: the id a step prefetches for, and the range a step
         // queues from, were loaded a step earlier, so neither the prefetch, the
         // gather nor the queueing waits for an id load; the argmin rows are
-        // prefetched into L2 two nodes ahead.  A node's first branch chain ids are
-        // loaded before its gather.
+        // prefetched into L2 two nodes ahead (into L1 as well was slower: 1.73 ->
+        // 1.96 ms at grid 4).  A node's first branch chain ids are loaded before
+        // its gather.
         auto node_at = [&](int k) { return k < e ? ld_ahead(t.chain_nodes + k) : -1; };
         auto prefetch_row = [&](int v) {
             if (v < 0) return;
             const char* a = reinterpret_cast<const char*>(allinds + (int64_t)v * len3);
             for (int k = 0; k < row_lines; k++) asm volatile("prefetch.global.L2 [%0];" ::"l"(a + 128 * k));
         };
+
         int cur = node_at(i), n1 = node_at(i + 1), n2 = node_at(i + 2);
         int cb0 = 0, cb1 = 0, nb0 = 0, nb1 = 0;
         if (cur >= 0) { cb0 = ld_ahead(t.branch_ptr + cur); cb1 = ld_ahead(t.branch_ptr + cur + 1); }

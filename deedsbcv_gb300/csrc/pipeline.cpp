@@ -990,21 +990,28 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
             cudaStream_t sdd = sd[d];
             float** pv = prev + 3 * d;
             float** c0 = cur0 + 3 * d;
+            // At the first level the forward field is zero, and warpAffine with the
+            // upsampled zero field adds +0 to the same coordinates as the affine-only
+            // warp: the warped moving image is warp0 bit for bit, and its codes are
+            // the level's field-independent ones (c_mov), so they are not recomputed.
+            const bool reuse = l == 0 && d == 0;
             {
                 StageScope sc(ctx, DEEDS_STAGE_TRANSFORM, sdd);
                 CK(launch_upsample(pv[0], pv[1], pv[2], m2, n2, o2, c0[0], c0[1], c0[2], m1, n1, o1, sdd));
                 FieldRef f{2, c0[0], c0[1], c0[2], m1, n1, o1};
-                if (d == 0) CK(launch_warp_affine(mov, X, f, m, n, o, warped[d], nullptr, nullptr, nullptr, sdd));
-                else CK(launch_warp_image(fix, f, m, n, o, warped[d], sdd));
+                if (d == 0 && !reuse)
+                    CK(launch_warp_affine(mov, X, f, m, n, o, warped[d], nullptr, nullptr, nullptr, sdd));
+                else if (d == 1)
+                    CK(launch_warp_image(fix, f, m, n, o, warped[d], sdd));
             }
-            {
+            if (!reuse) {
                 StageScope sc(ctx, DEEDS_STAGE_MIND, sdd);
                 CK(launch_mind_ssc(warped[d], m, n, o, qs, thr, mind_scr[d], c_warp[d], sdd));
             }
             {
                 StageScope sc(ctx, DEEDS_STAGE_DATACOST, sdd);
-                CK(data_cost_auto(ctx, d == 0 ? c_fix : c_mov, c_warp[d], mpad[d], m, n, o, g, hw, q, P->alpha,
-                                  cost[d], d_err + d, sdd));
+                CK(data_cost_auto(ctx, d == 0 ? c_fix : c_mov, reuse ? c_mov : c_warp[d], mpad[d], m, n, o, g, hw, q,
+                                  P->alpha, cost[d], d_err + d, sdd));
             }
         }
         if (l == 0 && B.steps.size() > 1) {
