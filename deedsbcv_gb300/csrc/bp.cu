@@ -32,6 +32,8 @@
 // Roofline: dependency bound (tree depth 265-987 per tree at 192x160x256).
 // Algorithmic traffic: one read + one write of the cost volume and one write of
 // the int16 argmin tables per tree.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -481,166 +483,186 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
     }
 }
 
-// The downward pass's queue of chains ready to walk: 64-bit entries (the label
-// of the chain's first node's parent in the high word, the chain id in the low
-// word; all ones = not yet written), exchanged between the threads of the one
-// CTA that runs the pass.  An entry carries all a walker needs, so relaxed
-// CTA-scope accesses suffice.
-__device__ __forceinline__ unsigned long long ld_queue(const unsigned long long* p) {
-    unsigned long long v;
-    asm volatile("ld.relaxed.cta.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+// ---- downward pass (src/regularisation.h:258-293)
+//
+// The root takes the first minimum of its cost row; every other node takes
+// allinds[node][label of its parent].  Nodes are walked along heavy-path chains
+// (from a chain's first node down through the child with the deepest subtree to
+// a leaf), one warp per chain.  A node's label is all that the chains starting at
+// its other children need: its walker publishes it in lbl[node] (-1 until then)
+// and the walker of such a chain waits for that entry.  Chains are numbered in
+// breadth order of their starts and taken by ticket in that order, so the chain
+// holding a waited-for node was taken earlier by a running warp and every wait
+// ends.  Ticket 0 is the root's chain (the longest root-leaf path): its warp
+// first takes the root's label.
+//
+// A step's only dependency is the gather allinds[node][label of the node above].
+// The warp copies the whole argmin rows of the next D nodes of its chain into a
+// shared-memory ring with cp.async (a row's contents do not depend on labels), so
+// the gather reads shared memory and a chain advances at about one shared-memory
+// round trip per node instead of one L2 or HBM round trip.  Rows start at 2-byte
+// offsets: a row's copy covers the 16-byte-aligned span around it, and the last
+// chunk of the table is zero-filled past its end, so nothing outside the table is
+// read.  Node ids and u0/v0/w0 are loaded 32 nodes at a time, a window ahead.
+// Waits are bounded (error 4 on expiry; the other walkers see the abort flag); a
+// label or table entry out of range records error 2 and reads label 0 instead.
+constexpr long long kDownSpinLimit = 1LL << 22;  // polls of a 32 ns sleep: > 0.13 s, far beyond a pass
+constexpr int kDownWarps = 4;                    // walkers per CTA
+
+__device__ __forceinline__ int ld_label(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ void st_queue(unsigned long long* p, unsigned long long v) {
-    asm volatile("st.relaxed.cta.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+// 16-byte cp.async (L2 only); src_bytes < 16 zero-fills the rest of the chunk
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, int src_bytes) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(src_bytes) : "memory");
 }
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-constexpr long long kDownSpinLimit = 1LL << 21;  // polls of a 64 ns sleep: ~0.13 s, far beyond a pass
-constexpr unsigned long long kQueueEmpty = ~0ull;
+// Bytes of one ring slot: the widest 16-byte-aligned span of a row.
+__host__ __device__ constexpr int down_slot_bytes(int len3) { return ((len3 * 2 + 15) / 16 + 1) * 16; }
 
-// Root argmin (first minimum), then the backtrack (src/regularisation.h:258-293)
-// over heavy-path chains (from a chain's first node down through the child with
-// the deepest subtree to a leaf).  The reference resolves one breadth level
-// after another; here a thread walks a whole chain, one argmin-table gather per
-// node with no barrier in between, and at every node it queues the chains that
-// start at the node's other children together with the node's label.  Threads
-// take queue slots by ticket (slot k holds the k-th chain queued; every chain is
-// queued exactly once), so a thread only ever waits for a chain that some walker
-// is about to queue, and the longest root-leaf path (chain 0) is walked without
-// waiting: the pass costs about one gather latency per node of that path.  Each
-// walker prefetches its argmin rows two nodes ahead into L2.  Waits are bounded
-// (error 4 on expiry); a label or a table entry out of range records error 2 and
-// reads label 0 instead.
-__global__ void __launch_bounds__(1024) k_bp_down(BpTree t, const float* __restrict__ cost,
-                                                 short* __restrict__ allinds, float* __restrict__ u1,
-                                                 float* __restrict__ v1, float* __restrict__ w1,
-                                                 unsigned long long* queue, int* __restrict__ err) {
-    __shared__ float s_val[32];
-    __shared__ int s_idx[32];
-    __shared__ int s_head, s_tail, s_abort;
+// lbl: [sz] labels (-1 = not yet known); ctl[0]: tickets handed out, ctl[1]: abort flag.
+template <int D>
+__global__ void __launch_bounds__(32 * kDownWarps) k_bp_down(BpTree t, const float* __restrict__ cost,
+                                                            short* __restrict__ allinds, float* __restrict__ u1,
+                                                            float* __restrict__ v1, float* __restrict__ w1,
+                                                            int* __restrict__ lbl, int* __restrict__ ctl,
+                                                            int* __restrict__ err) {
+    static_assert(D >= 1 && D <= 16 && (D & (D - 1)) == 0, "ring depth: a power of two, at most half a window");
+    extern __shared__ __align__(16) unsigned char down_smem[];
     const int len = t.len, len3 = len * len * len, hw = (len - 1) / 2;
-    const int root = t.root;
-    const float* rr = cost + (int64_t)root * len3;
-    float bv = INFINITY;
-    int bi = 0x7fffffff;
-    for (int l = threadIdx.x; l < len3; l += blockDim.x) {
-        const float v = __ldcg(rr + l);
-        if (v < bv || (v == bv && l < bi)) { bv = v; bi = l; }
-        allinds[(int64_t)root * len3 + l] = (short)l;
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-        if (ov < bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
-    }
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0) { s_val[w] = bv; s_idx[w] = bi; }
-    __syncthreads();
-    if (w == 0) {
-        bv = lane < (int)(blockDim.x >> 5) ? s_val[lane] : INFINITY;
-        bi = lane < (int)(blockDim.x >> 5) ? s_idx[lane] : 0x7fffffff;
-        for (int o = 16; o > 0; o >>= 1) {
-            const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
-            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-            if (ov < bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int slot_bytes = down_slot_bytes(len3);
+    unsigned char* ring = down_smem + (size_t)wid * D * slot_bytes;
+    const char* table = reinterpret_cast<const char*>(allinds);
+    const long long table_bytes = (long long)t.sz * len3 * 2;
+    const float q = t.q;
+    // copies the argmin row of node nd into ring slot s (nothing for nd < 0); one commit group per call
+    auto fetch = [&](int nd, int s) {
+        if (nd >= 0) {
+            const long long a = (long long)nd * len3 * 2, a0 = a & ~15LL, e = a + 2LL * len3;
+            const int nch = (int)((e - a0 + 15) >> 4);
+            unsigned char* dst = ring + s * slot_bytes;
+            for (int c = lane; c < nch; c += 32) {
+                const long long g = a0 + 16LL * c;
+                const long long left = table_bytes - g;
+                cp_async16(dst + 16 * c, table + g, left < 16 ? (int)left : 16);
+            }
         }
-        if (lane == 0) {
-            // the reference scans with value=cost[0], index=0 and '<' (src/regularisation.h:258-279):
-            // a NaN at 0 keeps index 0, NaNs elsewhere never win
-            if (isnan(__ldcg(rr)) || bi < 0 || bi >= len3) bi = 0;
-            const int i = bi % len, j = (bi / len) % len, k = bi / (len * len);
-            u1[root] = (float)(j - hw) * t.q + t.u0[root];
-            v1[root] = (float)(i - hw) * t.q + t.v0[root];
-            w1[root] = (float)(k - hw) * t.q + t.w0[root];
-            st_queue(queue, (unsigned long long)(unsigned)bi << 32);  // chain 0 starts at the root
-            s_head = 0;
-            s_tail = 1;
-            s_abort = 0;
-        }
-    }
-    __syncthreads();
-    const int row_lines = (len3 * 2 + 127) / 128;
-    auto enqueue = [&](int node, int label) {
-        for (int b = t.branch_ptr[node]; b < t.branch_ptr[node + 1]; b++) {
-            const int slot = atomicAdd(&s_tail, 1);
-            st_queue(queue + slot, (unsigned long long)(unsigned)label << 32 | (unsigned)t.branch_chain[b]);
-        }
+        cp_async_commit();
     };
     for (;;) {
-        const int ticket = atomicAdd(&s_head, 1);
-        if (ticket >= t.n_chains) return;
-        unsigned long long q;
-        long long it = 0;
-        while ((q = ld_queue(queue + ticket)) == kQueueEmpty) {  // queued, or about to be
-            if (++it > kDownSpinLimit || *(volatile int*)&s_abort) {
-                atomicCAS(err, 0, 4);
-                *(volatile int*)&s_abort = 1;
-                return;
-            }
-            __nanosleep(64);
-        }
-        const int c = (int)(q & 0xffffffffull);
-        int lp = (int)(q >> 32);
-        int i = t.chain_ptr[c];
-        const int e = t.chain_ptr[c + 1];
-        if (t.chain_nodes[i] == root) {  // chain 0: the root's label is lp; queue its other children's chains
-            enqueue(root, lp);
-            i++;
-        }
-        // The chain's node ids run three ahead of the walk and each node's range of
-        // branch chains one ahead: the id a step prefetches for, and the range a step
-        // queues from, were loaded a step earlier, so neither the prefetch, the
-        // gather nor the queueing waits for an id load; the argmin rows are
-        // prefetched into L2 two nodes ahead (into L1 as well was slower: 1.73 ->
-        // 1.96 ms at grid 4).  A node's first branch chain ids are loaded before
-        // its gather.
-        auto node_at = [&](int k) { return k < e ? ld_ahead(t.chain_nodes + k) : -1; };
-        auto prefetch_row = [&](int v) {
-            if (v < 0) return;
-            const char* a = reinterpret_cast<const char*>(allinds + (int64_t)v * len3);
-            for (int k = 0; k < row_lines; k++) asm volatile("prefetch.global.L2 [%0];" ::"l"(a + 128 * k));
-        };
-
-        int cur = node_at(i), n1 = node_at(i + 1), n2 = node_at(i + 2);
-        int cb0 = 0, cb1 = 0, nb0 = 0, nb1 = 0;
-        if (cur >= 0) { cb0 = ld_ahead(t.branch_ptr + cur); cb1 = ld_ahead(t.branch_ptr + cur + 1); }
-        if (n1 >= 0) { nb0 = ld_ahead(t.branch_ptr + n1); nb1 = ld_ahead(t.branch_ptr + n1 + 1); }
-        prefetch_row(n1);
-        while (cur >= 0) {
-            const int node = cur;
-            const int b0 = cb0, b1 = cb1;
-            const int n3 = node_at(i + 3);
-            prefetch_row(n2);
-            cb0 = nb0; cb1 = nb1;
-            if (n2 >= 0) { nb0 = ld_ahead(t.branch_ptr + n2); nb1 = ld_ahead(t.branch_ptr + n2 + 1); }
-            cur = n1; n1 = n2; n2 = n3;
-            constexpr int kBr = 4;  // branch chain ids held in registers (more are read in the loop)
-            int br[kBr];
+        int tk = 0;
+        if (lane == 0) tk = atomicAdd(ctl, 1);
+        const int c = __shfl_sync(0xffffffffu, tk, 0);
+        if (c >= t.n_chains) break;
+        const int s0 = ld_ahead(t.chain_ptr + c), n = ld_ahead(t.chain_ptr + c + 1) - s0;
+        // node ids: lane j of w_node holds node s0 + 32 W + j of the current window W,
+        // x_node the next window's; x_u/x_v/x_w are loaded half a window later
+        int w_node = lane < n ? ld_ahead(t.chain_nodes + s0 + lane) : -1;
+        int x_node = 32 + lane < n ? ld_ahead(t.chain_nodes + s0 + 32 + lane) : -1;
+        float w_u = 0.0f, w_v = 0.0f, w_w = 0.0f, x_u = 0.0f, x_v = 0.0f, x_w = 0.0f;
+        if (w_node >= 0) { w_u = ld_ahead(t.u0 + w_node); w_v = ld_ahead(t.v0 + w_node); w_w = ld_ahead(t.w0 + w_node); }
+        const int first = __shfl_sync(0xffffffffu, w_node, 0);
+        const bool root_chain = first == t.root;
 #pragma unroll
-            for (int k = 0; k < kBr; k++) br[k] = b0 + k < b1 ? ld_ahead(t.branch_chain + b0 + k) : -1;
-            const float a0 = t.u0[node], a1 = t.v0[node], a2 = t.w0[node];
-            if (lp < 0 || lp >= len3) {  // never for a completed upward pass; keeps reads in bounds
-                atomicCAS(err, 0, 2);
-                lp = 0;
+        for (int k = 0; k < D; k++) {
+            const int nd = __shfl_sync(0xffffffffu, w_node, k);
+            fetch(k < n && !(root_chain && k == 0) ? nd : -1, k);
+        }
+        int lp;  // label of the node above the next one
+        if (root_chain) {
+            // first minimum of the root's cost row; the reference scans with value=cost[0],
+            // index=0 and '<' (src/regularisation.h:258-279): a NaN at 0 keeps index 0, NaNs
+            // elsewhere never win
+            const float* rr = cost + (int64_t)first * len3;
+            float bv = INFINITY;
+            int bi = 0x7fffffff;
+            for (int l = lane; l < len3; l += 32) {
+                const float v = __ldcg(rr + l);
+                if (v < bv) { bv = v; bi = l; }
+                allinds[(int64_t)first * len3 + l] = (short)l;
             }
-            int l = allinds[(int64_t)node * len3 + lp];
-            if (l < 0 || l >= len3) {  // never for a completed upward pass; keeps reads in bounds
-                atomicCAS(err, 0, 2);
-                l = 0;
+            for (int o = 16; o > 0; o >>= 1) {
+                const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ov < bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
             }
-            const unsigned long long hi = (unsigned long long)(unsigned)l << 32;
-#pragma unroll
-            for (int k = 0; k < kBr; k++)
-                if (br[k] >= 0) st_queue(queue + atomicAdd(&s_tail, 1), hi | (unsigned)br[k]);
-            for (int b = b0 + kBr; b < b1; b++) st_queue(queue + atomicAdd(&s_tail, 1), hi | (unsigned)t.branch_chain[b]);
-            const int ii = l % len, jj = (l / len) % len, kk = l / (len * len);
-            u1[node] = (float)(jj - hw) * t.q + a0;
-            v1[node] = (float)(ii - hw) * t.q + a1;
-            w1[node] = (float)(kk - hw) * t.q + a2;
+            if (isnan(__ldcg(rr)) || bi < 0 || bi >= len3) bi = 0;
+            lp = bi;
+        } else {
+            const int p = ld_ahead(t.parents + first);
+            int v = -1;
+            if (lane == 0) {
+                long long it = 0;
+                while ((v = ld_label(lbl + p)) < 0) {
+                    if (++it > kDownSpinLimit || ld_label(ctl + 1) != 0) break;
+                    __nanosleep(32);
+                }
+            }
+            v = __shfl_sync(0xffffffffu, v, 0);
+            if (v < 0) {
+                if (lane == 0) {
+                    atomicCAS(err, 0, 4);
+                    st_relaxed_gpu(ctl + 1, 1);
+                }
+                break;
+            }
+            lp = v;
+        }
+        for (int k = 0; k < n; k++) {
+            if (k > 0 && (k & 31) == 0) {  // next window
+                w_node = x_node; w_u = x_u; w_v = x_v; w_w = x_w;
+                x_node = k + 32 + lane < n ? ld_ahead(t.chain_nodes + s0 + k + 32 + lane) : -1;
+            }
+            if ((k & 31) == 16 && x_node >= 0) {  // the next window's ids were loaded 16 steps ago
+                x_u = ld_ahead(t.u0 + x_node); x_v = ld_ahead(t.v0 + x_node); x_w = ld_ahead(t.w0 + x_node);
+            }
+            const int nd = __shfl_sync(0xffffffffu, w_node, k & 31);
+            const float a0 = __shfl_sync(0xffffffffu, w_u, k & 31);
+            const float a1 = __shfl_sync(0xffffffffu, w_v, k & 31);
+            const float a2 = __shfl_sync(0xffffffffu, w_w, k & 31);
+            cp_async_wait<D - 1>();  // this lane's chunks of row k have landed
+            __syncwarp();            // and every lane's
+            int l = lp;
+            if (!(root_chain && k == 0)) {
+                if (lp < 0 || lp >= len3) {  // never for a completed upward pass; keeps reads in bounds
+                    if (lane == 0) atomicCAS(err, 0, 2);
+                    lp = 0;
+                }
+                const unsigned char* row = ring + (k & (D - 1)) * slot_bytes + (int)(((long long)nd * len3 * 2) & 15);
+                l = reinterpret_cast<const short*>(row)[lp];
+                if (l < 0 || l >= len3) {  // never for a completed upward pass
+                    if (lane == 0) atomicCAS(err, 0, 2);
+                    l = 0;
+                }
+            }
+            __syncwarp();  // every lane has read the slot before it is refilled
+            if (lane == 0) st_relaxed_gpu(lbl + nd, l);
+            {
+                const int kn = k + D;
+                const int a = __shfl_sync(0xffffffffu, w_node, kn & 31);
+                const int b = __shfl_sync(0xffffffffu, x_node, kn & 31);
+                fetch(kn < n ? ((kn >> 5) == (k >> 5) ? a : b) : -1, kn & (D - 1));
+            }
+            if (lane == 0) {
+                const int ii = l % len, jj = (l / len) % len, kk = l / (len * len);
+                u1[nd] = (float)(jj - hw) * q + a0;
+                v1[nd] = (float)(ii - hw) * q + a1;
+                w1[nd] = (float)(kk - hw) * q + a2;
+            }
             lp = l;
-            i++;
         }
     }
+    cp_async_wait_all();  // no copy outlives the CTA
 }
 
 // Per node the offset of its edge in label units, (u0[parent] - u0[node]) / q
@@ -779,15 +801,40 @@ cudaError_t launch_bp_argmin(const BpTree& t, short* d_allinds, const float* d_p
     }
 }
 
-cudaError_t launch_bp_down(const BpTree& t, const float* d_cost, short* d_allinds, float* d_u1, float* d_v1,
-                           float* d_w1, unsigned long long* d_queue, int* d_err, cudaStream_t s) {
-    if (t.n_chains < 1 || !t.chain_ptr || !t.chain_nodes || !t.branch_ptr || !t.branch_chain)
-        return cudaErrorInvalidValue;
-    cudaError_t e = cudaMemsetAsync(d_queue, 0xff, sizeof(unsigned long long) * (size_t)t.n_chains, s);  // empty
+template <int D>
+static cudaError_t launch_down(const BpTree& t, const float* d_cost, short* d_allinds, float* d_u1, float* d_v1,
+                               float* d_w1, int* d_lbl, int* d_err, int sm_count, cudaStream_t s) {
+    const int len3 = t.len * t.len * t.len;
+    const size_t smem = (size_t)kDownWarps * D * down_slot_bytes(len3);
+    cudaError_t e = cudaFuncSetAttribute(k_bp_down<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_bp_down<<<1, 1024, 0, s>>>(t, d_cost, d_allinds, d_u1, d_v1, d_w1, d_queue, d_err);
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bp_down<D>, 32 * kDownWarps, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    // every CTA resident at once; no more walkers than chains
+    const int ctas = std::max(1, std::min(per_sm * sm_count, (t.n_chains + kDownWarps - 1) / kDownWarps));
+    // labels unknown (-1), ticket counter 0, abort flag 0
+    e = cudaMemsetAsync(d_lbl, 0xff, sizeof(int) * (size_t)t.sz, s);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(d_lbl + t.sz, 0, 2 * sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    k_bp_down<D><<<ctas, 32 * kDownWarps, smem, s>>>(t, d_cost, d_allinds, d_u1, d_v1, d_w1, d_lbl, d_lbl + t.sz,
+                                                     d_err);
     count_launches(1);
     return cudaGetLastError();
+}
+
+cudaError_t launch_bp_down(const BpTree& t, const float* d_cost, short* d_allinds, float* d_u1, float* d_v1,
+                           float* d_w1, int* d_lbl, int* d_err, int sm_count, cudaStream_t s) {
+    if (t.n_chains < 1 || !t.chain_ptr || !t.chain_nodes || sm_count < 1) return cudaErrorInvalidValue;
+    // the rows are copied in 16-byte chunks from a 16-byte-aligned table
+    if (reinterpret_cast<uintptr_t>(d_allinds) & 15) return cudaErrorInvalidValue;
+    const int slot = down_slot_bytes(t.len * t.len * t.len);
+    // ring depth by row size: at most ~200 KB of shared memory per CTA
+    if (slot <= 3072) return launch_down<8>(t, d_cost, d_allinds, d_u1, d_v1, d_w1, d_lbl, d_err, sm_count, s);
+    if (slot <= 12288) return launch_down<4>(t, d_cost, d_allinds, d_u1, d_v1, d_w1, d_lbl, d_err, sm_count, s);
+    return launch_down<2>(t, d_cost, d_allinds, d_u1, d_v1, d_w1, d_lbl, d_err, sm_count, s);
 }
 
 }  // namespace deeds

@@ -72,9 +72,10 @@ cudaError_t launch_bp_up(const BpTree& t, float* d_cost, short* d_allinds, float
 // the argmin tables (allinds) of the nodes the sweep left, from its stored rows (after launch_bp_up)
 cudaError_t launch_bp_argmin(const BpTree& t, short* d_allinds, const float* d_pre, const float* d_mins, int* d_work,
                              int* d_done, int* d_err, int sm_count, cudaStream_t s);
-// d_queue: t.n_chains 64-bit words of scratch (chains ready to walk)
+// d_lbl: t.sz + 2 ints of scratch (the nodes' labels as the walk resolves them, a
+// ticket counter, an abort flag); d_allinds 16-byte aligned
 cudaError_t launch_bp_down(const BpTree& t, const float* d_cost, short* d_allinds, float* d_u1, float* d_v1,
-                           float* d_w1, unsigned long long* d_queue, int* d_err, cudaStream_t s);
+                           float* d_w1, int* d_lbl, int* d_err, int sm_count, cudaStream_t s);
 cudaError_t launch_shift(const float* d_in, float* d_out, int64_t n, float shift, cudaStream_t s);
 cudaError_t launch_upsample(const float* u0, const float* v0, const float* w0, int m2, int n2, int o2, float* u,
                             float* v, float* w, int m, int n, int o, cudaStream_t s);

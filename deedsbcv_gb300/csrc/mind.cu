@@ -27,10 +27,6 @@ constexpr int kRing = 16;  // supports box radius r <= 7 (2r+2 <= 16)
 __constant__ int c_dx[6] = {1, 1, -1, 0, 1, 0};
 __constant__ int c_dy[6] = {1, -1, 0, -1, 0, 1};
 __constant__ int c_dz[6] = {0, 0, 1, 1, 1, 1};
-// The twelve SSC pairs: channel and neighbour offset (src/MINDSSCbox.h:136-140).
-__constant__ int c_sx[12] = {-1, 0, -1, 0, 0, 1, 0, 0, 0, -1, 0, 0};
-__constant__ int c_sy[12] = {0, -1, 0, 1, 0, 0, 0, 1, 0, 0, 0, -1};
-__constant__ int c_sz[12] = {0, 0, 0, 0, -1, 0, -1, 0, -1, 0, -1, 0};
 
 // i-axis pass: CTA = one k slice x TJ consecutive j lines x all 6 channels.
 // The image neighbourhood of an i-chunk (rows j-q..j+TJ+q at k and k+q, i-q..i+CH+q)
@@ -43,6 +39,7 @@ __constant__ int c_sz[12] = {0, 0, 0, 0, -1, 0, -1, 0, -1, 0, -1, 0};
 // tail outputs are emitted at the line's last step for the same reason.
 constexpr int TJ = 32;  // lines per CTA
 constexpr int CH = 32;  // i samples per chunk (a multiple of kRing)
+static_assert(CH == 32 && (6 * TJ) % 32 == 0, "tile rows are stored one lane per sample by whole warps");
 
 template <int QS>
 __global__ void __launch_bounds__(6 * TJ) k_pass_i(const float* __restrict__ im, float* __restrict__ D, int m, int n,
@@ -63,14 +60,22 @@ __global__ void __launch_bounds__(6 * TJ) k_pass_i(const float* __restrict__ im,
     float* gout = D + l * sz + (int64_t)j * m + (int64_t)k * mn;
     float ring[kRing];
     float P = 0.0f;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int kWarps = 6 * TJ / 32;
     for (int i0 = 0; i0 < m; i0 += CH) {
         __syncthreads();  // previous chunk's tiles are consumed
-        for (int e = threadIdx.x; e < 2 * R * WL; e += blockDim.x) {
-            const int ip = e % WL, r = (e / WL) % R, z = e / (WL * R);
-            const int ii = i0 - QS + ip, jr = j0 - QS + r, kz = k + z * QS;
-            float v = 0.0f;
-            if (ii >= 0 && ii < m && jr >= 0 && jr < n && kz < o) v = im[ii + (int64_t)jr * m + (int64_t)kz * mn];
-            T[(z * R + r) * W + ip] = v;
+        // one warp per tile row (no index division): rows of both k planes
+        for (int row = warp; row < 2 * R; row += kWarps) {
+            const int z = row / R, r = row - z * R;
+            const int jr = j0 - QS + r, kz = k + z * QS;
+            const bool row_ok = jr >= 0 && jr < n && kz < o;
+            const float* src = im + (int64_t)jr * m + (int64_t)kz * mn;
+            float* dst = T + row * W;
+#pragma unroll
+            for (int ip = lane; ip < WL; ip += 32) {
+                const int ii = i0 - QS + ip;
+                dst[ip] = (row_ok && ii >= 0 && ii < m) ? src[ii] : 0.0f;
+            }
         }
         __syncthreads();
         const int cend = min(CH, m - i0);
@@ -99,12 +104,13 @@ __global__ void __launch_bounds__(6 * TJ) k_pass_i(const float* __restrict__ im,
             }
         }
         __syncthreads();
-        // coalesced store of outputs i0-QS .. i0+cend-1-QS
-        for (int e = threadIdx.x; e < 6 * TJ * cend; e += blockDim.x) {
-            const int u = e % cend, line = e / cend;
-            const int ll = line / TJ, jl = line % TJ, jg = j0 + jl;
-            const int i = i0 + u - QS;
-            if (i >= 0 && jg < n) D[ll * sz + i + (int64_t)jg * m + (int64_t)k * mn] = O[(ll * TJ + jl) * (CH + 1) + u];
+        // coalesced store of outputs i0-QS .. i0+cend-1-QS: one warp per (channel, line)
+        // row, one lane per sample (CH == 32)
+        for (int line = warp; line < 6 * TJ; line += kWarps) {
+            const int ll = line / TJ, jg = j0 + (line - ll * TJ);
+            const int i = i0 + lane - QS;
+            if (lane < cend && i >= 0 && jg < n)
+                D[ll * sz + i + (int64_t)jg * m + (int64_t)k * mn] = O[line * (CH + 1) + lane];
         }
     }
 }
@@ -150,21 +156,33 @@ __global__ void k_pass_jk(float* __restrict__ D, int m, int n, int o, int axis) 
     }
 }
 
-__global__ void k_quantise(const float* __restrict__ D, uint64_t* __restrict__ codes, int m, int n, int o, int qs,
-                           float t0, float t1, float t2, float t3, float t4) {
+// The twelve SSC pairs (src/MINDSSCbox.h:136-140): pair l compares channel l / 2
+// at the voxel's neighbour QS away along one axis (0: i, 1: j, 2: k) in direction
+// kSign[l]; a neighbour outside the volume reads the voxel itself.  With QS a
+// compile-time constant every offset is a constant multiple of the line and
+// slice strides and each pair needs one bounds test.
+template <int QS>
+__global__ void __launch_bounds__(64) k_quantise(const float* __restrict__ D, uint64_t* __restrict__ codes, int m,
+                                                 int n, int o, float t0, float t1, float t2, float t3, float t4) {
+    constexpr int kAxis[12] = {1, 0, 1, 0, 2, 1, 2, 0, 2, 1, 2, 0};
+    constexpr int kSign[12] = {-1, -1, -1, 1, -1, 1, -1, 1, -1, -1, -1, -1};
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y;
     const int k = blockIdx.z;
     if (i >= m) return;
     const int64_t mn = (int64_t)m * n, sz = mn * o;
     const int64_t p = i + (int64_t)j * m + k * mn;
+    const float* c = D + p;
+    const bool lo_ok[3] = {i >= QS, j >= QS, k >= QS};
+    const bool hi_ok[3] = {i + QS < m, j + QS < n, k + QS < o};
+    const int64_t step[3] = {QS, (int64_t)QS * m, (int64_t)QS * mn};
     float v[12];
 #pragma unroll
     for (int l = 0; l < 12; l++) {
-        const int ii = i + c_sy[l] * qs, jj = j + c_sx[l] * qs, kk = k + c_sz[l] * qs;
-        const float* Dl = D + (l >> 1) * sz;
-        const bool ok = ii >= 0 && ii < m && jj >= 0 && jj < n && kk >= 0 && kk < o;
-        v[l] = __ldg(Dl + (ok ? ii + (int64_t)jj * m + kk * mn : p));
+        const int ax = kAxis[l];
+        const bool ok = kSign[l] < 0 ? lo_ok[ax] : hi_ok[ax];
+        const int64_t off = ok ? (kSign[l] < 0 ? -step[ax] : step[ax]) : 0;
+        v[l] = __ldg(c + (l >> 1) * sz + off);
     }
     float mn_v = v[0];
 #pragma unroll
@@ -198,30 +216,29 @@ __global__ void k_quantise(const float* __restrict__ D, uint64_t* __restrict__ c
 }  // namespace
 
 template <int QS>
-static void mind_passes(const float* d_im, int m, int n, int o, float* d_scratch, cudaStream_t s) {
+static void mind_passes(const float* d_im, int m, int n, int o, const float thr[5], float* d_scratch,
+                        uint64_t* d_codes, cudaStream_t s) {
     const size_t smem = (size_t)(2 * (TJ + 2 * QS) * (CH + 2 * QS + 1) + 6 * TJ * (CH + 1)) * sizeof(float);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_pass_i<QS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_pass_i<QS><<<dim3((n + TJ - 1) / TJ, o), 6 * TJ, smem, s>>>(d_im, d_scratch, m, n, o);
     // 64 i per block: the usual volume extents are multiples of 64, so no lane idles
     k_pass_jk<QS><<<dim3((m + 63) / 64, o, 6), 64, 0, s>>>(d_scratch, m, n, o, 1);
     k_pass_jk<QS><<<dim3((m + 63) / 64, n, 6), 64, 0, s>>>(d_scratch, m, n, o, 2);
+    k_quantise<QS><<<dim3((m + 63) / 64, n, o), 64, 0, s>>>(d_scratch, d_codes, m, n, o, thr[0], thr[1], thr[2],
+                                                            thr[3], thr[4]);
 }
 
 cudaError_t launch_mind_ssc(const float* d_im, int m, int n, int o, int qs, const float thr[5], float* d_scratch,
                             uint64_t* d_codes, cudaStream_t s) {
     switch (qs) {
-        case 1: mind_passes<1>(d_im, m, n, o, d_scratch, s); break;
-        case 2: mind_passes<2>(d_im, m, n, o, d_scratch, s); break;
-        case 3: mind_passes<3>(d_im, m, n, o, d_scratch, s); break;
-        case 4: mind_passes<4>(d_im, m, n, o, d_scratch, s); break;
-        case 5: mind_passes<5>(d_im, m, n, o, d_scratch, s); break;
-        case 6: mind_passes<6>(d_im, m, n, o, d_scratch, s); break;
-        case 7: mind_passes<7>(d_im, m, n, o, d_scratch, s); break;
+        case 1: mind_passes<1>(d_im, m, n, o, thr, d_scratch, d_codes, s); break;
+        case 2: mind_passes<2>(d_im, m, n, o, thr, d_scratch, d_codes, s); break;
+        case 3: mind_passes<3>(d_im, m, n, o, thr, d_scratch, d_codes, s); break;
+        case 4: mind_passes<4>(d_im, m, n, o, thr, d_scratch, d_codes, s); break;
+        case 5: mind_passes<5>(d_im, m, n, o, thr, d_scratch, d_codes, s); break;
+        case 6: mind_passes<6>(d_im, m, n, o, thr, d_scratch, d_codes, s); break;
+        case 7: mind_passes<7>(d_im, m, n, o, thr, d_scratch, d_codes, s); break;
         default: return cudaErrorInvalidValue;
-    }
-    {
-        dim3 blk(64), grd((m + 63) / 64, n, o);
-        k_quantise<<<grd, blk, 0, s>>>(d_scratch, d_codes, m, n, o, qs, thr[0], thr[1], thr[2], thr[3], thr[4]);
     }
     count_launches(4);
     return cudaGetLastError();

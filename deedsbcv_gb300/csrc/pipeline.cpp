@@ -420,7 +420,7 @@ deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTre
     int* d_arrived = dbuf<int>(ctx, "arrived_" + tag, pt.sz, &st);
     int* d_work = dbuf<int>(ctx, "work_" + tag, 3, &st);
     int* d_done = dbuf<int>(ctx, "done_" + tag, pt.sz, &st);
-    unsigned long long* d_queue = dbuf<unsigned long long>(ctx, "queue_" + tag, pt.sz, &st);
+    int* d_lbl = dbuf<int>(ctx, "labels_" + tag, (size_t)pt.sz + 2, &st);
     float* d_pre = dbuf<float>(ctx, "pre_" + tag, (size_t)pt.sz * len * len * len, &st);
     if (st) return st;
     CK(cudaMemcpyAsync(d_blk, h_blk, pt.total * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
@@ -444,7 +444,7 @@ deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTre
     }
     {
         StageScope sc(ctx, DEEDS_STAGE_BP_DOWN, s);
-        CK(launch_bp_down(bt, d_cost, d_allinds, u1, v1, w1, d_queue, d_err, s));
+        CK(launch_bp_down(bt, d_cost, d_allinds, u1, v1, w1, d_lbl, d_err, ctx->sm_count, s));
     }
     return DEEDS_OK;
 }
@@ -518,7 +518,7 @@ deeds_status acquire_buffers(deeds_ctx* ctx, int m, int n, int o, const deeds_pa
         dbuf<int>(ctx, "arrived_" + tg, B.max_sz1, &st);
         dbuf<int>(ctx, "work_" + tg, 3, &st);
         dbuf<int>(ctx, "done_" + tg, B.max_sz1, &st);
-        dbuf<unsigned long long>(ctx, "queue_" + tg, B.max_sz1, &st);
+        dbuf<int>(ctx, "labels_" + tg, B.max_sz1 + 2, &st);
         dbuf<float>(ctx, "pre_" + tg, B.max_cost, &st);  // scaled rows of the upward sweep (argmin input)
     }
     B.grid = dbuf<float>(ctx, "grid", 18 * B.max_sz1, &st);
