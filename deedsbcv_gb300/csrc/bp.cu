@@ -498,12 +498,13 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
 //
 // A step's only dependency is the gather allinds[node][label of the node above].
 // The warp copies the whole argmin rows of the next D nodes of its chain into a
-// shared-memory ring with cp.async (a row's contents do not depend on labels), so
-// the gather reads shared memory and a chain advances at about one shared-memory
-// round trip per node instead of one L2 or HBM round trip.  Rows start at 2-byte
-// offsets: a row's copy covers the 16-byte-aligned span around it, and the last
-// chunk of the table is zero-filled past its end, so nothing outside the table is
-// read.  Node ids and u0/v0/w0 are loaded 32 nodes at a time, a window ahead.
+// shared-memory ring, one bulk copy per row completing on the slot's mbarrier (a
+// row's contents do not depend on labels), so the gather reads shared memory and a
+// chain advances at about one shared-memory round trip per node instead of one L2
+// or HBM round trip.  Rows start at 2-byte offsets: a row's copy covers the
+// 16-byte-aligned span around it, except that the few bytes of the table's last
+// partial 16-byte chunk are copied with plain loads, so nothing outside the table
+// is read.  Node ids and u0/v0/w0 are loaded 32 nodes at a time, a window ahead.
 // Waits are bounded (error 4 on expiry; the other walkers see the abort flag); a
 // label or table entry out of range records error 2 and reads label 0 instead.
 constexpr long long kDownSpinLimit = 1LL << 22;  // polls of a 32 ns sleep: > 0.13 s, far beyond a pass
@@ -514,17 +515,13 @@ __device__ __forceinline__ int ld_label(const int* p) {
     asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
-// 16-byte cp.async (L2 only); src_bytes < 16 zero-fills the rest of the chunk
-__device__ __forceinline__ void cp_async16(void* dst, const void* src, int src_bytes) {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(src_bytes) : "memory");
+// Bulk copy global -> shared memory completing on an mbarrier (16-byte-aligned
+// addresses, a multiple of 16 bytes).
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // Bytes of one ring slot: the widest 16-byte-aligned span of a row.
 __host__ __device__ constexpr int down_slot_bytes(int len3) { return ((len3 * 2 + 15) / 16 + 1) * 16; }
@@ -532,32 +529,53 @@ __host__ __device__ constexpr int down_slot_bytes(int len3) { return ((len3 * 2 
 // lbl: [sz] labels (-1 = not yet known); ctl[0]: tickets handed out, ctl[1]: abort flag.
 template <int D>
 __global__ void __launch_bounds__(32 * kDownWarps) k_bp_down(BpTree t, const float* __restrict__ cost,
-                                                            short* __restrict__ allinds, float* __restrict__ u1,
-                                                            float* __restrict__ v1, float* __restrict__ w1,
-                                                            int* __restrict__ lbl, int* __restrict__ ctl,
-                                                            int* __restrict__ err) {
+                                                            short* __restrict__ allinds, int* __restrict__ lbl,
+                                                            int* __restrict__ ctl, int* __restrict__ err) {
     static_assert(D >= 1 && D <= 16 && (D & (D - 1)) == 0, "ring depth: a power of two, at most half a window");
     extern __shared__ __align__(16) unsigned char down_smem[];
-    const int len = t.len, len3 = len * len * len, hw = (len - 1) / 2;
+    const int len = t.len, len3 = len * len * len;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int slot_bytes = down_slot_bytes(len3);
     unsigned char* ring = down_smem + (size_t)wid * D * slot_bytes;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(down_smem + (size_t)kDownWarps * D * slot_bytes) + wid * D;
     const char* table = reinterpret_cast<const char*>(allinds);
     const long long table_bytes = (long long)t.sz * len3 * 2;
-    const float q = t.q;
-    // copies the argmin row of node nd into ring slot s (nothing for nd < 0); one commit group per call
+    if (lane == 0) {
+        for (int k = 0; k < D; k++) mbar_init(bars + k, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncwarp();
+    // per slot (bit s): the parity of its next phase, and whether a copy into it is
+    // in flight (warp-uniform)
+    uint32_t phase = 0, pending = 0;
+    // copies the argmin row of node nd into ring slot s (nothing for nd < 0)
     auto fetch = [&](int nd, int s) {
-        if (nd >= 0) {
+        if (nd < 0) return;
+        pending |= 1u << s;
+        if (lane == 0) {
             const long long a = (long long)nd * len3 * 2, a0 = a & ~15LL, e = a + 2LL * len3;
-            const int nch = (int)((e - a0 + 15) >> 4);
+            long long bulk = ((e - a0 + 15) >> 4) << 4;
+            if (a0 + bulk > table_bytes) bulk = (table_bytes - a0) & ~15LL;  // the table's last partial chunk
             unsigned char* dst = ring + s * slot_bytes;
-            for (int c = lane; c < nch; c += 32) {
-                const long long g = a0 + 16LL * c;
-                const long long left = table_bytes - g;
-                cp_async16(dst + 16 * c, table + g, left < 16 ? (int)left : 16);
-            }
+            // the slot's earlier contents were read (generic proxy) before this copy
+            // (async proxy) overwrites them
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_expect_tx(bars + s, (uint32_t)bulk);
+            if (bulk > 0) bulk_load(dst, table + a0, (uint32_t)bulk, bars + s);
+            for (long long g = a0 + bulk; g < e; g += 2)
+                *reinterpret_cast<short*>(dst + (g - a0)) = *reinterpret_cast<const short*>(table + g);
         }
-        cp_async_commit();
+    };
+    // waits for the copy into slot s; false if the bounded wait expired
+    auto wait_slot = [&](int s) {
+        const bool ok = mbar_wait_bounded(bars + s, (phase >> s) & 1u);
+        phase ^= 1u << s;
+        pending &= ~(1u << s);
+        return __all_sync(0xffffffffu, ok);
+    };
+    auto drain = [&]() {
+        for (int k = 0; k < D; k++)
+            if (pending & (1u << k)) wait_slot(k);
     };
     for (;;) {
         int tk = 0;
@@ -569,8 +587,6 @@ __global__ void __launch_bounds__(32 * kDownWarps) k_bp_down(BpTree t, const flo
         // x_node the next window's; x_u/x_v/x_w are loaded half a window later
         int w_node = lane < n ? ld_ahead(t.chain_nodes + s0 + lane) : -1;
         int x_node = 32 + lane < n ? ld_ahead(t.chain_nodes + s0 + 32 + lane) : -1;
-        float w_u = 0.0f, w_v = 0.0f, w_w = 0.0f, x_u = 0.0f, x_v = 0.0f, x_w = 0.0f;
-        if (w_node >= 0) { w_u = ld_ahead(t.u0 + w_node); w_v = ld_ahead(t.v0 + w_node); w_w = ld_ahead(t.w0 + w_node); }
         const int first = __shfl_sync(0xffffffffu, w_node, 0);
         const bool root_chain = first == t.root;
 #pragma unroll
@@ -614,31 +630,34 @@ __global__ void __launch_bounds__(32 * kDownWarps) k_bp_down(BpTree t, const flo
                     atomicCAS(err, 0, 4);
                     st_relaxed_gpu(ctl + 1, 1);
                 }
+                drain();
                 break;
             }
             lp = v;
         }
         for (int k = 0; k < n; k++) {
             if (k > 0 && (k & 31) == 0) {  // next window
-                w_node = x_node; w_u = x_u; w_v = x_v; w_w = x_w;
+                w_node = x_node;
                 x_node = k + 32 + lane < n ? ld_ahead(t.chain_nodes + s0 + k + 32 + lane) : -1;
             }
-            if ((k & 31) == 16 && x_node >= 0) {  // the next window's ids were loaded 16 steps ago
-                x_u = ld_ahead(t.u0 + x_node); x_v = ld_ahead(t.v0 + x_node); x_w = ld_ahead(t.w0 + x_node);
-            }
             const int nd = __shfl_sync(0xffffffffu, w_node, k & 31);
-            const float a0 = __shfl_sync(0xffffffffu, w_u, k & 31);
-            const float a1 = __shfl_sync(0xffffffffu, w_v, k & 31);
-            const float a2 = __shfl_sync(0xffffffffu, w_w, k & 31);
-            cp_async_wait<D - 1>();  // this lane's chunks of row k have landed
-            __syncwarp();            // and every lane's
             int l = lp;
             if (!(root_chain && k == 0)) {
+                if (!wait_slot(k & (D - 1))) {  // row k has landed (bounded)
+                    if (lane == 0) {
+                        atomicCAS(err, 0, 4);
+                        st_relaxed_gpu(ctl + 1, 1);
+                    }
+                    drain();
+                    return;
+                }
+                __syncwarp();  // and lane 0's plain-load tail bytes of it are visible
                 if (lp < 0 || lp >= len3) {  // never for a completed upward pass; keeps reads in bounds
                     if (lane == 0) atomicCAS(err, 0, 2);
                     lp = 0;
                 }
-                const unsigned char* row = ring + (k & (D - 1)) * slot_bytes + (int)(((long long)nd * len3 * 2) & 15);
+                // the row's offset in its 16-byte-aligned span (low bits of nd * len3 * 2)
+                const unsigned char* row = ring + (k & (D - 1)) * slot_bytes + (int)(((unsigned)nd * (unsigned)(2 * len3)) & 15u);
                 l = reinterpret_cast<const short*>(row)[lp];
                 if (l < 0 || l >= len3) {  // never for a completed upward pass
                     if (lane == 0) atomicCAS(err, 0, 2);
@@ -653,16 +672,30 @@ __global__ void __launch_bounds__(32 * kDownWarps) k_bp_down(BpTree t, const flo
                 const int b = __shfl_sync(0xffffffffu, x_node, kn & 31);
                 fetch(kn < n ? ((kn >> 5) == (k >> 5) ? a : b) : -1, kn & (D - 1));
             }
-            if (lane == 0) {
-                const int ii = l % len, jj = (l / len) % len, kk = l / (len * len);
-                u1[nd] = (float)(jj - hw) * q + a0;
-                v1[nd] = (float)(ii - hw) * q + a1;
-                w1[nd] = (float)(kk - hw) * q + a2;
-            }
             lp = l;
         }
     }
-    cp_async_wait_all();  // no copy outlives the CTA
+    drain();  // no copy outlives the CTA
+}
+
+// Every node's displacement from its resolved label (src/regularisation.h:275-292),
+// all nodes at once after the walk: u1 = (x index - hw) * q + u0, likewise v1 (y)
+// and w1 (z).  A label never resolved (only after an aborted walk) records error 2
+// and reads label 0.
+__global__ void k_bp_field(BpTree t, const int* __restrict__ lbl, float* __restrict__ u1, float* __restrict__ v1,
+                           float* __restrict__ w1, int* __restrict__ err) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= t.sz) return;
+    const int len = t.len, hw = (len - 1) / 2;
+    int l = lbl[v];
+    if (l < 0 || l >= len * len * len) {
+        atomicCAS(err, 0, 2);
+        l = 0;
+    }
+    const int ii = l % len, jj = (l / len) % len, kk = l / (len * len);
+    u1[v] = (float)(jj - hw) * t.q + t.u0[v];
+    v1[v] = (float)(ii - hw) * t.q + t.v0[v];
+    w1[v] = (float)(kk - hw) * t.q + t.w0[v];
 }
 
 // Per node the offset of its edge in label units, (u0[parent] - u0[node]) / q
@@ -805,7 +838,7 @@ template <int D>
 static cudaError_t launch_down(const BpTree& t, const float* d_cost, short* d_allinds, float* d_u1, float* d_v1,
                                float* d_w1, int* d_lbl, int* d_err, int sm_count, cudaStream_t s) {
     const int len3 = t.len * t.len * t.len;
-    const size_t smem = (size_t)kDownWarps * D * down_slot_bytes(len3);
+    const size_t smem = (size_t)kDownWarps * D * (down_slot_bytes(len3) + sizeof(uint64_t));
     cudaError_t e = cudaFuncSetAttribute(k_bp_down<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
@@ -819,9 +852,9 @@ static cudaError_t launch_down(const BpTree& t, const float* d_cost, short* d_al
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(d_lbl + t.sz, 0, 2 * sizeof(int), s);
     if (e != cudaSuccess) return e;
-    k_bp_down<D><<<ctas, 32 * kDownWarps, smem, s>>>(t, d_cost, d_allinds, d_u1, d_v1, d_w1, d_lbl, d_lbl + t.sz,
-                                                     d_err);
-    count_launches(1);
+    k_bp_down<D><<<ctas, 32 * kDownWarps, smem, s>>>(t, d_cost, d_allinds, d_lbl, d_lbl + t.sz, d_err);
+    k_bp_field<<<(t.sz + 255) / 256, 256, 0, s>>>(t, d_lbl, d_u1, d_v1, d_w1, d_err);
+    count_launches(2);
     return cudaGetLastError();
 }
 

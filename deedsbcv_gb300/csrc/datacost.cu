@@ -30,42 +30,11 @@ namespace deeds {
 
 namespace {
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, int count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-// One try_wait round, suspended at most kTryWaitNs (the suspend-time hint caps the
-// otherwise system-dependent suspension, so a wait of kWaitLimit rounds is bounded
-// by about kWaitLimit microseconds); returns as soon as the phase completes.
-constexpr uint32_t kTryWaitNs = 1000;
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity), "r"(kTryWaitNs)
-        : "memory");
-    return ok != 0;
-}
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2) {
     asm volatile(
         "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];"
         ::"r"(smem_u32(dst)), "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2)
         : "memory");
-}
-
-constexpr long long kWaitLimit = 1LL << 20;  // try_wait rounds of at most kTryWaitNs each: ~1 s
-
-// Bounded wait of one thread on an mbarrier phase; false if the limit expired.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-    for (long long i = 0; i < kWaitLimit; i++)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
 }
 
 // clamp-to-edge padded copy of the moving codes, row pitch mpp (even)

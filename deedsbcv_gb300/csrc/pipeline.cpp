@@ -67,6 +67,7 @@ struct deeds_ctx {
     bool prof = false;
     std::vector<cudaEvent_t> ev_pool;
     size_t ev_used = 0;
+    std::vector<cudaEvent_t> ev_mst;  // MST-input events of deeds_register_dev
     struct Mark { int stage; cudaEvent_t a, b; };
     std::vector<Mark> marks;
     double stage_ms[DEEDS_NUM_STAGES] = {0};
@@ -628,6 +629,7 @@ void deeds_destroy(deeds_ctx* ctx) {
     for (auto& kv : ctx->dev) if (kv.second.p) cudaFree(kv.second.p);
     for (auto& kv : ctx->host) if (kv.second.p) cudaFreeHost(kv.second.p);
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
+    for (cudaEvent_t e : ctx->ev_mst) cudaEventDestroy(e);
     for (cudaEvent_t e : {ctx->ev_a, ctx->ev_b, ctx->ev_c, ctx->ev_d, ctx->ev_e, ctx->ev_f, ctx->ev_g, ctx->ev_up[0],
                           ctx->ev_up[1], ctx->ev_arg[0], ctx->ev_arg[1]})
         if (e) cudaEventDestroy(e);
@@ -723,6 +725,8 @@ deeds_status deeds_tree_bp_dev(deeds_ctx* ctx, float* d_cost, const float* d_u0,
     if (!d_cost || !d_u0 || !d_v0 || !d_w0 || !ordered || !parents || !edgemst || !d_u1 || !d_v1 || !d_w1)
         return fail(ctx, DEEDS_ERR_INVALID, "null pointer");
     if (hw < 0 || hw > 10 || q < 1) return fail(ctx, DEEDS_ERR_INVALID, "radius %d / quant %d", hw, q);
+    if (reinterpret_cast<uintptr_t>(d_allinds) & 15)
+        return fail(ctx, DEEDS_ERR_INVALID, "d_allinds must be 16-byte aligned");
     CK(cudaSetDevice(ctx->device));
     cudaStream_t s = (cudaStream_t)stream;
     const int sz = m1 * n1 * o1;
@@ -891,58 +895,74 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
     }
 
     // ---- inputs, affine-only warp of the moving image
+    // MST-input events: [0] fixed image ready, [1] affine-warped moving image ready,
+    // [2 + d] image statistics of direction d on the host, [4 + t] block SADs of tree t
+    // on the host (t = 2 level + direction)
+    while (ctx->ev_mst.size() < 4 + 2 * (size_t)L) {
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ctx->ev_mst.push_back(e);
+    }
+    cudaEvent_t* ev = ctx->ev_mst.data();
     tl.dmark("start", s);
     CK(cudaMemsetAsync(d_err, 0, 2 * sizeof(int), s));
     CK(launch_shift(d_fixed, fix, (int64_t)sz, P->intensity_shift, s));
+    CK(cudaEventRecord(ev[0], s));
     CK(launch_shift(d_moving, mov, (int64_t)sz, P->intensity_shift, s));
     {
         StageScope sc(ctx, DEEDS_STAGE_TRANSFORM, s);
         FieldRef zero{0, nullptr, nullptr, nullptr, 0, 0, 0};
         CK(launch_warp_affine(mov, X, zero, m, n, o, warp0, nullptr, nullptr, nullptr, s));
     }
+    CK(cudaEventRecord(ev[1], s));
 
-    // ---- MST inputs on the side stream: the image statistics of both images
-    // (exact, on the device) to the host first, then every level's block SADs;
-    // host trees on worker threads
-    CK(cudaEventRecord(ctx->ev_a, s));
-    CK(cudaStreamWaitEvent(ctx->side, ctx->ev_a, 0));
-    {
-        StageScope sc(ctx, DEEDS_STAGE_MST, ctx->side);
-        CK(launch_image_stats(fix, warp0, 2, sz, B.stats_scr, B.d_stats, ctx->side));
-    }
-    CK(cudaMemcpyAsync(h_stats, B.d_stats, 4 * sizeof(float), cudaMemcpyDeviceToHost, ctx->side));
-    CK(cudaEventRecord(ctx->ev_b, ctx->side));
-    for (int l = L - 1; l >= 0; l--) {  // finest first: those trees take longest on the host
+    // ---- MST inputs on the side stream, to the host trees on worker threads.  The
+    // finest trees take longest on the host, the forward one (fixed image) most, so
+    // its inputs go first: the fixed image's statistics (exact, on the device) and
+    // its finest block SADs, then the moving side's, then the coarser levels'.  Each
+    // tree starts as soon as its own inputs are on the host.
+    auto side_sad = [&](int t) -> deeds_status {
+        const int l = t / 2, d = t % 2;
         const size_t sz1 = (size_t)m1s[l] * n1s[l] * o1s[l];
-        for (int d = 0; d < 2; d++) {
-            const int t = 2 * l + d;
-            {
-                StageScope sc(ctx, DEEDS_STAGE_MST, ctx->side);
-                CK(launch_edge_sad(d == 0 ? fix : warp0, m, n, o, P->grid[l], d_sad[t], ctx->side));
-            }
-            CK(cudaMemcpyAsync(h_sad[t], d_sad[t], 6 * sz1 * sizeof(float), cudaMemcpyDeviceToHost, ctx->side));
+        {
+            StageScope sc(ctx, DEEDS_STAGE_MST, ctx->side);
+            CK(launch_edge_sad(d == 0 ? fix : warp0, m, n, o, P->grid[l], d_sad[t], ctx->side));
         }
+        CK(cudaMemcpyAsync(h_sad[t], d_sad[t], 6 * sz1 * sizeof(float), cudaMemcpyDeviceToHost, ctx->side));
+        CK(cudaEventRecord(ev[4 + t], ctx->side));
+        return DEEDS_OK;
+    };
+    for (int d = 0; d < 2; d++) {
+        CK(cudaStreamWaitEvent(ctx->side, ev[d], 0));
+        {
+            StageScope sc(ctx, DEEDS_STAGE_MST, ctx->side);
+            CK(launch_image_stats(d == 0 ? fix : warp0, nullptr, 1, sz, B.stats_scr, B.d_stats + 2 * d, ctx->side));
+        }
+        CK(cudaMemcpyAsync(h_stats + 2 * d, B.d_stats + 2 * d, 2 * sizeof(float), cudaMemcpyDeviceToHost,
+                           ctx->side));
+        CK(cudaEventRecord(ev[2 + d], ctx->side));
+        if (deeds_status e = side_sad(2 * (L - 1) + d)) return e;
     }
-    CK(cudaEventRecord(ctx->ev_c, ctx->side));
+    for (int l = L - 2; l >= 0; l--)
+        for (int d = 0; d < 2; d++)
+            if (deeds_status e = side_sad(2 * l + d)) return e;
     std::vector<std::promise<void>> ready(2 * L);
     std::vector<std::shared_future<void>> ready_f(2 * L);
     for (int t = 0; t < 2 * L; t++) ready_f[t] = ready[t].get_future().share();
-    cudaEvent_t ev_stats = ctx->ev_b, ev_sads = ctx->ev_c;
     const int dev = ctx->device;
-    std::thread builder([&, ev_stats, ev_sads, dev]() {
+    std::thread builder([&, ev, dev]() {
         cudaSetDevice(dev);
-        cudaEventSynchronize(ev_stats);
-        const float sd_f = h_stats[1], sd_w = h_stats[3];
-        tl.mark("image statistics on host");
-        cudaEventSynchronize(ev_sads);
-        tl.mark("block SADs on host");
         // finest trees are the slowest: start the workers in reverse level order
         std::vector<std::thread> workers;
         for (int t = 2 * L - 1; t >= 0; t--) {
             workers.emplace_back([&, t]() {
                 const int l = t / 2, d = t % 2;
                 try {
-                    build_tree(h_sad[t], d == 0 ? sd_f : sd_w, m1s[l], n1s[l], o1s[l], P->grid[l], h_tree[t], pts[t]);
+                    cudaSetDevice(dev);
+                    if (cudaEventSynchronize(ev[2 + d]) != cudaSuccess || cudaEventSynchronize(ev[4 + t]) != cudaSuccess)
+                        throw std::runtime_error("MST inputs: CUDA error");
+                    if (t == 2 * L - 2) tl.mark("finest forward tree inputs on host");
+                    build_tree(h_sad[t], h_stats[2 * d + 1], m1s[l], n1s[l], o1s[l], P->grid[l], h_tree[t], pts[t]);
                     tl.mark("tree level " + std::to_string(l) + (d ? " backward" : " forward") + " built");
                     ready[t].set_value();
                 } catch (...) {

@@ -168,7 +168,8 @@ void deeds_mst_path_counts(long long out[4]);
  * d_cost (sz1*len3) is overwritten with the upward-pass state (each non-root
  * row = that node's message, root row = its total), as the reference leaves it.
  * ordered/parents/edgemst are host arrays (from deeds_prims_from_sad).
- * d_allinds (nullable, sz1*len3 int16) receives the argmin tables. Synchronous. */
+ * d_allinds (nullable, sz1*len3 int16, 16-byte aligned as any cudaMalloc block
+ * is) receives the argmin tables. Synchronous. */
 deeds_status deeds_tree_bp_dev(deeds_ctx* ctx, float* d_cost, const float* d_u0, const float* d_v0,
                                const float* d_w0, int m1, int n1, int o1, int hw, int q, const int* ordered,
                                const int* parents, const float* edgemst, float* d_u1, float* d_v1, float* d_w1,
