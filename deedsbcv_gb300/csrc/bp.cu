@@ -23,11 +23,10 @@
 // (fully unrolled for the compile-time label width), keeping the reference's
 // strict '<' so the first minimiser wins.
 //
-// Downward pass (root to leaves, :258-293): one CTA per tree takes the root's
-// first minimum, then its threads walk heavy-path chains (each follows the child
-// with the deepest subtree) from the argmin tables; a walker queues the chains
-// that branch off a node once it has that node's label; no barrier per breadth
-// level.
+// Downward pass (root to leaves, :258-293): warps across the GPU walk heavy-path
+// chains (each follows the child with the deepest subtree) from the argmin
+// tables staged ahead in shared memory, publishing every node's label for the
+// chains that branch off it; no barrier per breadth level.
 //
 // Roofline: dependency bound (tree depth 265-987 per tree at 192x160x256).
 // Algorithmic traffic: one read + one write of the cost volume and one write of

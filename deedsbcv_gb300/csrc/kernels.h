@@ -34,8 +34,6 @@ struct BpTree {
     int n_chains;            // heavy-path chains (downward pass)
     const int* chain_ptr;    // [n_chains+1] ranges into chain_nodes
     const int* chain_nodes;  // [sz] each chain's nodes from its start down to a leaf
-    const int* branch_ptr;   // [sz+1] per node: range of the chains starting at its children
-    const int* branch_chain; // [n_chains-1]
 };
 
 // A displacement field given at full resolution (mode 1), on a control grid

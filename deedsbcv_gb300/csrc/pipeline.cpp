@@ -80,9 +80,10 @@ struct deeds_ctx {
     std::shared_ptr<TuneTable> tune = std::make_shared<TuneTable>();
     // lanes of deeds_register_batch (child contexts on the same device)
     std::vector<deeds_ctx*> lanes;
-    // the last registration's full-resolution field (for deeds_warp_segmentation)
+    // the last registration's control-grid field (for deeds_warp_segmentation)
     bool have_field = false;
-    int fm = 0, fn = 0, fo = 0;
+    int fm = 0, fn = 0, fo = 0;      // its volume
+    int fm1 = 0, fn1 = 0, fo1 = 0;   // its control grid (field in the "keep_grid" buffer)
     float fX[16];
     // soft-min levels whose forward state stays resident for their backward
     // (deeds_soft_forward_keep_dev); index = slot
@@ -333,7 +334,7 @@ deeds_status check_params(deeds_ctx* ctx, const deeds_params* p, int m, int n, i
 struct PackedTree {
     int sz = 0, n_leaves = 0, n_levels = 0, max_width = 0, n_chains = 0;
     size_t o_ordered, o_parents, o_edgemst, o_cptr, o_children, o_leaves, o_lstart, o_ppos, o_chptr, o_chnodes,
-        o_brptr, o_brchain, total;
+        total;
 };
 
 PackedTree pack_layout(int sz) {
@@ -350,8 +351,6 @@ PackedTree pack_layout(int sz) {
     t.o_ppos = o; o += sz;
     t.o_chptr = o; o += sz + 1;
     t.o_chnodes = o; o += sz;
-    t.o_brptr = o; o += sz + 1;
-    t.o_brchain = o; o += sz;
     t.total = o;
     return t;
 }
@@ -368,8 +367,6 @@ void pack_schedule(const TreeSchedule& s, uint32_t* blk, PackedTree& t) {
     t.n_chains = (int)s.chain_ptr.size() - 1;
     std::memcpy(blk + t.o_chptr, s.chain_ptr.data(), sizeof(int) * s.chain_ptr.size());
     std::memcpy(blk + t.o_chnodes, s.chain_nodes.data(), sizeof(int) * s.chain_nodes.size());
-    std::memcpy(blk + t.o_brptr, s.branch_ptr.data(), sizeof(int) * s.branch_ptr.size());
-    std::memcpy(blk + t.o_brchain, s.branch_chain.data(), sizeof(int) * s.branch_chain.size());
 }
 
 // Build one tree on the host into the packed pinned block `blk`.
@@ -406,15 +403,14 @@ BpTree device_tree(const PackedTree& t, const uint32_t* dblk, const uint32_t* hb
     b.n_chains = t.n_chains;
     b.chain_ptr = reinterpret_cast<const int*>(dblk + t.o_chptr);
     b.chain_nodes = reinterpret_cast<const int*>(dblk + t.o_chnodes);
-    b.branch_ptr = reinterpret_cast<const int*>(dblk + t.o_brptr);
-    b.branch_chain = reinterpret_cast<const int*>(dblk + t.o_brchain);
     return b;
 }
 
 // Run BP on one tree: upload its schedule, upward pass, downward pass.
 deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTree& pt, const uint32_t* h_blk,
                          float* d_cost, short* d_allinds, int len, int q, const float* u0, const float* v0,
-                         const float* w0, float* u1, float* v1, float* w1, int* d_err, cudaStream_t s) {
+                         const float* w0, float* u1, float* v1, float* w1, int* d_err, cudaStream_t s,
+                         Timeline* tl = nullptr, const std::string& what = "") {
     deeds_status st = DEEDS_OK;
     uint32_t* d_blk = dbuf<uint32_t>(ctx, "tree_" + tag, pt.total, &st);
     float* d_mins = dbuf<float>(ctx, "mins_" + tag, 4 * (size_t)pt.sz, &st);  // mins | edge offsets x, y, z
@@ -430,6 +426,7 @@ deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTre
         StageScope sc(ctx, DEEDS_STAGE_BP_UP, s);
         CK(launch_bp_up(bt, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, ctx->sm_count, s));
     }
+    if (tl) tl->dmark(what + " sweep done", s);
     {
         // the argmin tables on the direction's low-priority stream, joined back before
         // the downward pass
@@ -443,6 +440,7 @@ deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTre
         CK(cudaEventRecord(ctx->ev_arg[dl], ctx->low[dl]));
         CK(cudaStreamWaitEvent(s, ctx->ev_arg[dl], 0));
     }
+    if (tl) tl->dmark(what + " argmins joined", s);
     {
         StageScope sc(ctx, DEEDS_STAGE_BP_DOWN, s);
         CK(launch_bp_down(bt, d_cost, d_allinds, u1, v1, w1, d_lbl, d_err, ctx->sm_count, s));
@@ -468,7 +466,7 @@ struct PairBuffers {
     float* cost[2];
     short* allinds[2];
     uint64_t* mpad[2];
-    float *grid, *ku, *kv, *kw, *cons_scr;
+    float *grid, *kgrid, *cons_scr;  // kgrid: the last result's control-grid field (u | v | w)
     void* stats_scr;  // image statistics (deeds::launch_image_stats)
     float *d_stats, *h_stats;  // mean, std of the fixed and of the affine-warped moving image
     std::vector<float*> h_sad, d_sad;
@@ -523,9 +521,7 @@ deeds_status acquire_buffers(deeds_ctx* ctx, int m, int n, int o, const deeds_pa
         dbuf<float>(ctx, "pre_" + tg, B.max_cost, &st);  // scaled rows of the upward sweep (argmin input)
     }
     B.grid = dbuf<float>(ctx, "grid", 18 * B.max_sz1, &st);
-    B.ku = dbuf<float>(ctx, "keep_u", sz, &st);
-    B.kv = dbuf<float>(ctx, "keep_v", sz, &st);
-    B.kw = dbuf<float>(ctx, "keep_w", sz, &st);
+    B.kgrid = dbuf<float>(ctx, "keep_grid", 3 * B.max_sz1, &st);
     B.cons_scr = dbuf<float>(ctx, "consistent", 12 * B.max_sz1, &st);
     B.stats_scr = dbuf<char>(ctx, "stats_scr", image_stats_scratch_bytes(sz, 2), &st);
     B.d_stats = dbuf<float>(ctx, "stats", 4, &st);
@@ -876,9 +872,6 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
     uint64_t** mpad = B.mpad;
     const char* tags[2] = {"f", "b"};
     float* grid = B.grid;
-    float* ku = B.ku;
-    float* kv = B.kv;
-    float* kw = B.kw;
     float* cons_scr = B.cons_scr;
     float* h_stats = B.h_stats;
     std::vector<float*>& h_sad = B.h_sad;
@@ -895,10 +888,9 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
     }
 
     // ---- inputs, affine-only warp of the moving image
-    // MST-input events: [0] fixed image ready, [1] affine-warped moving image ready,
-    // [2 + d] image statistics of direction d on the host, [4 + t] block SADs of tree t
-    // on the host (t = 2 level + direction)
-    while (ctx->ev_mst.size() < 4 + 2 * (size_t)L) {
+    // MST-input events: [0] affine-warped moving image ready, [1] image statistics on
+    // the host, [2 + t] block SADs of tree t on the host (t = 2 level + direction)
+    while (ctx->ev_mst.size() < 2 + 2 * (size_t)L) {
         cudaEvent_t e;
         CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         ctx->ev_mst.push_back(e);
@@ -907,45 +899,43 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
     tl.dmark("start", s);
     CK(cudaMemsetAsync(d_err, 0, 2 * sizeof(int), s));
     CK(launch_shift(d_fixed, fix, (int64_t)sz, P->intensity_shift, s));
-    CK(cudaEventRecord(ev[0], s));
     CK(launch_shift(d_moving, mov, (int64_t)sz, P->intensity_shift, s));
     {
         StageScope sc(ctx, DEEDS_STAGE_TRANSFORM, s);
         FieldRef zero{0, nullptr, nullptr, nullptr, 0, 0, 0};
         CK(launch_warp_affine(mov, X, zero, m, n, o, warp0, nullptr, nullptr, nullptr, s));
     }
-    CK(cudaEventRecord(ev[1], s));
+    CK(cudaEventRecord(ev[0], s));
 
-    // ---- MST inputs on the side stream, to the host trees on worker threads.  The
-    // finest trees take longest on the host, the forward one (fixed image) most, so
-    // its inputs go first: the fixed image's statistics (exact, on the device) and
-    // its finest block SADs, then the moving side's, then the coarser levels'.  Each
-    // tree starts as soon as its own inputs are on the host.
-    auto side_sad = [&](int t) -> deeds_status {
-        const int l = t / 2, d = t % 2;
-        const size_t sz1 = (size_t)m1s[l] * n1s[l] * o1s[l];
-        {
-            StageScope sc(ctx, DEEDS_STAGE_MST, ctx->side);
-            CK(launch_edge_sad(d == 0 ? fix : warp0, m, n, o, P->grid[l], d_sad[t], ctx->side));
-        }
-        CK(cudaMemcpyAsync(h_sad[t], d_sad[t], 6 * sz1 * sizeof(float), cudaMemcpyDeviceToHost, ctx->side));
-        CK(cudaEventRecord(ev[4 + t], ctx->side));
-        return DEEDS_OK;
-    };
-    for (int d = 0; d < 2; d++) {
-        CK(cudaStreamWaitEvent(ctx->side, ev[d], 0));
-        {
-            StageScope sc(ctx, DEEDS_STAGE_MST, ctx->side);
-            CK(launch_image_stats(d == 0 ? fix : warp0, nullptr, 1, sz, B.stats_scr, B.d_stats + 2 * d, ctx->side));
-        }
-        CK(cudaMemcpyAsync(h_stats + 2 * d, B.d_stats + 2 * d, 2 * sizeof(float), cudaMemcpyDeviceToHost,
-                           ctx->side));
-        CK(cudaEventRecord(ev[2 + d], ctx->side));
-        if (deeds_status e = side_sad(2 * (L - 1) + d)) return e;
+    // ---- MST inputs on the side stream, to the host trees on worker threads: the
+    // image statistics of both images (exact, on the device), then the block SADs
+    // in the order the trees are needed: the finest forward tree takes longest on
+    // the host, the first level's trees start the device's level loop, the finest
+    // backward tree is next longest, then the other levels.  Each tree starts as
+    // soon as its own inputs are on the host.
+    CK(cudaStreamWaitEvent(ctx->side, ev[0], 0));
+    {
+        StageScope sc(ctx, DEEDS_STAGE_MST, ctx->side);
+        CK(launch_image_stats(fix, warp0, 2, sz, B.stats_scr, B.d_stats, ctx->side));
     }
-    for (int l = L - 2; l >= 0; l--)
-        for (int d = 0; d < 2; d++)
-            if (deeds_status e = side_sad(2 * l + d)) return e;
+    CK(cudaMemcpyAsync(h_stats, B.d_stats, 4 * sizeof(float), cudaMemcpyDeviceToHost, ctx->side));
+    CK(cudaEventRecord(ev[1], ctx->side));
+    {
+        std::vector<int> order = {2 * (L - 1)};
+        if (L > 1) order.insert(order.end(), {0, 1});
+        order.push_back(2 * (L - 1) + 1);
+        for (int l = L - 2; l >= 1; l--) order.insert(order.end(), {2 * l, 2 * l + 1});
+        for (int t : order) {
+            const int l = t / 2, d = t % 2;
+            const size_t sz1 = (size_t)m1s[l] * n1s[l] * o1s[l];
+            {
+                StageScope sc(ctx, DEEDS_STAGE_MST, ctx->side);
+                CK(launch_edge_sad(d == 0 ? fix : warp0, m, n, o, P->grid[l], d_sad[t], ctx->side));
+            }
+            CK(cudaMemcpyAsync(h_sad[t], d_sad[t], 6 * sz1 * sizeof(float), cudaMemcpyDeviceToHost, ctx->side));
+            CK(cudaEventRecord(ev[2 + t], ctx->side));
+        }
+    }
     std::vector<std::promise<void>> ready(2 * L);
     std::vector<std::shared_future<void>> ready_f(2 * L);
     for (int t = 0; t < 2 * L; t++) ready_f[t] = ready[t].get_future().share();
@@ -959,7 +949,7 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
                 const int l = t / 2, d = t % 2;
                 try {
                     cudaSetDevice(dev);
-                    if (cudaEventSynchronize(ev[2 + d]) != cudaSuccess || cudaEventSynchronize(ev[4 + t]) != cudaSuccess)
+                    if (cudaEventSynchronize(ev[1]) != cudaSuccess || cudaEventSynchronize(ev[2 + t]) != cudaSuccess)
                         throw std::runtime_error("MST inputs: CUDA error");
                     if (t == 2 * L - 2) tl.mark("finest forward tree inputs on host");
                     build_tree(h_sad[t], h_stats[2 * d + 1], m1s[l], n1s[l], o1s[l], P->grid[l], h_tree[t], pts[t]);
@@ -1079,7 +1069,8 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
             tl.dmark("level " + std::to_string(l) + (d ? " backward" : " forward") + " BP starts", sd[d]);
             st = run_tree_bp(ctx, tags[d], pts[t], h_tree[t], cost[d], allinds[d], len, q, cur0[3 * d],
                              cur0[3 * d + 1], cur0[3 * d + 2], nxt[3 * d], nxt[3 * d + 1], nxt[3 * d + 2], d_err + d,
-                             sd[d]);
+                             sd[d],
+                             &tl, "level " + std::to_string(l) + (d ? " backward" : " forward"));
             if (st) return st;
             tl.dmark("level " + std::to_string(l) + (d ? " backward" : " forward") + " BP done", sd[d]);
         }
@@ -1099,15 +1090,24 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
         m2 = m1; n2 = n1; o2 = o1;
     }
 
-    // ---- outputs (src/deedsBCV0.cpp:339-356)
+    // ---- outputs (src/deedsBCV0.cpp:339-356): the control-grid flow, kept on the
+    // context as well (deeds_warp_segmentation upsamples it on the fly, with the
+    // arithmetic of upsample-then-warp); the warped moving image only on request
     const size_t sz1 = (size_t)m2 * n2 * o2;
-    for (int c = 0; c < 3; c++)
-        CK(cudaMemcpyAsync(d_flow_out + c * sz1, prev[c], sz1 * sizeof(float), cudaMemcpyDeviceToDevice, s));
-    {
+    if (prev[1] == prev[0] + sz1 && prev[2] == prev[1] + sz1) {  // u, v, w adjacent (finest grid)
+        CK(cudaMemcpyAsync(d_flow_out, prev[0], 3 * sz1 * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(B.kgrid, prev[0], 3 * sz1 * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    } else {
+        for (int c = 0; c < 3; c++) {
+            CK(cudaMemcpyAsync(d_flow_out + c * sz1, prev[c], sz1 * sizeof(float), cudaMemcpyDeviceToDevice, s));
+            CK(cudaMemcpyAsync(B.kgrid + c * sz1, prev[c], sz1 * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        }
+    }
+    if (d_warped_out) {
         StageScope sc(ctx, DEEDS_STAGE_TRANSFORM, s);
         FieldRef f{2, prev[0], prev[1], prev[2], m2, n2, o2};
-        CK(launch_warp_affine(mov, X, f, m, n, o, warped[0], ku, kv, kw, s));
-        if (d_warped_out) CK(launch_shift(warped[0], d_warped_out, (int64_t)sz, -P->intensity_shift, s));
+        CK(launch_warp_affine(mov, X, f, m, n, o, warped[0], nullptr, nullptr, nullptr, s));
+        CK(launch_shift(warped[0], d_warped_out, (int64_t)sz, -P->intensity_shift, s));
     }
     tl.dmark("output done", s);
     int herr[2] = {0, 0};
@@ -1125,6 +1125,7 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
         return fail(ctx, DEEDS_ERR_INTERNAL, "belief propagation produced an out-of-range argmin index");
     ctx->have_field = true;
     ctx->fm = m; ctx->fn = n; ctx->fo = o;
+    ctx->fm1 = m2; ctx->fn1 = n2; ctx->fo1 = o2;
     std::memcpy(ctx->fX, X, sizeof(ctx->fX));
     return DEEDS_OK;
 }
@@ -1230,8 +1231,9 @@ deeds_status deeds_warp_segmentation(deeds_ctx* ctx, const int16_t* seg, int16_t
     if (st) return st;
     cudaStream_t s = ctx->stream;
     CK(cudaMemcpyAsync(d_in, seg, sz * sizeof(short), cudaMemcpyHostToDevice, s));
-    FieldRef f{1, static_cast<float*>(ctx->dev["keep_u"].p), static_cast<float*>(ctx->dev["keep_v"].p),
-               static_cast<float*>(ctx->dev["keep_w"].p), 0, 0, 0};
+    float* kg = static_cast<float*>(ctx->dev["keep_grid"].p);
+    const size_t sz1 = (size_t)ctx->fm1 * ctx->fn1 * ctx->fo1;
+    FieldRef f{2, kg, kg + sz1, kg + 2 * sz1, ctx->fm1, ctx->fn1, ctx->fo1};
     CK(launch_warp_seg(d_in, ctx->fX, f, ctx->fm, ctx->fn, ctx->fo, d_out, s));
     CK(cudaMemcpyAsync(seg_out, d_out, sz * sizeof(short), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));

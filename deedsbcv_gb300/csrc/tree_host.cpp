@@ -544,23 +544,39 @@ void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int 
     const int mn1 = m1 * n1;
     // neighbour offsets in the reference's direction order -x,+x,-y,+y,-z,+z (src/primsMST.h:70-72)
     const int off[6] = {-m1, m1, -1, 1, -mn1, mn1};
-    bool symmetric = true;
-    for (int v = 0; v < sz; v++) {
-        const int k = v / mn1, rem = v - k * mn1, j = rem / m1, i = rem - j * m1;
-        const bool has[3] = {j + 1 < n1, i + 1 < m1, k + 1 < o1};
-        for (int ax = 0; ax < 3; ax++) {
-            if (!has[ax]) continue;
-            const int nb = 2 * ax + 1, u = v + off[nb];
-            const float s1 = sad[(size_t)nb * sz + v], s2 = sad[(size_t)(nb - 1) * sz + u];
-            const float wt = -std::exp(-(s1 / g3) / twostd);
-            w[(size_t)v * 6 + nb] = wt;
-            if (std::memcmp(&s1, &s2, 4) == 0) {
-                w[(size_t)u * 6 + nb - 1] = wt;
-            } else {
-                w[(size_t)u * 6 + nb - 1] = -std::exp(-(s2 / g3) / twostd);
-                symmetric = false;
+    // vertices [v0, v1) write the weights of their +x, +y, +z edges in both directions:
+    // disjoint entries, so ranges run on separate threads
+    auto weights = [&](int v0, int v1) {
+        bool sym = true;
+        for (int v = v0; v < v1; v++) {
+            const int k = v / mn1, rem = v - k * mn1, j = rem / m1, i = rem - j * m1;
+            const bool has[3] = {j + 1 < n1, i + 1 < m1, k + 1 < o1};
+            for (int ax = 0; ax < 3; ax++) {
+                if (!has[ax]) continue;
+                const int nb = 2 * ax + 1, u = v + off[nb];
+                const float s1 = sad[(size_t)nb * sz + v], s2 = sad[(size_t)(nb - 1) * sz + u];
+                const float wt = -std::exp(-(s1 / g3) / twostd);
+                w[(size_t)v * 6 + nb] = wt;
+                if (std::memcmp(&s1, &s2, 4) == 0) {
+                    w[(size_t)u * 6 + nb - 1] = wt;
+                } else {
+                    w[(size_t)u * 6 + nb - 1] = -std::exp(-(s2 / g3) / twostd);
+                    sym = false;
+                }
             }
         }
+        return sym;
+    };
+    bool symmetric = true;
+    {
+        const int nt = sz >= (1 << 16) ? 4 : 1;
+        std::vector<std::thread> th;
+        std::vector<char> sym(nt, 1);
+        for (int t = 1; t < nt; t++)
+            th.emplace_back([&, t]() { sym[t] = weights((int)((long long)sz * t / nt), (int)((long long)sz * (t + 1) / nt)); });
+        sym[0] = weights(0, (int)((long long)sz / nt));
+        for (auto& x : th) x.join();
+        for (char c : sym) symmetric = symmetric && c;
     }
     std::vector<int> depth(sz, 0);
     for (int v = 0; v < sz; v++) parents[v] = -1;
@@ -570,20 +586,60 @@ void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int 
     // edges, plus the walk itself only until it has made its picks in every
     // ambiguous tie group (its heap decides those ties); no walk when no group is
     // ambiguous.  A NaN weight, or an edge whose two directions differ: the whole
-    // walk.
+    // walk.  The tie-group analysis runs on its own thread while the walk starts;
+    // the walk records its picks until the analysis is in, then counts them.
     MstGroups G;
-    const bool grouped = sz > 1 && symmetric && mst_groups(w.data(), m1, n1, o1, G);
+    std::atomic<int> g_state{symmetric && sz > 1 ? 0 : 2};  // 0 running, 1 grouped, 2 no grouping
+    std::thread grouper;
+    if (g_state.load() == 0)
+        grouper = std::thread([&]() {
+            bool ok = false;
+            try {
+                ok = mst_groups(w.data(), m1, n1, o1, G);
+            } catch (...) {
+                ok = false;
+            }
+            g_state.store(ok ? 1 : 2, std::memory_order_release);
+        });
+    struct JoinAtExit {
+        std::thread& t;
+        ~JoinAtExit() { if (t.joinable()) t.join(); }
+    } join_grouper{grouper};
+    std::vector<int> picks;           // edges the walk took before the analysis was in
     std::vector<int> tree_edges;
-    if (grouped) tree_edges = G.forced;
-    int pending = grouped ? (int)G.amb_rank.size() : -1;  // ambiguous groups still open (-1: full walk)
-    std::vector<int> taken(grouped ? G.amb_rank.size() : 0, 0);
+    std::vector<int> taken;
+    bool grouped = false;
+    int pending = -2;  // ambiguous groups still open; -1: full walk; -2: analysis not in yet
+    // the analysis is in: forced edges, and the walk's picks so far counted per group
+    auto settle = [&]() {
+        grouped = g_state.load(std::memory_order_acquire) == 1;
+        if (!grouped) {
+            pending = -1;
+            return;
+        }
+        tree_edges = G.forced;
+        taken.assign(G.amb_rank.size(), 0);
+        pending = (int)G.amb_rank.size();
+        for (int id : picks) {
+            const int gi = G.amb_of_edge[id];
+            if (gi >= 0) {
+                tree_edges.push_back(id);
+                if (++taken[gi] == G.amb_rank[gi]) pending--;
+            }
+        }
+    };
     long long steps = 0;
-    if (pending != 0) {
+    {
         EdgeHeap heap((size_t)sz * 3);
         std::vector<uint8_t> in_tree(sz, 0);
         in_tree[root] = 1;
         int last = root;
+        picks.reserve(sz);
         for (int added = 1; added < sz && pending != 0; added++) {
+            if (pending == -2 && (added & 1023) == 0 && g_state.load(std::memory_order_acquire) != 0) {
+                settle();
+                if (pending == 0) break;
+            }
             // push the new vertex's edges to its in-grid neighbours, in direction order
             const int k = last / mn1, rem = last - k * mn1, j = rem / m1, i = rem - j * m1;
             const bool ok[6] = {j > 0, j + 1 < n1, i > 0, i + 1 < m1, k > 0, k + 1 < o1};
@@ -607,20 +663,27 @@ void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int 
             parents[to] = from;
             last = to;
             steps++;
-            if (pending > 0) {
+            if (pending != -1) {
                 // the undirected id of the edge just added: from its pushing end and direction
                 const int ef = (int)(dir >> 3), nb = (int)(dir & 7u);
                 const int id = (nb & 1) ? 3 * ef + nb / 2 : 3 * (ef + off[nb]) + nb / 2;
-                const int gi = G.amb_of_edge[id];
-                if (gi >= 0) {
-                    tree_edges.push_back(id);
-                    if (++taken[gi] == G.amb_rank[gi]) pending--;
+                if (pending == -2) {
+                    picks.push_back(id);
+                } else {
+                    const int gi = G.amb_of_edge[id];
+                    if (gi >= 0) {
+                        tree_edges.push_back(id);
+                        if (++taken[gi] == G.amb_rank[gi]) pending--;
+                    }
                 }
             }
         }
     }
+    if (grouper.joinable()) grouper.join();
+    if (pending == -2) settle();  // the walk ended first (small trees)
     g_mst_counts[grouped && G.amb_rank.empty() ? 0 : 1]++;
-    g_mst_counts[2] += steps;
+    // a unique tree's walk only ran while the analysis was out: it counts no steps
+    g_mst_counts[2] += grouped && G.amb_rank.empty() ? 0 : steps;
     g_mst_counts[3] += sz - 1;
     if (grouped) {
         // parents and depths of the assembled tree: breadth-first from the root
@@ -739,14 +802,6 @@ void build_schedule(const int* ordered, const int* parents, int sz, TreeSchedule
         for (int c = v; c >= 0; c = heavy[c]) s.chain_nodes.push_back(c);
     }
     s.chain_ptr.push_back((int)s.chain_nodes.size());
-    // per node, the chains that start at its children (every chain but the first)
-    const int n_chains = (int)s.chain_ptr.size() - 1;
-    s.branch_ptr.assign(sz + 1, 0);
-    for (int c = 1; c < n_chains; c++) s.branch_ptr[parents[s.chain_nodes[s.chain_ptr[c]]] + 1]++;
-    for (int v = 0; v < sz; v++) s.branch_ptr[v + 1] += s.branch_ptr[v];
-    s.branch_chain.assign(n_chains > 0 ? n_chains - 1 : 0, 0);
-    std::vector<int> bfill(s.branch_ptr.begin(), s.branch_ptr.end() - 1);
-    for (int c = 1; c < n_chains; c++) s.branch_chain[bfill[parents[s.chain_nodes[s.chain_ptr[c]]]]++] = c;
 }
 
 }  // namespace deeds

@@ -19,8 +19,6 @@ struct TreeSchedule {
     // leaf; chains in breadth order of their starts, every node in exactly one.
     std::vector<int> chain_ptr;    // [n_chains+1] ranges into chain_nodes
     std::vector<int> chain_nodes;  // [sz]
-    std::vector<int> branch_ptr;   // [sz+1] per node: range of the chains that start at its children
-    std::vector<int> branch_chain; // [n_chains-1] those chain ids, ascending
 };
 
 void image_stats(const float* im, size_t sz, float* mean_out, float* std_out);
@@ -28,9 +26,11 @@ void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int 
                     float* edgemst);
 void build_schedule(const int* ordered, const int* parents, int sz, TreeSchedule& s);
 // Process-wide counts of the MST constructions: trees whose minimum spanning tree
-// is unique (no Prim walk), trees with ambiguous ties (a Prim walk until its tie
-// picks are made, or all of it when a weight is NaN), Prim steps walked, and the
-// steps full walks of the same trees would take.
+// is unique (no Prim walk needed), trees with ambiguous ties (a Prim walk until
+// its tie picks are made, or all of it when a weight is NaN), Prim steps walked
+// for the latter (the walk starts while the tie analysis runs; for a unique tree
+// those steps are discarded and not counted), and the steps full walks of the
+// same trees would take.
 void mst_path_counts(long long out[4]);
 
 }  // namespace deeds

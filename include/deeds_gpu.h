@@ -159,8 +159,10 @@ deeds_status deeds_image_stats_dev(deeds_ctx* ctx, const float* d_im, size_t cou
 /* Diagnostic counters of the host MST construction (process-wide, since load):
  * out[0] trees whose minimum spanning tree is unique (built without a Prim
  * walk), out[1] trees with ambiguous equal-weight edges (Prim's heap walk decides
- * them, stopped once it has), out[2] Prim steps walked, out[3] steps that full
- * walks of the same trees would take.  Every tree equals primsGraph()'s. */
+ * them, stopped once it has), out[2] Prim steps walked for those trees (the
+ * walk starts while the tie analysis runs; a unique tree's steps are discarded),
+ * out[3] steps that full walks of the same trees would take.  Every tree equals
+ * primsGraph()'s. */
 void deeds_mst_path_counts(long long out[4]);
 
 /* regularisationCL(): exact min-sum belief propagation on the MST with 3-D
