@@ -14,6 +14,8 @@
 // scan would change the rounding and with it codes near thresholds.
 // Roofline: HBM-bound; per call ~ 4 B read + 24 B write (pass i), 2 x 48 B
 // (passes j, k), 24 B read + 8 B write (quantise) per voxel = 152 B/voxel.
+#include <cmath>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -39,7 +41,7 @@ __constant__ int c_dz[6] = {0, 0, 1, 1, 1, 1};
 // tail outputs are emitted at the line's last step for the same reason.
 constexpr int TJ = 32;  // lines per CTA
 constexpr int CH = 32;  // i samples per chunk (a multiple of kRing)
-static_assert(CH == 32 && (6 * TJ) % 32 == 0, "tile rows are stored one lane per sample by whole warps");
+static_assert(CH == 32 && TJ == 32, "one lane per sample; warp l of a CTA is channel l");
 
 template <int QS>
 __global__ void __launch_bounds__(6 * TJ) k_pass_i(const float* __restrict__ im, float* __restrict__ D, int m, int n,
@@ -48,8 +50,8 @@ __global__ void __launch_bounds__(6 * TJ) k_pass_i(const float* __restrict__ im,
     constexpr int W = CH + 2 * QS + 1;     // padded row length of the image tile
     constexpr int WL = CH + 2 * QS;        // loaded row length
     constexpr int R = TJ + 2 * QS;         // image rows per k slice
-    float* T = sm;                         // [2][R][W]
-    float* O = sm + 2 * R * W;             // [6][TJ][CH+1]
+    float* Tbuf = sm;                      // two tiles [2][R][W]: the chunk's, and the next one's in flight
+    float* O = sm + 4 * R * W;             // [6][TJ][CH+1]
     const int k = blockIdx.y, j0 = blockIdx.x * TJ;
     const int l = threadIdx.x / TJ, jj = threadIdx.x % TJ, j = j0 + jj;
     const int64_t mn = (int64_t)m * n, sz = mn * o;
@@ -62,24 +64,51 @@ __global__ void __launch_bounds__(6 * TJ) k_pass_i(const float* __restrict__ im,
     float P = 0.0f;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr int kWarps = 6 * TJ / 32;
-    for (int i0 = 0; i0 < m; i0 += CH) {
-        __syncthreads();  // previous chunk's tiles are consumed
-        // one warp per tile row (no index division): rows of both k planes
+    // the image tile of the chunk at i0 into Tb with 4-byte cp.async, one warp per
+    // tile row (rows of both k planes); samples outside the volume are zero-filled
+    // (no bytes read)
+    auto load_tile = [&](int i0, float* Tb) {
         for (int row = warp; row < 2 * R; row += kWarps) {
             const int z = row / R, r = row - z * R;
             const int jr = j0 - QS + r, kz = k + z * QS;
             const bool row_ok = jr >= 0 && jr < n && kz < o;
-            const float* src = im + (int64_t)jr * m + (int64_t)kz * mn;
-            float* dst = T + row * W;
+            const float* src = im + (int64_t)(row_ok ? jr : 0) * m + (int64_t)(row_ok ? kz : 0) * mn;
+            float* dst = Tb + row * W;
 #pragma unroll
             for (int ip = lane; ip < WL; ip += 32) {
                 const int ii = i0 - QS + ip;
-                dst[ip] = (row_ok && ii >= 0 && ii < m) ? src[ii] : 0.0f;
+                const bool ok = row_ok && ii >= 0 && ii < m;
+                const unsigned d = (unsigned)__cvta_generic_to_shared(dst + ip);
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(ok ? src + ii : im),
+                             "r"(ok ? 4 : 0)
+                             : "memory");
             }
         }
-        __syncthreads();
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    load_tile(0, Tbuf);
+    for (int i0 = 0, c = 0; i0 < m; i0 += CH, c++) {
+        float* T = Tbuf + (c & 1) * 2 * R * W;
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        __syncthreads();  // this chunk's tile has landed; the previous chunk's tile is consumed
+        if (i0 + CH < m) load_tile(i0 + CH, Tbuf + ((c + 1) & 1) * 2 * R * W);  // in flight during this chunk
         const int cend = min(CH, m - i0);
-        if (line_ok) {
+        // interior chunk: no line start or end, no shifted sample outside the line, all
+        // CH samples present; the steps need no index checks
+        const bool interior = i0 >= CH && i0 + CH + QS <= m;
+        if (line_ok && interior) {
+            const float* self = T + (jj + QS) * W + QS;
+            // a partner line outside the volume compares the voxel with itself (d = 0)
+            const float* oth = other_ok ? T + (kk * R + jj + QS + dx) * W + QS + dy : self;
+            float* out = O + (l * TJ + jj) * (CH + 1);
+#pragma unroll
+            for (int u = 0; u < CH; u++) {
+                const float d = oth[u] - self[u];
+                P = P + d * d;
+                ring[u & (kRing - 1)] = P;  // i0 is a multiple of kRing
+                out[u] = P - ring[(u - 2 * QS - 1) & (kRing - 1)];
+            }
+        } else if (line_ok) {
             const float* self = T + (jj + QS) * W + QS;
             const float* oth = T + (kk * R + jj + QS + dx) * W + QS + dy;
             float* out = O + (l * TJ + jj) * (CH + 1);
@@ -103,14 +132,18 @@ __global__ void __launch_bounds__(6 * TJ) k_pass_i(const float* __restrict__ im,
                 }
             }
         }
-        __syncthreads();
-        // coalesced store of outputs i0-QS .. i0+cend-1-QS: one warp per (channel, line)
-        // row, one lane per sample (CH == 32)
-        for (int line = warp; line < 6 * TJ; line += kWarps) {
-            const int ll = line / TJ, jg = j0 + (line - ll * TJ);
+        __syncwarp();  // a warp stores the output rows its own lanes wrote (warp = channel)
+        // coalesced store of outputs i0-QS .. i0+cend-1-QS: the warp of channel l stores
+        // its TJ lines, one lane per sample (CH == 32)
+        {
             const int i = i0 + lane - QS;
-            if (lane < cend && i >= 0 && jg < n)
-                D[ll * sz + i + (int64_t)jg * m + (int64_t)k * mn] = O[line * (CH + 1) + lane];
+            if (lane < cend && i >= 0) {
+                const int nl = min(TJ, n - j0);
+                float* dst = D + warp * sz + (int64_t)k * mn + (int64_t)j0 * m + i;
+                const float* src = O + warp * TJ * (CH + 1) + lane;
+#pragma unroll 8
+                for (int jl = 0; jl < nl; jl++) dst[(int64_t)jl * m] = src[jl * (CH + 1)];
+            }
         }
     }
 }
@@ -156,14 +189,22 @@ __global__ void k_pass_jk(float* __restrict__ D, int m, int n, int o, int axis) 
     }
 }
 
+// The five quantisation thresholds and, around each, a window of 2^-20 relative
+// width: the product y = v * RN(1/noise) is within 1.5 ulp of the correctly rounded
+// quotient RN(v/noise), so a threshold whose window does not hold y compares with
+// the quotient as it compares with y.
+struct QuantThr {
+    float t[5], lo[5], hi[5];
+};
+
 // The twelve SSC pairs (src/MINDSSCbox.h:136-140): pair l compares channel l / 2
 // at the voxel's neighbour QS away along one axis (0: i, 1: j, 2: k) in direction
 // kSign[l]; a neighbour outside the volume reads the voxel itself.  With QS a
 // compile-time constant every offset is a constant multiple of the line and
 // slice strides and each pair needs one bounds test.
-template <int QS>
+template <int QS, bool LOGTHR>
 __global__ void __launch_bounds__(64) k_quantise(const float* __restrict__ D, uint64_t* __restrict__ codes, int m,
-                                                 int n, int o, float t0, float t1, float t2, float t3, float t4) {
+                                                 int n, int o, QuantThr th) {
     constexpr int kAxis[12] = {1, 0, 1, 0, 2, 1, 2, 0, 2, 1, 2, 0};
     constexpr int kSign[12] = {-1, -1, -1, 1, -1, 1, -1, 1, -1, -1, -1, -1};
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -202,12 +243,34 @@ __global__ void __launch_bounds__(64) k_quantise(const float* __restrict__ D, ui
     uint64_t code = 0;
 #pragma unroll
     for (int l = 0; l < 12; l++) {
-        float x = __fmul_rn(v[l], rcp);
-        const float lo = __fmul_rn(x, 1.0f - 0x1p-20f), hi = __fmul_rn(x, 1.0f + 0x1p-20f);
-        const bool near = (t0 >= lo && t0 <= hi) | (t1 >= lo && t1 <= hi) | (t2 >= lo && t2 <= hi) |
-                          (t3 >= lo && t3 <= hi) | (t4 >= lo && t4 <= hi);
-        if (near) x = __fdiv_rn(v[l], noise);
-        const int lvl = (t0 > x) + (t1 > x) + (t2 > x) + (t3 > x) + (t4 > x);
+        const float y = __fmul_rn(v[l], rcp);
+        int lvl = 0;
+        bool exact;
+        if (LOGTHR) {
+            // thresholds -log((c+1.5)/6), c = 0..4: c counts when c < z = 6 exp(-x) - 1.5,
+            // so the level is ceil(z) clamped to [0, 5].  z from y and the fast exponential
+            // is within 2^-17 of the z of the quotient and of the float thresholds; within
+            // 2^-12 of an integer (or NaN) the IEEE division decides.
+            const float z = __fadd_rn(__fmul_rn(6.0f, __expf(-y)), -1.5f);
+            exact = !(fabsf(__fsub_rn(z, rintf(z))) >= 0x1p-12f);
+            lvl = min(max((int)ceilf(z), 0), 5);
+        } else {
+            // y outside every threshold's window: each threshold is above or below the
+            // quotient as it is above or below y; y inside a window: the IEEE division decides
+            int cnt = 0;
+#pragma unroll
+            for (int q = 0; q < 5; q++) {
+                lvl += y < th.lo[q];
+                cnt += y <= th.hi[q];
+            }
+            exact = cnt != lvl;
+        }
+        if (exact) {
+            const float x = __fdiv_rn(v[l], noise);
+            lvl = 0;
+#pragma unroll
+            for (int q = 0; q < 5; q++) lvl += th.t[q] > x;
+        }
         code |= (uint64_t)((1u << lvl) - 1u) << (5 * l);  // thermometer {0,1,3,7,15,31}
     }
     codes[p] = code;
@@ -218,14 +281,28 @@ __global__ void __launch_bounds__(64) k_quantise(const float* __restrict__ D, ui
 template <int QS>
 static void mind_passes(const float* d_im, int m, int n, int o, const float thr[5], float* d_scratch,
                         uint64_t* d_codes, cudaStream_t s) {
-    const size_t smem = (size_t)(2 * (TJ + 2 * QS) * (CH + 2 * QS + 1) + 6 * TJ * (CH + 1)) * sizeof(float);
+    const size_t smem = (size_t)(4 * (TJ + 2 * QS) * (CH + 2 * QS + 1) + 6 * TJ * (CH + 1)) * sizeof(float);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k_pass_i<QS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     k_pass_i<QS><<<dim3((n + TJ - 1) / TJ, o), 6 * TJ, smem, s>>>(d_im, d_scratch, m, n, o);
     // 64 i per block: the usual volume extents are multiples of 64, so no lane idles
     k_pass_jk<QS><<<dim3((m + 63) / 64, o, 6), 64, 0, s>>>(d_scratch, m, n, o, 1);
     k_pass_jk<QS><<<dim3((m + 63) / 64, n, 6), 64, 0, s>>>(d_scratch, m, n, o, 2);
-    k_quantise<QS><<<dim3((m + 63) / 64, n, o), 64, 0, s>>>(d_scratch, d_codes, m, n, o, thr[0], thr[1], thr[2],
-                                                            thr[3], thr[4]);
+    QuantThr th;
+    for (int q = 0; q < 5; q++) {
+        // a window of 2^-20 (relative) on either side of the threshold
+        const float a = thr[q] * (1.0f - 0x1p-20f), b = thr[q] * (1.0f + 0x1p-20f);
+        th.t[q] = thr[q];
+        th.lo[q] = a < b ? a : b;
+        th.hi[q] = a < b ? b : a;
+    }
+    // the reference's thresholds -logf((c+1.5)/6) (within 2^-20): the level from one exponential
+    bool logthr = true;
+    for (int q = 0; q < 5; q++) {
+        const double ref = -std::log((q + 1.5) / 6.0);
+        logthr = logthr && std::fabs((double)thr[q] - ref) <= 0x1p-20 * ref;
+    }
+    if (logthr) k_quantise<QS, true><<<dim3((m + 63) / 64, n, o), 64, 0, s>>>(d_scratch, d_codes, m, n, o, th);
+    else k_quantise<QS, false><<<dim3((m + 63) / 64, n, o), 64, 0, s>>>(d_scratch, d_codes, m, n, o, th);
 }
 
 cudaError_t launch_mind_ssc(const float* d_im, int m, int n, int o, int qs, const float thr[5], float* d_scratch,

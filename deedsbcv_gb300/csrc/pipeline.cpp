@@ -56,7 +56,7 @@ struct deeds_ctx {
     // per direction: the argmin tables of a sweep at the lowest priority, so that
     // they yield SMs to the other direction's latency-bound sweep
     cudaStream_t low[2] = {nullptr, nullptr};
-    cudaEvent_t ev_up[2] = {nullptr, nullptr}, ev_arg[2] = {nullptr, nullptr};
+    cudaEvent_t ev_up[2] = {nullptr, nullptr}, ev_arg[2] = {nullptr, nullptr}, ev_cost[2] = {nullptr, nullptr};
     cudaEvent_t ev_e = nullptr, ev_f = nullptr, ev_g = nullptr;
     cudaEvent_t ev_a = nullptr, ev_b = nullptr, ev_c = nullptr, ev_d = nullptr;
     std::string err;
@@ -602,6 +602,7 @@ deeds_status deeds_create(deeds_ctx** out, int device) {
             CK(cudaStreamCreateWithPriority(&c->low[d], cudaStreamNonBlocking, least));
             CK(cudaEventCreateWithFlags(&c->ev_up[d], cudaEventDisableTiming));
             CK(cudaEventCreateWithFlags(&c->ev_arg[d], cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&c->ev_cost[d], cudaEventDisableTiming));
         }
     }
     CK(cudaEventCreateWithFlags(&c->ev_a, cudaEventDisableTiming));
@@ -627,7 +628,7 @@ void deeds_destroy(deeds_ctx* ctx) {
     for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
     for (cudaEvent_t e : ctx->ev_mst) cudaEventDestroy(e);
     for (cudaEvent_t e : {ctx->ev_a, ctx->ev_b, ctx->ev_c, ctx->ev_d, ctx->ev_e, ctx->ev_f, ctx->ev_g, ctx->ev_up[0],
-                          ctx->ev_up[1], ctx->ev_arg[0], ctx->ev_arg[1]})
+                          ctx->ev_up[1], ctx->ev_arg[0], ctx->ev_arg[1], ctx->ev_cost[0], ctx->ev_cost[1]})
         if (e) cudaEventDestroy(e);
     for (cudaStream_t st : {ctx->stream, ctx->stream_b, ctx->side, ctx->bg, ctx->low[0], ctx->low[1]})
         if (st) cudaStreamDestroy(st);
@@ -1023,6 +1024,7 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
                 CK(data_cost_auto(ctx, d == 0 ? c_fix : c_mov, reuse ? c_mov : c_warp[d], mpad[d], m, n, o, g, hw, q,
                                   P->alpha, cost[d], d_err + d, sdd));
             }
+            CK(cudaEventRecord(ctx->ev_cost[d], sdd));
         }
         if (l == 0 && B.steps.size() > 1) {
             // the other levels' field-independent codes on their own stream, after both
@@ -1066,6 +1068,10 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
                         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
             }
             const int t = 2 * l + d;
+            // a sweep is latency bound and runs at about half speed beside a cost-volume
+            // kernel on the same SMs (2.8 ms alone, 7.9 ms beside one at grid 8), so it
+            // starts once the other direction's cost volume is done too
+            CK(cudaStreamWaitEvent(sd[d], ctx->ev_cost[1 - d], 0));
             tl.dmark("level " + std::to_string(l) + (d ? " backward" : " forward") + " BP starts", sd[d]);
             st = run_tree_bp(ctx, tags[d], pts[t], h_tree[t], cost[d], allinds[d], len, q, cur0[3 * d],
                              cur0[3 * d + 1], cur0[3 * d + 2], nxt[3 * d], nxt[3 * d + 1], nxt[3 * d + 2], d_err + d,

@@ -67,6 +67,20 @@ def test_mind_golden(api, golden, qs):
         assert same_bits(codes, g[f"{key}_q{qs}"]), (key, qs, int(np.count_nonzero(codes != g[f"{key}_q{qs}"])))
 
 
+@pytest.mark.parametrize("shape,top", [((100, 37, 29), 3), ((64, 33, 17), 1), ((20, 70, 11), 7), ((161, 12, 9), 2)])
+def test_mind_integer_images_vs_oracle(api, shape, top):
+    """Small-integer images: the distances are integers, so many SSC quotients are
+    equal or near-equal across voxels and some fall close to a threshold (where the
+    quantiser divides exactly); line lengths that leave partial and interior
+    i-chunks."""
+    rng = np.random.default_rng(sum(shape) + top)
+    im = rng.integers(0, top + 1, int(np.prod(shape))).astype(np.float32)
+    for qs in (1, 2, 3):
+        gpu = host(api.descriptor(cu(im), *shape, qs), np.uint64)
+        ref = orc.descriptor(im, *shape, qs)
+        assert same_bits(gpu, ref), (shape, qs, int(np.count_nonzero(gpu != ref)))
+
+
 def test_mind_phantom_vs_oracle(api):
     from deedsbcv_gb300 import phantom
     shape = (96, 80, 128)
