@@ -279,6 +279,17 @@ __device__ __forceinline__ int ld_acquire_gpu(const int* p) {
 __device__ __forceinline__ void st_relaxed_gpu(int* p, int v) {
     asm volatile("st.relaxed.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+__device__ __forceinline__ int ld_relaxed_gpu(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Children (by position among the parent's children) whose rows a chain step may
+// hold in registers when every sibling has already arrived: within the register
+// budget of the sweep's thread count and its other state, and leaving room on the
+// SM for the argmin kernel that runs beside the other direction's sweep.
+constexpr int sweep_sibling_regs(int len) { return len <= 9 ? 3 : (len == 13 ? 2 : (len <= 15 ? 1 : 0)); }
 
 constexpr long long kArgminSpinLimit = 1LL << 21;  // polls of a 256 ns sleep: ~0.5 s, far beyond a sweep
 
@@ -319,7 +330,14 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
     short* ib = ia + LEN3;
     int* s_chain = reinterpret_cast<int*>(ib + LEN3);  // this chain's finished nodes (2 LEN3 shorts: 4-aligned)
     __shared__ float red[32];
-    __shared__ int s_node, s_last;
+    __shared__ int s_node, s_last, s_ready;
+    // A thread with no line in the transform passes (the line slots are padded past
+    // LEN^2) probes, during the passes, whether the parent's other children have
+    // all arrived already.
+    constexpr int kProbe = bp_line_slots(LEN) - 1;
+    static_assert(kProbe >= LEN * LEN && kProbe < T, "the probe thread has no transform line");
+    constexpr int KS = sweep_sibling_regs(LEN);
+    static_assert(KS <= kKidRegs, "sibling rows are held by child position");
     const int tid = threadIdx.x;
     __shared__ int s_nchain;  // entries of s_chain (written by thread 0)
     if (tid == 0) s_nchain = 0;
@@ -389,11 +407,38 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
             const float opx = ld_ahead(off + p), opy = ld_ahead(off + t.sz + p), opz = ld_ahead(off + 2 * t.sz + p);
             int ggp = gp;
             if (gp != t.root) ggp = ld_ahead(t.parents + gp);
+            // The parent's other children may all have arrived before this step: then
+            // this CTA is the last arriver without the arrival atomic, and their rows
+            // are loaded during the last pass instead of after the message.  The probe
+            // reads the count relaxed (no wait) and, when it is complete, a fence makes
+            // it an acquire of every sibling's release; the barrier after the second
+            // pass passes that on to the CTA's loads.
+            int probe = -1;
+            if (KS > 0 && tid == kProbe && c1 - c0 > 1) probe = ld_relaxed_gpu(arrived + p);
             __syncthreads();
             dt_lines_val<LEN, 0>(A, B, oy);
             __syncthreads();
+            if (KS > 0 && tid == kProbe) {
+                const bool all = c1 - c0 > 1 && probe == c1 - c0 - 1;
+                if (all) asm volatile("fence.acq_rel.gpu;" ::: "memory");
+                s_ready = all;
+            }
             dt_lines_val<LEN, 1>(B, A, ox);
             __syncthreads();
+            const bool ready = KS > 0 && c1 - c0 > 1 && s_ready;
+            float sib[KS > 0 ? KS : 1][NL], sibm[KS > 0 ? KS : 1];
+#pragma unroll
+            for (int k = 0; k < KS; k++) {
+                if (ready && c0 + k < c1 && kid[k] != node) {
+                    const float* chrow = cost + (int64_t)kid[k] * LEN3;
+                    sibm[k] = ld_cg(mins + kid[k]);
+#pragma unroll
+                    for (int q = 0; q < NL; q++) {
+                        const int l = tid + q * T;
+                        sib[k][q] = l < LEN3 ? ld_cg(chrow + l) : 0.0f;
+                    }
+                }
+            }
             dt_lines_val<LEN, 2>(A, B, oz);  // message in B (its argmins: k_bp_argmin, from `pre`)
             __syncthreads();
             float mn = INFINITY;
@@ -411,7 +456,7 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
                 if (s_nchain == kChainSlots) publish_list();
                 s_chain[s_nchain++] = node;
             }
-            if (c1 - c0 > 1) {
+            if (c1 - c0 > 1 && !ready) {
                 // siblings exist: the last of them to arrive continues with the parent
                 if (tid == 0) {
                     mins[node] = mn;
@@ -449,8 +494,19 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
                 }
             };
 #pragma unroll
-            for (int k = 0; k < kKidRegs; k++)
-                if (c0 + k < c1) add_child(kid[k]);
+            for (int k = 0; k < kKidRegs; k++) {
+                if (c0 + k < c1) {
+                    if (k < KS && ready && kid[k] != node) {  // the row loaded during the last pass
+#pragma unroll
+                        for (int q = 0; q < NL; q++) {
+                            const int l = tid + q * T;
+                            if (l < LEN3) acc[q] = acc[q] + (sib[k < KS ? k : 0][q] - sibm[k < KS ? k : 0]);
+                        }
+                    } else {
+                        add_child(kid[k]);
+                    }
+                }
+            }
             for (int ci = c0 + kKidRegs; ci < c1; ci++) add_child(t.children[ci]);
             if (p == t.root) {
                 float* rrow = cost + (int64_t)p * LEN3;
