@@ -15,12 +15,14 @@
 // columns, as the reference's skipx/skipz do).  Two boxes are in flight
 // (double buffering on two mbarriers).  Threads own one (node, ly) label each
 // and reduce the node's samples with fully unrolled loops: per sample one
-// 64-bit shared load of the moving code, one broadcast load of the fixed code,
-// XOR, two POPC and an add.  The fixed codes of the tile are staged once.
+// 64-bit shared load of the moving code and an XOR with the fixed code (held in
+// registers); three samples' XORs go through a carry-save adder so that they cost
+// two 64-bit POPCs instead of three.
 // NY is chosen per level by the autotuner in pipeline.cpp.
 //
-// Roofline: integer-pipe bound (two 32-bit POPC per 64-bit sample; GB300 issues
-// 16 POPC/clk/SM).  Work per launch = sz1 * len^3 * samples popc64.
+// Roofline: integer-pipe bound (32-bit POPCs: GB300 issues 16 per clock per SM;
+// four per three 64-bit samples with the carry-save adder, against two per sample
+// in the XOR + POPC probe).  Work per launch = sz1 * len^3 * samples popc64.
 #include <cuda.h>
 
 #include "common.cuh"
@@ -146,8 +148,23 @@ __global__ void __launch_bounds__(256) k_data_cost_tma(const __grid_constant__ C
             int acc[LF];
 #pragma unroll
             for (int u = 0; u < LF; u++) acc[u] = 0;
+            // samples three at a time through a carry-save adder: for the XORs a, b, c,
+            // popc(a) + popc(b) + popc(c) = popc(a ^ b ^ c) + 2 popc(maj(a, b, c)), two
+            // 64-bit POPCs (the kernel's bound: 16 per clock per SM) instead of three
 #pragma unroll
-            for (int c = 0; c < NC; c++) {
+            for (int c = 0; c + 3 <= NC; c += 3) {
+                const uint64_t* ca = sb + c * yb + pos;
+                const uint64_t* cb = ca + yb;
+                const uint64_t* cc = cb + yb;
+#pragma unroll
+                for (int u = 0; u < LF; u++) {
+                    const uint64_t a = fr[c] ^ ca[u * QF], b = fr[c + 1] ^ cb[u * QF], x = fr[c + 2] ^ cc[u * QF];
+                    const uint64_t sum = a ^ b ^ x, carry = (a & b) | (x & (a ^ b));
+                    acc[u] += __popcll(sum) + 2 * __popcll(carry);
+                }
+            }
+#pragma unroll
+            for (int c = NC - NC % 3; c < NC; c++) {
                 const uint64_t* col = sb + c * yb + pos;
 #pragma unroll
                 for (int u = 0; u < LF; u++) acc[u] += __popcll(fr[c] ^ col[u * QF]);
@@ -375,22 +392,26 @@ namespace {
 // Register-only throughput probe of the cost-volume inner operation
 // (64-bit XOR, two 32-bit POPC, accumulate): 8 independent chains per thread.
 __global__ void k_popc_probe(int iters, unsigned long long* sink) {
-    uint64_t v[8];
-    int acc[8];
+    // the cost volume's inner operation, register only: nine 64-bit samples per
+    // iteration, each XORed with its own key, summed three at a time through the
+    // carry-save adder (two 64-bit POPCs per three samples)
+    uint64_t v[9];
+    int acc[3] = {0, 0, 0};
 #pragma unroll
-    for (int j = 0; j < 8; j++) {
-        v[j] = 0x9E3779B97F4A7C15ull * (uint64_t)(threadIdx.x * 8 + j + 1) ^ (uint64_t)blockIdx.x;
-        acc[j] = 0;
-    }
-    uint64_t key = (uint64_t)clock64();
+    for (int j = 0; j < 9; j++) v[j] = 0x9E3779B97F4A7C15ull * (uint64_t)(threadIdx.x * 9 + j + 1) ^ (uint64_t)blockIdx.x;
+    uint64_t k1 = (uint64_t)clock64(), k2 = k1 * 0x2545F4914F6CDD1Dull, k3 = k1 ^ 0xD1B54A32D192ED03ull;
     for (int it = 0; it < iters; it++) {
 #pragma unroll
-        for (int j = 0; j < 8; j++) acc[j] += __popcll(v[j] ^ key);
-        key += 0x5851F42D4C957F2Dull;
+        for (int g = 0; g < 3; g++) {
+            const uint64_t a = v[3 * g] ^ k1, b = v[3 * g + 1] ^ k2, x = v[3 * g + 2] ^ k3;
+            const uint64_t sum = a ^ b ^ x, carry = (a & b) | (x & (a ^ b));
+            acc[g] += __popcll(sum) + 2 * __popcll(carry);
+        }
+        k1 += 0x5851F42D4C957F2Dull;
+        k2 ^= k1;
+        k3 += k2;
     }
-    int t = 0;
-#pragma unroll
-    for (int j = 0; j < 8; j++) t += acc[j];
+    const int t = acc[0] + acc[1] + acc[2];
     if (t == -1) sink[0] = (unsigned long long)t;  // never true; keeps the loop live
 }
 }  // namespace

@@ -952,7 +952,7 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
                     cudaSetDevice(dev);
                     if (cudaEventSynchronize(ev[1]) != cudaSuccess || cudaEventSynchronize(ev[2 + t]) != cudaSuccess)
                         throw std::runtime_error("MST inputs: CUDA error");
-                    if (t == 2 * L - 2) tl.mark("finest forward tree inputs on host");
+                    tl.mark("tree level " + std::to_string(l) + (d ? " backward" : " forward") + " inputs on host");
                     build_tree(h_sad[t], h_stats[2 * d + 1], m1s[l], n1s[l], o1s[l], P->grid[l], h_tree[t], pts[t]);
                     tl.mark("tree level " + std::to_string(l) + (d ? " backward" : " forward") + " built");
                     ready[t].set_value();
@@ -1415,7 +1415,7 @@ deeds_status deeds_measure_popc_rate(deeds_ctx* ctx, double* rate) {
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, a, b));
     ctx->ev_used = 0;
-    *rate = (double)blocks * threads * iters * 8.0 / (ms * 1e-3);
+    *rate = (double)blocks * threads * iters * 9.0 / (ms * 1e-3);  // 64-bit samples per second
     return DEEDS_OK;
 }
 

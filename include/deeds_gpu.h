@@ -252,9 +252,10 @@ deeds_status deeds_stage_times(deeds_ctx* ctx, float* ms, long long* launches);
 deeds_status deeds_reset_stage_times(deeds_ctx* ctx);
 /* Number of kernels this library has launched in the process so far. */
 long long deeds_kernel_launches(void);
-/* Measure this GPU's 64-bit population-count throughput (XOR + 2 POPC + add per
- * element, the cost-volume inner loop) with a register-only probe kernel;
- * returns popc64 operations per second. Synchronous, ~0.2 s. */
+/* Measure this GPU's rate of the cost-volume inner operation with a register-only
+ * probe kernel: 64-bit samples XORed with a key and summed three at a time
+ * through a carry-save adder (two 64-bit POPCs per three samples); returns
+ * samples (popc64 equivalents) per second. Synchronous, ~0.2 s. */
 deeds_status deeds_measure_popc_rate(deeds_ctx* ctx, double* popc64_per_s);
 
 /* ---------------------------------------------------------------------------
