@@ -26,11 +26,6 @@ struct BpTree {
     const float* u0;         // [sz] current displacement (label offsets are relative)
     const float* v0;
     const float* w0;
-    int n_levels;            // breadth levels
-    int max_width;           // widest breadth level
-    const int* level_start;  // [n_levels+1] ranges into ordered
-    const int* ordered;      // [sz] breadth-level order
-    const int* parent_pos;   // [sz] position in `ordered` of the parent of ordered[t]
     int n_chains;            // heavy-path chains (downward pass)
     const int* chain_ptr;    // [n_chains+1] ranges into chain_nodes
     const int* chain_nodes;  // [sz] each chain's nodes from its start down to a leaf

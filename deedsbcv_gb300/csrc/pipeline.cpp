@@ -332,8 +332,8 @@ deeds_status check_params(deeds_ctx* ctx, const deeds_params* p, int m, int n, i
 
 // One tree's host arrays packed for a single H2D copy (4-byte words).
 struct PackedTree {
-    int sz = 0, n_leaves = 0, n_levels = 0, max_width = 0, n_chains = 0;
-    size_t o_ordered, o_parents, o_edgemst, o_cptr, o_children, o_leaves, o_lstart, o_ppos, o_chptr, o_chnodes,
+    int sz = 0, n_leaves = 0, n_chains = 0;
+    size_t o_ordered, o_parents, o_edgemst, o_cptr, o_children, o_leaves, o_chptr, o_chnodes,
         total;
 };
 
@@ -347,8 +347,6 @@ PackedTree pack_layout(int sz) {
     t.o_cptr = o; o += sz + 1;
     t.o_children = o; o += sz;
     t.o_leaves = o; o += sz;
-    t.o_lstart = o; o += sz + 1;
-    t.o_ppos = o; o += sz;
     t.o_chptr = o; o += sz + 1;
     t.o_chnodes = o; o += sz;
     t.total = o;
@@ -357,13 +355,9 @@ PackedTree pack_layout(int sz) {
 
 void pack_schedule(const TreeSchedule& s, uint32_t* blk, PackedTree& t) {
     t.n_leaves = (int)s.leaves.size();
-    t.n_levels = s.n_levels;
-    t.max_width = s.max_width;
     std::memcpy(blk + t.o_cptr, s.child_ptr.data(), sizeof(int) * s.child_ptr.size());
     std::memcpy(blk + t.o_children, s.children.data(), sizeof(int) * s.children.size());
     std::memcpy(blk + t.o_leaves, s.leaves.data(), sizeof(int) * s.leaves.size());
-    std::memcpy(blk + t.o_lstart, s.level_start.data(), sizeof(int) * s.level_start.size());
-    std::memcpy(blk + t.o_ppos, s.parent_pos.data(), sizeof(int) * s.parent_pos.size());
     t.n_chains = (int)s.chain_ptr.size() - 1;
     std::memcpy(blk + t.o_chptr, s.chain_ptr.data(), sizeof(int) * s.chain_ptr.size());
     std::memcpy(blk + t.o_chnodes, s.chain_nodes.data(), sizeof(int) * s.chain_nodes.size());
@@ -395,11 +389,6 @@ BpTree device_tree(const PackedTree& t, const uint32_t* dblk, const uint32_t* hb
     b.parents = reinterpret_cast<const int*>(dblk + t.o_parents);
     b.edgemst = reinterpret_cast<const float*>(dblk + t.o_edgemst);
     b.u0 = u0; b.v0 = v0; b.w0 = w0;
-    b.n_levels = t.n_levels;
-    b.max_width = t.max_width;
-    b.level_start = reinterpret_cast<const int*>(dblk + t.o_lstart);
-    b.ordered = reinterpret_cast<const int*>(dblk + t.o_ordered);
-    b.parent_pos = reinterpret_cast<const int*>(dblk + t.o_ppos);
     b.n_chains = t.n_chains;
     b.chain_ptr = reinterpret_cast<const int*>(dblk + t.o_chptr);
     b.chain_nodes = reinterpret_cast<const int*>(dblk + t.o_chnodes);

@@ -590,17 +590,22 @@ void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int 
     // the walk records its picks until the analysis is in, then counts them.
     MstGroups G;
     std::atomic<int> g_state{symmetric && sz > 1 ? 0 : 2};  // 0 running, 1 grouped, 2 no grouping
+    auto analyse = [&]() {
+        bool ok = false;
+        try {
+            ok = mst_groups(w.data(), m1, n1, o1, G);
+        } catch (...) {
+            ok = false;
+        }
+        g_state.store(ok ? 1 : 2, std::memory_order_release);
+    };
+    // its own thread for large trees only: a registration builds ten trees at once,
+    // and the long walks of the finest two should not share cores with helpers
     std::thread grouper;
-    if (g_state.load() == 0)
-        grouper = std::thread([&]() {
-            bool ok = false;
-            try {
-                ok = mst_groups(w.data(), m1, n1, o1, G);
-            } catch (...) {
-                ok = false;
-            }
-            g_state.store(ok ? 1 : 2, std::memory_order_release);
-        });
+    if (g_state.load() == 0) {
+        if (sz >= (1 << 16)) grouper = std::thread(analyse);
+        else analyse();
+    }
     struct JoinAtExit {
         std::thread& t;
         ~JoinAtExit() { if (t.joinable()) t.join(); }
@@ -750,18 +755,6 @@ void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int 
 }
 
 void build_schedule(const int* ordered, const int* parents, int sz, TreeSchedule& s) {
-    // breadth levels from the ordering (src/regularisation.h:145-169)
-    std::vector<int> depth(sz, 0), pos(sz, 0);
-    for (int t = 0; t < sz; t++) pos[ordered[t]] = t;
-    for (int t = 1; t < sz; t++) depth[ordered[t]] = depth[parents[ordered[t]]] + 1;
-    int maxd = 0;
-    for (int v = 0; v < sz; v++) maxd = std::max(maxd, depth[v]);
-    s.n_levels = maxd + 1;
-    s.level_start.assign(s.n_levels + 1, 0);
-    for (int v = 0; v < sz; v++) s.level_start[depth[v] + 1]++;
-    for (int l = 1; l <= s.n_levels; l++) s.level_start[l] += s.level_start[l - 1];
-    s.max_width = 0;
-    for (int l = 0; l < s.n_levels; l++) s.max_width = std::max(s.max_width, s.level_start[l + 1] - s.level_start[l]);
     // children per node in ordering order (ordering is breadth-level, so a
     // parent's children appear in the order the reference adds them)
     s.child_ptr.assign(sz + 1, 0);
@@ -779,8 +772,6 @@ void build_schedule(const int* ordered, const int* parents, int sz, TreeSchedule
         const int v = ordered[t];
         if (s.child_ptr[v + 1] == s.child_ptr[v]) s.leaves.push_back(v);
     }
-    s.parent_pos.assign(sz, 0);
-    for (int t = 1; t < sz; t++) s.parent_pos[t] = pos[parents[ordered[t]]];
     // heavy children: subtree heights bottom-up (ordering is breadth-level, so every
     // child is visited before its parent); in reverse order '>=' keeps the first
     // child of equal height

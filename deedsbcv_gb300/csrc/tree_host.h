@@ -6,13 +6,9 @@
 namespace deeds {
 
 struct TreeSchedule {
-    int n_levels = 0;
-    int max_width = 0;
-    std::vector<int> level_start;  // [n_levels+1] ranges into ordered
     std::vector<int> child_ptr;    // [sz+1] CSR of children per node
     std::vector<int> children;     // in MST ordering order
     std::vector<int> leaves;       // nodes without children (root excluded), deepest first
-    std::vector<int> parent_pos;   // [sz] position in ordered of the parent of ordered[t]
     // Heavy-path chains for the downward pass: from each chain start (the root,
     // and every child that is not its parent's heavy child) down through heavy
     // children (the child with the deepest subtree, the first such on ties) to a
