@@ -804,7 +804,7 @@ constexpr size_t bp_smem(bool sweep) {
 
 template <int LEN>
 cudaError_t launch_up(const BpTree& t, float* cost, short* allinds, float* pre, float* mins, int* arrived,
-                      int* work, int* done, int* err, int sm_count, cudaStream_t s) {
+                      int* work, int* done, int* err, int sm_count, int concurrent, cudaStream_t s) {
     constexpr int T = bp_threads(LEN);
     const size_t smem = bp_smem<LEN>(true);
     cudaError_t e = cudaFuncSetAttribute(k_bp_up<LEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -813,11 +813,16 @@ cudaError_t launch_up(const BpTree& t, float* cost, short* allinds, float* pre, 
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bp_up<LEN>, T, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    // at most two CTAs per SM: the sweep is bound by its deepest chain, whose steps
-    // slow down when more CTAs share its SM (the two directions' sweeps run
-    // concurrently), while two per SM still finish the rest of the nodes well
-    // within the chain's time
-    int ctas = (per_sm < 2 ? per_sm : 2) * sm_count;
+    // At most two CTAs per SM: the sweep is bound by its deepest chain, whose steps
+    // slow down when more CTAs share its SM, while two per SM still finish the rest
+    // of the nodes well within the chain's time.  With `concurrent` sweeps running
+    // at once (the two directions of a registration) each takes its share of the
+    // SMs' CTA slots: persistent CTAs of a sweep that took every slot would keep the
+    // other sweep's CTAs from starting until its own ended (at label widths 13-17 a
+    // single CTA fills an SM's registers).
+    const int slots = per_sm * sm_count / (concurrent > 1 ? concurrent : 1);
+    int ctas = slots < 2 * sm_count ? slots : 2 * sm_count;
+    if (ctas < 1) ctas = 1;
     if (ctas > t.n_leaves) ctas = t.n_leaves;
     float* off = mins + t.sz;
     k_bp_offsets<<<(t.sz + 255) / 256, 256, 0, s>>>(t, off);
@@ -848,24 +853,24 @@ cudaError_t launch_argmin(const BpTree& t, short* allinds, const float* pre, con
 }  // namespace
 
 cudaError_t launch_bp_up(const BpTree& t, float* d_cost, short* d_allinds, float* d_pre, float* d_mins, int* d_arrived,
-                         int* d_work, int* d_done, int* d_err, int sm_count, cudaStream_t s) {
+                         int* d_work, int* d_done, int* d_err, int sm_count, int concurrent, cudaStream_t s) {
     if (t.n_leaves <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(d_arrived, 0, sizeof(int) * (size_t)t.sz, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d_work, 0, 3 * sizeof(int), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d_done, 0xff, sizeof(int) * (size_t)t.sz, s);  // -1: not written
     if (e != cudaSuccess) return e;
     switch (t.len) {
-        case 1: return launch_up<1>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, s);
-        case 3: return launch_up<3>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, s);
-        case 5: return launch_up<5>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, s);
-        case 7: return launch_up<7>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, s);
-        case 9: return launch_up<9>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, s);
-        case 11: return launch_up<11>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, s);
-        case 13: return launch_up<13>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, s);
-        case 15: return launch_up<15>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, s);
-        case 17: return launch_up<17>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, s);
-        case 19: return launch_up<19>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, s);
-        case 21: return launch_up<21>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, s);
+        case 1: return launch_up<1>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, concurrent, s);
+        case 3: return launch_up<3>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, concurrent, s);
+        case 5: return launch_up<5>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, concurrent, s);
+        case 7: return launch_up<7>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, concurrent, s);
+        case 9: return launch_up<9>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, concurrent, s);
+        case 11: return launch_up<11>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, concurrent, s);
+        case 13: return launch_up<13>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, concurrent, s);
+        case 15: return launch_up<15>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, concurrent, s);
+        case 17: return launch_up<17>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, concurrent, s);
+        case 19: return launch_up<19>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, concurrent, s);
+        case 21: return launch_up<21>(t, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, sm_count, concurrent, s);
         default: return cudaErrorInvalidValue;
     }
 }

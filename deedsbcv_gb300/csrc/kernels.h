@@ -60,8 +60,9 @@ cudaError_t launch_image_stats(const float* im0, const float* im1, int nimg, siz
 // d_pre: t.sz * len^3 floats (each node's scaled row, the transform's input)
 // d_work: 3 ints; d_done: t.sz ints (list of finished nodes); d_err: error word (4: a bounded wait expired).
 // The sweep's idle CTAs compute the argmin tables of finished nodes.
+// concurrent: sweeps expected to run at once on the GPU (each takes its share of the CTA slots)
 cudaError_t launch_bp_up(const BpTree& t, float* d_cost, short* d_allinds, float* d_pre, float* d_mins, int* d_arrived,
-                         int* d_work, int* d_done, int* d_err, int sm_count, cudaStream_t s);
+                         int* d_work, int* d_done, int* d_err, int sm_count, int concurrent, cudaStream_t s);
 // the argmin tables (allinds) of the nodes the sweep left, from its stored rows (after launch_bp_up)
 cudaError_t launch_bp_argmin(const BpTree& t, short* d_allinds, const float* d_pre, const float* d_mins, int* d_work,
                              int* d_done, int* d_err, int sm_count, cudaStream_t s);

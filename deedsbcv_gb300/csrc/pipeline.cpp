@@ -399,7 +399,7 @@ BpTree device_tree(const PackedTree& t, const uint32_t* dblk, const uint32_t* hb
 deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTree& pt, const uint32_t* h_blk,
                          float* d_cost, short* d_allinds, int len, int q, const float* u0, const float* v0,
                          const float* w0, float* u1, float* v1, float* w1, int* d_err, cudaStream_t s,
-                         Timeline* tl = nullptr, const std::string& what = "") {
+                         Timeline* tl = nullptr, const std::string& what = "", int concurrent = 1) {
     deeds_status st = DEEDS_OK;
     uint32_t* d_blk = dbuf<uint32_t>(ctx, "tree_" + tag, pt.total, &st);
     float* d_mins = dbuf<float>(ctx, "mins_" + tag, 4 * (size_t)pt.sz, &st);  // mins | edge offsets x, y, z
@@ -413,7 +413,8 @@ deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTre
     const BpTree bt = device_tree(pt, d_blk, h_blk, len, (float)q, u0, v0, w0);
     {
         StageScope sc(ctx, DEEDS_STAGE_BP_UP, s);
-        CK(launch_bp_up(bt, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, ctx->sm_count, s));
+        CK(launch_bp_up(bt, d_cost, d_allinds, d_pre, d_mins, d_arrived, d_work, d_done, d_err, ctx->sm_count,
+                        concurrent, s));
     }
     if (tl) tl->dmark(what + " sweep done", s);
     {
@@ -1065,7 +1066,7 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
             st = run_tree_bp(ctx, tags[d], pts[t], h_tree[t], cost[d], allinds[d], len, q, cur0[3 * d],
                              cur0[3 * d + 1], cur0[3 * d + 2], nxt[3 * d], nxt[3 * d + 1], nxt[3 * d + 2], d_err + d,
                              sd[d],
-                             &tl, "level " + std::to_string(l) + (d ? " backward" : " forward"));
+                             &tl, "level " + std::to_string(l) + (d ? " backward" : " forward"), 2);
             if (st) return st;
             tl.dmark("level " + std::to_string(l) + (d ? " backward" : " forward") + " BP done", sd[d]);
         }
