@@ -326,9 +326,7 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
     extern __shared__ float smem[];
     float* A = smem;
     float* B = A + LEN3;
-    short* ia = reinterpret_cast<short*>(B + LEN3);
-    short* ib = ia + LEN3;
-    int* s_chain = reinterpret_cast<int*>(ib + LEN3);  // this chain's finished nodes (2 LEN3 shorts: 4-aligned)
+    int* s_chain = reinterpret_cast<int*>(B + LEN3);  // this chain's finished nodes
     __shared__ float red[32];
     __shared__ int s_node, s_last, s_ready;
     // A thread with no line in the transform passes (the line slots are padded past
@@ -341,13 +339,12 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
     const int tid = threadIdx.x;
     __shared__ int s_nchain;  // entries of s_chain (written by thread 0)
     if (tid == 0) s_nchain = 0;
-    // The argmin tables of a chain's nodes: when the chain ends at a sibling (this
-    // CTA did not arrive last at the parent, so nobody waits for it) the CTA computes
-    // them itself; the chain that reaches the root (the sweep's last) appends its
-    // nodes to the list of finished nodes (`done`, work[2] counts entries), which
-    // k_bp_argmin_rest works off across the GPU after the sweep.  The barrier before
-    // an append makes every thread's rows visible to thread 0, whose GPU-scope fence
-    // orders them before its relaxed list stores.
+    // The argmin tables: every chain appends its nodes to the list of finished nodes
+    // (`done`, work[2] counts entries) when it ends (at a sibling, or at the root)
+    // or its shared-memory list is full, and k_bp_argmin_rest makes their tables
+    // across the GPU after the sweep, from the stored scaled rows.  The barrier
+    // before an append makes every thread's rows visible to thread 0, whose
+    // GPU-scope fence orders them before its relaxed list stores.
     auto publish_list = [&]() {  // thread 0
         __threadfence();
         const int slot = atomicAdd(work + 2, s_nchain);
@@ -464,13 +461,10 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
                 }
                 __syncthreads();
                 if (!s_last) {
-                    // every thread's scaled rows were stored before the barriers since
-                    for (int k = 0; k < s_nchain; k++) {
-                        __syncthreads();
-                        node_argmin<LEN>(t, s_chain[k], pre, off, allinds, A, B, ia, ib);
-                    }
-                    __syncthreads();
-                    if (tid == 0) s_nchain = 0;
+                    // the chain ends at a sibling: its nodes' argmin tables are made after
+                    // the sweep (made here, that work would share the SMs with the other
+                    // chains' steps: two concurrent sweeps ran at about half speed)
+                    if (tid == 0) publish_list();
                     break;
                 }
             }
@@ -794,12 +788,12 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_argmin_rest(BpTree t, co
     }
 }
 
-// dynamic shared memory of the sweep and of the argmin kernel: A, B (floats),
-// ia, ib (shorts, padded to a word), and for the sweep the chain list
+// dynamic shared memory of the sweep (A, B floats, the chain list) and of the argmin
+// kernel (A, B floats, ia, ib shorts)
 template <int LEN>
 constexpr size_t bp_smem(bool sweep) {
     constexpr size_t LEN3 = (size_t)LEN * LEN * LEN;
-    return LEN3 * 2 * sizeof(float) + 2 * LEN3 * sizeof(short) + (sweep ? kChainSlots * sizeof(int) : 0);
+    return LEN3 * 2 * sizeof(float) + (sweep ? kChainSlots * sizeof(int) : 2 * LEN3 * sizeof(short));
 }
 
 template <int LEN>
