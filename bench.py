@@ -151,8 +151,9 @@ def tree_depth(ordered, parents):
 
 def isolated_bp(api, ctx, pair, shape, reps=3):
     """Each level's tree belief propagation timed alone on the workload's own
-    cost volume and MST (forward direction, zero prior field): the upward sweep
-    (k_bp_up), the argmin tables (k_bp_argmin) and the downward pass (k_bp_down)
+    cost volume and MST (forward direction, zero prior field), as the registration
+    runs it (no argmin tables: the downward pass evaluates each node's entry from
+    its stored row): the upward sweep (k_bp_up) and the downward pass (k_bp_down)
     from the library's per-stage CUDA events.  Returns per-level rows and the sums
     over the 5 levels of one direction."""
     import torch
@@ -170,14 +171,13 @@ def isolated_bp(api, ctx, pair, shape, reps=3):
         sz1 = m1 * n1 * o1
         z = torch.zeros(sz1, dtype=torch.float32, device=fx.device)
         c = cost0.clone()
-        api.regularisationCL(c, z, z, z, m1, n1, o1, hw, q, ordered, parents, edgemst, want_allinds=True, ctx=ctx)
+        api.regularisationCL(c, z, z, z, m1, n1, o1, hw, q, ordered, parents, edgemst, ctx=ctx)
         torch.cuda.synchronize()
         ctx.reset_stage_times()
         ctx.set_profiling(True)
         for _ in range(reps):
             c.copy_(cost0)
-            api.regularisationCL(c, z, z, z, m1, n1, o1, hw, q, ordered, parents, edgemst, want_allinds=True,
-                                 ctx=ctx)
+            api.regularisationCL(c, z, z, z, m1, n1, o1, hw, q, ordered, parents, edgemst, ctx=ctx)
         torch.cuda.synchronize()
         ctx.set_profiling(False)
         st = ctx.stage_times()

@@ -318,7 +318,7 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
                                                            float* __restrict__ pre, float* __restrict__ mins,
                                                            const float* __restrict__ off,
                                                            int* __restrict__ arrived, int* __restrict__ work,
-                                                           int* __restrict__ done, short* __restrict__ allinds,
+                                                           int* __restrict__ done, int lists,
                                                            int* __restrict__ err) {
     constexpr int LEN3 = LEN * LEN * LEN;
     constexpr int T = bp_threads(LEN);
@@ -339,11 +339,13 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
     const int tid = threadIdx.x;
     __shared__ int s_nchain;  // entries of s_chain (written by thread 0)
     if (tid == 0) s_nchain = 0;
-    // The argmin tables: every chain appends its nodes to the list of finished nodes
-    // (`done`, work[2] counts entries) when it ends (at a sibling, or at the root)
-    // or its shared-memory list is full, and k_bp_argmin_rest makes their tables
-    // across the GPU after the sweep, from the stored scaled rows.  The barrier
-    // before an append makes every thread's rows visible to thread 0, whose
+    // The argmin tables (only when they are wanted, `lists`; the registration's
+    // downward pass evaluates the one entry per node it reads from the stored
+    // scaled rows instead): every chain appends its nodes to the list of finished
+    // nodes (`done`, work[2] counts entries) when it ends (at a sibling, or at the
+    // root) or its shared-memory list is full, and k_bp_argmin_rest makes their
+    // tables across the GPU after the sweep, from the stored scaled rows.  The
+    // barrier before an append makes every thread's rows visible to thread 0, whose
     // GPU-scope fence orders them before its relaxed list stores.
     auto publish_list = [&]() {  // thread 0
         __threadfence();
@@ -449,7 +451,7 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
             // *std::min_element (src/regularisation.h:222) starts from element 0 and only
             // replaces it on '<': a NaN first element is the result, later NaNs are skipped
             if (isnan(B[0])) mn = B[0];
-            if (tid == 0) {
+            if (tid == 0 && lists) {
                 if (s_nchain == kChainSlots) publish_list();
                 s_chain[s_nchain++] = node;
             }
@@ -464,7 +466,7 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
                     // the chain ends at a sibling: its nodes' argmin tables are made after
                     // the sweep (made here, that work would share the SMs with the other
                     // chains' steps: two concurrent sweeps ran at about half speed)
-                    if (tid == 0) publish_list();
+                    if (tid == 0 && lists) publish_list();
                     break;
                 }
             }
@@ -510,7 +512,7 @@ __global__ void __launch_bounds__(bp_threads(LEN)) k_bp_up(BpTree t, float* __re
                     if (l < LEN3) rrow[l] = acc[k];
                 }
                 __syncthreads();
-                if (tid == 0) publish_list();
+                if (tid == 0 && lists) publish_list();
                 break;
             }
             __syncthreads();  // B (this message) has been consumed by every thread
@@ -572,23 +574,93 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
                  : "memory");
 }
 
-// Bytes of one ring slot: the widest 16-byte-aligned span of a row.
-__host__ __device__ constexpr int down_slot_bytes(int len3) { return ((len3 * 2 + 15) / 16 + 1) * 16; }
+// Bytes of one ring slot: the widest 16-byte-aligned span of a row of `len3`
+// elements of `elem` bytes.
+__host__ __device__ constexpr int down_slot_bytes(int len3, int elem) {
+    return ((len3 * elem + 15) / 16 + 1) * 16;
+}
+
+// The child label for parent label lp from a node's scaled row `in` (LEN^3 floats,
+// the input of its three transform passes) and edge offsets: the one entry of its
+// argmin table that the downward pass reads, evaluated the way the full passes
+// compute every entry (src/regularisation.h:37-107, node_argmin above): pass 0 at
+// output Ly on every (x, z) line, pass 1 at output Lx on the (Ly, z) lines, pass 2
+// at output Lz, each a strict-'<' first-minimiser scan with the same float sums,
+// carrying the input index.  LEN^3 + LEN^2 + LEN candidates instead of 3 LEN^4.
+// The warp's lanes share pass 0; sv/si (LEN^2) and sv2/si2 (LEN) are its scratch.
+template <int LEN>
+__device__ __forceinline__ int lazy_argmin(const float* in, int lp, float ox, float oy, float oz, float* sv,
+                                           int* si, float* sv2, int* si2, int lane) {
+    const int Ly = lp % LEN, Lx = (lp / LEN) % LEN, Lz = lp / (LEN * LEN);
+    auto zz = [](int k, float off) {
+        const float d = (float)k + off;
+        return d * d;
+    };
+    for (int q = lane; q < LEN * LEN; q += 32) {  // pass 0 (y): line q = x + z LEN
+        const float* line = in + q * LEN;
+        float best = line[0] + zz(Ly, oy);
+        int bu = 0;
+#pragma unroll
+        for (int u = 1; u < LEN; u++) {
+            const float c = line[u] + zz(Ly - u, oy);
+            if (c < best) { best = c; bu = u; }
+        }
+        sv[q] = best;
+        si[q] = q * LEN + bu;
+    }
+    __syncwarp();
+    if (lane < LEN) {  // pass 1 (x): the (Ly, z = lane) line
+        const int z = lane;
+        float best = sv[z * LEN] + zz(Lx, ox);
+        int bt = 0;
+#pragma unroll
+        for (int x = 1; x < LEN; x++) {
+            const float c = sv[x + z * LEN] + zz(Lx - x, ox);
+            if (c < best) { best = c; bt = x; }
+        }
+        sv2[z] = best;
+        si2[z] = si[bt + z * LEN];
+    }
+    __syncwarp();
+    float best = sv2[0] + zz(Lz, oz);  // pass 2 (z): the (Ly, Lx) line, every lane alike
+    int bs = 0;
+#pragma unroll
+    for (int z = 1; z < LEN; z++) {
+        const float c = sv2[z] + zz(Lz - z, oz);
+        if (c < best) { best = c; bs = z; }
+    }
+    const int l = si2[bs];
+    __syncwarp();  // sv, sv2 are rewritten by the next node's passes
+    return l;
+}
 
 // lbl: [sz] labels (-1 = not yet known); ctl[0]: tickets handed out, ctl[1]: abort flag.
-template <int D>
+// LEN = 0: rows of the argmin tables (allinds, int16) are gathered; LEN > 0: rows of
+// the stored scaled inputs (pre, float) and the edge offsets (off: x | y | z) give
+// the child label through lazy_argmin, and no argmin table is read or written.
+template <int D, int LEN>
 __global__ void __launch_bounds__(32 * kDownWarps) k_bp_down(BpTree t, const float* __restrict__ cost,
-                                                            short* __restrict__ allinds, int* __restrict__ lbl,
+                                                            short* __restrict__ allinds,
+                                                            const float* __restrict__ pre,
+                                                            const float* __restrict__ off, int* __restrict__ lbl,
                                                             int* __restrict__ ctl, int* __restrict__ err) {
     static_assert(D >= 1 && D <= 16 && (D & (D - 1)) == 0, "ring depth: a power of two, at most half a window");
+    constexpr bool kLazy = LEN > 0;
+    constexpr int kElem = kLazy ? 4 : 2;
     extern __shared__ __align__(16) unsigned char down_smem[];
-    const int len = t.len, len3 = len * len * len;
+    const int len = kLazy ? LEN : t.len, len3 = len * len * len;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int slot_bytes = down_slot_bytes(len3);
+    const int slot_bytes = down_slot_bytes(len3, kElem);
     unsigned char* ring = down_smem + (size_t)wid * D * slot_bytes;
     uint64_t* bars = reinterpret_cast<uint64_t*>(down_smem + (size_t)kDownWarps * D * slot_bytes) + wid * D;
-    const char* table = reinterpret_cast<const char*>(allinds);
-    const long long table_bytes = (long long)t.sz * len3 * 2;
+    // lazy scratch per warp: sv, si [LEN^2], sv2, si2 [LEN]
+    constexpr int kScratch = kLazy ? 2 * (LEN * LEN + LEN) : 1;
+    float* sv = reinterpret_cast<float*>(down_smem + (size_t)kDownWarps * D * (slot_bytes + 8)) + wid * kScratch;
+    int* si = reinterpret_cast<int*>(sv + (kLazy ? LEN * LEN : 0));
+    float* sv2 = reinterpret_cast<float*>(si + (kLazy ? LEN * LEN : 0));
+    int* si2 = reinterpret_cast<int*>(sv2 + (kLazy ? LEN : 0));
+    const char* table = kLazy ? reinterpret_cast<const char*>(pre) : reinterpret_cast<const char*>(allinds);
+    const long long table_bytes = (long long)t.sz * len3 * kElem;
     if (lane == 0) {
         for (int k = 0; k < D; k++) mbar_init(bars + k, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -597,12 +669,12 @@ __global__ void __launch_bounds__(32 * kDownWarps) k_bp_down(BpTree t, const flo
     // per slot (bit s): the parity of its next phase, and whether a copy into it is
     // in flight (warp-uniform)
     uint32_t phase = 0, pending = 0;
-    // copies the argmin row of node nd into ring slot s (nothing for nd < 0)
+    // copies the row of node nd into ring slot s (nothing for nd < 0)
     auto fetch = [&](int nd, int s) {
         if (nd < 0) return;
         pending |= 1u << s;
         if (lane == 0) {
-            const long long a = (long long)nd * len3 * 2, a0 = a & ~15LL, e = a + 2LL * len3;
+            const long long a = (long long)nd * len3 * kElem, a0 = a & ~15LL, e = a + (long long)kElem * len3;
             long long bulk = ((e - a0 + 15) >> 4) << 4;
             if (a0 + bulk > table_bytes) bulk = (table_bytes - a0) & ~15LL;  // the table's last partial chunk
             unsigned char* dst = ring + s * slot_bytes;
@@ -633,9 +705,14 @@ __global__ void __launch_bounds__(32 * kDownWarps) k_bp_down(BpTree t, const flo
         if (c >= t.n_chains) break;
         const int s0 = ld_ahead(t.chain_ptr + c), n = ld_ahead(t.chain_ptr + c + 1) - s0;
         // node ids: lane j of w_node holds node s0 + 32 W + j of the current window W,
-        // x_node the next window's; x_u/x_v/x_w are loaded half a window later
+        // x_node the next window's; in lazy mode the nodes' edge offsets likewise
+        // (the next window's loaded half a window later)
         int w_node = lane < n ? ld_ahead(t.chain_nodes + s0 + lane) : -1;
         int x_node = 32 + lane < n ? ld_ahead(t.chain_nodes + s0 + 32 + lane) : -1;
+        float w_ox = 0.0f, w_oy = 0.0f, w_oz = 0.0f, x_ox = 0.0f, x_oy = 0.0f, x_oz = 0.0f;
+        if (kLazy && w_node >= 0) {
+            w_ox = ld_ahead(off + w_node); w_oy = ld_ahead(off + t.sz + w_node); w_oz = ld_ahead(off + 2 * t.sz + w_node);
+        }
         const int first = __shfl_sync(0xffffffffu, w_node, 0);
         const bool root_chain = first == t.root;
 #pragma unroll
@@ -654,7 +731,7 @@ __global__ void __launch_bounds__(32 * kDownWarps) k_bp_down(BpTree t, const flo
             for (int l = lane; l < len3; l += 32) {
                 const float v = __ldcg(rr + l);
                 if (v < bv) { bv = v; bi = l; }
-                allinds[(int64_t)first * len3 + l] = (short)l;
+                if (!kLazy) allinds[(int64_t)first * len3 + l] = (short)l;
             }
             for (int o = 16; o > 0; o >>= 1) {
                 const float ov = __shfl_xor_sync(0xffffffffu, bv, o);
@@ -687,7 +764,11 @@ __global__ void __launch_bounds__(32 * kDownWarps) k_bp_down(BpTree t, const flo
         for (int k = 0; k < n; k++) {
             if (k > 0 && (k & 31) == 0) {  // next window
                 w_node = x_node;
+                w_ox = x_ox; w_oy = x_oy; w_oz = x_oz;
                 x_node = k + 32 + lane < n ? ld_ahead(t.chain_nodes + s0 + k + 32 + lane) : -1;
+            }
+            if (kLazy && (k & 31) == 16 && x_node >= 0) {  // the next window's ids were loaded 16 steps ago
+                x_ox = ld_ahead(off + x_node); x_oy = ld_ahead(off + t.sz + x_node); x_oz = ld_ahead(off + 2 * t.sz + x_node);
             }
             const int nd = __shfl_sync(0xffffffffu, w_node, k & 31);
             int l = lp;
@@ -705,9 +786,18 @@ __global__ void __launch_bounds__(32 * kDownWarps) k_bp_down(BpTree t, const flo
                     if (lane == 0) atomicCAS(err, 0, 2);
                     lp = 0;
                 }
-                // the row's offset in its 16-byte-aligned span (low bits of nd * len3 * 2)
-                const unsigned char* row = ring + (k & (D - 1)) * slot_bytes + (int)(((unsigned)nd * (unsigned)(2 * len3)) & 15u);
-                l = reinterpret_cast<const short*>(row)[lp];
+                // the row's offset in its 16-byte-aligned span (low bits of nd * len3 * elem)
+                const unsigned char* row =
+                    ring + (k & (D - 1)) * slot_bytes + (int)(((unsigned)nd * (unsigned)(kElem * len3)) & 15u);
+                if constexpr (kLazy) {
+                    const float ox = __shfl_sync(0xffffffffu, w_ox, k & 31);
+                    const float oy = __shfl_sync(0xffffffffu, w_oy, k & 31);
+                    const float oz = __shfl_sync(0xffffffffu, w_oz, k & 31);
+                    l = lazy_argmin<kLazy ? LEN : 1>(reinterpret_cast<const float*>(row), lp, ox, oy, oz, sv, si, sv2,
+                                                     si2, lane);
+                } else {
+                    l = reinterpret_cast<const short*>(row)[lp];
+                }
                 if (l < 0 || l >= len3) {  // never for a completed upward pass
                     if (lane == 0) atomicCAS(err, 0, 2);
                     l = 0;
@@ -820,7 +910,7 @@ cudaError_t launch_up(const BpTree& t, float* cost, short* allinds, float* pre, 
     if (ctas > t.n_leaves) ctas = t.n_leaves;
     float* off = mins + t.sz;
     k_bp_offsets<<<(t.sz + 255) / 256, 256, 0, s>>>(t, off);
-    k_bp_up<LEN><<<ctas, T, smem, s>>>(t, cost, pre, mins, off, arrived, work, done, allinds, err);
+    k_bp_up<LEN><<<ctas, T, smem, s>>>(t, cost, pre, mins, off, arrived, work, done, allinds ? 1 : 0, err);
     count_launches(2);
     return cudaGetLastError();
 }
@@ -888,15 +978,21 @@ cudaError_t launch_bp_argmin(const BpTree& t, short* d_allinds, const float* d_p
     }
 }
 
-template <int D>
-static cudaError_t launch_down(const BpTree& t, const float* d_cost, short* d_allinds, float* d_u1, float* d_v1,
-                               float* d_w1, int* d_lbl, int* d_err, int sm_count, cudaStream_t s) {
+// Ring depth by row size: at most ~200 KB of shared memory per CTA.
+constexpr int down_ring(int slot) { return slot <= 3072 ? 8 : (slot <= 12288 ? 4 : (slot <= 20480 ? 2 : 1)); }
+
+template <int D, int LEN>
+static cudaError_t launch_down(const BpTree& t, const float* d_cost, short* d_allinds, const float* d_pre,
+                               const float* d_off, float* d_u1, float* d_v1, float* d_w1, int* d_lbl, int* d_err,
+                               int sm_count, cudaStream_t s) {
+    constexpr int kElem = LEN > 0 ? 4 : 2;
     const int len3 = t.len * t.len * t.len;
-    const size_t smem = (size_t)kDownWarps * D * (down_slot_bytes(len3) + sizeof(uint64_t));
-    cudaError_t e = cudaFuncSetAttribute(k_bp_down<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const size_t scratch = LEN > 0 ? 2 * (size_t)(LEN * LEN + LEN) * 4 : 4;
+    const size_t smem = (size_t)kDownWarps * (D * (down_slot_bytes(len3, kElem) + sizeof(uint64_t)) + scratch);
+    cudaError_t e = cudaFuncSetAttribute(k_bp_down<D, LEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bp_down<D>, 32 * kDownWarps, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bp_down<D, LEN>, 32 * kDownWarps, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
     // every CTA resident at once; no more walkers than chains
@@ -906,22 +1002,44 @@ static cudaError_t launch_down(const BpTree& t, const float* d_cost, short* d_al
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(d_lbl + t.sz, 0, 2 * sizeof(int), s);
     if (e != cudaSuccess) return e;
-    k_bp_down<D><<<ctas, 32 * kDownWarps, smem, s>>>(t, d_cost, d_allinds, d_lbl, d_lbl + t.sz, d_err);
+    k_bp_down<D, LEN><<<ctas, 32 * kDownWarps, smem, s>>>(t, d_cost, d_allinds, d_pre, d_off, d_lbl, d_lbl + t.sz,
+                                                         d_err);
     k_bp_field<<<(t.sz + 255) / 256, 256, 0, s>>>(t, d_lbl, d_u1, d_v1, d_w1, d_err);
     count_launches(2);
     return cudaGetLastError();
 }
 
-cudaError_t launch_bp_down(const BpTree& t, const float* d_cost, short* d_allinds, float* d_u1, float* d_v1,
-                           float* d_w1, int* d_lbl, int* d_err, int sm_count, cudaStream_t s) {
+template <int LEN>
+static cudaError_t launch_down_lazy(const BpTree& t, const float* d_cost, const float* d_pre, const float* d_off,
+                                    float* d_u1, float* d_v1, float* d_w1, int* d_lbl, int* d_err, int sm_count,
+                                    cudaStream_t s) {
+    constexpr int D = down_ring(down_slot_bytes(LEN * LEN * LEN, 4));
+    return launch_down<D, LEN>(t, d_cost, nullptr, d_pre, d_off, d_u1, d_v1, d_w1, d_lbl, d_err, sm_count, s);
+}
+
+cudaError_t launch_bp_down(const BpTree& t, const float* d_cost, short* d_allinds, const float* d_pre,
+                           const float* d_mins, float* d_u1, float* d_v1, float* d_w1, int* d_lbl, int* d_err,
+                           int sm_count, cudaStream_t s) {
     if (t.n_chains < 1 || !t.chain_ptr || !t.chain_nodes || sm_count < 1) return cudaErrorInvalidValue;
+    if (!d_allinds) {
+        // no tables: the one entry per node from the stored scaled rows (16-byte aligned)
+        if (!d_pre || !d_mins || (reinterpret_cast<uintptr_t>(d_pre) & 15)) return cudaErrorInvalidValue;
+        const float* off = d_mins + t.sz;
+#define DEEDS_LAZY(L) \
+    case L: return launch_down_lazy<L>(t, d_cost, d_pre, off, d_u1, d_v1, d_w1, d_lbl, d_err, sm_count, s);
+        switch (t.len) {
+            DEEDS_LAZY(1) DEEDS_LAZY(3) DEEDS_LAZY(5) DEEDS_LAZY(7) DEEDS_LAZY(9) DEEDS_LAZY(11) DEEDS_LAZY(13)
+            DEEDS_LAZY(15) DEEDS_LAZY(17) DEEDS_LAZY(19) DEEDS_LAZY(21)
+            default: return cudaErrorInvalidValue;
+        }
+#undef DEEDS_LAZY
+    }
     // the rows are copied in 16-byte chunks from a 16-byte-aligned table
     if (reinterpret_cast<uintptr_t>(d_allinds) & 15) return cudaErrorInvalidValue;
-    const int slot = down_slot_bytes(t.len * t.len * t.len);
-    // ring depth by row size: at most ~200 KB of shared memory per CTA
-    if (slot <= 3072) return launch_down<8>(t, d_cost, d_allinds, d_u1, d_v1, d_w1, d_lbl, d_err, sm_count, s);
-    if (slot <= 12288) return launch_down<4>(t, d_cost, d_allinds, d_u1, d_v1, d_w1, d_lbl, d_err, sm_count, s);
-    return launch_down<2>(t, d_cost, d_allinds, d_u1, d_v1, d_w1, d_lbl, d_err, sm_count, s);
+    const int slot = down_slot_bytes(t.len * t.len * t.len, 2);
+    if (slot <= 3072) return launch_down<8, 0>(t, d_cost, d_allinds, nullptr, nullptr, d_u1, d_v1, d_w1, d_lbl, d_err, sm_count, s);
+    if (slot <= 12288) return launch_down<4, 0>(t, d_cost, d_allinds, nullptr, nullptr, d_u1, d_v1, d_w1, d_lbl, d_err, sm_count, s);
+    return launch_down<2, 0>(t, d_cost, d_allinds, nullptr, nullptr, d_u1, d_v1, d_w1, d_lbl, d_err, sm_count, s);
 }
 
 }  // namespace deeds

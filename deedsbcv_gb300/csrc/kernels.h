@@ -60,16 +60,21 @@ cudaError_t launch_image_stats(const float* im0, const float* im1, int nimg, siz
 // d_pre: t.sz * len^3 floats (each node's scaled row, the transform's input)
 // d_work: 3 ints; d_done: t.sz ints (list of finished nodes); d_err: error word (4: a bounded wait expired).
 // The sweep's idle CTAs compute the argmin tables of finished nodes.
-// concurrent: sweeps expected to run at once on the GPU (each takes its share of the CTA slots)
+// concurrent: sweeps expected to run at once on the GPU (each takes its share of the CTA slots);
+// d_allinds non-NULL: the argmin tables are wanted (the sweep lists its nodes for launch_bp_argmin)
 cudaError_t launch_bp_up(const BpTree& t, float* d_cost, short* d_allinds, float* d_pre, float* d_mins, int* d_arrived,
                          int* d_work, int* d_done, int* d_err, int sm_count, int concurrent, cudaStream_t s);
 // the argmin tables (allinds) of the nodes the sweep left, from its stored rows (after launch_bp_up)
 cudaError_t launch_bp_argmin(const BpTree& t, short* d_allinds, const float* d_pre, const float* d_mins, int* d_work,
                              int* d_done, int* d_err, int sm_count, cudaStream_t s);
 // d_lbl: t.sz + 2 ints of scratch (the nodes' labels as the walk resolves them, a
-// ticket counter, an abort flag); d_allinds 16-byte aligned
-cudaError_t launch_bp_down(const BpTree& t, const float* d_cost, short* d_allinds, float* d_u1, float* d_v1,
-                           float* d_w1, int* d_lbl, int* d_err, int sm_count, cudaStream_t s);
+// ticket counter, an abort flag).  With d_allinds (16-byte aligned) the labels are
+// gathered from the argmin tables; with d_allinds NULL each node's one needed
+// entry is evaluated from its stored scaled row (d_pre, 16-byte aligned) and edge
+// offsets (d_mins + t.sz: x | y | z), and no table is read or written.
+cudaError_t launch_bp_down(const BpTree& t, const float* d_cost, short* d_allinds, const float* d_pre,
+                           const float* d_mins, float* d_u1, float* d_v1, float* d_w1, int* d_lbl, int* d_err,
+                           int sm_count, cudaStream_t s);
 cudaError_t launch_shift(const float* d_in, float* d_out, int64_t n, float shift, cudaStream_t s);
 cudaError_t launch_upsample(const float* u0, const float* v0, const float* w0, int m2, int n2, int o2, float* u,
                             float* v, float* w, int m, int n, int o, cudaStream_t s);

@@ -417,9 +417,10 @@ deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTre
                         concurrent, s));
     }
     if (tl) tl->dmark(what + " sweep done", s);
-    {
+    if (d_allinds) {
         // the argmin tables on the direction's low-priority stream, joined back before
-        // the downward pass
+        // the downward pass (without tables the downward pass evaluates the one entry
+        // per node it needs from the stored scaled rows)
         const int dl = tag == "b" ? 1 : 0;
         CK(cudaEventRecord(ctx->ev_up[dl], s));
         CK(cudaStreamWaitEvent(ctx->low[dl], ctx->ev_up[dl], 0));
@@ -429,11 +430,11 @@ deeds_status run_tree_bp(deeds_ctx* ctx, const std::string& tag, const PackedTre
         }
         CK(cudaEventRecord(ctx->ev_arg[dl], ctx->low[dl]));
         CK(cudaStreamWaitEvent(s, ctx->ev_arg[dl], 0));
+        if (tl) tl->dmark(what + " argmins joined", s);
     }
-    if (tl) tl->dmark(what + " argmins joined", s);
     {
         StageScope sc(ctx, DEEDS_STAGE_BP_DOWN, s);
-        CK(launch_bp_down(bt, d_cost, d_allinds, u1, v1, w1, d_lbl, d_err, ctx->sm_count, s));
+        CK(launch_bp_down(bt, d_cost, d_allinds, d_pre, d_mins, u1, v1, w1, d_lbl, d_err, ctx->sm_count, s));
     }
     return DEEDS_OK;
 }
@@ -454,7 +455,6 @@ struct PairBuffers {
     uint64_t* c_warp[2];
     float* mind_scr[2];
     float* cost[2];
-    short* allinds[2];
     uint64_t* mpad[2];
     float *grid, *kgrid, *cons_scr;  // kgrid: the last result's control-grid field (u | v | w)
     void* stats_scr;  // image statistics (deeds::launch_image_stats)
@@ -500,7 +500,6 @@ deeds_status acquire_buffers(deeds_ctx* ctx, int m, int n, int o, const deeds_pa
         B.c_warp[d] = dbuf<uint64_t>(ctx, "c_warp_" + tg, sz, &st);
         B.mind_scr[d] = dbuf<float>(ctx, "mind_" + tg, 6 * sz, &st);
         B.cost[d] = dbuf<float>(ctx, "cost_" + tg, B.max_cost, &st);
-        B.allinds[d] = dbuf<short>(ctx, "allinds_" + tg, B.max_cost, &st);
         B.mpad[d] = dbuf<uint64_t>(ctx, "mpad_" + tg, B.max_pad, &st);
         dbuf<uint32_t>(ctx, "tree_" + tg, pack_layout((int)B.max_sz1).total, &st);
         dbuf<float>(ctx, "mins_" + tg, 4 * B.max_sz1, &st);
@@ -718,11 +717,10 @@ deeds_status deeds_tree_bp_dev(deeds_ctx* ctx, float* d_cost, const float* d_u0,
     cudaStream_t s = (cudaStream_t)stream;
     const int sz = m1 * n1 * o1;
     const int len = 2 * hw + 1;
-    const size_t len3 = (size_t)len * len * len;
     deeds_status st = DEEDS_OK;
     PackedTree pt = pack_layout(sz);
     uint32_t* h = hbuf<uint32_t>(ctx, "tree_stage", pt.total, &st);
-    short* allinds = d_allinds ? reinterpret_cast<short*>(d_allinds) : dbuf<short>(ctx, "allinds_stage", sz * len3, &st);
+    short* allinds = reinterpret_cast<short*>(d_allinds);  // NULL: no tables (the downward pass evaluates its entries)
     int* d_err = dbuf<int>(ctx, "err_stage", 1, &st);
     if (st) return st;
     CK(cudaStreamSynchronize(s));  // the pinned staging block is reused across calls
@@ -859,7 +857,6 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
     uint64_t** c_warp = B.c_warp;
     float** mind_scr = B.mind_scr;
     float** cost = B.cost;
-    short** allinds = B.allinds;
     uint64_t** mpad = B.mpad;
     const char* tags[2] = {"f", "b"};
     float* grid = B.grid;
@@ -1063,7 +1060,7 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
             // starts once the other direction's cost volume is done too
             CK(cudaStreamWaitEvent(sd[d], ctx->ev_cost[1 - d], 0));
             tl.dmark("level " + std::to_string(l) + (d ? " backward" : " forward") + " BP starts", sd[d]);
-            st = run_tree_bp(ctx, tags[d], pts[t], h_tree[t], cost[d], allinds[d], len, q, cur0[3 * d],
+            st = run_tree_bp(ctx, tags[d], pts[t], h_tree[t], cost[d], nullptr, len, q, cur0[3 * d],
                              cur0[3 * d + 1], cur0[3 * d + 2], nxt[3 * d], nxt[3 * d + 1], nxt[3 * d + 2], d_err + d,
                              sd[d],
                              &tl, "level " + std::to_string(l) + (d ? " backward" : " forward"), 2);

@@ -159,6 +159,12 @@ def test_tree_bp_golden(api, golden, key):
     got = host(ai).reshape(-1, len3)[mask]
     exp = ref_ai.reshape(-1, len3)[mask]
     assert np.mean(got == exp) >= ARGMIN_AGREE
+    # without tables the downward pass evaluates each node's one entry from its stored
+    # row: the same fields bit for bit
+    lu, lv, lw = api.regularisationCL(cu(cost), cu(r[f"u0_{key}"]), cu(r[f"v0_{key}"]), cu(r[f"w0_{key}"]), m1, n1, o1,
+                                      hw, q, p[f"ordered_{gs}"], p[f"parents_{gs}"], p[f"edgemst_{gs}"])
+    for a, b in ((lu, u1), (lv, v1), (lw, w1)):
+        assert same_bits(host(a), host(b))
 
 
 def test_tree_bp_bit_exact_on_phantom(api):
