@@ -596,37 +596,46 @@ __device__ __forceinline__ int lazy_argmin(const float* in, int lp, float ox, fl
         const float d = (float)k + off;
         return d * d;
     };
+    float zy[LEN];  // the parabola values of each pass, once per node
+#pragma unroll
+    for (int u = 0; u < LEN; u++) zy[u] = zz(Ly - u, oy);
     for (int q = lane; q < LEN * LEN; q += 32) {  // pass 0 (y): line q = x + z LEN
         const float* line = in + q * LEN;
-        float best = line[0] + zz(Ly, oy);
+        float best = line[0] + zy[0];
         int bu = 0;
 #pragma unroll
         for (int u = 1; u < LEN; u++) {
-            const float c = line[u] + zz(Ly - u, oy);
+            const float c = line[u] + zy[u];
             if (c < best) { best = c; bu = u; }
         }
         sv[q] = best;
         si[q] = q * LEN + bu;
     }
+    float zx[LEN];
+#pragma unroll
+    for (int x = 0; x < LEN; x++) zx[x] = zz(Lx - x, ox);
     __syncwarp();
     if (lane < LEN) {  // pass 1 (x): the (Ly, z = lane) line
         const int z = lane;
-        float best = sv[z * LEN] + zz(Lx, ox);
+        float best = sv[z * LEN] + zx[0];
         int bt = 0;
 #pragma unroll
         for (int x = 1; x < LEN; x++) {
-            const float c = sv[x + z * LEN] + zz(Lx - x, ox);
+            const float c = sv[x + z * LEN] + zx[x];
             if (c < best) { best = c; bt = x; }
         }
         sv2[z] = best;
         si2[z] = si[bt + z * LEN];
     }
+    float zzz[LEN];
+#pragma unroll
+    for (int z = 0; z < LEN; z++) zzz[z] = zz(Lz - z, oz);
     __syncwarp();
-    float best = sv2[0] + zz(Lz, oz);  // pass 2 (z): the (Ly, Lx) line, every lane alike
+    float best = sv2[0] + zzz[0];  // pass 2 (z): the (Ly, Lx) line, every lane alike
     int bs = 0;
 #pragma unroll
     for (int z = 1; z < LEN; z++) {
-        const float c = sv2[z] + zz(Lz - z, oz);
+        const float c = sv2[z] + zzz[z];
         if (c < best) { best = c; bs = z; }
     }
     const int l = si2[bs];

@@ -1006,6 +1006,11 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
                 StageScope sc(ctx, DEEDS_STAGE_MIND, sdd);
                 CK(launch_mind_ssc(warped[d], m, n, o, qs, thr, mind_scr[d], c_warp[d], sdd));
             }
+            // the first level's cost volumes (long-running CTAs that fill the SMs) wait
+            // for the image statistics: beside them the thirteen small, latency-bound
+            // statistics kernels took twice as long, and every host tree (the finest
+            // ones end on the critical path) waits for the statistics
+            if (l == 0) CK(cudaStreamWaitEvent(sdd, ev[1], 0));
             {
                 StageScope sc(ctx, DEEDS_STAGE_DATACOST, sdd);
                 CK(data_cost_auto(ctx, d == 0 ? c_fix : c_mov, reuse ? c_mov : c_warp[d], mpad[d], m, n, o, g, hw, q,
