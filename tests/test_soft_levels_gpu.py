@@ -189,11 +189,15 @@ def test_soft_kept_state_matches_recompute(api):
     # Same kernels on the same inputs, but the cost kernels and the adjoints sum
     # with float atomics, whose order varies between runs: across three levels
     # the fields differ by ~1e-5 voxels.  A backward over the wrong or a stale
-    # state differs at order one.
+    # state differs at order one.  Between the two forwards, a finer level's
+    # trilinear warp samples the coarser field, whose derivative in position
+    # jumps at voxel faces: the few nodes whose sample sits on a face carry a
+    # different gradient, so the two runs agree to 1e-2 and a backward repeated
+    # over one forward's graph to 1e-3.
     assert (d0 - d1).abs().max().item() <= 1e-4
-    for got in (k[0], k[1], r[1]):
+    for got, tol in ((k[0], 1e-2), (k[1], 1e-2), (r[1], 1e-3)):
         for x, y in zip(got, r[0]):
-            assert _rel(x.cpu().double(), y.cpu().double()) < 1e-3
+            assert _rel(x.cpu().double(), y.cpu().double()) < tol
 
 
 def test_soft_kept_slot_checks(api):
@@ -286,8 +290,12 @@ def test_soft_batch_matches_single_pairs(api, keep):
         ((di - gt[i]) ** 2).mean().backward()
         # float atomics in the cost kernels and adjoints: ~1e-5 voxels across levels
         assert (d[i].detach() - di.detach()).abs().max().item() <= 1e-4
-        assert _rel(first[0][i].cpu().double(), Fi.grad.cpu().double()) < 1e-3
-        assert _rel(first[1][i].cpu().double(), Mi.grad.cpu().double()) < 1e-3
+        # The two runs are separate forwards whose coarser fields differ by ~1e-5
+        # voxels; the next level's trilinear warp has a derivative in position that
+        # jumps at voxel faces, so the few nodes whose sample sits on a face carry a
+        # different gradient (3.6e-3 relative seen on 1 of ~5 runs): 1e-2 here.
+        assert _rel(first[0][i].cpu().double(), Fi.grad.cpu().double()) < 1e-2
+        assert _rel(first[1][i].cpu().double(), Mi.grad.cpu().double()) < 1e-2
         ga_total += ai.grad.item()
     assert abs(first[2].item() - ga_total) <= 1e-3 * abs(ga_total) + 1e-5
 
