@@ -371,7 +371,7 @@ void build_tree(const float* sad, float stddev, int m1, int n1, int o1, int g, u
     float* edgemst = reinterpret_cast<float*>(blk + t.o_edgemst);
     prims_from_sad(sad, stddev, m1, n1, o1, g, ordered, parents, edgemst);
     TreeSchedule s;
-    build_schedule(ordered, parents, sz, s);
+    build_schedule(ordered, parents, sz, s, true);  // prims_from_sad: levels in node order
     pack_schedule(s, blk, t);
 }
 

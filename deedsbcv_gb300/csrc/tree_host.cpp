@@ -634,10 +634,12 @@ void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int 
         }
     };
     long long steps = 0;
+    // the walk's vertices; their parents and depths from the walk are final
+    std::vector<uint8_t> in_tree(sz, 0);
+    in_tree[root] = 1;
+    int walked = 1;
     {
         EdgeHeap heap((size_t)sz * 3);
-        std::vector<uint8_t> in_tree(sz, 0);
-        in_tree[root] = 1;
         int last = root;
         picks.reserve(sz);
         for (int added = 1; added < sz && pending != 0; added++) {
@@ -664,6 +666,7 @@ void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int 
                 }
             }
             in_tree[to] = 1;
+            walked++;
             depth[to] = depth[from] + 1;
             parents[to] = from;
             last = to;
@@ -691,47 +694,56 @@ void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int 
     g_mst_counts[2] += grouped && G.amb_rank.empty() ? 0 : steps;
     g_mst_counts[3] += sz - 1;
     if (grouped) {
-        // parents and depths of the assembled tree: breadth-first from the root
+        // Parents and depths of the assembled tree.  Every edge the walk added is a
+        // tree edge and no other tree edge joins two walked vertices (it would close
+        // a cycle with the walk's tree), so the walked vertices keep the parents and
+        // depths the walk gave them, and the remaining tree edges (those with an end
+        // outside the walk) attach the other vertices as subtrees of walked ones:
+        // breadth-first from those attachment edges.
         if ((int)tree_edges.size() != sz - 1) throw std::runtime_error("MST assembly: wrong edge count");
-        std::vector<int> deg_ptr(sz + 1, 0), adj(2 * (size_t)(sz - 1));
-        auto ends = [&](int id, int& p, int& q) {
-            const int v = id / 3, ax = id % 3;
-            p = v;
-            q = v + (ax == 0 ? m1 : ax == 1 ? 1 : mn1);
-        };
-        for (int id : tree_edges) {
-            int p, q;
-            ends(id, p, q);
-            deg_ptr[p + 1]++;
-            deg_ptr[q + 1]++;
-        }
-        for (int v = 0; v < sz; v++) deg_ptr[v + 1] += deg_ptr[v];
-        std::vector<int> fill(deg_ptr.begin(), deg_ptr.end() - 1);
-        for (int id : tree_edges) {
-            int p, q;
-            ends(id, p, q);
-            adj[fill[p]++] = q;
-            adj[fill[q]++] = p;
-        }
-        for (int v = 0; v < sz; v++) parents[v] = -1;
-        std::vector<int> queue(sz);
-        std::vector<uint8_t> seen(sz, 0);
-        size_t qh = 0, qt = 0;
-        queue[qt++] = root;
-        seen[root] = 1;
-        depth[root] = 0;
-        while (qh < qt) {
-            const int v = queue[qh++];
-            for (int e = deg_ptr[v]; e < deg_ptr[v + 1]; e++) {
-                const int u = adj[e];
-                if (seen[u]) continue;
-                seen[u] = 1;
-                parents[u] = v;
-                depth[u] = depth[v] + 1;
-                queue[qt++] = u;
+        if (walked < sz) {
+            // the tree's edges as a bitmap over the undirected edge ids
+            std::vector<uint64_t> is_tree(((size_t)3 * sz + 63) / 64, 0);
+            for (int id : tree_edges) is_tree[(size_t)id >> 6] |= 1ull << (id & 63);
+            auto tree_nb = [&](int v, int nb, int& u) {  // v's tree neighbour in direction nb, if any
+                const int k = v / mn1, rem = v - k * mn1, j = rem / m1, i = rem - j * m1;
+                const bool in_grid = nb == 0 ? j > 0 : nb == 1 ? j + 1 < n1 : nb == 2 ? i > 0 : nb == 3 ? i + 1 < m1
+                                   : nb == 4 ? k > 0 : k + 1 < o1;
+                if (!in_grid) return false;
+                u = v + off[nb];
+                const int id = (nb & 1) ? 3 * v + nb / 2 : 3 * u + nb / 2;
+                return ((is_tree[(size_t)id >> 6] >> (id & 63)) & 1ull) != 0;
+            };
+            // attachment edges (one end walked, which is the parent), then breadth-first
+            std::vector<int> queue;
+            queue.reserve((size_t)(sz - walked));
+            std::vector<uint8_t> walked_at_end(in_tree);
+            for (int v = 0; v < sz; v++) {
+                if (walked_at_end[v]) continue;
+                for (int nb = 0; nb < 6; nb++) {
+                    int u;
+                    if (tree_nb(v, nb, u) && walked_at_end[u]) {
+                        in_tree[v] = 1;
+                        parents[v] = u;
+                        depth[v] = depth[u] + 1;
+                        queue.push_back(v);
+                        break;
+                    }
+                }
             }
+            for (size_t qh = 0; qh < queue.size(); qh++) {
+                const int v = queue[qh];
+                for (int nb = 0; nb < 6; nb++) {
+                    int u;
+                    if (!tree_nb(v, nb, u) || in_tree[u]) continue;
+                    in_tree[u] = 1;
+                    parents[u] = v;
+                    depth[u] = depth[v] + 1;
+                    queue.push_back(u);
+                }
+            }
+            if ((int)queue.size() != sz - walked) throw std::runtime_error("MST assembly: tree does not span the grid");
         }
-        if ((int)qt != sz) throw std::runtime_error("MST assembly: tree does not span the grid");
     }
     // breadth-level order, stable in node id (src/primsMST.h:166-190)
     int maxd = 0;
@@ -743,56 +755,92 @@ void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int 
     // weight of each child's edge to its parent (src/primsMST.h:198-211)
     // The reference forms the neighbour index without a bounds check here, so on
     // grids with a dimension of 1 an out-of-grid direction can alias the parent;
-    // the same unchecked index (last match wins) is used.
-    for (int v = 0; v < sz; v++) edgemst[v] = 0.0f;
-    for (int t = 1; t < sz; t++) {
-        const int c = ordered[t], p = parents[c];
-        const int k = c / mn1, rem = c - k * mn1, j = rem / m1, i = rem - j * m1;
-        const int dxs[6] = {-1, 1, 0, 0, 0, 0}, dys[6] = {0, 0, -1, 1, 0, 0}, dzs[6] = {0, 0, 0, 0, -1, 1};
-        for (int nb = 0; nb < 6; nb++)
-            if (i + dys[nb] + (j + dxs[nb]) * m1 + (k + dzs[nb]) * mn1 == p) edgemst[c] = -w[(size_t)c * 6 + nb];
+    // the same unchecked index (last match wins) is used.  That index is the child's
+    // plus the direction's offset, so the direction is found from parent - child.
+    for (int c = 0; c < sz; c++) {
+        float e = 0.0f;
+        if (c != root) {
+            const int d = parents[c] - c;
+            int sel = -1;
+            for (int nb = 0; nb < 6; nb++) {  // masks: no data-dependent branch
+                const int mk = -(int)(d == off[nb]);
+                sel = (sel & ~mk) | (nb & mk);
+            }
+            if (sel >= 0) e = -w[(size_t)c * 6 + sel];
+        }
+        edgemst[c] = e;
     }
 }
 
-void build_schedule(const int* ordered, const int* parents, int sz, TreeSchedule& s) {
+void build_schedule(const int* ordered, const int* parents, int sz, TreeSchedule& s, bool levels_by_id) {
     // children per node in ordering order (ordering is breadth-level, so a
-    // parent's children appear in the order the reference adds them)
+    // parent's children appear in the order the reference adds them); every node
+    // but ordered[0] is a child, so the counts can be taken in node order
     s.child_ptr.assign(sz + 1, 0);
-    for (int t = 1; t < sz; t++) s.child_ptr[parents[ordered[t]] + 1]++;
+    const int r0 = sz > 0 ? ordered[0] : -1;
+    for (int v = 0; v < sz; v++)
+        if (v != r0) s.child_ptr[parents[v] + 1]++;
     for (int v = 0; v < sz; v++) s.child_ptr[v + 1] += s.child_ptr[v];
     s.children.assign(sz > 0 ? sz - 1 : 0, 0);
-    std::vector<int> fill(s.child_ptr.begin(), s.child_ptr.end() - 1);
-    for (int t = 1; t < sz; t++) {
-        const int c = ordered[t];
-        s.children[fill[parents[c]]++] = c;
-    }
-    // leaves, deepest first (long chains start early)
-    s.leaves.clear();
-    for (int t = sz - 1; t >= 1; t--) {
-        const int v = ordered[t];
-        if (s.child_ptr[v + 1] == s.child_ptr[v]) s.leaves.push_back(v);
-    }
-    // heavy children: subtree heights bottom-up (ordering is breadth-level, so every
-    // child is visited before its parent); in reverse order '>=' keeps the first
-    // child of equal height
-    std::vector<int> height(sz, 0), heavy(sz, -1);
-    for (int t = sz - 1; t >= 1; t--) {
-        const int c = ordered[t], p = parents[c];
-        if (height[c] + 1 >= height[p]) {
-            height[p] = height[c] + 1;
-            heavy[p] = c;
+    {
+        std::vector<int> fill(s.child_ptr.begin(), s.child_ptr.end() - 1);
+        if (levels_by_id) {
+            // a node's children share a breadth level, ordered there by node id:
+            // node order gives each parent its children in ordering order
+            for (int v = 0; v < sz; v++)
+                if (v != r0) s.children[fill[parents[v]]++] = v;
+        } else {
+            for (int t = 1; t < sz; t++) {
+                const int c = ordered[t];
+                s.children[fill[parents[c]]++] = c;
+            }
         }
     }
-    s.chain_ptr.clear();
-    s.chain_nodes.clear();
-    s.chain_nodes.reserve(sz);
-    for (int t = 0; t < sz; t++) {
-        const int v = ordered[t];
-        if (t > 0 && heavy[parents[v]] == v) continue;  // continues its parent's chain
-        s.chain_ptr.push_back((int)s.chain_nodes.size());
-        for (int c = v; c >= 0; c = heavy[c]) s.chain_nodes.push_back(c);
+    // leaves, deepest first (long chains start early), and the heavy children:
+    // subtree heights bottom-up (ordering is breadth-level, so every child is
+    // visited before its parent; a node visited with height 0 has no children);
+    // in reverse order '>=' keeps the first child of equal height.  A node's
+    // height, heavy child and chain slot share one 16-byte record.
+    struct Aux {
+        int height, heavy, slot, pad;
+    };
+    std::vector<Aux> aux((size_t)sz, Aux{0, -1, 0, 0});
+    s.leaves.clear();
+    s.leaves.reserve((size_t)sz);
+    for (int t = sz - 1; t >= 1; t--) {
+        const int c = ordered[t], p = parents[c];
+        const int h = aux[c].height;
+        if (h == 0) s.leaves.push_back(c);
+        const int hc = h + 1, hp = aux[p].height, kp = aux[p].heavy;
+        const bool take = hc >= hp;  // selects: the outcome is data-dependent
+        aux[p].height = take ? hc : hp;
+        aux[p].heavy = take ? c : kp;
     }
-    s.chain_ptr.push_back((int)s.chain_nodes.size());
+    // Chains in ordering order of their starts, each from its start down through
+    // heavy children to a leaf.  A heavy child's subtree is one level lower than
+    // its parent's, so a chain starting at v holds height[v] + 1 nodes: the chains'
+    // ranges follow from the starts alone, and a node's slot is its parent's + 1
+    // (no walk along the chain).
+    s.chain_ptr.clear();
+    s.chain_nodes.assign((size_t)sz, 0);
+    {
+        int next = 0;
+        for (int t = 0; t < sz; t++) {
+            const int v = ordered[t];
+            int k;
+            if (t > 0 && aux[parents[v]].heavy == v) {  // continues its parent's chain
+                k = aux[parents[v]].slot + 1;
+            } else {
+                s.chain_ptr.push_back(next);
+                k = next;
+                next += aux[v].height + 1;
+            }
+            aux[v].slot = k;
+            s.chain_nodes[(size_t)k] = v;
+        }
+        s.chain_ptr.push_back(next);
+        if (next != sz) throw std::runtime_error("tree schedule: chains do not cover the tree");
+    }
 }
 
 }  // namespace deeds

@@ -20,7 +20,10 @@ struct TreeSchedule {
 void image_stats(const float* im, size_t sz, float* mean_out, float* std_out);
 void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int g, int* ordered, int* parents,
                     float* edgemst);
-void build_schedule(const int* ordered, const int* parents, int sz, TreeSchedule& s);
+// levels_by_id: `ordered` is breadth-level order with every level in increasing
+// node id (prims_from_sad's ordering); any order where parents precede their
+// children otherwise.  Both give the same schedule for such an ordering.
+void build_schedule(const int* ordered, const int* parents, int sz, TreeSchedule& s, bool levels_by_id = false);
 // Process-wide counts of the MST constructions: trees whose minimum spanning tree
 // is unique (no Prim walk needed), trees with ambiguous ties (a Prim walk until
 // its tie picks are made, or all of it when a weight is NaN), Prim steps walked
