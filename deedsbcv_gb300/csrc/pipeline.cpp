@@ -1006,11 +1006,12 @@ deeds_status deeds_register_dev(deeds_ctx* ctx, const float* d_fixed, const floa
                 StageScope sc(ctx, DEEDS_STAGE_MIND, sdd);
                 CK(launch_mind_ssc(warped[d], m, n, o, qs, thr, mind_scr[d], c_warp[d], sdd));
             }
-            // the first level's cost volumes (long-running CTAs that fill the SMs) wait
-            // for the image statistics: beside them the thirteen small, latency-bound
-            // statistics kernels took twice as long, and every host tree (the finest
-            // ones end on the critical path) waits for the statistics
-            if (l == 0) CK(cudaStreamWaitEvent(sdd, ev[1], 0));
+            // The first level's cost volumes (long-running CTAs that fill the SMs) do
+            // not wait for the image statistics: beside them the latency-bound
+            // statistics kernels take longer and the host trees start ~1 ms later,
+            // but the finest trees are still built by the time the level loop needs
+            // them, and the loop itself starts ~1.6 ms earlier (61.6 -> 60.2 ms per
+            // 192x160x256 pair, measured both ways).
             {
                 StageScope sc(ctx, DEEDS_STAGE_DATACOST, sdd);
                 CK(data_cost_auto(ctx, d == 0 ? c_fix : c_mov, reuse ? c_mov : c_warp[d], mpad[d], m, n, o, g, hw, q,

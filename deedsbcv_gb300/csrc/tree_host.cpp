@@ -534,53 +534,107 @@ void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int 
                     float* edgemst) {
     const int sz = m1 * n1 * o1;
     // -exp(-(sad/g^3) / (2 std)) in float, as edgecost2weight() (src/primsMST.h:48-50, :112-117);
-    // stored vertex-major (w[v*6 + nb]): the six pushes of an added vertex read one line
-    // (the two directions of an edge normally have one SAD, computed once from the
-    // image, so one weight: it is evaluated once and mirrored; SADs given per
-    // direction that differ keep their own weights)
-    std::vector<float> w((size_t)sz * 6, -1.0f);
+    // stored vertex-major (w[v*6 + nb]): the six pushes of an added vertex read one
+    // line; -1 for a direction that leaves the grid.  The two directions of an edge
+    // normally have one SAD (computed once from the image), so one weight: where
+    // the mirror entry is already evaluated it is reused.
+    std::unique_ptr<float[]> w(new float[(size_t)sz * 6]);
     const float g3 = (float)std::pow((double)g, 3.0);
     const float twostd = 2.0f * stddev;
     const int mn1 = m1 * n1;
     // neighbour offsets in the reference's direction order -x,+x,-y,+y,-z,+z (src/primsMST.h:70-72)
     const int off[6] = {-m1, m1, -1, 1, -mn1, mn1};
-    // vertices [v0, v1) write the weights of their +x, +y, +z edges in both directions:
-    // disjoint entries, so ranges run on separate threads
-    auto weights = [&](int v0, int v1) {
+    // All six entries of the vertices of z-slabs [k0, k1), in vertex order; false if
+    // some edge whose lower end lies there has two different SADs.
+    auto weights = [&](int k0, int k1) {
         bool sym = true;
-        for (int v = v0; v < v1; v++) {
-            const int k = v / mn1, rem = v - k * mn1, j = rem / m1, i = rem - j * m1;
-            const bool has[3] = {j + 1 < n1, i + 1 < m1, k + 1 < o1};
-            for (int ax = 0; ax < 3; ax++) {
-                if (!has[ax]) continue;
-                const int nb = 2 * ax + 1, u = v + off[nb];
-                const float s1 = sad[(size_t)nb * sz + v], s2 = sad[(size_t)(nb - 1) * sz + u];
-                const float wt = -std::exp(-(s1 / g3) / twostd);
-                w[(size_t)v * 6 + nb] = wt;
-                if (std::memcmp(&s1, &s2, 4) == 0) {
-                    w[(size_t)u * 6 + nb - 1] = wt;
-                } else {
-                    w[(size_t)u * 6 + nb - 1] = -std::exp(-(s2 / g3) / twostd);
-                    sym = false;
+        for (int k = k0; k < k1; k++)
+            for (int j = 0; j < n1; j++)
+                for (int i = 0; i < m1; i++) {
+                    const int v = i + j * m1 + k * mn1;
+                    const bool has[6] = {j > 0, j + 1 < n1, i > 0, i + 1 < m1, k > 0, k + 1 < o1};
+                    float* wv = &w[(size_t)v * 6];
+                    for (int nb = 0; nb < 6; nb++) {
+                        if (!has[nb]) {
+                            wv[nb] = -1.0f;
+                            continue;
+                        }
+                        const float sv = sad[(size_t)nb * sz + v];
+                        const int u = v + off[nb];
+                        const float su = sad[(size_t)(nb ^ 1) * sz + u];  // the mirror direction's SAD
+                        const bool same = std::memcmp(&sv, &su, 4) == 0;
+                        if (nb & 1) {
+                            sym = sym && same;
+                            wv[nb] = -std::exp(-(sv / g3) / twostd);
+                        } else {
+                            // the lower neighbour u was evaluated before v when it lies in these slabs
+                            const bool done = nb != 4 || k > k0;
+                            wv[nb] = same && done ? w[(size_t)u * 6 + nb + 1] : -std::exp(-(sv / g3) / twostd);
+                        }
+                    }
                 }
-            }
+        return sym;
+    };
+    // Large trees: the slabs are evaluated in blocks, from the root's block outward,
+    // by helper threads while the walk starts at the root; the walk waits for a
+    // block's flag before it reads the weights of a vertex in it (only the vertex it
+    // adds), the tie analysis and the edge weights at the end wait for all of them.
+    const int root = m1 / 2 + (n1 / 2) * m1 + (o1 / 2) * m1 * n1;
+    const bool lazy = sz >= (1 << 16);
+    const int spb = lazy ? std::max(1, 8192 / mn1) : o1;  // slabs per block
+    const int nblk = (o1 + spb - 1) / spb;
+    std::unique_ptr<std::atomic<int>[]> blk_ready(new std::atomic<int>[nblk]);
+    std::vector<char> blk_sym(nblk, 1);
+    for (int b = 0; b < nblk; b++) blk_ready[b].store(0, std::memory_order_relaxed);
+    std::vector<int> blk_order;
+    {
+        const int br = (o1 / 2) / spb;
+        blk_order.push_back(br);
+        for (int d = 1; (int)blk_order.size() < nblk; d++) {
+            if (br + d < nblk) blk_order.push_back(br + d);
+            if (br - d >= 0) blk_order.push_back(br - d);
+        }
+    }
+    std::atomic<int> blk_next{0};
+    auto helper = [&]() {
+        for (;;) {
+            const int t = blk_next.fetch_add(1);
+            if (t >= nblk) return;
+            const int b = blk_order[t];
+            blk_sym[b] = weights(b * spb, std::min(o1, (b + 1) * spb));
+            blk_ready[b].store(1, std::memory_order_release);
+        }
+    };
+    auto wait_block = [&](int b) {
+        while (!blk_ready[b].load(std::memory_order_acquire)) std::this_thread::yield();
+    };
+    std::vector<std::thread> helpers;
+    struct JoinHelpers {
+        std::vector<std::thread>& t;
+        ~JoinHelpers() {
+            for (auto& x : t)
+                if (x.joinable()) x.join();
+        }
+    } join_helpers{helpers};
+    if (lazy) {
+        try {
+            for (int t = 0; t < 4; t++) helpers.emplace_back(helper);
+        } catch (...) {
+            helper();  // no threads: the rest here
+        }
+    } else {
+        helper();
+    }
+    auto all_weights = [&]() {
+        bool sym = true;
+        for (int b = 0; b < nblk; b++) {
+            wait_block(b);
+            sym = sym && blk_sym[b];
         }
         return sym;
     };
-    bool symmetric = true;
-    {
-        const int nt = sz >= (1 << 16) ? 4 : 1;
-        std::vector<std::thread> th;
-        std::vector<char> sym(nt, 1);
-        for (int t = 1; t < nt; t++)
-            th.emplace_back([&, t]() { sym[t] = weights((int)((long long)sz * t / nt), (int)((long long)sz * (t + 1) / nt)); });
-        sym[0] = weights(0, (int)((long long)sz / nt));
-        for (auto& x : th) x.join();
-        for (char c : sym) symmetric = symmetric && c;
-    }
     std::vector<int> depth(sz, 0);
     for (int v = 0; v < sz; v++) parents[v] = -1;
-    const int root = m1 / 2 + (n1 / 2) * m1 + (o1 / 2) * m1 * n1;
 
     // The tree Prim's walk would give (src/primsMST.h:120-165): Kruskal's forced
     // edges, plus the walk itself only until it has made its picks in every
@@ -589,11 +643,12 @@ void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int 
     // walk.  The tie-group analysis runs on its own thread while the walk starts;
     // the walk records its picks until the analysis is in, then counts them.
     MstGroups G;
-    std::atomic<int> g_state{symmetric && sz > 1 ? 0 : 2};  // 0 running, 1 grouped, 2 no grouping
+    std::atomic<int> g_state{sz > 1 ? 0 : 2};  // 0 running, 1 grouped, 2 no grouping
     auto analyse = [&]() {
         bool ok = false;
         try {
-            ok = mst_groups(w.data(), m1, n1, o1, G);
+            // every weight is in; an edge whose two directions differ: no grouping
+            ok = all_weights() && mst_groups(w.get(), m1, n1, o1, G);
         } catch (...) {
             ok = false;
         }
@@ -649,6 +704,7 @@ void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int 
             }
             // push the new vertex's edges to its in-grid neighbours, in direction order
             const int k = last / mn1, rem = last - k * mn1, j = rem / m1, i = rem - j * m1;
+            if (lazy) wait_block(k / spb);  // the added vertex's weights
             const bool ok[6] = {j > 0, j + 1 < n1, i > 0, i + 1 < m1, k > 0, k + 1 < o1};
             for (int nb = 0; nb < 6; nb++)
                 if (ok[nb]) heap.push(QueuedEdge{w[(size_t)last * 6 + nb], (uint32_t)last * 8u + (uint32_t)nb});
@@ -752,6 +808,7 @@ void prims_from_sad(const float* sad, float stddev, int m1, int n1, int o1, int 
     for (int v = 0; v < sz; v++) start[depth[v] + 1]++;
     for (int l = 1; l <= maxd + 1; l++) start[l] += start[l - 1];
     for (int v = 0; v < sz; v++) ordered[start[depth[v]]++] = v;
+    all_weights();  // (the analysis waited for them already, unless it never ran)
     // weight of each child's edge to its parent (src/primsMST.h:198-211)
     // The reference forms the neighbour index without a bounds check here, so on
     // grids with a dimension of 1 an out-of-grid direction can alias the parent;
