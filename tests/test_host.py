@@ -286,12 +286,16 @@ def test_unique_mst_without_prim_walk(lib, dims):
     assert after[0] - before[0] == 1 and after[2] == before[2], (before, after)
 
 
-@pytest.mark.parametrize("dims,levels", [((24, 20, 32), 40), ((48, 40, 64), 400), ((13, 11, 17), 3)])
+@pytest.mark.parametrize("dims,levels", [((24, 20, 32), 40), ((48, 40, 64), 400), ((13, 11, 17), 3),
+                                         ((100, 90, 8), 50), ((300, 250, 1), 20)])
 def test_ambiguous_ties_decided_by_partial_prim_walk(lib, dims, levels):
     """Symmetric SADs from a few values: many equal weights on cycles, so Prim's
     heap decides ties.  The library walks Prim's heap only until every ambiguous
     group has its picks and takes the rest from Kruskal's forced edges; the tree
-    must still equal the full walk's."""
+    must still equal the full walk's.  Trees of 2^16 nodes and more have their
+    weights evaluated in slab blocks by helper threads while the walk starts
+    (one slab per block where a slab holds more than 8192 nodes, one block for a
+    single slab)."""
     rng = np.random.default_rng(levels)
     sad = _symmetric_sad(*dims, lambda k: rng.integers(0, levels, k) * 64.0)
     before = _counts(lib)
